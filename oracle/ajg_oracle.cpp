@@ -1,0 +1,1395 @@
+/*
+ * Oracle for the PT-MIS / PLOC path (TEST INFRASTRUCTURE ONLY, see
+ * ajg_oracle.h).  A CPU restatement of the reference's algorithm, written to
+ * reproduce its float arithmetic operation by operation: every expression
+ * keeps the reference's evaluation order, and the file is compiled with
+ * -ffp-contract=off so no multiply-add is fused.  References are to files of
+ * siyuanpan/ajisai_render (paths relative to its root).
+ */
+#include "ajg_oracle.h"
+#include "counter_rng.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace {
+
+/* ---------------------------------------------------------------- math --- */
+/* ajisai/math/vector.h:63-69 (dot), vector3.h:90-95 (cross),
+ * vector.h:201-216 (length, normalized = v * (1 / length)). */
+struct V3 {
+  float x, y, z;
+};
+inline V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 operator+(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 operator-(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 operator*(V3 a, V3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline V3 operator/(V3 a, V3 b) { return mk(a.x / b.x, a.y / b.y, a.z / b.z); }
+inline V3 operator*(V3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+inline V3 operator*(float s, V3 a) { return a * s; }
+inline V3 operator/(V3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+inline V3 operator-(V3 a) { return mk(-a.x, -a.y, -a.z); }
+inline float dot(V3 a, V3 b) {
+  float o = 0.f;
+  o += a.x * b.x;
+  o += a.y * b.y;
+  o += a.z * b.z;
+  return o;
+}
+inline V3 cross(V3 a, V3 b) {
+  return mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x,
+            a.x * b.y - b.x * a.y);
+}
+inline float length(V3 v) { return std::sqrt(dot(v, v)); }
+inline V3 normalized(V3 v) { return v * (1.f / length(v)); }
+/* vector.h:36-45: Min(a,b) = b < a ? b : a, Max(a,b) = a < b ? b : a */
+inline float fmin_ref(float a, float b) { return b < a ? b : a; }
+inline float fmax_ref(float a, float b) { return a < b ? b : a; }
+inline V3 vmin(V3 a, V3 b) {
+  return mk(fmin_ref(a.x, b.x), fmin_ref(a.y, b.y), fmin_ref(a.z, b.z));
+}
+inline V3 vmax(V3 a, V3 b) {
+  return mk(fmax_ref(a.x, b.x), fmax_ref(a.y, b.y), fmax_ref(a.z, b.z));
+}
+inline float maxc(V3 v) { return fmax_ref(fmax_ref(v.x, v.y), v.z); }
+inline float minc(V3 v) { return fmin_ref(fmin_ref(v.x, v.y), v.z); }
+inline bool is_black(V3 v) { return maxc(v) <= 0.f; } /* spectrum.h:70 */
+inline V3 ld3(const float* p) { return mk(p[0], p[1], p[2]); }
+
+/* ajisai/math/constants.h:35-37 */
+constexpr float kPi = 3.141592654f;
+constexpr float kPi2 = 1.570796327f;
+constexpr float kPi4 = 0.785398163f;
+constexpr float kInvPi = 1.f / kPi;
+constexpr float kEps = 1e-4f; /* Ray::Eps, ray.h:43 */
+
+/* spectrum.h:80-82: evaluated in double, rounded to float */
+inline float luminance(V3 c) {
+  return (float)(0.2126 * c.x + 0.7152 * c.y + 0.0722 * c.z);
+}
+
+/* libstdc++'s std::lerp (C++20 <cmath>) for float operands */
+inline float std_lerp(float a, float b, float t) {
+  if ((a <= 0 && b >= 0) || (a >= 0 && b <= 0)) return t * b + (1 - t) * a;
+  if (t == 1) return b;
+  const float x = a + t * (b - a);
+  return (t > 1) == (b > a) ? (b < x ? x : b) : (b > x ? x : b);
+}
+/* disney.cpp:48-52: the file-local Lerp, min * (1 - val) + max * val */
+inline float dlerp(float a, float b, float t) { return a * (1 - t) + b * t; }
+inline V3 dlerp(V3 a, V3 b, float t) { return a * (1 - t) + b * t; }
+inline float clampf(float v, float lo, float hi) {
+  return v < lo ? lo : (hi < v ? hi : v);
+}
+
+/* ------------------------------------------------------------- bounds --- */
+struct Box {
+  V3 lo, hi;
+};
+/* ajisai/math/bounds.h:108-113: a point box is absorbed */
+inline bool is_point(const Box& b) {
+  return b.lo.x == b.hi.x && b.lo.y == b.hi.y && b.lo.z == b.hi.z;
+}
+inline Box join(const Box& a, const Box& b) {
+  if (is_point(a)) return b;
+  if (is_point(b)) return a;
+  return Box{vmin(a.lo, b.lo), vmax(a.hi, b.hi)};
+}
+/* bounds.h:98-101 */
+inline float area(const Box& b) {
+  V3 d = b.hi - b.lo;
+  return 2.f * (d.x * d.y + d.x * d.z + d.y * d.z);
+}
+inline Box tri_box(const float* t) { /* ploc_aggregate.cpp:168-182 */
+  Box b{mk(FLT_MAX, FLT_MAX, FLT_MAX), mk(-FLT_MAX, -FLT_MAX, -FLT_MAX)};
+  for (int k = 0; k < 3; ++k) {
+    V3 v = ld3(t + 3 * k);
+    b.lo = vmin(b.lo, v);
+    b.hi = vmax(b.hi, v);
+  }
+  return b;
+}
+
+/* ------------------------------------------------------------- morton --- */
+/* ploc_aggregate.cpp:37-82: 10 bits per axis, 30-bit code in uint32 */
+inline uint32_t morton_split(uint32_t x) {
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+struct MortonEnc {
+  V3 w2g, off;
+  explicit MortonEnc(const Box& bb) {
+    V3 size = bb.hi - bb.lo;
+    V3 inv = mk(1.f / size.x, 1.f / size.y, 1.f / size.z);
+    w2g = inv * 1024.f;
+    off = (-bb.lo) * w2g;
+  }
+  uint32_t enc(V3 p) const {
+    V3 g = p * w2g + off;
+    /* A flat axis makes size 0 and the grid coordinate NaN; the reference's
+     * float-to-integer conversion yields 0 there on x86-64 and aarch64. */
+    auto q = [](float f) -> uint32_t {
+      float g = fmax_ref(f, 0.f);
+      if (g != g) return 0u;
+      uint32_t m = g >= 4294967296.f ? 0xffffffffu : (uint32_t)g;
+      return std::min<uint32_t>(1023u, m);
+    };
+    return morton_split(q(g.x)) | (morton_split(q(g.y)) << 1) |
+           (morton_split(q(g.z)) << 2);
+  }
+};
+inline V3 box_center(const Box& b) { return (b.hi + b.lo) / 2.f; }
+
+/* --------------------------------------------------------------- PLOC --- */
+struct Node {
+  Box b;
+  int64_t count, first;
+};
+
+/* RadixSort<10> over 3 passes (ploc_aggregate.cpp:84-132): a stable LSD
+ * counting sort, i.e. the stable order by 30-bit key. */
+std::vector<int64_t> morton_order(const std::vector<uint32_t>& codes) {
+  int64_t n = (int64_t)codes.size();
+  std::vector<int64_t> idx(n), tmp(n);
+  std::vector<uint32_t> k(codes), kt(n);
+  for (int64_t i = 0; i < n; ++i) idx[i] = i;
+  for (int bit = 0; bit < 30; bit += 10) {
+    std::vector<int64_t> cnt(1025, 0);
+    for (int64_t i = 0; i < n; ++i) cnt[((k[i] >> bit) & 1023u) + 1]++;
+    for (int d = 0; d < 1024; ++d) cnt[d + 1] += cnt[d];
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t j = cnt[(k[i] >> bit) & 1023u]++;
+      kt[j] = k[i];
+      tmp[j] = idx[i];
+    }
+    k.swap(kt);
+    idx.swap(tmp);
+  }
+  return idx;
+}
+
+/* RadixSort<10>::Sort exactly as the reference runs it
+ * (ploc_aggregate.cpp:89-131): buckets_accum[0] is zeroed once before the
+ * pass loop, so from the second pass on the digit-0 keys are scattered from
+ * the previous passes' digit-0 total instead of from 0.  Later writes win,
+ * unwritten slots keep the stale contents of the destination buffer (the
+ * zero-initialised copies, then the original arrays, then pass-1 output).
+ * Returns false when a write would leave the array (undefined behaviour in
+ * the reference). */
+bool morton_order_compat(const std::vector<uint32_t>& codes,
+                         std::vector<int64_t>& out) {
+  int64_t n = (int64_t)codes.size();
+  std::vector<uint32_t> ka(codes), kb(n, 0u);
+  std::vector<int64_t> va(n), vb(n, 0);
+  for (int64_t i = 0; i < n; ++i) va[i] = i;
+  std::vector<uint32_t>* keys = &ka;
+  std::vector<uint32_t>* kcopy = &kb;
+  std::vector<int64_t>* vals = &va;
+  std::vector<int64_t>* vcopy = &vb;
+  std::vector<int64_t> accum(1024, 0);
+  for (int bit = 0; bit < 30; bit += 10) {
+    std::vector<int64_t> cnt(1024, 0);
+    for (int64_t i = 0; i < n; ++i) cnt[((*keys)[i] >> bit) & 1023u]++;
+    int64_t sum = cnt[0];
+    for (int d = 1; d < 1024; ++d) {
+      accum[d] = sum;
+      sum += cnt[d];
+    }
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t j = accum[((*keys)[i] >> bit) & 1023u]++;
+      if (j < 0 || j >= n) return false;
+      (*kcopy)[j] = (*keys)[i];
+      (*vcopy)[j] = (*vals)[i];
+    }
+    std::swap(kcopy, keys);
+    std::swap(vcopy, vals);
+  }
+  out = *vals;
+  return true;
+}
+
+/* PLOCAggregate::Cluster (ploc_aggregate.cpp:400-511).  Nearest neighbour by
+ * area of the joined box within +-r, first minimum in ascending index order;
+ * mutual pairs merge; the parent takes the right partner's slot. */
+void ploc_cluster(const std::vector<Node>& in, std::vector<Node>& out,
+                  std::vector<int64_t>& nb, std::vector<int64_t>& mi,
+                  int64_t begin, int64_t end, int64_t pre_end, int64_t r,
+                  int64_t* nbeg, int64_t* nend) {
+  for (int64_t i = begin; i < end; ++i) {
+    int64_t sb = i > begin + r ? i - r : begin;
+    int64_t se = std::min(i + r + 1, end);
+    float best = std::numeric_limits<float>::max();
+    int64_t bj = -1;
+    for (int64_t j = sb; j < se; ++j) {
+      if (j == i) continue;
+      float d = area(join(in[i].b, in[j].b));
+      if (d < best) {
+        best = d;
+        bj = j;
+      }
+    }
+    nb[i] = bj;
+  }
+  int64_t acc = 0;
+  for (int64_t i = begin; i < end; ++i) {
+    int64_t j = nb[i];
+    acc += (i < j && nb[j] == i) ? 1 : 0;
+    mi[i] = acc;
+  }
+  int64_t merged = mi[end - 1];
+  int64_t unmerged = end - begin - merged;
+  int64_t children = merged * 2;
+  int64_t children_begin = end - children;
+  int64_t unmerged_begin = end - (children + unmerged);
+  for (int64_t i = begin; i < end; ++i) {
+    int64_t j = nb[i];
+    if (nb[j] == i) {
+      if (i < j) {
+        Node& p = out[unmerged_begin + j - begin - mi[j]];
+        int64_t fc = children_begin + (mi[i] - 1) * 2;
+        p.b = join(in[j].b, in[i].b);
+        p.count = 0;
+        p.first = fc;
+        out[fc + 0] = in[i];
+        out[fc + 1] = in[j];
+      }
+    } else {
+      out[unmerged_begin + i - begin - mi[i]] = in[i];
+    }
+  }
+  for (int64_t i = end; i < pre_end; ++i) out[i] = in[i];
+  *nbeg = unmerged_begin;
+  *nend = children_begin;
+}
+
+Box world_box(const float* w) { return Box{ld3(w), ld3(w + 3)}; }
+
+bool ploc_build(const float* tris, int64_t n, const float* world, int64_t r,
+                bool radix_compat, std::vector<Node>& nodes,
+                std::vector<int64_t>& perm) {
+  Box bb = world_box(world);
+  MortonEnc enc(bb);
+  std::vector<uint32_t> codes(n);
+  for (int64_t i = 0; i < n; ++i)
+    codes[i] = enc.enc(box_center(tri_box(tris + 9 * i)));
+  if (radix_compat) {
+    if (!morton_order_compat(codes, perm)) return false;
+  } else {
+    perm = morton_order(codes);
+  }
+  int64_t nn = 2 * n - 1;
+  std::vector<Node> a(nn), b(nn);
+  std::vector<int64_t> nb(nn), mi(nn);
+  int64_t begin = nn - n, end = nn, pre_end = end;
+  for (int64_t i = 0; i < n; ++i) {
+    Node& x = a[begin + i];
+    x.b = tri_box(tris + 9 * perm[i]);
+    x.count = 1;
+    x.first = i;
+  }
+  while (end - begin > 1) {
+    int64_t nbg, nen;
+    ploc_cluster(a, b, nb, mi, begin, end, pre_end, r, &nbg, &nen);
+    a.swap(b);
+    pre_end = end;
+    begin = nbg;
+    end = nen;
+  }
+  nodes.swap(a);
+  return true;
+}
+
+/* ---------------------------------------------------------- ray tests --- */
+struct Ray {
+  V3 o, d;
+  float tmin, tmax;
+};
+/* Ray ctor (ray.h:33-39): origin pushed by Eps along the normalised
+ * direction, direction normalised. */
+inline Ray make_ray(V3 o, V3 d, float tmin = kEps,
+                    float tmax = std::numeric_limits<float>::infinity()) {
+  V3 dn = normalized(d);
+  Ray r;
+  r.o = o + dn * kEps;
+  r.d = normalized(d);
+  r.tmin = tmin;
+  r.tmax = tmax;
+  return r;
+}
+
+/* Triangle::Intersect / Occlude test (ploc_aggregate.cpp:184-242):
+ * Moller-Trumbore with the absolute determinant cull |a| < 1e-6. */
+inline bool mt_test(const Ray& r, const float* tri, float* t_out, float* u_out,
+                    float* v_out) {
+  V3 v0 = ld3(tri), v1 = ld3(tri + 3), v2 = ld3(tri + 6);
+  V3 e0 = v1 - v0, e1 = v2 - v0;
+  V3 h = cross(r.d, e1);
+  float a = dot(e0, h);
+  if (a > -1e-6f && a < 1e-6f) return false;
+  float f = 1.f / a;
+  V3 s = r.o - v0;
+  float u = f * dot(s, h);
+  if (u < 0.f || u > 1.f) return false;
+  V3 q = cross(s, e0);
+  float v = f * dot(r.d, q);
+  if (v < 0.f || u + v > 1.f) return false;
+  float t = f * dot(e1, q);
+  if (!(t > r.tmin && t < r.tmax)) return false;
+  *t_out = t;
+  *u_out = u;
+  *v_out = v;
+  return true;
+}
+
+/* Watertight test of Woop, Benthin and Wald, "Watertight Ray/Triangle
+ * Intersection", JCGT 2(1), 2013, without the double-precision fallback.
+ * Barycentrics are reported in the Moller-Trumbore convention (u for b,
+ * v for c). */
+struct WtRay {
+  int kx, ky, kz;
+  float sx, sy, sz;
+};
+inline WtRay wt_setup(const Ray& r) {
+  WtRay w;
+  float ax = std::fabs(r.d.x), ay = std::fabs(r.d.y), az = std::fabs(r.d.z);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1 == 3 ? 0 : kz + 1;
+  int ky = kx + 1 == 3 ? 0 : kx + 1;
+  const float d[3] = {r.d.x, r.d.y, r.d.z};
+  if (d[kz] < 0.f) std::swap(kx, ky);
+  w.kx = kx;
+  w.ky = ky;
+  w.kz = kz;
+  w.sx = d[kx] / d[kz];
+  w.sy = d[ky] / d[kz];
+  w.sz = 1.f / d[kz];
+  return w;
+}
+inline bool wt_test(const Ray& r, const WtRay& w, const float* tri,
+                    float* t_out, float* u_out, float* v_out) {
+  const float o[3] = {r.o.x, r.o.y, r.o.z};
+  float A[3], B[3], C[3];
+  for (int k = 0; k < 3; ++k) {
+    A[k] = tri[k] - o[k];
+    B[k] = tri[3 + k] - o[k];
+    C[k] = tri[6 + k] - o[k];
+  }
+  const float Ax = A[w.kx] - w.sx * A[w.kz], Ay = A[w.ky] - w.sy * A[w.kz];
+  const float Bx = B[w.kx] - w.sx * B[w.kz], By = B[w.ky] - w.sy * B[w.kz];
+  const float Cx = C[w.kx] - w.sx * C[w.kz], Cy = C[w.ky] - w.sy * C[w.kz];
+  const float U = Cx * By - Cy * Bx;
+  const float V = Ax * Cy - Ay * Cx;
+  const float W = Bx * Ay - By * Ax;
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f))
+    return false;
+  const float det = U + V + W;
+  if (det == 0.f) return false;
+  const float Az = w.sz * A[w.kz], Bz = w.sz * B[w.kz], Cz = w.sz * C[w.kz];
+  const float T = U * Az + V * Bz + W * Cz;
+  const float rcp = 1.f / det;
+  const float t = T * rcp;
+  if (!(t > r.tmin && t < r.tmax)) return false;
+  *t_out = t;
+  *u_out = V * rcp;
+  *v_out = W * rcp;
+  return true;
+}
+
+/* Conservative slab test shared with the GPU traversal: the reference's
+ * (bound - o) * inv_dir form (ploc_aggregate.cpp:154-162) with the far
+ * distance widened by 1 + 2*gamma(3) (Pharr, Jakob, Humphreys, PBRT 3rd ed.,
+ * 3.9.2), and an inclusive comparison against the current best t so that an
+ * equal-t hit on a lower primitive index is never culled. */
+constexpr float kSlabWiden = 1.0000003576278687f; /* 1 + 2 * 3u/(1-3u) */
+inline bool slab(const Box& b, const Ray& r, V3 inv, float tlimit) {
+  float tx0 = (b.lo.x - r.o.x) * inv.x, tx1 = (b.hi.x - r.o.x) * inv.x;
+  float ty0 = (b.lo.y - r.o.y) * inv.y, ty1 = (b.hi.y - r.o.y) * inv.y;
+  float tz0 = (b.lo.z - r.o.z) * inv.z, tz1 = (b.hi.z - r.o.z) * inv.z;
+  float tn = std::fmax(std::fmax(std::fmin(tx0, tx1), std::fmin(ty0, ty1)),
+                       std::fmin(tz0, tz1));
+  float tf = std::fmin(std::fmin(std::fmax(tx0, tx1), std::fmax(ty0, ty1)),
+                       std::fmax(tz0, tz1));
+  tf = tf * kSlabWiden;
+  return tn <= tf && tn <= tlimit && tf >= r.tmin;
+}
+
+struct Hit {
+  float t, u, v;
+  int32_t prim;
+};
+
+struct Accel {
+  const float* tris;
+  int64_t n;
+  const Node* nodes; /* reference layout */
+  const int64_t* perm;
+};
+
+inline bool tri_test(int mode, const Ray& r, const WtRay& w, const float* tri,
+                     float* t, float* u, float* v) {
+  return mode == ORC_TEST_MT ? mt_test(r, tri, t, u, v)
+                             : wt_test(r, w, tri, t, u, v);
+}
+
+Hit trace_closest(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
+  Hit h{std::numeric_limits<float>::infinity(), 0.f, 0.f, -1};
+  WtRay w = wt_setup(r);
+  auto consider = [&](int32_t prim) {
+    float t, u, v;
+    if (!tri_test(mode, r, w, acc.tris + 9 * (int64_t)prim, &t, &u, &v))
+      return;
+    if (t < h.t || (t == h.t && prim < h.prim)) h = Hit{t, u, v, prim};
+  };
+  if (!use_bvh) {
+    for (int64_t i = 0; i < acc.n; ++i) consider((int32_t)i);
+    return h;
+  }
+  V3 inv = mk(1.f / r.d.x, 1.f / r.d.y, 1.f / r.d.z);
+  std::vector<int64_t> st;
+  st.reserve(128);
+  st.push_back(0);
+  while (!st.empty()) {
+    int64_t k = st.back();
+    st.pop_back();
+    const Node& nd = acc.nodes[k];
+    float lim = std::fmin(h.t, r.tmax);
+    if (!slab(nd.b, r, inv, lim)) continue;
+    if (nd.count) {
+      consider((int32_t)acc.perm[nd.first]);
+    } else {
+      st.push_back(nd.first + 1);
+      st.push_back(nd.first);
+    }
+  }
+  return h;
+}
+
+bool trace_any(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
+  WtRay w = wt_setup(r);
+  float t, u, v;
+  if (!use_bvh) {
+    for (int64_t i = 0; i < acc.n; ++i)
+      if (tri_test(mode, r, w, acc.tris + 9 * i, &t, &u, &v)) return true;
+    return false;
+  }
+  V3 inv = mk(1.f / r.d.x, 1.f / r.d.y, 1.f / r.d.z);
+  std::vector<int64_t> st;
+  st.reserve(128);
+  st.push_back(0);
+  while (!st.empty()) {
+    int64_t k = st.back();
+    st.pop_back();
+    const Node& nd = acc.nodes[k];
+    if (!slab(nd.b, r, inv, r.tmax)) continue;
+    if (nd.count) {
+      if (tri_test(mode, r, w, acc.tris + 9 * acc.perm[nd.first], &t, &u, &v))
+        return true;
+    } else {
+      st.push_back(nd.first + 1);
+      st.push_back(nd.first);
+    }
+  }
+  return false;
+}
+
+template <class F>
+void parallel_rows(int64_t n, int threads, F&& f) {
+  if (threads <= 1 || n < 64) {
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  std::vector<std::thread> pool;
+  const int64_t chunk = 64;
+  for (int t = 0; t < threads; ++t)
+    pool.emplace_back([&]() {
+      for (;;) {
+        int64_t b = next.fetch_add(chunk);
+        if (b >= n) break;
+        int64_t e = std::min(n, b + chunk);
+        for (int64_t i = b; i < e; ++i) f(i);
+      }
+    });
+  for (auto& th : pool) th.join();
+}
+
+/* ------------------------------------------------------------- frames --- */
+/* CoordinateSystem (coordinate_system.h:37-52, Duff et al. 2017) */
+struct Frame {
+  V3 dx, dy, dz;
+  explicit Frame(V3 n) : dz(n) {
+    float sign = std::copysign(1.f, n.z);
+    const float a = -1.f / (sign + n.z);
+    const float b = n.x * n.y * a;
+    dx = mk(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    dy = mk(b, sign + n.y * n.y * a, -n.y);
+  }
+  V3 to_local(V3 v) const { return mk(dot(v, dx), dot(v, dy), dot(v, dz)); }
+  V3 to_world(V3 v) const { return dx * v.x + dy * v.y + dz * v.z; }
+};
+
+/* warp.h:29-72 */
+inline void concentric(float sx, float sy, float* px, float* py) {
+  float ox = 2.f * sx - 1.f, oy = 2.f * sy - 1.f;
+  float r, phi;
+  if (ox == 0 && oy == 0) {
+    *px = 0.f;
+    *py = 0.f;
+    return;
+  } else if (std::fabs(ox) > std::fabs(oy)) {
+    r = ox;
+    phi = kPi4 * (oy / ox);
+  } else {
+    r = oy;
+    phi = kPi2 - kPi4 * (ox / oy);
+  }
+  *px = r * std::cos(phi);
+  *py = r * std::sin(phi);
+}
+inline V3 cosine_hemisphere(float sx, float sy, float* pdf) {
+  float px, py;
+  concentric(sx, sy, &px, &py);
+  float r = 0.f;
+  r += px * px;
+  r += py * py;
+  float z = std::sqrt(fmax_ref(0.0f, 1 - r));
+  if (z == 0) z = 1e-10f;
+  if (pdf) *pdf = z * kInvPi;
+  return mk(px, py, z);
+}
+/* warp.h:74-80, 100-104 */
+inline V3 uniform_cone(float u0, float u1, float cos_max) {
+  float ct = (1.f - u0) + u0 * cos_max;
+  float st = std::sqrt(fmax_ref(0.f, 1.f - ct * ct));
+  float phi = u1 * 2 * kPi;
+  return mk(std::cos(phi) * st, std::sin(phi) * st, ct);
+}
+inline float uniform_cone_pdf(float cos_max) {
+  if (cos_max == 1.0f) return 1.0f;
+  return 1.0f / (2.0f * kPi * (1.0f - cos_max));
+}
+/* bsdf.h:42-46 */
+inline float correct_shading_normal(V3 ng, V3 ns, V3 wi) {
+  const float denom = std::fabs(dot(ng, wi));
+  return denom == 0 ? 1.f : std::fabs(dot(ns, wi) / denom);
+}
+
+/* --------------------------------------------------------------- BSDF --- */
+struct Sample {
+  V3 dir, f;
+  float pdf;
+  bool valid;
+};
+inline Sample invalid_sample() {
+  return Sample{mk(0, 0, 0), mk(0, 0, 0), 0.f, false};
+}
+
+struct Mat {
+  int type;
+  V3 base;
+  float subsurface, metallic, specular, specular_tint, roughness, anisotropic,
+      sheen, sheen_tint, clearcoat, clearcoat_gloss;
+  float lum; /* base.Luminance() */
+};
+Mat load_mat(const float* m) {
+  Mat x;
+  x.type = (int)m[0];
+  x.base = mk(m[1], m[2], m[3]);
+  x.subsurface = m[4];
+  x.metallic = m[5];
+  x.specular = m[6];
+  x.specular_tint = m[7];
+  x.roughness = m[8];
+  x.anisotropic = m[9];
+  x.sheen = m[10];
+  x.sheen_tint = m[11];
+  x.clearcoat = m[12];
+  x.clearcoat_gloss = m[13];
+  x.lum = luminance(x.base);
+  return x;
+}
+
+/* Lambertian: Diffuse::Shade builds an AggregateBSDF with one
+ * DiffuseComponent of weight 1 (diffuse.cpp:35-48,
+ * aggregate_bsdf.cpp:43-131, diffuse_component.cpp:28-64, bsdf.cpp:30-63). */
+struct Lambert {
+  V3 ng, ns, albedo, coef;
+  Frame gf, sf;
+  Lambert(V3 ng_, V3 ns_, V3 alb)
+      : ng(ng_), ns(ns_), albedo(alb), coef(alb / kPi), gf(ng_), sf(ns_) {}
+  bool fringes(V3 w) const { return (dot(ng, w) > 0) != (dot(ns, w) > 0); }
+  Sample sample(V3 wo, V3 sam) const {
+    if (fringes(wo)) {
+      if (dot(ng, wo) <= 0.f) return invalid_sample();
+      float pdf;
+      V3 lwi = cosine_hemisphere(sam.x, sam.y, &pdf);
+      if (pdf < FLT_EPSILON) return invalid_sample();
+      V3 wi = normalized(gf.to_world(lwi));
+      float factor = correct_shading_normal(ng, ns, wi);
+      return Sample{wi, albedo / kPi * factor, pdf, true};
+    }
+    V3 lwo = normalized(sf.to_local(wo));
+    if (lwo.z <= 0.f) return invalid_sample();
+    /* component selection over one weight always picks index 0 */
+    if (lwo.z < 0) return invalid_sample();
+    float pdf;
+    V3 lwi = cosine_hemisphere(sam.y, sam.z, &pdf);
+    if ((double)pdf < 1e-3) return invalid_sample();
+    if (pdf == 0) return invalid_sample();
+    lwi = normalized(lwi);
+    pdf *= 1.f;
+    V3 wi = sf.to_world(lwi);
+    float factor = correct_shading_normal(ng, ns, wi);
+    return Sample{wi, coef * factor, pdf, true};
+  }
+  V3 eval(V3 wi, V3 wo) const {
+    if (fringes(wo)) {
+      if ((dot(ng, wi) <= 0.f) || (dot(ng, wo) <= 0.f)) return mk(0, 0, 0);
+      return albedo / kPi;
+    }
+    V3 lwi = normalized(sf.to_local(wi));
+    V3 lwo = normalized(sf.to_local(wo));
+    if (lwi.z <= 0.f || lwo.z <= 0.f) return mk(0, 0, 0);
+    return mk(0, 0, 0) + coef;
+  }
+  float pdf(V3 wi, V3 wo) const {
+    if (fringes(wo)) {
+      if ((dot(ng, wi) > 0.f) != (dot(ng, wo) > 0.f)) return 0.f;
+      V3 local = normalized(gf.to_local(wi));
+      return local.z * kInvPi;
+    }
+    V3 lwi = normalized(sf.to_local(wi));
+    V3 lwo = normalized(sf.to_local(wo));
+    if (lwi.z <= 0.f || lwo.z <= 0.f) return 0.f;
+    float wsum = 0.f, p = 0.f;
+    wsum += 1.f;
+    p += 1.f * (lwi.z * kInvPi);
+    return wsum > 0 ? p / wsum : 0;
+  }
+};
+
+/* DisneyBSDF (disney.cpp:58-473), including the clearcoat pdf that reads the
+ * world-space wo (disney.cpp:208-220). */
+struct Disney {
+  const Mat& m;
+  Frame sf;
+  Disney(const Mat& mat, V3 ns) : m(mat), sf(ns) {}
+
+  static float cos2(V3 v) { return v.z * v.z; }
+  static float tan_theta(V3 v) {
+    float temp = 1 - v.z * v.z;
+    if (temp <= 0.0f) return 0.0f;
+    return std::sqrt(temp) / v.z;
+  }
+  static float tan2(V3 v) {
+    float tmp = 1.f - v.z * v.z;
+    if (tmp <= 0.f) return 0.f;
+    return tmp / (v.z * v.z);
+  }
+  static V3 reflect(V3 vi, V3 n) { return vi + (2 * dot(-vi, n) * n); }
+  static float ggx_d(V3 wh, float alpha) {
+    if (wh.z <= 0.f) return 0.f;
+    const float t2 = tan2(wh);
+    const float c2 = cos2(wh);
+    const float root = alpha / (c2 * (alpha * alpha + t2));
+    return kInvPi * (root * root);
+  }
+  static float smith_g(V3 v, V3 wh, float alpha) {
+    const float tt = std::fabs(tan_theta(v));
+    if (tt == 0.0f) return 1.0f;
+    if (dot(v, wh) * v.z <= 0) return 0.0f;
+    const float root = alpha * tt;
+    return 2.0f / (1.0f + std::sqrt(1.0f + root * root));
+  }
+  static float ggx_g(V3 wi, V3 wo, V3 wh, float alpha) {
+    return smith_g(wo, wh, alpha) * smith_g(wi, wh, alpha);
+  }
+  static float pdf_vn(V3 wi, V3 h, float alpha) {
+    float D = ggx_d(h, alpha);
+    return smith_g(wi, h, alpha) * std::fabs(dot(wi, h)) * D /
+           (std::fabs(wi.z) + 1e-4f);
+  }
+  static void vn_unit(float thetaI, float u1, float u2, float* sx, float* sy) {
+    if (thetaI < 1e-4f) {
+      float R = std::sqrt(fmax_ref(u1 / ((1 - u1) + 1e-6f), 0.0f));
+      float SinPhi = std::sin(2 * kPi * u2);
+      float CosPhi = std::cos(2 * kPi * u2);
+      *sx = R * CosPhi;
+      *sy = R * SinPhi;
+      return;
+    }
+    float TanThetaI = std::tan(thetaI);
+    float a = 1 / TanThetaI;
+    float G1 =
+        2.0f / (1.0f + std::sqrt(fmax_ref(1.0f + 1.0f / (a * a), 0.0f)));
+    float A = 2.0f * u1 / G1 - 1.0f;
+    if (std::fabs(A) == 1) A -= (A >= 0.0f ? 1.0f : -1.0f) * 1e-4f;
+    float Temp = 1.0f / (A * A - 1.0f);
+    float B = TanThetaI;
+    float D = std::sqrt(
+        fmax_ref(B * B * Temp * Temp - (A * A - B * B) * Temp, 0.0f));
+    float x1 = B * Temp - D;
+    float x2 = B * Temp + D;
+    *sx = (A < 0.0f || x2 > 1.0f / TanThetaI) ? x1 : x2;
+    float S;
+    if (u2 > 0.5f) {
+      S = 1.0f;
+      u2 = 2.0f * (u2 - 0.5f);
+    } else {
+      S = -1.0f;
+      u2 = 2.0f * (0.5f - u2);
+    }
+    /* the published rational fit, evaluated in double as in the source */
+    float z = (float)((u2 * (u2 * (u2 * (-0.365728915865723) +
+                                   0.790235037209296) -
+                             0.424965825137544) +
+                       0.000152998850436920) /
+                      (u2 * (u2 * (u2 * (u2 * 0.169507819808272 -
+                                         0.397203533833404) -
+                                   0.232500544458471) +
+                             1) -
+                       0.539825872510702));
+    *sy = S * z * std::sqrt(1.0f + (*sx) * (*sx));
+  }
+  static V3 sample_vn(V3 wi_in, float u1, float u2, float* pdf, float Alpha) {
+    V3 wi = normalized(mk(Alpha * wi_in.x, Alpha * wi_in.y, wi_in.z));
+    float Theta = 0, Phi = 0;
+    if (wi.z < float(0.99999f)) {
+      Theta = std::acos(wi.z);
+      Phi = std::atan2(wi.y, wi.x);
+    }
+    float SinPhi = std::sin(Phi), CosPhi = std::cos(Phi);
+    float sx, sy;
+    vn_unit(Theta, u1, u2, &sx, &sy);
+    float rx = CosPhi * sx - SinPhi * sy;
+    float ry = SinPhi * sx + CosPhi * sy;
+    rx *= Alpha;
+    ry *= Alpha;
+    float Norm = (float)1.f / std::sqrt(rx * rx + ry * ry + (float)1.0);
+    V3 H = mk(-rx * Norm, -ry * Norm, Norm);
+    *pdf = pdf_vn(wi_in, H, Alpha);
+    return H;
+  }
+  float fresnel_conductor(float cosi, const float& eta, const float k) const {
+    float tmp = (eta * eta + k * k) * cosi * cosi;
+    float Rparl2 =
+        (tmp - (2.f * eta * cosi) + 1) / (tmp + (2.f * eta * cosi) + 1);
+    float tmp_f = eta * eta + k * k;
+    float Rperp2 = (tmp_f - (2.f * eta * cosi) + cosi * cosi) /
+                   (tmp_f + (2.f * eta * cosi) + cosi * cosi);
+    return 0.5f * (Rparl2 + Rperp2);
+  }
+  float fresnel_schlick(float cosD, float R0) const {
+    float omc = 1.f - cosD;
+    float omc2 = omc * omc;
+    float fr = R0 + (1.f - R0) * omc2 * omc2 * omc;
+    float fc = fresnel_conductor(cosD, 0.4f, 1.6f);
+    return std_lerp(fr, fc, m.metallic);
+  }
+  static float fresnel_coat(float cosD) {
+    float omc = 1.0f - cosD;
+    float omc2 = omc * omc;
+    return 0.04f + (1.0f - 0.04f) * omc2 * omc2 * omc;
+  }
+  float diffuse_term(V3 wi, V3 wo, float idh, float rough) const {
+    if (m.metallic == 1.f) return 0.f;
+    float l = 1.f - std::fabs(wi.z), l2 = l * l;
+    float v = 1.f - std::fabs(wo.z), v2 = v * v;
+    float FD90 = 0.5f + 2.f * idh * rough;
+    return kInvPi * (1.f + (FD90 - 1.f) * l2 * l2 * l) *
+           (1.f + (FD90 - 1.f) * v2 * v2 * v);
+  }
+  float specular_term(V3 wi, V3 wo, V3 wh, float odh, float rough) const {
+    if (wi.z * wo.z <= 0.f) return 0.f;
+    float D = ggx_d(wh, rough * rough);
+    if (D == 0.f) return 0.f;
+    float nr = std_lerp(0.f, 0.08f, m.specular);
+    float F = fresnel_schlick(odh, nr);
+    float rg = (0.5f + 0.5f * rough);
+    float G = ggx_g(wi, wo, wh, rg * rg);
+    return F * D * G / (4.f * std::fabs(wi.z) * std::fabs(wo.z));
+  }
+  float subsurface_term(V3 wi, V3 wo, float idh, float rough) const {
+    if (m.subsurface == 0.0f) return 0.0f;
+    float l = 1.0f - std::fabs(wi.z), l2 = l * l;
+    float v = 1.0f - std::fabs(wo.z), v2 = v * v;
+    float F = idh * idh * rough;
+    float S = (1.0f + (F - 1.0f) * l2 * l2 * l) *
+              (1.0f + (F - 1.0f) * v2 * v2 * v);
+    return kInvPi * 1.25f *
+           (S * (1.0f / (std::fabs(wo.z) + std::fabs(wi.z)) - 0.5f) + 0.5f);
+  }
+  float clearcoat_term(V3 wi, V3 wo, V3 wh, float idh, float gloss) const {
+    if (m.clearcoat == 0.0f) return 0.0f;
+    float rough = dlerp(0.005f, 0.1f, gloss);
+    float D = ggx_d(wh, rough);
+    if (D == 0.0f) return 0.0f;
+    float F = fresnel_coat(idh);
+    float G = ggx_g(wo, wi, wh, 0.25f);
+    return m.clearcoat * D * F * G /
+           (4.0f * std::fabs(wi.z) * std::fabs(wo.z));
+  }
+  V3 eval(V3 wi, V3 wo) const {
+    const V3 lwi = normalized(sf.to_local(wi));
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (std::fabs(lwi.z) < FLT_EPSILON || std::fabs(lwo.z) < FLT_EPSILON)
+      return mk(0, 0, 0);
+    float rough = clampf(m.roughness, 0.02f, 1.f);
+    V3 untinted = mk(m.lum, m.lum, m.lum);
+    V3 spec_alb =
+        dlerp(dlerp(m.base, untinted, 1.0f - m.specular_tint), m.base,
+              m.metallic);
+    V3 sheen_alb = dlerp(untinted, m.base, m.sheen_tint);
+    V3 wh = normalized(lwo + lwi);
+    float odh = dot(lwo, wh);
+    float idh = dot(lwi, wh);
+    float omo = 1.f - odh;
+    spec_alb = dlerp(spec_alb, untinted, omo * omo * omo);
+    float F = fresnel_schlick(odh, 0.0f);
+    V3 sheen_term = F * m.sheen * sheen_alb;
+    float dl = dlerp(diffuse_term(lwi, lwo, idh, rough),
+                     subsurface_term(lwi, lwo, idh, rough), m.subsurface);
+    V3 t1 = (1.0f - m.metallic) * (m.base * dl + sheen_term);
+    V3 t2 = spec_alb * specular_term(lwi, lwo, wh, odh, rough);
+    float cc = clearcoat_term(lwi, lwo, wh, idh, m.clearcoat_gloss);
+    return t1 + t2 + mk(cc, cc, cc);
+  }
+  float pdf(V3 wi, V3 wo) const {
+    const V3 lwi = normalized(sf.to_local(wi));
+    const V3 lwo = normalized(sf.to_local(wo));
+    V3 wh = normalized(lwo + lwi);
+    if (maxc(wh) <= 0.f) return 0.f;
+    float rough = clampf(m.roughness, 0.02f, 1.f);
+    float mpdf = pdf_vn(lwo, wh, rough * rough);
+    float p = 0.f;
+    float dwhdwi = 1.f / (4.f * std::fabs(dot(lwi, wh)));
+    float spec_pdf = mpdf * dwhdwi;
+    float nr = std_lerp(0.f, 0.08f, m.specular);
+    float odh = dot(lwo, wh);
+    float ps = fresnel_schlick(odh, nr);
+    p += spec_pdf * ps;
+    p += std::fabs(lwi.z) * kInvPi * (1.f - ps);
+    if (m.clearcoat > 0.f) {
+      float cw = m.clearcoat / (m.clearcoat + m.lum);
+      float fc = fresnel_coat(std::fabs(wo.z));
+      float pc = (fc * cw) / (fc * cw + (1 - fc) * (1 - cw));
+      float cr = std_lerp(0.005f, 0.10f, m.clearcoat_gloss);
+      float chp = pdf_vn(wo, wh, cr);
+      float cp = chp * dwhdwi;
+      p *= 1.0f - pc;
+      p += cp * pc;
+    }
+    return p;
+  }
+  Sample sample(V3 wo, V3 sam) const {
+    const V3 lwo = normalized(sf.to_local(wo));
+    V3 lwi, lwh;
+    bool coat = false;
+    float r0 = sam.x, r1 = sam.y, r2 = sam.z;
+    if (m.clearcoat > 0.f) {
+      float cw = m.clearcoat / (m.clearcoat + m.lum);
+      float fc = fresnel_coat(std::fabs(lwo.z));
+      float pc = (fc * cw) / (fc * cw + (1.f - fc) * (1.f - cw));
+      if (sam.y < pc) {
+        coat = true;
+        r1 /= pc;
+        float cr = std_lerp(0.005f, 0.1f, m.clearcoat_gloss);
+        float cpdf;
+        lwh = sample_vn(lwo, r0, r1, &cpdf, cr);
+        lwi = reflect(-lwo, lwh);
+      } else {
+        coat = false;
+        r1 = (sam.y - pc) / (1.f - pc);
+      }
+    }
+    if (!coat) {
+      float mpdf;
+      float rough = clampf(m.roughness, 0.02f, 1.0f);
+      lwh = sample_vn(lwo, r0, r1, &mpdf, rough * rough);
+      float nr = std_lerp(0.0f, 0.08f, m.specular);
+      float odh = dot(lwo, lwh);
+      float ps = fresnel_schlick(odh, nr);
+      if (r2 <= ps) {
+        lwi = reflect(-lwo, lwh);
+      } else {
+        lwi = cosine_hemisphere(r0, r1, nullptr);
+        if (lwo.z < 0.0f) lwi.z *= -1.0f;
+      }
+    }
+    if (lwi.z <= 0.0f) return invalid_sample();
+    const V3 wi = sf.to_world(lwi);
+    return Sample{wi, eval(wi, wo), pdf(wi, wo), true};
+  }
+};
+
+struct Bsdf {
+  int type;
+  Lambert lam;
+  Disney dis;
+  Bsdf(const Mat& m, V3 ng, V3 ns)
+      : type(m.type), lam(ng, ns, m.base), dis(m, ns) {}
+  Sample sample(V3 wo, V3 s) const {
+    return type == ORC_MAT_DIFFUSE ? lam.sample(wo, s) : dis.sample(wo, s);
+  }
+  V3 eval(V3 wi, V3 wo) const {
+    return type == ORC_MAT_DIFFUSE ? lam.eval(wi, wo) : dis.eval(wi, wo);
+  }
+  float pdf(V3 wi, V3 wo) const {
+    return type == ORC_MAT_DIFFUSE ? lam.pdf(wi, wo) : dis.pdf(wi, wo);
+  }
+};
+
+/* ---------------------------------------------------------------- RNG --- */
+/* Counter-based stand-in for RandomSampler (random_sampler.cpp:28-45), see
+ * counter_rng.h. */
+inline uint64_t path_key(uint64_t seed, uint32_t pixel, uint32_t sample) {
+  return ajg_path_key(seed, pixel, sample);
+}
+inline float key_float(uint64_t key, uint32_t dim) {
+  return ajg_key_float(key, dim);
+}
+struct Rng {
+  uint64_t key;
+  uint32_t dim = 0;
+  float next() { return key_float(key, dim++); }
+};
+
+/* ------------------------------------------------------------- lights --- */
+struct Light {
+  int type;
+  V3 rgb;      /* directional radiance / env texel */
+  V3 dir;      /* normalised toward-light direction */
+  float cosmax;
+  float scaler, rot;
+  Frame frame;
+  bool env_ok; /* luminance > 0: Distribution2D has mass */
+  Light(const float* l)
+      : type((int)l[0]),
+        rgb(mk(l[1], l[2], l[3])),
+        dir(normalized(mk(l[4], l[5], l[6]))),
+        cosmax(l[7]),
+        scaler(l[8]),
+        rot(l[9]),
+        frame(normalized(mk(l[4], l[5], l[6]))) {
+    /* env_light.cpp:29-48 with a 1x1 texture: weight = lum * sin(pi/2) */
+    float w = luminance(rgb) * std::sin(kPi * (0 + 0.5f) / float(1));
+    env_ok = w * (1.f / float(1)) > 0.f;
+  }
+};
+
+struct LightSample {
+  V3 pos, radiance;
+  float pdf;
+};
+
+/* --------------------------------------------------------- integrator --- */
+struct Scene {
+  Accel acc;
+  const float* corner_n;
+  const int32_t* tri_mat;
+  const int32_t* tri_flags;
+  std::vector<Mat> mats;
+  std::vector<Light> lights;
+  int env = -1;
+  float radius; /* (aabb.max - aabb.center).length() */
+  int mode;
+};
+
+struct HitInfo {
+  V3 pos, ng, ns, wr;
+  int mat;
+};
+
+/* Triangle hit completion: Triangle::Intersect's normal plus the
+ * geometry's PostIntersect (quad.cpp:73-90, cube.cpp:96-108,
+ * mesh.cpp:183-204, two_sided.cpp:44-53). */
+HitInfo complete_hit(const Scene& s, const Ray& r, const Hit& h) {
+  HitInfo hi;
+  const float* t = s.acc.tris + 9 * (int64_t)h.prim;
+  V3 a = ld3(t), b = ld3(t + 3), c = ld3(t + 6);
+  int fl = s.tri_flags[h.prim];
+  hi.pos = r.o + h.t * r.d;
+  if (fl & ORC_TRI_NG_REVERSED)
+    hi.ng = normalized(cross(b - c, a - c));
+  else
+    hi.ng = normalized(cross(b - a, c - a));
+  if (fl & ORC_TRI_HAS_NORMALS) {
+    const float* cn = s.corner_n + 9 * (int64_t)h.prim;
+    hi.ns = (1 - h.u - h.v) * ld3(cn) + h.u * ld3(cn + 3) + h.v * ld3(cn + 6);
+  } else {
+    hi.ns = hi.ng;
+  }
+  hi.wr = -r.d;
+  if (fl & ORC_TRI_TWO_SIDED) {
+    if (dot(hi.ng, hi.wr) < 0) {
+      hi.ng = hi.ng * -1.f;
+      hi.ns = hi.ns * -1.f;
+    }
+  }
+  hi.mat = s.tri_mat[h.prim];
+  return hi;
+}
+
+inline V3 eps_offset(const HitInfo& h, V3 dir) { /* intersection.h:42-47 */
+  if (dot(dir, h.ng) > 0.f) return h.pos + h.ng * kEps;
+  return h.pos - h.ng * kEps;
+}
+
+inline float power_heuristic(float a, float b) { /* helper.h:38-42 */
+  a *= a;
+  b *= b;
+  return a / (a + b);
+}
+
+/* EnvLight::Pdf (env_light.cpp:152-170) for a 1x1 texture */
+float env_pdf(const Light& L, V3 ref2light) {
+  const V3 d = normalized(ref2light);
+  float theta = std::acos(clampf(d.y, -1.f, 1.f));
+  float st = std::sin(theta);
+  float p2 = L.env_ok ? 1.f : 0.f;
+  return p2 / (2.f * kPi * kPi * st);
+}
+
+/* MISSampleLight / MISSampleEnvLight (helper.h:73-133) */
+V3 mis_light(const Scene& s, const Light& L, const HitInfo& h, const Bsdf& f,
+             Rng& rng) {
+  LightSample ls;
+  if (L.type == ORC_LIGHT_DIRECTIONAL) {
+    float u0 = rng.next(), u1 = rng.next();
+    V3 r2l = L.frame.to_world(uniform_cone(u0, u1, L.cosmax));
+    ls.pdf = uniform_cone_pdf(L.cosmax);
+    ls.pos = h.pos + 2.f * s.radius * r2l;
+    ls.radiance = L.rgb;
+  } else {
+    /* the two Next1D() arguments of SampleContinuous are evaluated right to
+     * left by g++: the first draw is v, the second u */
+    float v = rng.next(), u = rng.next();
+    if (!L.env_ok) return mk(0, 0, 0);
+    float pdf = 1.f;
+    constexpr float inv_2_pi = 1.f / (2.f * kPi);
+    constexpr float two_pi = 2.f * kPi;
+    u -= L.rot / 180 * kPi * inv_2_pi;
+    if (u > 1.f) u -= 1.f;
+    if (u < 0.f) u += 1.f;
+    float phi = u * two_pi;
+    float theta = v * kPi;
+    float st = std::sin(theta);
+    pdf = st != 0.f ? pdf / (2.f * kPi * kPi * st) : 0.f;
+    V3 dir = mk(-std::sin(theta) * std::cos(phi), std::cos(theta),
+                -std::sin(theta) * std::sin(phi));
+    ls.pos = h.pos + 2.f * s.radius * dir;
+    ls.radiance = L.rgb;
+    ls.pdf = pdf;
+  }
+  if (is_black(ls.radiance) || ls.pdf <= 0.f) return mk(0, 0, 0);
+  const float len = length(ls.pos - h.pos) - kEps;
+  if (len < kEps) return mk(0, 0, 0);
+  const V3 w = normalized(ls.pos - h.pos);
+  Ray sr = make_ray(h.pos, w, kEps, 0.99f * len);
+  if (trace_any(s.acc, sr, s.mode, true)) return mk(0, 0, 0);
+  const V3 bf = f.eval(w, h.wr);
+  if (is_black(bf)) return mk(0, 0, 0);
+  const V3 n = normalized(h.ns);
+  V3 fv;
+  if (L.type == ORC_LIGHT_DIRECTIONAL)
+    fv = mk(1.f, 1.f, 1.f) * ls.radiance * bf * std::fabs(dot(w, n));
+  else
+    fv = ls.radiance * bf * std::fabs(dot(w, n));
+  const float bp = f.pdf(w, h.wr);
+  return fv / ls.pdf * power_heuristic(ls.pdf, bp);
+}
+
+/* MISSampleBsdf (helper.h:209-265).  No primitive emits, so only a ray
+ * that escapes to the environment contributes. */
+V3 mis_bsdf(const Scene& s, const HitInfo& h, const Bsdf& f, Rng& rng) {
+  float a = rng.next(), b = rng.next(), c = rng.next();
+  Sample bs = f.sample(h.wr, mk(a, b, c));
+  if (is_black(bs.f) || bs.pdf == 0.f) return mk(0, 0, 0);
+  bs.dir = normalized(bs.dir);
+  Ray r = make_ray(eps_offset(h, bs.dir), bs.dir);
+  Hit hh = trace_closest(s.acc, r, s.mode, true);
+  if (hh.prim >= 0) return mk(0, 0, 0);
+  if (s.env < 0) return mk(0, 0, 0);
+  const Light& L = s.lights[s.env];
+  V3 rad = L.scaler * L.rgb;
+  if (is_black(rad)) return mk(0, 0, 0);
+  V3 fv = rad * bs.f * std::fabs(dot(h.ns, r.d));
+  float lp = env_pdf(L, r.d);
+  V3 out = mk(0, 0, 0);
+  out = out + fv / bs.pdf * power_heuristic(bs.pdf, lp);
+  return out;
+}
+
+/* PathTracing::TraceMIS (pt.cpp:98-227) and Trace (pt.cpp:229-311) */
+V3 trace_path(const Scene& s, Ray ray, Rng& rng, int min_b, int max_b,
+              float cont, bool use_mis) {
+  V3 L = mk(0, 0, 0);
+  V3 T = mk(1.f, 1.f, 1.f);
+  for (int bounce = 0; bounce < max_b; bounce++) {
+    if (bounce > min_b) {
+      if (rng.next() > cont) return L;
+      T = T / cont;
+    }
+    Hit h = trace_closest(s.acc, ray, s.mode, true);
+    if (h.prim < 0) {
+      if ((bounce == 0 || !use_mis) && s.env >= 0) {
+        const Light& E = s.lights[s.env];
+        L = L + E.scaler * E.rgb;
+      }
+      return L;
+    }
+    HitInfo hi = complete_hit(s, ray, h);
+    const Mat& m = s.mats[hi.mat];
+    Bsdf f(m, hi.ng, hi.ns);
+    T = T * mk(1.f, 1.f, 1.f); /* void medium: SampleScattering throughput */
+    if (use_mis) {
+      V3 direct = mk(0, 0, 0);
+      for (const Light& lt : s.lights) direct = direct + T * mis_light(s, lt, hi, f, rng);
+      direct = direct + T * mis_bsdf(s, hi, f, rng);
+      L = L + 1.f / 1 * direct;
+    }
+    float a = rng.next(), b = rng.next(), c = rng.next();
+    Sample bs = f.sample(hi.wr, mk(a, b, c));
+    if (is_black(bs.f) || bs.pdf < 0.f) return L;
+    T = T * (bs.f * std::fabs(dot(hi.ng, bs.dir)) / bs.pdf);
+    ray = make_ray(eps_offset(hi, bs.dir), bs.dir);
+  }
+  return L;
+}
+
+/* ThinLensCamera::GenerateRay (thin_lens.cpp:62-83) */
+inline void mat_vec(const float* M, const float v[4], float out[4]) {
+  for (int row = 0; row < 4; ++row) {
+    float o = 0.f;
+    for (int pos = 0; pos < 4; ++pos) o += M[pos * 4 + row] * v[pos];
+    out[row] = o;
+  }
+}
+inline V3 xform_point(const float* M, V3 p) {
+  float v[4] = {p.x, p.y, p.z, 1.f}, o[4];
+  mat_vec(M, v, o);
+  return mk(o[0], o[1], o[2]) / o[3];
+}
+inline V3 xform_vec(const float* M, V3 p) {
+  float v[4] = {p.x, p.y, p.z, 0.f}, o[4];
+  mat_vec(M, v, o);
+  return mk(o[0], o[1], o[2]);
+}
+Ray camera_ray(const float* cam, float rx, float ry, float lx, float ly) {
+  const float* r2c = cam;
+  const float* c2w = cam + 16;
+  float lens_r = cam[32], focal = cam[33];
+  V3 cc = xform_point(r2c, mk(rx, ry, 1.f));
+  V3 o = mk(0.f, 0.f, 0.f);
+  V3 d = normalized(cc);
+  if (lens_r > 0 && focal > 0) {
+    float px, py;
+    concentric(lx, ly, &px, &py);
+    float lxp = px * lens_r, lyp = py * lens_r;
+    float ft = focal / d.z;
+    V3 focus = o + ft * d;
+    o = mk(lxp, lyp, 0.f);
+    d = normalized(focus - o);
+  }
+  return make_ray(xform_point(c2w, o), xform_vec(c2w, d));
+}
+
+}  // namespace
+
+/* ----------------------------------------------------------------- API --- */
+extern "C" {
+
+void orc_morton(const float* tris, int64_t n, const float* world,
+                uint32_t* codes) {
+  MortonEnc enc(world_box(world));
+  for (int64_t i = 0; i < n; ++i)
+    codes[i] = enc.enc(box_center(tri_box(tris + 9 * i)));
+}
+
+int orc_ploc_build(const float* tris, int64_t n, const float* world,
+                   int64_t search_radius, int radix_compat, float* node_bounds,
+                   int64_t* node_count_first, int64_t* perm) {
+  if (n < 1) return -1;
+  std::vector<Node> nodes;
+  std::vector<int64_t> p;
+  if (!ploc_build(tris, n, world, search_radius, radix_compat != 0, nodes, p))
+    return -2;
+  for (int64_t i = 0; i < 2 * n - 1; ++i) {
+    const Node& x = nodes[i];
+    float* b = node_bounds + 6 * i;
+    b[0] = x.b.lo.x; b[1] = x.b.lo.y; b[2] = x.b.lo.z;
+    b[3] = x.b.hi.x; b[4] = x.b.hi.y; b[5] = x.b.hi.z;
+    node_count_first[2 * i] = x.count;
+    node_count_first[2 * i + 1] = x.first;
+  }
+  for (int64_t i = 0; i < n; ++i) perm[i] = p[i];
+  return 0;
+}
+
+static std::vector<Node> unpack_nodes(const float* nb, const int64_t* ncf,
+                                      int64_t n) {
+  std::vector<Node> nodes(2 * n - 1);
+  for (int64_t i = 0; i < 2 * n - 1; ++i) {
+    const float* b = nb + 6 * i;
+    nodes[i].b = Box{mk(b[0], b[1], b[2]), mk(b[3], b[4], b[5])};
+    nodes[i].count = ncf[2 * i];
+    nodes[i].first = ncf[2 * i + 1];
+  }
+  return nodes;
+}
+
+int orc_trace(const float* tris, int64_t n_tris, const float* node_bounds,
+              const int64_t* node_count_first, const int64_t* perm,
+              int use_bvh, const float* rays, int64_t n_rays, int any_hit,
+              int tri_test_mode, float* out_t, int32_t* out_prim,
+              float* out_u, float* out_v, int threads) {
+  std::vector<Node> nodes;
+  if (use_bvh) nodes = unpack_nodes(node_bounds, node_count_first, n_tris);
+  Accel acc{tris, n_tris, use_bvh ? nodes.data() : nullptr, perm};
+  parallel_rows(n_rays, threads, [&](int64_t i) {
+    const float* q = rays + 8 * i;
+    Ray r{mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), q[6], q[7]};
+    if (any_hit) {
+      bool o = trace_any(acc, r, tri_test_mode, use_bvh != 0);
+      out_prim[i] = o ? 1 : -1;
+      out_t[i] = 0.f;
+      out_u[i] = 0.f;
+      out_v[i] = 0.f;
+    } else {
+      Hit h = trace_closest(acc, r, tri_test_mode, use_bvh != 0);
+      out_t[i] = h.t;
+      out_prim[i] = h.prim;
+      out_u[i] = h.u;
+      out_v[i] = h.v;
+    }
+  });
+  return 0;
+}
+
+void orc_bsdf(const float* material, const float* ng, const float* ns,
+              const float* wo, const float* wi, const float* sam, int op,
+              float* out) {
+  Mat m = load_mat(material);
+  Bsdf f(m, ld3(ng), ld3(ns));
+  for (int k = 0; k < 8; ++k) out[k] = 0.f;
+  if (op == 0) {
+    V3 v = f.eval(ld3(wi), ld3(wo));
+    out[0] = v.x; out[1] = v.y; out[2] = v.z;
+    out[3] = f.pdf(ld3(wi), ld3(wo));
+    out[7] = 1.f;
+  } else {
+    Sample s = f.sample(ld3(wo), ld3(sam));
+    out[0] = s.f.x; out[1] = s.f.y; out[2] = s.f.z;
+    out[3] = s.pdf;
+    out[4] = s.dir.x; out[5] = s.dir.y; out[6] = s.dir.z;
+    out[7] = s.valid ? 1.f : 0.f;
+  }
+}
+
+void orc_camera_rays(const float* camera, const float* raster, int64_t n,
+                     float* rays) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* q = raster + 4 * i;
+    Ray r = camera_ray(camera, q[0], q[1], q[2], q[3]);
+    float* o = rays + 6 * i;
+    o[0] = r.o.x; o[1] = r.o.y; o[2] = r.o.z;
+    o[3] = r.d.x; o[4] = r.d.y; o[5] = r.d.z;
+  }
+}
+
+float orc_rng(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) {
+  return key_float(path_key(seed, pixel, sample), dim);
+}
+
+int orc_render(const float* tris, const float* corner_n,
+               const int32_t* tri_mat, const int32_t* tri_flags, int64_t n_tris,
+               const float* materials, int32_t n_materials,
+               const float* lights, int32_t n_lights, const float* world,
+               const float* camera, const double* params, uint64_t seed,
+               int64_t pixel_begin, int64_t pixel_end, float* out_li,
+               double* out_film, int threads) {
+  if (n_tris < 1) return -1;
+  const int spp = (int)params[0];
+  const int min_b = (int)params[1], max_b = (int)params[2];
+  const float cont = (float)params[3];
+  const bool use_mis = params[4] != 0;
+  const int mode = (int)params[5];
+  const int64_t r = (int64_t)params[6];
+  const int W = (int)camera[34], H = (int)camera[35];
+
+  std::vector<Node> nodes;
+  std::vector<int64_t> perm;
+  if (!ploc_build(tris, n_tris, world, r, params[7] != 0, nodes, perm))
+    return -2;
+  Scene s;
+  s.acc = Accel{tris, n_tris, nodes.data(), perm.data()};
+  s.corner_n = corner_n;
+  s.tri_mat = tri_mat;
+  s.tri_flags = tri_flags;
+  for (int i = 0; i < n_materials; ++i)
+    s.mats.push_back(load_mat(materials + 16 * i));
+  for (int i = 0; i < n_lights; ++i) {
+    s.lights.emplace_back(lights + 12 * i);
+    if (s.lights.back().type == ORC_LIGHT_ENV) s.env = i;
+  }
+  Box wb = world_box(world);
+  s.radius = length(wb.hi - box_center(wb));
+  s.mode = mode;
+
+  const int64_t npix = (int64_t)W * H;
+  if (pixel_end > npix) pixel_end = npix;
+  const int64_t count = pixel_end - pixel_begin;
+  std::vector<double> src(count > 0 ? 3 * count : 0, 0.0);
+  parallel_rows(count, threads, [&](int64_t k) {
+    int64_t p = pixel_begin + k;
+    int x = (int)(p % W), y = (int)(p / W);
+    double acc[3] = {0, 0, 0};
+    for (int smp = 0; smp < spp; ++smp) {
+      Rng rng{path_key(seed, (uint32_t)p, (uint32_t)smp)};
+      const float u = x + rng.next();
+      const float v = y + rng.next();
+      float l0 = rng.next(), l1 = rng.next();
+      Ray ray = camera_ray(camera, u, v, l0, l1);
+      V3 L = trace_path(s, ray, rng, min_b, max_b, cont, use_mis);
+      if (out_li) {
+        float* o = out_li + 3 * ((p - pixel_begin) * (int64_t)spp + smp);
+        o[0] = L.x; o[1] = L.y; o[2] = L.z;
+      }
+      acc[0] += L.x; acc[1] += L.y; acc[2] += L.z;
+    }
+    src[3 * k] = acc[0];
+    src[3 * k + 1] = acc[1];
+    src[3 * k + 2] = acc[2];
+  });
+  if (out_film) {
+    /* Tile::AddSample's 2x2 footprint with the clamping merge: a sample at
+     * (x, y) lands on (x-1..x, y-1..y), row/column -1 folding into 0. */
+    for (int64_t i = 0; i < 4 * npix; ++i) out_film[i] = 0.0;
+    for (int64_t k = 0; k < count; ++k) {
+      int64_t p = pixel_begin + k;
+      int x = (int)(p % W), y = (int)(p / W);
+      for (int dy = -1; dy <= 0; ++dy)
+        for (int dx = -1; dx <= 0; ++dx) {
+          int tx = std::max(0, x + dx), ty = std::max(0, y + dy);
+          double* o = out_film + 4 * ((int64_t)ty * W + tx);
+          o[0] += src[3 * k];
+          o[1] += src[3 * k + 1];
+          o[2] += src[3 * k + 2];
+          o[3] += spp;
+        }
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"
