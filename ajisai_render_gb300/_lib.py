@@ -1,0 +1,141 @@
+"""ctypes binding of libajisai_gpu.so (include/ajisai_gpu.h).
+
+The library is loaded from the package's _build directory.  There is no CPU
+fallback: if the shared library is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libajisai_gpu.so"
+
+AJG_OK = 0
+STATUS = {0: "AJG_OK", 1: "AJG_ERR_INVALID", 2: "AJG_ERR_CUDA", 3: "AJG_ERR_OOM",
+          4: "AJG_ERR_UNSUPPORTED", 5: "AJG_ERR_DEVICE", 6: "AJG_ERR_NOT_FOUND",
+          7: "AJG_ERR_CANCELLED"}
+
+
+class AjgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("wave_paths", C.c_uint32),
+                ("hbm_budget_bytes", C.c_uint64)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p),
+                ("indices", C.c_void_p), ("num_vertices", C.c_uint32),
+                ("num_triangles", C.c_uint32), ("material", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("base_color", C.c_float * 3),
+                ("params", C.c_float * 10), ("pad", C.c_float * 2)]
+
+
+class Light(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("rgb", C.c_float * 3),
+                ("direction", C.c_float * 3), ("cos_angle", C.c_float),
+                ("scaler", C.c_float), ("rot_deg", C.c_float),
+                ("pad", C.c_float * 2)]
+
+
+class SceneOpts(C.Structure):
+    _fields_ = [("search_radius", C.c_uint32), ("tri_test", C.c_uint32),
+                ("radix_compat", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("raster2camera", C.c_float * 16), ("camera2world", C.c_float * 16),
+                ("lens_radius", C.c_float), ("focal_distance", C.c_float),
+                ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("min_bounces", C.c_int32),
+                ("max_bounces", C.c_int32), ("cont_prob", C.c_float),
+                ("use_mis", C.c_uint32), ("flags", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint64), ("num_nodes", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("ploc_iterations", C.c_uint32),
+                ("build_ms", C.c_float)]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "closest_rays", "any_rays", "nodes_visited", "tris_tested",
+        "closest_nodes", "closest_tris", "any_nodes", "any_tris", "paths")]
+
+
+assert C.sizeof(Material) == 64 and C.sizeof(Light) == 48
+assert C.sizeof(Camera) == 144 and C.sizeof(RenderParams) == 32
+
+_P = C.c_void_p
+SIGNATURES = {
+    "ajg_abi_version": ([], C.c_int),
+    "ajg_create_context": ([C.POINTER(Config), C.POINTER(_P)], C.c_int),
+    "ajg_destroy_context": ([_P], C.c_int),
+    "ajg_last_error": ([_P], C.c_char_p),
+    "ajg_get_stats": ([_P, C.POINTER(Stats), C.c_int], C.c_int),
+    "ajg_scene_create": ([_P, C.POINTER(MeshDesc), C.c_uint32, C.POINTER(Material),
+                          C.c_uint32, C.POINTER(Light), C.c_uint32,
+                          C.POINTER(SceneOpts), C.POINTER(_P)], C.c_int),
+    "ajg_scene_create_flat": ([_P, _P, _P, _P, _P, C.c_uint64, _P,
+                               C.POINTER(Material), C.c_uint32, C.POINTER(Light),
+                               C.c_uint32, C.POINTER(SceneOpts), C.POINTER(_P)],
+                              C.c_int),
+    "ajg_scene_release": ([_P], C.c_int),
+    "ajg_scene_get_info": ([_P, C.POINTER(SceneInfo)], C.c_int),
+    "ajg_scene_download_bvh": ([_P, _P, _P, _P], C.c_int),
+    "ajg_trace_closest": ([_P, _P, C.c_uint64, _P], C.c_int),
+    "ajg_trace_any": ([_P, _P, C.c_uint64, _P], C.c_int),
+    "ajg_trace_closest_device": ([_P, _P, C.c_uint64, _P, _P], C.c_int),
+    "ajg_trace_any_device": ([_P, _P, C.c_uint64, _P, _P], C.c_int),
+    "ajg_bsdf_query": ([_P, _P, _P, _P, _P, _P, _P, _P, C.c_uint64, _P], C.c_int),
+    "ajg_camera_rays": ([_P, C.POINTER(Camera), _P, C.c_uint64, _P], C.c_int),
+    "ajg_render": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P], C.c_int),
+    "ajg_render_device": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P, _P],
+                          C.c_int),
+    "ajg_render_samples": ([_P, C.POINTER(Camera), C.POINTER(RenderParams),
+                            C.c_uint64, C.c_uint64, _P], C.c_int),
+}
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Load the shared library (raises if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build it with `python -m ajisai_render_gb300.build`"
+            " (there is no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if lib.ajg_abi_version() != 1:
+        raise RuntimeError("libajisai_gpu ABI version mismatch")
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(rc: int, ctx=None):
+    if rc != AJG_OK:
+        msg = load().ajg_last_error(ctx)
+        raise AjgError(rc, msg.decode() if msg else "")

@@ -1,0 +1,271 @@
+"""Host-side mirror of the reference's interface for the PT path.
+
+The names follow the reference's factory functions and interfaces:
+
+  Context                     one CUDA device, stream and wavefront arena
+  CreatePLOCAggregate(r)      aggregate options (core/aggregate/aggregate.h:45)
+  CreateDefaultScene(...)     GpuScene: PLOC BVH built on the GPU
+                              (core/scene/scene.h:64)
+  GpuScene.Intersect/Occlude  batched Aggregate::Intersect / Occlude
+  CreatePTRenderer(args)      PTRenderer with Render(scene, camera, film)
+                              (core/renderer/renderer.h:37-80)
+  Film                        per-pixel (sum of radiance, sum of weights)
+
+Everything runs in libajisai_gpu.so; this module only packs arguments.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .scenes import FlatScene, Scene, flatten
+
+F32 = np.float32
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+class Context:
+    def __init__(self, device: int = 0, wave_paths: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = _lib.load()
+        cfg = _lib.Config(device, wave_paths, hbm_budget_bytes)
+        h = C.c_void_p()
+        _lib.check(self.lib.ajg_create_context(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ajg_destroy_context(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        _lib.check(rc, self.h)
+
+    def stats(self, reset: bool = False) -> dict:
+        s = _lib.Stats()
+        self.check(self.lib.ajg_get_stats(self.h, C.byref(s), int(reset)))
+        return {n: getattr(s, n) for n, _ in s._fields_}
+
+    def bsdf_query(self, materials, ng, ns, wo, wi, sam, op):
+        """BSDF::EvalAll+PdfAll (op 0) or SampleAll (op 1) after
+        Material::Shade, one query per row; returns [n, 8]."""
+        mats = np.ascontiguousarray(materials, F32).reshape(-1, 16)
+        n = mats.shape[0]
+        recs = (_lib.Material * n)()
+        C.memmove(recs, mats.ctypes.data, mats.nbytes)
+        for i in range(n):
+            recs[i].type = int(mats[i, 0])
+        arrs = [np.ascontiguousarray(x, F32).reshape(n, 3) for x in (ng, ns, wo, wi, sam)]
+        opa = np.ascontiguousarray(op, np.int32).reshape(n)
+        out = np.zeros((n, 8), F32)
+        self.check(self.lib.ajg_bsdf_query(self.h, C.cast(recs, C.c_void_p),
+                                           *[_ptr(a) for a in arrs], _ptr(opa),
+                                           n, _ptr(out)))
+        return out
+
+    def camera_rays(self, camera36, raster):
+        cam = camera_struct(camera36)
+        r = np.ascontiguousarray(raster, F32).reshape(-1, 4)
+        out = np.zeros((r.shape[0], 6), F32)
+        self.check(self.lib.ajg_camera_rays(self.h, C.byref(cam), _ptr(r),
+                                            r.shape[0], _ptr(out)))
+        return out
+
+
+@dataclass
+class AggregateOptions:
+    search_radius: int = 14
+    tri_test: int = 0          # 0 Moller-Trumbore (as the reference), 1 watertight
+    radix_compat: bool = False  # reproduce the reference's Morton sort exactly
+
+
+def CreatePLOCAggregate(search_radius: int = 14, tri_test: int = 0,
+                        radix_compat: bool = False) -> AggregateOptions:
+    return AggregateOptions(search_radius, tri_test, radix_compat)
+
+
+def camera_struct(camera36) -> _lib.Camera:
+    c = np.ascontiguousarray(camera36, F32)
+    cam = _lib.Camera()
+    C.memmove(cam.raster2camera, c[0:16].ctypes.data, 64)
+    C.memmove(cam.camera2world, c[16:32].ctypes.data, 64)
+    cam.lens_radius = float(c[32])
+    cam.focal_distance = float(c[33])
+    cam.width = int(c[34])
+    cam.height = int(c[35])
+    return cam
+
+
+def _materials(arr):
+    arr = np.ascontiguousarray(arr, F32).reshape(-1, 16)
+    recs = (_lib.Material * arr.shape[0])()
+    C.memmove(recs, arr.ctypes.data, arr.nbytes)
+    for i in range(arr.shape[0]):
+        recs[i].type = int(arr[i, 0])
+    return recs
+
+
+def _lights(arr):
+    arr = np.ascontiguousarray(arr, F32).reshape(-1, 12)
+    recs = (_lib.Light * max(1, arr.shape[0]))()
+    if arr.shape[0]:
+        C.memmove(recs, arr.ctypes.data, arr.nbytes)
+    for i in range(arr.shape[0]):
+        recs[i].type = int(arr[i, 0])
+    return recs
+
+
+class GpuScene:
+    """A scene resident on the GPU: triangles, materials, lights and the PLOC
+    tree built by the GPU (PLOCAggregate::Build + DefaultScene)."""
+
+    def __init__(self, ctx: Context, scene, aggregate: AggregateOptions | None = None):
+        self.ctx = ctx
+        agg = aggregate or AggregateOptions()
+        flat = scene if isinstance(scene, FlatScene) else flatten(scene)
+        self.flat = flat
+        opts = _lib.SceneOpts(agg.search_radius, agg.tri_test, int(agg.radix_compat), 0)
+        mats = _materials(flat.materials)
+        lights = _lights(flat.lights)
+        tris = np.ascontiguousarray(flat.tris, F32)
+        cn = np.ascontiguousarray(flat.corner_n, F32)
+        tm = np.ascontiguousarray(flat.tri_mat, np.int32)
+        tf = np.ascontiguousarray(flat.tri_flags, np.int32)
+        world = np.ascontiguousarray(flat.world, F32)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.ajg_scene_create_flat(
+            ctx.h, _ptr(tris), _ptr(cn), _ptr(tm), _ptr(tf), tris.shape[0],
+            _ptr(world), mats, flat.materials.shape[0], lights,
+            flat.lights.shape[0], C.byref(opts), C.byref(h)))
+        self.h = h
+
+    def release(self):
+        if self.h:
+            self.ctx.lib.ajg_scene_release(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        i = _lib.SceneInfo()
+        self.ctx.check(self.ctx.lib.ajg_scene_get_info(self.h, C.byref(i)))
+        return {n: getattr(i, n) for n, _ in i._fields_}
+
+    def download_bvh(self):
+        n = self.flat.n_tris
+        nb = np.zeros((2 * n - 1, 6), F32)
+        ncf = np.zeros((2 * n - 1, 2), np.int64)
+        perm = np.zeros(n, np.int64)
+        self.ctx.check(self.ctx.lib.ajg_scene_download_bvh(self.h, _ptr(nb), _ptr(ncf),
+                                                           _ptr(perm)))
+        return nb, ncf, perm
+
+    def Intersect(self, rays):
+        """Closest hits of rays [n, 8] (o, d, t_min, t_max): returns
+        (t, prim, u, v); prim -1 on a miss."""
+        r = np.ascontiguousarray(rays, F32).reshape(-1, 8)
+        out = np.zeros((r.shape[0], 4), F32)
+        self.ctx.check(self.ctx.lib.ajg_trace_closest(self.h, _ptr(r), r.shape[0],
+                                                      _ptr(out)))
+        prim = out[:, 3].view(np.int32).copy()
+        return out[:, 0].copy(), prim, out[:, 1].copy(), out[:, 2].copy()
+
+    def Occlude(self, rays):
+        r = np.ascontiguousarray(rays, F32).reshape(-1, 8)
+        out = np.zeros(r.shape[0], np.uint8)
+        self.ctx.check(self.ctx.lib.ajg_trace_any(self.h, _ptr(r), r.shape[0], _ptr(out)))
+        return out.astype(bool)
+
+
+def CreateDefaultScene(ctx: Context, scene: Scene | FlatScene,
+                       aggregate: AggregateOptions | None = None) -> GpuScene:
+    return GpuScene(ctx, scene, aggregate)
+
+
+@dataclass
+class PTRendererArgs:
+    """PTRendererArgs (core/renderer/renderer.h:37-45) with the defaults of
+    the YAML creator (factory/creator/renderer_creators.cpp:33-39)."""
+    spp: int
+    tile_size: int = 16
+    min_bounces: int = 5
+    max_bounces: int = 10
+    cont_prob: float = 0.9
+    use_mis: bool = True
+    specular_depth: int = 20
+
+
+class Film:
+    """The film of a render: rgbw [h, w, 4] = (sum of radiance, sum of
+    weights) per pixel in the reference's box-footprint convention."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = width, height
+        self.rgbw = np.zeros((height, width, 4), F32)
+
+    def image(self) -> np.ndarray:
+        w = self.rgbw[..., 3:4]
+        return np.where(w != 0, self.rgbw[..., :3] / np.where(w != 0, w, 1), 0).astype(F32)
+
+    def write_pfm(self, path):
+        """Little-endian float32 PFM of image() (bottom row first)."""
+        img = self.image()
+        with open(path, "wb") as f:
+            f.write(b"PF\n%d %d\n-1.0\n" % (self.width, self.height))
+            f.write(np.ascontiguousarray(img[::-1], "<f4").tobytes())
+
+
+class PTRenderer:
+    """Renderer::Render for the PT path, on the GPU."""
+
+    def __init__(self, args: PTRendererArgs, seed: int = 0, fp64_film: bool = False,
+                 drop_nonfinite: bool = False):
+        self.args = args
+        self.seed = seed
+        self.fp64_film = fp64_film
+        self.drop_nonfinite = drop_nonfinite
+
+    def params(self) -> _lib.RenderParams:
+        a = self.args
+        flags = (1 if self.fp64_film else 0) | (2 if self.drop_nonfinite else 0)
+        return _lib.RenderParams(a.spp, a.min_bounces, a.max_bounces, a.cont_prob,
+                                 int(a.use_mis), flags, self.seed)
+
+    def Render(self, scene: GpuScene, camera, film: Film | None = None) -> Film:
+        cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+        cam = camera_struct(cam36)
+        film = film or Film(cam.width, cam.height)
+        p = self.params()
+        scene.ctx.check(scene.ctx.lib.ajg_render(scene.h, C.byref(cam), C.byref(p),
+                                                 _ptr(film.rgbw)))
+        return film
+
+    def RenderSamples(self, scene: GpuScene, camera, pixel_begin=0, pixel_end=None):
+        """Per-sample radiance [pixels, spp, 3] (parity checks)."""
+        cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+        cam = camera_struct(cam36)
+        pe = pixel_end if pixel_end is not None else cam.width * cam.height
+        out = np.zeros((pe - pixel_begin, self.args.spp, 3), F32)
+        p = self.params()
+        scene.ctx.check(scene.ctx.lib.ajg_render_samples(
+            scene.h, C.byref(cam), C.byref(p), pixel_begin, pe, _ptr(out)))
+        return out
+
+
+def CreatePTRenderer(args: PTRendererArgs, seed: int = 0) -> PTRenderer:
+    return PTRenderer(args, seed)

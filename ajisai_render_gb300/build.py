@@ -1,0 +1,91 @@
+"""Build libajisai_gpu.so for sm_103a with nvcc (in-tree, no torch).
+
+    python -m ajisai_render_gb300.build [--force]
+
+Each .cu file compiles in parallel to an object under _build/obj, then one
+shared library links them with the static CUDA runtime.  Every file is
+compiled with -fmad=false (device) and -ffp-contract=off (host): no
+multiply-add is contracted, so the non-transcendental arithmetic matches the
+reference compiled for baseline x86-64 bit for bit.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+CSRC = HERE / "csrc"
+INCLUDE = HERE.parent / "include"
+BUILD = HERE / "_build"
+LIB = BUILD / "libajisai_gpu.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and Path(c).exists():
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def sources():
+    return sorted(CSRC.glob("*.cu"))
+
+
+def headers():
+    return sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
+
+
+def flags(extra=()):
+    return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
+            "--expt-relaxed-constexpr", "-Xcompiler",
+            "-fPIC,-ffp-contract=off,-fvisibility=hidden",
+            "-I", str(INCLUDE), *extra]
+
+
+def _stale(out: Path, deps) -> bool:
+    if not out.exists():
+        return True
+    t = out.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    srcs = sources()
+    if not force and not _stale(LIB, srcs + headers() + [Path(__file__)]):
+        return LIB
+    obj = BUILD / "obj"
+    obj.mkdir(parents=True, exist_ok=True)
+    cc = nvcc()
+    procs = []
+    for s in srcs:
+        o = obj / (s.stem + ".o")
+        cmd = [cc, *flags(), "-c", str(s), "-o", str(o)]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        procs.append((s, o, subprocess.Popen(cmd, stdout=subprocess.PIPE,
+                                             stderr=subprocess.PIPE, text=True)))
+    objs, errs = [], []
+    for s, o, p in procs:
+        out, err = p.communicate()
+        if p.returncode != 0:
+            errs.append(f"== {s.name}\n{out}{err}")
+        elif verbose and err:
+            sys.stderr.write(f"== {s.name}\n{err}")
+        objs.append(o)
+    if errs:
+        raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
+    tmp = LIB.with_suffix(".so.tmp")
+    r = subprocess.run([cc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp),
+                        *map(str, objs)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

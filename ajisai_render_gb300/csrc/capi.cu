@@ -1,0 +1,636 @@
+// The C ABI of include/ajisai_gpu.h: contexts, scenes, ray and shading
+// queries, renders.  Every entry point validates its arguments, runs on the
+// context's stream under the context mutex, and turns CUDA or device-guard
+// failures into a status code plus a message for ajg_last_error().
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "shade.cuh"
+#include "trace.cuh"
+
+using namespace ajg;
+
+namespace {
+
+thread_local std::string g_error;  // errors before a context exists
+
+int fail(ajg_ctx* ctx, int code, const std::string& m) {
+  if (ctx)
+    ctx->last_error = m;
+  else
+    g_error = m;
+  return code;
+}
+
+int cuda_fail(ajg_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? AJG_ERR_OOM : AJG_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// After a synchronised call: surface a device guard as AJG_ERR_DEVICE and
+// clear the flag so the context stays usable.
+int check_device(ajg_ctx* ctx) {
+  uint32_t e = 0;
+  cudaError_t ce =
+      cudaMemcpy(&e, ctx->d_error, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "reading the error flag");
+  if (!e) return AJG_OK;
+  cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
+  const char* what = e == kDevStackOverflow      ? "traversal stack overflow"
+                     : e == kDevQueueOverflow    ? "queue capacity exceeded"
+                     : e == kDevIterationBound   ? "iteration bound reached"
+                     : e == kDevSortOutOfBounds  ? "sort out of bounds"
+                                                 : "unknown device guard";
+  return fail(ctx, AJG_ERR_DEVICE, std::string("device guard: ") + what);
+}
+
+// Run work on the context stream ordered after `user`, and make `user` wait
+// for it: one arena per context, so work of a context never overlaps.
+struct StreamJoin {
+  cudaStream_t ctx_s, user;
+  StreamJoin(cudaStream_t c, cudaStream_t u) : ctx_s(c), user(u) {
+    if (user && user != ctx_s) {
+      cudaEvent_t e;
+      cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+      cudaEventRecord(e, user);
+      cudaStreamWaitEvent(ctx_s, e, 0);
+      cudaEventDestroy(e);
+    }
+  }
+  ~StreamJoin() {
+    if (user && user != ctx_s) {
+      cudaEvent_t e;
+      cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+      cudaEventRecord(e, ctx_s);
+      cudaStreamWaitEvent(user, e, 0);
+      cudaEventDestroy(e);
+    }
+  }
+};
+
+float host_lum(const float* rgb) {  // spectrum.h:80-82 in double
+  return (float)(0.2126 * (double)rgb[0] + 0.7152 * (double)rgb[1] +
+                 0.0722 * (double)rgb[2]);
+}
+
+__global__ void k_bsdf_query(const ajg_material* __restrict__ mats,
+                             const float* __restrict__ ng,
+                             const float* __restrict__ ns,
+                             const float* __restrict__ wo,
+                             const float* __restrict__ wi,
+                             const float* __restrict__ sam,
+                             const int32_t* __restrict__ op, uint64_t n,
+                             float* __restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const float* m = reinterpret_cast<const float*>(mats + i);
+    float rec[16];
+    for (int k = 0; k < 16; ++k) rec[k] = m[k];
+    rec[0] = (float)mats[i].type;
+    const float lum = (float)(0.2126 * (double)rec[1] + 0.7152 * (double)rec[2] +
+                              0.0722 * (double)rec[3]);
+    Bsdf f;
+    f.type = (int)mats[i].type;
+    f.ng = ld3(ng + 3 * i);
+    f.ns = ld3(ns + 3 * i);
+    f.m = load_material(rec, lum);
+    float* o = out + 8 * i;
+    if (op[i] == 0) {
+      const F3 v = f.eval(ld3(wi + 3 * i), ld3(wo + 3 * i));
+      o[0] = v.x;
+      o[1] = v.y;
+      o[2] = v.z;
+      o[3] = f.pdf(ld3(wi + 3 * i), ld3(wo + 3 * i));
+      o[4] = o[5] = o[6] = 0.f;
+      o[7] = 1.f;
+    } else {
+      const BsdfSample s = f.sample(ld3(wo + 3 * i), ld3(sam + 3 * i));
+      o[0] = s.f.x;
+      o[1] = s.f.y;
+      o[2] = s.f.z;
+      o[3] = s.pdf;
+      o[4] = s.dir.x;
+      o[5] = s.dir.y;
+      o[6] = s.dir.z;
+      const bool invalid = black3(s.f) && s.pdf == 0.f && maxc3(s.dir) <= 0.f &&
+                           ref_min(ref_min(s.dir.x, s.dir.y), s.dir.z) >= 0.f;
+      o[7] = invalid ? 0.f : 1.f;
+    }
+  }
+}
+
+__global__ void k_camera_rays(ajg_camera cam, const float* __restrict__ raster,
+                              uint64_t n, float* __restrict__ rays) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const float* q = raster + 4 * i;
+    F3 o, d;
+    camera_ray(cam, q[0], q[1], q[2], q[3], o, d);
+    float* r = rays + 6 * i;
+    r[0] = o.x;
+    r[1] = o.y;
+    r[2] = o.z;
+    r[3] = d.x;
+    r[4] = d.y;
+    r[5] = d.z;
+  }
+}
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  cudaStream_t s = nullptr;
+  cudaError_t alloc(uint64_t count, cudaStream_t st) {
+    s = st;
+    return cudaMallocAsync((void**)&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16,
+                           st);
+  }
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+#define CK(expr, what)                            \
+  do {                                            \
+    cudaError_t e_ = (expr);                      \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int ajg_abi_version(void) { return AJG_ABI_VERSION; }
+
+const char* ajg_last_error(ajg_ctx* ctx) {
+  return ctx ? ctx->last_error.c_str() : g_error.c_str();
+}
+
+int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
+  if (!out) return fail(nullptr, AJG_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int dev = cfg ? cfg->device : 0;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0)
+    return fail(nullptr, AJG_ERR_CUDA, "no CUDA device available");
+  if (dev < 0 || dev >= count)
+    return fail(nullptr, AJG_ERR_INVALID, "device ordinal out of range");
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess) return fail(nullptr, AJG_ERR_CUDA, cudaGetErrorString(e));
+  auto* ctx = new ajg_ctx();
+  ctx->device = dev;
+  if (cfg && cfg->wave_paths) ctx->wave_paths = cfg->wave_paths;
+  if (ctx->wave_paths < 1024) ctx->wave_paths = 1024;
+  if (cfg) ctx->hbm_budget = cfg->hbm_budget_bytes;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) !=
+          cudaSuccess ||
+      cudaMalloc(&ctx->d_error, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_counters, 2 * sizeof(TraceCounters)) != cudaSuccess) {
+    delete ctx;
+    return fail(nullptr, AJG_ERR_CUDA, "context allocation failed");
+  }
+  cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
+  cudaMemset(ctx->d_counters, 0, 2 * sizeof(TraceCounters));
+  *out = ctx;
+  return AJG_OK;
+}
+
+int ajg_destroy_context(ajg_ctx* ctx) {
+  if (!ctx) return AJG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& b : ctx->arena) cudaFree(b.ptr);
+  cudaFree(ctx->d_error);
+  cudaFree(ctx->d_counters);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return AJG_OK;
+}
+
+int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset) {
+  if (!ctx || !out) return fail(ctx, AJG_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  TraceCounters c[2];
+  CK(cudaStreamSynchronize(ctx->stream), "stats");
+  CK(cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost),
+     "stats");
+  out->closest_rays = c[0].rays;
+  out->any_rays = c[1].rays;
+  out->closest_nodes = c[0].nodes;
+  out->closest_tris = c[0].tris;
+  out->any_nodes = c[1].nodes;
+  out->any_tris = c[1].tris;
+  out->nodes_visited = c[0].nodes + c[1].nodes;
+  out->tris_tested = c[0].tris + c[1].tris;
+  out->paths = ctx->paths_total;
+  if (reset) {
+    CK(cudaMemset(ctx->d_counters, 0, sizeof(c)), "stats");
+    ctx->paths_total = 0;
+  }
+  return AJG_OK;
+}
+
+int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
+                          const float* corner_normals,
+                          const int32_t* tri_material,
+                          const int32_t* tri_flags, uint64_t n,
+                          const float* world, const ajg_material* materials,
+                          uint32_t num_materials, const ajg_light* lights,
+                          uint32_t num_lights, const ajg_scene_opts* opts,
+                          ajg_scene** out) {
+  if (!ctx || !out) return fail(ctx, AJG_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (!tris || !tri_material || !tri_flags || !world || n == 0)
+    return fail(ctx, AJG_ERR_INVALID, "empty scene or NULL arrays");
+  if (!materials || num_materials == 0)
+    return fail(ctx, AJG_ERR_INVALID, "a scene needs at least one material");
+  if (num_lights > 15 || (num_lights && !lights))
+    return fail(ctx, AJG_ERR_UNSUPPORTED, "at most 15 lights");
+  ajg_scene_opts o{14, AJG_TRI_MOLLER_TRUMBORE, 0, 0};
+  if (opts) o = *opts;
+  if (o.tri_test > AJG_TRI_WATERTIGHT)
+    return fail(ctx, AJG_ERR_INVALID, "unknown triangle test");
+  for (uint64_t i = 0; i < n; ++i) {
+    if (tri_material[i] < 0 || (uint32_t)tri_material[i] >= num_materials)
+      return fail(ctx, AJG_ERR_INVALID, "triangle material index out of range");
+    if ((tri_flags[i] & AJG_MESH_HAS_NORMALS) && !corner_normals)
+      return fail(ctx, AJG_ERR_INVALID, "HAS_NORMALS without normals");
+    if (tri_flags[i] & ~7)
+      return fail(ctx, AJG_ERR_INVALID, "unknown triangle flag");
+  }
+  for (uint32_t m = 0; m < num_materials; ++m)
+    if (materials[m].type > AJG_MAT_DISNEY)
+      return fail(ctx, AJG_ERR_UNSUPPORTED, "unknown material type");
+  for (uint32_t l = 0; l < num_lights; ++l)
+    if (lights[l].type > AJG_LIGHT_ENV)
+      return fail(ctx, AJG_ERR_UNSUPPORTED, "unknown light type");
+  // admission by the HBM budget: resident scene bytes per triangle
+  const uint64_t est = n * (64 + 48 + 16 + 32 + 4 + 36) + (1u << 20);
+  if (ctx->hbm_budget && ctx->resident_bytes + est > ctx->hbm_budget)
+    return fail(ctx, AJG_ERR_OOM, "scene exceeds the HBM admission budget");
+
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  auto* s = new ajg_scene();
+  s->ctx = ctx;
+  // lights: records as given, env records get the two mass flags of the
+  // 1x1 Distribution2D (utility/distribution.h:40-60, 135-144)
+  s->host_lights.resize(12 * (size_t)num_lights);
+  int env = -1;
+  for (uint32_t l = 0; l < num_lights; ++l) {
+    float* r = &s->host_lights[12 * l];
+    std::memcpy(r, &lights[l], sizeof(ajg_light));
+    r[0] = (float)lights[l].type;
+    if (lights[l].type == AJG_LIGHT_ENV) {
+      env = (int)l;
+      const float w = host_lum(lights[l].rgb) * std::sin(kPi * (0 + 0.5f) / 1.f);
+      const float func_int = 0.f + w * (1.f / 1.f);
+      r[10] = func_int > 0.f ? 1.f : 0.f;
+      r[11] = func_int * func_int != 0.f ? 1.f : 0.f;
+    } else {
+      r[10] = r[11] = 0.f;
+    }
+  }
+  s->host_materials.resize(16 * (size_t)num_materials);
+  std::vector<float4> lum(num_materials);
+  for (uint32_t m = 0; m < num_materials; ++m) {
+    float* r = &s->host_materials[16 * m];
+    std::memcpy(r, &materials[m], sizeof(ajg_material));
+    r[0] = (float)materials[m].type;
+    lum[m] = make_float4(host_lum(materials[m].base_color), 0, 0, 0);
+  }
+  auto keep = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes > 0 ? bytes : 16) != cudaSuccess) return nullptr;
+    s->allocations.push_back(p);
+    s->info.device_bytes += bytes;
+    return p;
+  };
+  float* d_mat = (float*)keep(s->host_materials.size() * sizeof(float));
+  float* d_light = (float*)keep(std::max<size_t>(1, s->host_lights.size()) *
+                                sizeof(float));
+  float4* d_lum = (float4*)keep(num_materials * sizeof(float4));
+  if (!d_mat || !d_light || !d_lum) {
+    ajg_scene_release(s);
+    return fail(ctx, AJG_ERR_OOM, "device allocation failed (scene tables)");
+  }
+  cudaMemcpy(d_mat, s->host_materials.data(),
+             s->host_materials.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (num_lights)
+    cudaMemcpy(d_light, s->host_lights.data(),
+               s->host_lights.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(d_lum, lum.data(), num_materials * sizeof(float4),
+             cudaMemcpyHostToDevice);
+  s->d.materials = d_mat;
+  s->d.lights = d_light;
+  s->d.mat_lum = d_lum;
+  s->d.num_materials = num_materials;
+  s->d.num_lights = num_lights;
+  s->d.env = env;
+  int rc = build_scene(ctx, s, tris, corner_normals, tri_material, tri_flags,
+                       n, world, o);
+  if (rc != AJG_OK) {
+    std::string m = ctx->last_error;
+    ajg_scene_release(s);
+    ctx->last_error = m;
+    return rc;
+  }
+  ctx->resident_bytes += s->info.device_bytes;
+  *out = s;
+  return AJG_OK;
+}
+
+int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
+                     uint32_t num_meshes, const ajg_material* materials,
+                     uint32_t num_materials, const ajg_light* lights,
+                     uint32_t num_lights, const ajg_scene_opts* opts,
+                     ajg_scene** out) {
+  if (!ctx || !out || (!meshes && num_meshes))
+    return fail(ctx, AJG_ERR_INVALID, "NULL argument");
+  uint64_t n = 0;
+  bool any_normals = false;
+  for (uint32_t m = 0; m < num_meshes; ++m) {
+    const ajg_mesh_desc& d = meshes[m];
+    if (d.num_triangles && (!d.positions || !d.indices))
+      return fail(ctx, AJG_ERR_INVALID, "mesh without positions or indices");
+    if ((d.flags & AJG_MESH_HAS_NORMALS) && !d.normals)
+      return fail(ctx, AJG_ERR_INVALID, "HAS_NORMALS without normals");
+    n += d.num_triangles;
+    any_normals |= (d.flags & AJG_MESH_HAS_NORMALS) != 0;
+  }
+  std::vector<float> tris(9 * n), cn(any_normals ? 9 * n : 0);
+  std::vector<int32_t> mat(n), flags(n);
+  // world = Join of the primitives' AABBs (default_scene.cpp:32-39), each
+  // primitive's AABB spanning all of its vertices (mesh.cpp:71-74)
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  uint64_t t = 0;
+  for (uint32_t m = 0; m < num_meshes; ++m) {
+    const ajg_mesh_desc& d = meshes[m];
+    float plo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float phi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t v = 0; v < d.num_vertices; ++v)
+      for (int k = 0; k < 3; ++k) {
+        plo[k] = ref_min(plo[k], d.positions[3 * v + k]);
+        phi[k] = ref_max(phi[k], d.positions[3 * v + k]);
+      }
+    const bool lpoint = lo[0] == hi[0] && lo[1] == hi[1] && lo[2] == hi[2];
+    const bool ppoint = plo[0] == phi[0] && plo[1] == phi[1] && plo[2] == phi[2];
+    if (d.num_vertices) {
+      if (lpoint) {
+        std::memcpy(lo, plo, sizeof(lo));
+        std::memcpy(hi, phi, sizeof(hi));
+      } else if (!ppoint) {
+        for (int k = 0; k < 3; ++k) {
+          lo[k] = ref_min(lo[k], plo[k]);
+          hi[k] = ref_max(hi[k], phi[k]);
+        }
+      }
+    }
+    for (uint32_t i = 0; i < d.num_triangles; ++i, ++t) {
+      for (int c = 0; c < 3; ++c) {
+        const uint32_t vi = d.indices[3 * i + c];
+        if (vi >= d.num_vertices)
+          return fail(ctx, AJG_ERR_INVALID, "vertex index out of range");
+        std::memcpy(&tris[9 * t + 3 * c], d.positions + 3 * (uint64_t)vi,
+                    3 * sizeof(float));
+        if (d.flags & AJG_MESH_HAS_NORMALS)
+          std::memcpy(&cn[9 * t + 3 * c], d.normals + 3 * (uint64_t)vi,
+                      3 * sizeof(float));
+      }
+      mat[t] = (int32_t)d.material;
+      flags[t] = (int32_t)d.flags;
+    }
+  }
+  const float world[6] = {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+  return ajg_scene_create_flat(ctx, tris.data(), any_normals ? cn.data() : nullptr,
+                               mat.data(), flags.data(), n, world, materials,
+                               num_materials, lights, num_lights, opts, out);
+}
+
+int ajg_scene_release(ajg_scene* s) {
+  if (!s) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (void* p : s->allocations) cudaFree(p);
+  if (ctx->resident_bytes >= s->info.device_bytes)
+    ctx->resident_bytes -= s->info.device_bytes;
+  delete s;
+  return AJG_OK;
+}
+
+int ajg_scene_get_info(ajg_scene* s, ajg_scene_info* out) {
+  if (!s || !out) return AJG_ERR_INVALID;
+  *out = s->info;
+  return AJG_OK;
+}
+
+int ajg_scene_download_bvh(ajg_scene* s, float* node_bounds,
+                           int64_t* node_count_first, int64_t* perm) {
+  if (!s || !node_bounds || !node_count_first || !perm) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const uint64_t m = s->info.num_nodes, n = s->info.num_triangles;
+  std::vector<float4> nodes(2 * m);
+  std::vector<int32_t> p(n);
+  CK(cudaMemcpy(nodes.data(), s->ploc_nodes, 2 * m * sizeof(float4),
+                cudaMemcpyDeviceToHost),
+     "download_bvh");
+  CK(cudaMemcpy(p.data(), s->perm, n * sizeof(int32_t), cudaMemcpyDeviceToHost),
+     "download_bvh");
+  for (uint64_t i = 0; i < m; ++i) {
+    const float4 a = nodes[2 * i], b = nodes[2 * i + 1];
+    float* o = node_bounds + 6 * i;
+    o[0] = a.x; o[1] = a.y; o[2] = a.z;
+    o[3] = b.x; o[4] = b.y; o[5] = b.z;
+    int32_t first, count;
+    std::memcpy(&first, &a.w, 4);
+    std::memcpy(&count, &b.w, 4);
+    node_count_first[2 * i] = count;
+    node_count_first[2 * i + 1] = first;
+  }
+  for (uint64_t i = 0; i < n; ++i) perm[i] = p[i];
+  return AJG_OK;
+}
+
+static int trace_host(ajg_scene* s, const ajg_ray* rays, uint64_t n,
+                      void* out, bool any) {
+  if (!s || (n && (!rays || !out))) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  if (n == 0) return AJG_OK;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  DevBuf<ajg_ray> dr;
+  CK(dr.alloc(n, st), "trace: alloc");
+  CK(cudaMemcpyAsync(dr.p, rays, n * sizeof(ajg_ray), cudaMemcpyHostToDevice, st),
+     "trace: copy in");
+  if (any) {
+    DevBuf<uint8_t> dh;
+    CK(dh.alloc(n, st), "trace: alloc");
+    launch_trace_any(s->d, dr.p, n, dh.p, &ctx->d_counters[1], ctx->d_error, st);
+    CK(cudaMemcpyAsync(out, dh.p, n, cudaMemcpyDeviceToHost, st), "trace: copy out");
+  } else {
+    DevBuf<ajg_hit> dh;
+    CK(dh.alloc(n, st), "trace: alloc");
+    launch_trace_closest(s->d, dr.p, n, dh.p, &ctx->d_counters[0], ctx->d_error,
+                         st);
+    CK(cudaMemcpyAsync(out, dh.p, n * sizeof(ajg_hit), cudaMemcpyDeviceToHost, st),
+       "trace: copy out");
+  }
+  CK(cudaStreamSynchronize(st), "trace");
+  return check_device(ctx);
+}
+
+int ajg_trace_closest(ajg_scene* s, const ajg_ray* rays, uint64_t n,
+                      ajg_hit* hits) {
+  return trace_host(s, rays, n, hits, false);
+}
+
+int ajg_trace_any(ajg_scene* s, const ajg_ray* rays, uint64_t n,
+                  uint8_t* occluded) {
+  return trace_host(s, rays, n, occluded, true);
+}
+
+int ajg_trace_closest_device(ajg_scene* s, const ajg_ray* d_rays, uint64_t n,
+                             ajg_hit* d_hits, void* stream) {
+  if (!s || (n && (!d_rays || !d_hits))) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  StreamJoin j(ctx->stream, (cudaStream_t)stream);
+  launch_trace_closest(s->d, d_rays, n, d_hits, &ctx->d_counters[0],
+                       ctx->d_error, ctx->stream);
+  CK(cudaGetLastError(), "trace_closest_device");
+  return AJG_OK;
+}
+
+int ajg_trace_any_device(ajg_scene* s, const ajg_ray* d_rays, uint64_t n,
+                         uint8_t* d_occluded, void* stream) {
+  if (!s || (n && (!d_rays || !d_occluded))) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  StreamJoin j(ctx->stream, (cudaStream_t)stream);
+  launch_trace_any(s->d, d_rays, n, d_occluded, &ctx->d_counters[1],
+                   ctx->d_error, ctx->stream);
+  CK(cudaGetLastError(), "trace_any_device");
+  return AJG_OK;
+}
+
+int ajg_bsdf_query(ajg_ctx* ctx, const ajg_material* materials,
+                   const float* ng, const float* ns, const float* wo,
+                   const float* wi, const float* sam, const int32_t* op,
+                   uint64_t n, float* out) {
+  if (!ctx) return fail(nullptr, AJG_ERR_INVALID, "NULL context");
+  if (n && (!materials || !ng || !ns || !wo || !wi || !sam || !op || !out))
+    return fail(ctx, AJG_ERR_INVALID, "NULL array");
+  if (!n) return AJG_OK;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  DevBuf<ajg_material> dm;
+  DevBuf<float> dv, dout;
+  DevBuf<int32_t> dop;
+  CK(dm.alloc(n, st), "bsdf_query");
+  CK(dv.alloc(15 * n, st), "bsdf_query");
+  CK(dout.alloc(8 * n, st), "bsdf_query");
+  CK(dop.alloc(n, st), "bsdf_query");
+  cudaMemcpyAsync(dm.p, materials, n * sizeof(ajg_material), cudaMemcpyHostToDevice, st);
+  const float* srcs[5] = {ng, ns, wo, wi, sam};
+  for (int k = 0; k < 5; ++k)
+    cudaMemcpyAsync(dv.p + 3 * n * k, srcs[k], 3 * n * sizeof(float),
+                    cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dop.p, op, n * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+  k_bsdf_query<<<grid_for(n, 128), 128, 0, st>>>(
+      dm.p, dv.p, dv.p + 3 * n, dv.p + 6 * n, dv.p + 9 * n, dv.p + 12 * n,
+      dop.p, n, dout.p);
+  cudaMemcpyAsync(out, dout.p, 8 * n * sizeof(float), cudaMemcpyDeviceToHost, st);
+  CK(cudaStreamSynchronize(st), "bsdf_query");
+  return AJG_OK;
+}
+
+int ajg_camera_rays(ajg_ctx* ctx, const ajg_camera* cam, const float* raster,
+                    uint64_t n, float* rays) {
+  if (!ctx) return fail(nullptr, AJG_ERR_INVALID, "NULL context");
+  if (!cam || (n && (!raster || !rays)))
+    return fail(ctx, AJG_ERR_INVALID, "NULL argument");
+  if (!n) return AJG_OK;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  DevBuf<float> din, dout;
+  CK(din.alloc(4 * n, st), "camera_rays");
+  CK(dout.alloc(6 * n, st), "camera_rays");
+  cudaMemcpyAsync(din.p, raster, 4 * n * sizeof(float), cudaMemcpyHostToDevice, st);
+  k_camera_rays<<<grid_for(n, 128), 128, 0, st>>>(*cam, din.p, n, dout.p);
+  cudaMemcpyAsync(rays, dout.p, 6 * n * sizeof(float), cudaMemcpyDeviceToHost, st);
+  CK(cudaStreamSynchronize(st), "camera_rays");
+  return AJG_OK;
+}
+
+int ajg_render(ajg_scene* s, const ajg_camera* cam,
+               const ajg_render_params* params, float* out_rgbw) {
+  if (!s || !cam || !params || !out_rgbw) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const uint64_t npix = (uint64_t)cam->width * cam->height;
+  DevBuf<float4> d;
+  CK(d.alloc(npix, st), "render: alloc");
+  int rc = render_impl(s, *cam, *params, d.p, 0, 0, nullptr, st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out_rgbw, d.p, npix * sizeof(float4),
+                     cudaMemcpyDeviceToHost, st),
+     "render: copy out");
+  CK(cudaStreamSynchronize(st), "render");
+  return check_device(ctx);
+}
+
+int ajg_render_device(ajg_scene* s, const ajg_camera* cam,
+                      const ajg_render_params* params, float* d_out_rgbw,
+                      void* stream) {
+  if (!s || !cam || !params || !d_out_rgbw) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  StreamJoin j(ctx->stream, (cudaStream_t)stream);
+  int rc = render_impl(s, *cam, *params, reinterpret_cast<float4*>(d_out_rgbw),
+                       0, 0, nullptr, ctx->stream);
+  if (rc) return rc;
+  CK(cudaGetLastError(), "render_device");
+  return AJG_OK;
+}
+
+int ajg_render_samples(ajg_scene* s, const ajg_camera* cam,
+                       const ajg_render_params* params, uint64_t pixel_begin,
+                       uint64_t pixel_end, float* out_li) {
+  if (!s || !cam || !params || !out_li) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  const uint64_t npix = (uint64_t)cam->width * cam->height;
+  if (pixel_begin >= pixel_end || pixel_end > npix)
+    return fail(ctx, AJG_ERR_INVALID, "pixel range out of the film");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const uint64_t count = (pixel_end - pixel_begin) * params->spp * 3;
+  DevBuf<float> d;
+  CK(d.alloc(count, st), "render_samples: alloc");
+  int rc = render_impl(s, *cam, *params, nullptr, pixel_begin, pixel_end, d.p,
+                       st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out_li, d.p, count * sizeof(float), cudaMemcpyDeviceToHost,
+                     st),
+     "render_samples: copy out");
+  CK(cudaStreamSynchronize(st), "render_samples");
+  return check_device(ctx);
+}
+
+}  // extern "C"

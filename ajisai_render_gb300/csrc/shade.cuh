@@ -1,0 +1,581 @@
+// Device shading for the PT-MIS path: hit completion (PostIntersect rules),
+// the Lambertian AggregateBSDF and the Disney BSDF, directional and constant
+// environment lights, and the thin-lens camera.  Each function keeps the
+// reference's evaluation order (cited per function); transcendental
+// functions are CUDA's own (sinf, cosf, acosf, atan2f, tanf), so shading is
+// within a few ulp of the reference rather than bit-equal.
+#pragma once
+#include <cfloat>
+
+#include "common.cuh"
+#include "scene.cuh"
+
+namespace ajg {
+
+// libstdc++'s std::lerp for floats (C++20 <cmath>)
+__device__ __forceinline__ float std_lerp(float a, float b, float t) {
+  if ((a <= 0 && b >= 0) || (a >= 0 && b <= 0)) return t * b + (1 - t) * a;
+  if (t == 1) return b;
+  const float x = a + t * (b - a);
+  return (t > 1) == (b > a) ? (b < x ? x : b) : (b > x ? x : b);
+}
+// core/material/disney.cpp:48-52
+__device__ __forceinline__ float dlerp(float a, float b, float t) {
+  return a * (1 - t) + b * t;
+}
+__device__ __forceinline__ F3 dlerp(F3 a, F3 b, float t) {
+  return a * (1 - t) + b * t;
+}
+__device__ __forceinline__ float clampf(float v, float lo, float hi) {
+  return v < lo ? lo : (hi < v ? hi : v);
+}
+
+// CoordinateSystem (core/coordinate_system.h:37-52)
+struct Frame {
+  F3 dx, dy, dz;
+  __device__ __forceinline__ explicit Frame(F3 n) : dz(n) {
+    const float sign = copysignf(1.f, n.z);
+    const float a = -1.f / (sign + n.z);
+    const float b = n.x * n.y * a;
+    dx = mk3(1.f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    dy = mk3(b, sign + n.y * n.y * a, -n.y);
+  }
+  __device__ __forceinline__ F3 to_local(F3 v) const {
+    return mk3(dot3(v, dx), dot3(v, dy), dot3(v, dz));
+  }
+  __device__ __forceinline__ F3 to_world(F3 v) const {
+    return dx * v.x + dy * v.y + dz * v.z;
+  }
+};
+
+// core/warp.h:29-72
+__device__ __forceinline__ void concentric(float sx, float sy, float& px,
+                                           float& py) {
+  const float ox = 2.f * sx - 1.f, oy = 2.f * sy - 1.f;
+  float r, phi;
+  if (ox == 0 && oy == 0) {
+    px = 0.f;
+    py = 0.f;
+    return;
+  } else if (fabsf(ox) > fabsf(oy)) {
+    r = ox;
+    phi = kPi4 * (oy / ox);
+  } else {
+    r = oy;
+    phi = kPi2 - kPi4 * (ox / oy);
+  }
+  px = r * cosf(phi);
+  py = r * sinf(phi);
+}
+__device__ __forceinline__ F3 cosine_hemisphere(float sx, float sy,
+                                                float* pdf) {
+  float px, py;
+  concentric(sx, sy, px, py);
+  float r = 0.f;
+  r += px * px;
+  r += py * py;
+  float z = sqrtf(ref_max(0.0f, 1 - r));
+  if (z == 0) z = 1e-10f;
+  if (pdf) *pdf = z * kInvPi;
+  return mk3(px, py, z);
+}
+// core/warp.h:74-80, 100-104
+__device__ __forceinline__ F3 uniform_cone(float u0, float u1, float cmax) {
+  const float ct = (1.f - u0) + u0 * cmax;
+  const float st = sqrtf(ref_max(0.f, 1.f - ct * ct));
+  const float phi = u1 * 2 * kPi;
+  return mk3(cosf(phi) * st, sinf(phi) * st, ct);
+}
+__device__ __forceinline__ float uniform_cone_pdf(float cmax) {
+  if (cmax == 1.0f) return 1.0f;
+  return 1.0f / (2.0f * kPi * (1.0f - cmax));
+}
+// core/bsdf/bsdf.h:42-46
+__device__ __forceinline__ float correct_shading_normal(F3 ng, F3 ns, F3 wi) {
+  const float denom = fabsf(dot3(ng, wi));
+  return denom == 0 ? 1.f : fabsf(dot3(ns, wi) / denom);
+}
+
+struct BsdfSample {
+  F3 dir, f;
+  float pdf;
+};
+__device__ __forceinline__ BsdfSample invalid_sample() {
+  BsdfSample s;
+  s.dir = mk3(0, 0, 0);
+  s.f = mk3(0, 0, 0);
+  s.pdf = 0.f;
+  return s;
+}
+
+struct MatParams {
+  int type;
+  F3 base;
+  float subsurface, metallic, specular, specular_tint, roughness, sheen,
+      sheen_tint, clearcoat, clearcoat_gloss, lum;
+};
+__device__ __forceinline__ MatParams load_material(const float* m,
+                                                   float lum) {
+  MatParams p;
+  p.type = (int)m[0];
+  p.base = mk3(m[1], m[2], m[3]);
+  p.subsurface = m[4];
+  p.metallic = m[5];
+  p.specular = m[6];
+  p.specular_tint = m[7];
+  p.roughness = m[8];
+  p.sheen = m[10];
+  p.sheen_tint = m[11];
+  p.clearcoat = m[12];
+  p.clearcoat_gloss = m[13];
+  p.lum = lum;
+  return p;
+}
+
+// ----------------------------------------------------------- Lambertian --
+// Diffuse::Shade -> AggregateBSDF{DiffuseComponent, weight 1}
+// (core/material/diffuse.cpp:35-48, core/bsdf/aggregate_bsdf.cpp:43-131,
+// core/bsdf/diffuse_component.cpp:28-64, core/bsdf/bsdf.cpp:30-63)
+struct Lambert {
+  F3 ng, ns, albedo, coef;
+  __device__ __forceinline__ Lambert(F3 ng_, F3 ns_, F3 alb)
+      : ng(ng_), ns(ns_), albedo(alb), coef(alb / kPi) {}
+  __device__ __forceinline__ bool fringes(F3 w) const {
+    return (dot3(ng, w) > 0) != (dot3(ns, w) > 0);
+  }
+  __device__ BsdfSample sample(F3 wo, F3 sam) const {
+    if (fringes(wo)) {
+      if (dot3(ng, wo) <= 0.f) return invalid_sample();
+      float pdf;
+      const F3 lwi = cosine_hemisphere(sam.x, sam.y, &pdf);
+      if (pdf < FLT_EPSILON) return invalid_sample();
+      const F3 wi = normalize3(Frame(ng).to_world(lwi));
+      const float factor = correct_shading_normal(ng, ns, wi);
+      BsdfSample s;
+      s.dir = wi;
+      s.f = albedo / kPi * factor;
+      s.pdf = pdf;
+      return s;
+    }
+    const Frame sf(ns);
+    const F3 lwo = normalize3(sf.to_local(wo));
+    if (lwo.z <= 0.f) return invalid_sample();
+    float pdf;
+    F3 lwi = cosine_hemisphere(sam.y, sam.z, &pdf);
+    if ((double)pdf < 1e-3) return invalid_sample();
+    lwi = normalize3(lwi);
+    pdf *= 1.f;
+    const F3 wi = sf.to_world(lwi);
+    const float factor = correct_shading_normal(ng, ns, wi);
+    BsdfSample s;
+    s.dir = wi;
+    s.f = coef * factor;
+    s.pdf = pdf;
+    return s;
+  }
+  __device__ F3 eval(F3 wi, F3 wo) const {
+    if (fringes(wo)) {
+      if ((dot3(ng, wi) <= 0.f) || (dot3(ng, wo) <= 0.f)) return mk3(0, 0, 0);
+      return albedo / kPi;
+    }
+    const Frame sf(ns);
+    const F3 lwi = normalize3(sf.to_local(wi));
+    const F3 lwo = normalize3(sf.to_local(wo));
+    if (lwi.z <= 0.f || lwo.z <= 0.f) return mk3(0, 0, 0);
+    return mk3(0, 0, 0) + coef;
+  }
+  __device__ float pdf(F3 wi, F3 wo) const {
+    if (fringes(wo)) {
+      if ((dot3(ng, wi) > 0.f) != (dot3(ng, wo) > 0.f)) return 0.f;
+      const F3 local = normalize3(Frame(ng).to_local(wi));
+      return local.z * kInvPi;
+    }
+    const Frame sf(ns);
+    const F3 lwi = normalize3(sf.to_local(wi));
+    const F3 lwo = normalize3(sf.to_local(wo));
+    if (lwi.z <= 0.f || lwo.z <= 0.f) return 0.f;
+    float wsum = 0.f, p = 0.f;
+    wsum += 1.f;
+    p += 1.f * (lwi.z * kInvPi);
+    return wsum > 0 ? p / wsum : 0;
+  }
+};
+
+// --------------------------------------------------------------- Disney --
+// DisneyBSDF (core/material/disney.cpp:58-473)
+struct DisneyB {
+  const MatParams& m;
+  Frame sf;
+  __device__ __forceinline__ DisneyB(const MatParams& mat, F3 ns)
+      : m(mat), sf(ns) {}
+
+  __device__ static float tan_theta(F3 v) {
+    const float temp = 1 - v.z * v.z;
+    if (temp <= 0.0f) return 0.0f;
+    return sqrtf(temp) / v.z;
+  }
+  __device__ static float tan2(F3 v) {
+    const float tmp = 1.f - v.z * v.z;
+    if (tmp <= 0.f) return 0.f;
+    return tmp / (v.z * v.z);
+  }
+  __device__ static F3 reflect(F3 vi, F3 n) {
+    return vi + (2 * dot3(-vi, n) * n);
+  }
+  __device__ static float ggx_d(F3 wh, float alpha) {
+    if (wh.z <= 0.f) return 0.f;
+    const float t2 = tan2(wh);
+    const float c2 = wh.z * wh.z;
+    const float root = alpha / (c2 * (alpha * alpha + t2));
+    return kInvPi * (root * root);
+  }
+  __device__ static float smith_g(F3 v, F3 wh, float alpha) {
+    const float tt = fabsf(tan_theta(v));
+    if (tt == 0.0f) return 1.0f;
+    if (dot3(v, wh) * v.z <= 0) return 0.0f;
+    const float root = alpha * tt;
+    return 2.0f / (1.0f + sqrtf(1.0f + root * root));
+  }
+  __device__ static float ggx_g(F3 wi, F3 wo, F3 wh, float alpha) {
+    return smith_g(wo, wh, alpha) * smith_g(wi, wh, alpha);
+  }
+  __device__ static float pdf_vn(F3 wi, F3 h, float alpha) {
+    const float D = ggx_d(h, alpha);
+    return smith_g(wi, h, alpha) * fabsf(dot3(wi, h)) * D /
+           (fabsf(wi.z) + 1e-4f);
+  }
+  __device__ static void vn_unit(float thetaI, float u1, float u2, float& sx,
+                                 float& sy) {
+    if (thetaI < 1e-4f) {
+      const float R = sqrtf(ref_max(u1 / ((1 - u1) + 1e-6f), 0.0f));
+      const float SinPhi = sinf(2 * kPi * u2);
+      const float CosPhi = cosf(2 * kPi * u2);
+      sx = R * CosPhi;
+      sy = R * SinPhi;
+      return;
+    }
+    const float TanThetaI = tanf(thetaI);
+    const float a = 1 / TanThetaI;
+    const float G1 = 2.0f / (1.0f + sqrtf(ref_max(1.0f + 1.0f / (a * a), 0.0f)));
+    float A = 2.0f * u1 / G1 - 1.0f;
+    if (fabsf(A) == 1) A -= (A >= 0.0f ? 1.0f : -1.0f) * 1e-4f;
+    const float Temp = 1.0f / (A * A - 1.0f);
+    const float B = TanThetaI;
+    const float D =
+        sqrtf(ref_max(B * B * Temp * Temp - (A * A - B * B) * Temp, 0.0f));
+    const float x1 = B * Temp - D;
+    const float x2 = B * Temp + D;
+    sx = (A < 0.0f || x2 > 1.0f / TanThetaI) ? x1 : x2;
+    float S;
+    if (u2 > 0.5f) {
+      S = 1.0f;
+      u2 = 2.0f * (u2 - 0.5f);
+    } else {
+      S = -1.0f;
+      u2 = 2.0f * (0.5f - u2);
+    }
+    // the published rational fit of the slope distribution, in double as
+    // written (disney.cpp:400-407)
+    const double d2 = u2;
+    const float z =
+        (float)((d2 * (d2 * (d2 * (-0.365728915865723) + 0.790235037209296) -
+                       0.424965825137544) +
+                 0.000152998850436920) /
+                (d2 * (d2 * (d2 * (d2 * 0.169507819808272 - 0.397203533833404) -
+                             0.232500544458471) +
+                       1) -
+                 0.539825872510702));
+    sy = S * z * sqrtf(1.0f + sx * sx);
+  }
+  __device__ static F3 sample_vn(F3 wi_in, float u1, float u2, float Alpha) {
+    const F3 wi = normalize3(mk3(Alpha * wi_in.x, Alpha * wi_in.y, wi_in.z));
+    float Theta = 0, Phi = 0;
+    if (wi.z < 0.99999f) {
+      Theta = acosf(wi.z);
+      Phi = atan2f(wi.y, wi.x);
+    }
+    const float SinPhi = sinf(Phi), CosPhi = cosf(Phi);
+    float sx, sy;
+    vn_unit(Theta, u1, u2, sx, sy);
+    float rx = CosPhi * sx - SinPhi * sy;
+    float ry = SinPhi * sx + CosPhi * sy;
+    rx *= Alpha;
+    ry *= Alpha;
+    const float Norm = 1.f / sqrtf(rx * rx + ry * ry + 1.0f);
+    return mk3(-rx * Norm, -ry * Norm, Norm);
+  }
+  __device__ float fresnel_conductor(float cosi, float eta, float k) const {
+    const float tmp = (eta * eta + k * k) * cosi * cosi;
+    const float Rparl2 =
+        (tmp - (2.f * eta * cosi) + 1) / (tmp + (2.f * eta * cosi) + 1);
+    const float tmp_f = eta * eta + k * k;
+    const float Rperp2 = (tmp_f - (2.f * eta * cosi) + cosi * cosi) /
+                         (tmp_f + (2.f * eta * cosi) + cosi * cosi);
+    return 0.5f * (Rparl2 + Rperp2);
+  }
+  __device__ float fresnel_schlick(float cosD, float R0) const {
+    const float omc = 1.f - cosD;
+    const float omc2 = omc * omc;
+    const float fr = R0 + (1.f - R0) * omc2 * omc2 * omc;
+    const float fc = fresnel_conductor(cosD, 0.4f, 1.6f);
+    return std_lerp(fr, fc, m.metallic);
+  }
+  __device__ static float fresnel_coat(float cosD) {
+    const float omc = 1.0f - cosD;
+    const float omc2 = omc * omc;
+    return 0.04f + (1.0f - 0.04f) * omc2 * omc2 * omc;
+  }
+  __device__ float diffuse_term(F3 wi, F3 wo, float idh, float rough) const {
+    if (m.metallic == 1.f) return 0.f;
+    const float l = 1.f - fabsf(wi.z), l2 = l * l;
+    const float v = 1.f - fabsf(wo.z), v2 = v * v;
+    const float FD90 = 0.5f + 2.f * idh * rough;
+    return kInvPi * (1.f + (FD90 - 1.f) * l2 * l2 * l) *
+           (1.f + (FD90 - 1.f) * v2 * v2 * v);
+  }
+  __device__ float specular_term(F3 wi, F3 wo, F3 wh, float odh,
+                                 float rough) const {
+    if (wi.z * wo.z <= 0.f) return 0.f;
+    const float D = ggx_d(wh, rough * rough);
+    if (D == 0.f) return 0.f;
+    const float nr = std_lerp(0.f, 0.08f, m.specular);
+    const float F = fresnel_schlick(odh, nr);
+    const float rg = (0.5f + 0.5f * rough);
+    const float G = ggx_g(wi, wo, wh, rg * rg);
+    return F * D * G / (4.f * fabsf(wi.z) * fabsf(wo.z));
+  }
+  __device__ float subsurface_term(F3 wi, F3 wo, float idh,
+                                   float rough) const {
+    if (m.subsurface == 0.0f) return 0.0f;
+    const float l = 1.0f - fabsf(wi.z), l2 = l * l;
+    const float v = 1.0f - fabsf(wo.z), v2 = v * v;
+    const float F = idh * idh * rough;
+    const float S = (1.0f + (F - 1.0f) * l2 * l2 * l) *
+                    (1.0f + (F - 1.0f) * v2 * v2 * v);
+    return kInvPi * 1.25f *
+           (S * (1.0f / (fabsf(wo.z) + fabsf(wi.z)) - 0.5f) + 0.5f);
+  }
+  __device__ float clearcoat_term(F3 wi, F3 wo, F3 wh, float idh,
+                                  float gloss) const {
+    if (m.clearcoat == 0.0f) return 0.0f;
+    const float rough = dlerp(0.005f, 0.1f, gloss);
+    const float D = ggx_d(wh, rough);
+    if (D == 0.0f) return 0.0f;
+    const float F = fresnel_coat(idh);
+    const float G = ggx_g(wo, wi, wh, 0.25f);
+    return m.clearcoat * D * F * G / (4.0f * fabsf(wi.z) * fabsf(wo.z));
+  }
+  __device__ F3 eval(F3 wi, F3 wo) const {
+    const F3 lwi = normalize3(sf.to_local(wi));
+    const F3 lwo = normalize3(sf.to_local(wo));
+    if (fabsf(lwi.z) < FLT_EPSILON || fabsf(lwo.z) < FLT_EPSILON)
+      return mk3(0, 0, 0);
+    const float rough = clampf(m.roughness, 0.02f, 1.f);
+    const F3 untinted = mk3(m.lum, m.lum, m.lum);
+    F3 spec_alb = dlerp(dlerp(m.base, untinted, 1.0f - m.specular_tint),
+                        m.base, m.metallic);
+    const F3 sheen_alb = dlerp(untinted, m.base, m.sheen_tint);
+    const F3 wh = normalize3(lwo + lwi);
+    const float odh = dot3(lwo, wh);
+    const float idh = dot3(lwi, wh);
+    const float omo = 1.f - odh;
+    spec_alb = dlerp(spec_alb, untinted, omo * omo * omo);
+    const float F = fresnel_schlick(odh, 0.0f);
+    const F3 sheen_term = F * m.sheen * sheen_alb;
+    const float dl = dlerp(diffuse_term(lwi, lwo, idh, rough),
+                           subsurface_term(lwi, lwo, idh, rough), m.subsurface);
+    const F3 t1 = (1.0f - m.metallic) * (m.base * dl + sheen_term);
+    const F3 t2 = spec_alb * specular_term(lwi, lwo, wh, odh, rough);
+    const float cc = clearcoat_term(lwi, lwo, wh, idh, m.clearcoat_gloss);
+    return t1 + t2 + mk3(cc, cc, cc);
+  }
+  __device__ float pdf(F3 wi, F3 wo) const {
+    const F3 lwi = normalize3(sf.to_local(wi));
+    const F3 lwo = normalize3(sf.to_local(wo));
+    const F3 wh = normalize3(lwo + lwi);
+    if (maxc3(wh) <= 0.f) return 0.f;
+    const float rough = clampf(m.roughness, 0.02f, 1.f);
+    const float mpdf = pdf_vn(lwo, wh, rough * rough);
+    float p = 0.f;
+    const float dwhdwi = 1.f / (4.f * fabsf(dot3(lwi, wh)));
+    const float spec_pdf = mpdf * dwhdwi;
+    const float nr = std_lerp(0.f, 0.08f, m.specular);
+    const float odh = dot3(lwo, wh);
+    const float ps = fresnel_schlick(odh, nr);
+    p += spec_pdf * ps;
+    p += fabsf(lwi.z) * kInvPi * (1.f - ps);
+    if (m.clearcoat > 0.f) {
+      // the clearcoat lobe reads the world-space wo (disney.cpp:208-220)
+      const float cw = m.clearcoat / (m.clearcoat + m.lum);
+      const float fc = fresnel_coat(fabsf(wo.z));
+      const float pc = (fc * cw) / (fc * cw + (1 - fc) * (1 - cw));
+      const float cr = std_lerp(0.005f, 0.10f, m.clearcoat_gloss);
+      const float chp = pdf_vn(wo, wh, cr);
+      const float cp = chp * dwhdwi;
+      p *= 1.0f - pc;
+      p += cp * pc;
+    }
+    return p;
+  }
+  __device__ BsdfSample sample(F3 wo, F3 sam) const {
+    const F3 lwo = normalize3(sf.to_local(wo));
+    F3 lwi, lwh;
+    bool coat = false;
+    float r0 = sam.x, r1 = sam.y;
+    const float r2 = sam.z;
+    if (m.clearcoat > 0.f) {
+      const float cw = m.clearcoat / (m.clearcoat + m.lum);
+      const float fc = fresnel_coat(fabsf(lwo.z));
+      const float pc = (fc * cw) / (fc * cw + (1.f - fc) * (1.f - cw));
+      if (sam.y < pc) {
+        coat = true;
+        r1 /= pc;
+        const float cr = std_lerp(0.005f, 0.1f, m.clearcoat_gloss);
+        lwh = sample_vn(lwo, r0, r1, cr);
+        lwi = reflect(-lwo, lwh);
+      } else {
+        r1 = (sam.y - pc) / (1.f - pc);
+      }
+    }
+    if (!coat) {
+      const float rough = clampf(m.roughness, 0.02f, 1.0f);
+      lwh = sample_vn(lwo, r0, r1, rough * rough);
+      const float nr = std_lerp(0.0f, 0.08f, m.specular);
+      const float odh = dot3(lwo, lwh);
+      const float ps = fresnel_schlick(odh, nr);
+      if (r2 <= ps) {
+        lwi = reflect(-lwo, lwh);
+      } else {
+        lwi = cosine_hemisphere(r0, r1, nullptr);
+        if (lwo.z < 0.0f) lwi.z *= -1.0f;
+      }
+    }
+    if (lwi.z <= 0.0f) return invalid_sample();
+    BsdfSample s;
+    s.dir = sf.to_world(lwi);
+    s.f = eval(s.dir, wo);
+    s.pdf = pdf(s.dir, wo);
+    return s;
+  }
+};
+
+struct Bsdf {
+  int type;
+  F3 ng, ns;
+  MatParams m;
+  __device__ __forceinline__ BsdfSample sample(F3 wo, F3 s) const {
+    if (type == AJG_MAT_DIFFUSE) return Lambert(ng, ns, m.base).sample(wo, s);
+    return DisneyB(m, ns).sample(wo, s);
+  }
+  __device__ __forceinline__ F3 eval(F3 wi, F3 wo) const {
+    if (type == AJG_MAT_DIFFUSE) return Lambert(ng, ns, m.base).eval(wi, wo);
+    return DisneyB(m, ns).eval(wi, wo);
+  }
+  __device__ __forceinline__ float pdf(F3 wi, F3 wo) const {
+    if (type == AJG_MAT_DIFFUSE) return Lambert(ng, ns, m.base).pdf(wi, wo);
+    return DisneyB(m, ns).pdf(wi, wo);
+  }
+};
+
+// ------------------------------------------------------------ hit record --
+struct HitInfo {
+  F3 pos, ng, ns, wr;
+  uint32_t mat;
+};
+
+// Triangle::Intersect's normal and the primitive's PostIntersect
+// (core/geometry/quad.cpp:73-90, cube.cpp:96-108, mesh.cpp:183-204,
+// two_sided.cpp:44-53): pos = o + t d, wr = -d.
+__device__ __forceinline__ HitInfo complete_hit(const DeviceScene& s, F3 o,
+                                                F3 d, float t, float u,
+                                                float v, int prim) {
+  HitInfo h;
+  const float4 sh = __ldg(s.shade + prim);
+  const uint32_t w = __float_as_uint(sh.w);
+  const uint32_t fl = w >> 24;
+  h.pos = o + t * d;
+  h.ng = mk3(sh.x, sh.y, sh.z);
+  if (fl & AJG_MESH_HAS_NORMALS) {
+    const float* cn = s.corner + 9 * (uint64_t)prim;
+    h.ns = (1 - u - v) * ld3(cn) + u * ld3(cn + 3) + v * ld3(cn + 6);
+  } else {
+    h.ns = h.ng;
+  }
+  h.wr = -d;
+  if (fl & AJG_MESH_TWO_SIDED) {
+    if (dot3(h.ng, h.wr) < 0) {
+      h.ng = h.ng * -1.f;
+      h.ns = h.ns * -1.f;
+    }
+  }
+  h.mat = w & 0xffffffu;
+  return h;
+}
+
+// intersection.h:42-47
+__device__ __forceinline__ F3 eps_offset(const HitInfo& h, F3 dir) {
+  if (dot3(dir, h.ng) > 0.f) return h.pos + h.ng * kRayEps;
+  return h.pos - h.ng * kRayEps;
+}
+// renderer/helper.h:38-42
+__device__ __forceinline__ float power_heuristic(float a, float b) {
+  a *= a;
+  b *= b;
+  return a / (a + b);
+}
+
+// The Ray constructor (ray.h:33-39).
+__device__ __forceinline__ void make_ray(F3 o, F3 d, F3& ro, F3& rd) {
+  const F3 dn = normalize3(d);
+  ro = o + dn * kRayEps;
+  rd = normalize3(d);
+}
+
+// EnvLight::Pdf for a 1x1 texture (env_light.cpp:152-170): the 2D
+// distribution's density is 1 when the texel has luminance.
+__device__ __forceinline__ float env_pdf(bool env_has_mass, F3 ref2light) {
+  const F3 d = normalize3(ref2light);
+  const float theta = acosf(clampf(d.y, -1.f, 1.f));
+  const float st = sinf(theta);
+  const float p2 = env_has_mass ? 1.f : 0.f;
+  return p2 / (2.f * kPi * kPi * st);
+}
+
+// ----------------------------------------------------------------- camera --
+__device__ __forceinline__ void mat_vec(const float* M, const float v[4],
+                                        float out[4]) {
+#pragma unroll
+  for (int row = 0; row < 4; ++row) {
+    float o = 0.f;
+#pragma unroll
+    for (int pos = 0; pos < 4; ++pos) o += M[pos * 4 + row] * v[pos];
+    out[row] = o;
+  }
+}
+// ThinLensCamera::GenerateRay (thin_lens.cpp:62-83), then the Ray ctor.
+__device__ __forceinline__ void camera_ray(const ajg_camera& cam, float rx,
+                                           float ry, float lx, float ly,
+                                           F3& ro, F3& rd) {
+  float p[4] = {rx, ry, 1.f, 1.f}, q[4];
+  mat_vec(cam.raster2camera, p, q);
+  const F3 cc = mk3(q[0], q[1], q[2]) / q[3];
+  F3 o = mk3(0.f, 0.f, 0.f);
+  F3 d = normalize3(cc);
+  if (cam.lens_radius > 0 && cam.focal_distance > 0) {
+    float px, py;
+    concentric(lx, ly, px, py);
+    const float lxp = px * cam.lens_radius, lyp = py * cam.lens_radius;
+    const float ft = cam.focal_distance / d.z;
+    const F3 focus = o + ft * d;
+    o = mk3(lxp, lyp, 0.f);
+    d = normalize3(focus - o);
+  }
+  float po[4] = {o.x, o.y, o.z, 1.f}, wo[4];
+  mat_vec(cam.camera2world, po, wo);
+  const F3 wpo = mk3(wo[0], wo[1], wo[2]) / wo[3];
+  float pd[4] = {d.x, d.y, d.z, 0.f}, wd[4];
+  mat_vec(cam.camera2world, pd, wd);
+  make_ray(wpo, mk3(wd[0], wd[1], wd[2]), ro, rd);
+}
+
+}  // namespace ajg

@@ -1,0 +1,251 @@
+// BVH2 traversal for closest-hit and any-hit queries.
+//
+// Results are defined independently of the tree shape and of the visiting
+// order: the closest hit is the minimum t over every triangle the test
+// accepts, ties in t going to the lowest primitive index, and the node test
+// never culls a box that can hold such a hit -- it is the reference's slab
+// test, (bound - o) * inv_dir (ploc_aggregate.cpp:154-162), with the far
+// distance widened by 1 + 2*gamma(3) (Pharr, Jakob, Humphreys, PBRT 3rd ed.,
+// 3.9.2) and inclusive comparisons against the current best t.  Children are
+// visited nearest first; leaf children are tested as soon as their box
+// passes.  The per-thread stack lives in registers/local memory and is
+// guarded: overflow sets the device error word and ends the ray.
+#pragma once
+#include "scene.cuh"
+
+namespace ajg {
+
+constexpr int kStackSize = 96;
+constexpr float kSlabWiden = 1.0000003576278687f;  // 1 + 2*gamma(3)
+
+struct Hit {
+  float t, u, v;
+  int prim;
+};
+
+struct RayQ {
+  F3 o, d, inv;
+  float tmin, tmax;
+};
+
+// Triangle::Intersect / Occlude's Moller-Trumbore test
+// (ploc_aggregate.cpp:184-242), with the reference's absolute determinant
+// cull and open (t_min, t_max) interval.
+__device__ __forceinline__ bool mt_test(const RayQ& r, float4 A, float4 B,
+                                        float4 Cv, float& t_out, float& u_out,
+                                        float& v_out) {
+  const F3 v0 = xyz(A), v1 = xyz(B), v2 = xyz(Cv);
+  const F3 e0 = v1 - v0, e1 = v2 - v0;
+  const F3 h = cross3(r.d, e1);
+  const float a = dot3f(e0, h);
+  if (a > -1e-6f && a < 1e-6f) return false;
+  const float f = 1.f / a;
+  const F3 s = r.o - v0;
+  const float u = f * dot3f(s, h);
+  if (u < 0.f || u > 1.f) return false;
+  const F3 q = cross3(s, e0);
+  const float v = f * dot3f(r.d, q);
+  if (v < 0.f || u + v > 1.f) return false;
+  const float t = f * dot3f(e1, q);
+  if (!(t > r.tmin && t < r.tmax)) return false;
+  t_out = t;
+  u_out = u;
+  v_out = v;
+  return true;
+}
+
+// Watertight test (Woop, Benthin, Wald, JCGT 2(1), 2013), no double
+// fallback; barycentrics reported for b and c as Moller-Trumbore does.
+struct WtSetup {
+  int kx, ky, kz;
+  float sx, sy, sz;
+};
+__device__ __forceinline__ WtSetup wt_setup(const RayQ& r) {
+  WtSetup w;
+  const float ax = fabsf(r.d.x), ay = fabsf(r.d.y), az = fabsf(r.d.z);
+  int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  int kx = kz + 1 == 3 ? 0 : kz + 1;
+  int ky = kx + 1 == 3 ? 0 : kx + 1;
+  const float d[3] = {r.d.x, r.d.y, r.d.z};
+  if (d[kz] < 0.f) {
+    int t = kx;
+    kx = ky;
+    ky = t;
+  }
+  w.kx = kx;
+  w.ky = ky;
+  w.kz = kz;
+  w.sx = d[kx] / d[kz];
+  w.sy = d[ky] / d[kz];
+  w.sz = 1.f / d[kz];
+  return w;
+}
+__device__ __forceinline__ float comp(F3 v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : v.z);
+}
+__device__ __forceinline__ bool wt_test(const RayQ& r, const WtSetup& w,
+                                        float4 A4, float4 B4, float4 C4,
+                                        float& t_out, float& u_out,
+                                        float& v_out) {
+  const F3 A = xyz(A4) - r.o, B = xyz(B4) - r.o, C = xyz(C4) - r.o;
+  const float Az0 = comp(A, w.kz), Bz0 = comp(B, w.kz), Cz0 = comp(C, w.kz);
+  const float Ax = comp(A, w.kx) - w.sx * Az0, Ay = comp(A, w.ky) - w.sy * Az0;
+  const float Bx = comp(B, w.kx) - w.sx * Bz0, By = comp(B, w.ky) - w.sy * Bz0;
+  const float Cx = comp(C, w.kx) - w.sx * Cz0, Cy = comp(C, w.ky) - w.sy * Cz0;
+  const float U = Cx * By - Cy * Bx;
+  const float V = Ax * Cy - Ay * Cx;
+  const float W = Bx * Ay - By * Ax;
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f))
+    return false;
+  const float det = U + V + W;
+  if (det == 0.f) return false;
+  const float T = U * (w.sz * Az0) + V * (w.sz * Bz0) + W * (w.sz * Cz0);
+  const float rcp = 1.f / det;
+  const float t = T * rcp;
+  if (!(t > r.tmin && t < r.tmax)) return false;
+  t_out = t;
+  u_out = V * rcp;
+  v_out = W * rcp;
+  return true;
+}
+
+__device__ __forceinline__ bool slab2(float lox, float hix, float loy,
+                                      float hiy, float loz, float hiz,
+                                      const RayQ& r, float lim, float& tn) {
+  const float tx0 = (lox - r.o.x) * r.inv.x, tx1 = (hix - r.o.x) * r.inv.x;
+  const float ty0 = (loy - r.o.y) * r.inv.y, ty1 = (hiy - r.o.y) * r.inv.y;
+  const float tz0 = (loz - r.o.z) * r.inv.z, tz1 = (hiz - r.o.z) * r.inv.z;
+  tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+  tf = tf * kSlabWiden;
+  return tn <= tf && tn <= lim && tf >= r.tmin;
+}
+
+__device__ __forceinline__ RayQ make_query(F3 o, F3 d, float tmin,
+                                           float tmax) {
+  RayQ r;
+  r.o = o;
+  r.d = d;
+  r.inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  r.tmin = tmin;
+  r.tmax = tmax;
+  return r;
+}
+
+// TEST: AJG_TRI_*; ANY: occlusion query (returns at the first hit).
+template <int TEST, bool ANY>
+__device__ __forceinline__ bool traverse(const DeviceScene& s, const RayQ& r,
+                                         Hit& hit, uint32_t& n_nodes,
+                                         uint32_t& n_tris, uint32_t* err) {
+  WtSetup w;
+  if (TEST == AJG_TRI_WATERTIGHT) w = wt_setup(r);
+  hit.t = __int_as_float(0x7f800000);  // +inf
+  hit.prim = -1;
+  hit.u = hit.v = 0.f;
+  int stack_node[kStackSize];
+  float stack_t[kStackSize];
+  int sp = 0;
+  int node = 0;
+  const float4* __restrict__ bvh = s.bvh;
+  const float4* __restrict__ tris = s.tris;
+  for (;;) {
+    ++n_nodes;
+    const float4 n0 = __ldg(bvh + 4 * node + 0);
+    const float4 n1 = __ldg(bvh + 4 * node + 1);
+    const float4 n2 = __ldg(bvh + 4 * node + 2);
+    const float4 n3 = __ldg(bvh + 4 * node + 3);
+    const float lim = ANY ? r.tmax : fminf(hit.t, r.tmax);
+    float tn0, tn1;
+    bool h0 = slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
+    bool h1 = slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
+    const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const bool hc = c == 0 ? h0 : h1;
+      const int rc = c == 0 ? r0 : r1;
+      if (hc && rc < 0) {
+        const int slot = ~rc;
+        ++n_tris;
+        const float4 A = __ldg(tris + 3 * slot + 0);
+        const float4 B = __ldg(tris + 3 * slot + 1);
+        const float4 C = __ldg(tris + 3 * slot + 2);
+        float t, u, v;
+        const bool ok = TEST == AJG_TRI_WATERTIGHT
+                            ? wt_test(r, w, A, B, C, t, u, v)
+                            : mt_test(r, A, B, C, t, u, v);
+        if (ok) {
+          const int prim = __float_as_int(A.w);
+          if (ANY) {
+            hit.t = t;
+            hit.u = u;
+            hit.v = v;
+            hit.prim = prim;
+            return true;
+          }
+          if (t < hit.t || (t == hit.t && prim < hit.prim)) {
+            hit.t = t;
+            hit.u = u;
+            hit.v = v;
+            hit.prim = prim;
+          }
+        }
+        if (c == 0)
+          h0 = false;
+        else
+          h1 = false;
+      }
+    }
+    if (h0 && h1) {
+      const bool first0 = tn0 <= tn1;
+      if (sp >= kStackSize) {
+        raise_device_error(err, kDevStackOverflow);
+        return hit.prim >= 0;
+      }
+      stack_node[sp] = first0 ? r1 : r0;
+      stack_t[sp] = first0 ? tn1 : tn0;
+      ++sp;
+      node = first0 ? r0 : r1;
+      continue;
+    }
+    if (h0) {
+      node = r0;
+      continue;
+    }
+    if (h1) {
+      node = r1;
+      continue;
+    }
+    // pop, skipping boxes a closer hit has since excluded
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      const float lim2 = ANY ? r.tmax : fminf(hit.t, r.tmax);
+      if (stack_t[sp] <= lim2) {
+        node = stack_node[sp];
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+  }
+  return hit.prim >= 0;
+}
+
+__device__ __forceinline__ void flush_counters(TraceCounters* c, uint32_t rays,
+                                               uint32_t nodes, uint32_t tris) {
+  if (!c) return;
+  unsigned long long a = rays, b = nodes, t = tris;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&c->rays, a);
+    atomicAdd(&c->nodes, b);
+    atomicAdd(&c->tris, t);
+  }
+}
+
+}  // namespace ajg

@@ -1,0 +1,260 @@
+/*
+ * ajisai_gpu: GB300 (sm_103a) wavefront path tracer for Ajisai's PT-MIS
+ * path over a PLOC BVH.  Plain C ABI: plain pointers and sizes, int status
+ * returns, no exceptions and no CUDA or torch types across the boundary.
+ *
+ * What each entry point replaces in the reference (siyuanpan/ajisai_render):
+ *
+ *   ajg_scene_create*    PLOCAggregate::Build      core/aggregate/ploc_aggregate.cpp:252-327
+ *                        + DefaultScene ctor       core/scene/default_scene.cpp:31-61
+ *   ajg_trace_closest    Aggregate::Intersect      core/aggregate/aggregate.h:36-37
+ *                        (PLOCAggregate::Intersect ploc_aggregate.cpp:329-335,367-391)
+ *   ajg_trace_any        Aggregate::Occlude        core/aggregate/aggregate.h:39
+ *                        (PLOCAggregate::Occlude   ploc_aggregate.cpp:337-365)
+ *   ajg_camera_rays      Camera::GenerateRay       core/camera/camera.h:38-39
+ *                        (ThinLensCamera           core/camera/thin_lens.cpp:62-83)
+ *   ajg_bsdf_query       BSDF::SampleAll/EvalAll/PdfAll after Material::Shade
+ *                                                  core/bsdf/bsdf.h:80-96, core/material/material.h:32-38
+ *   ajg_render*          Renderer::Render          core/renderer/renderer.h:53-59
+ *                        (TiledIntegrator::Render  core/renderer/pt.cpp:40-73 with
+ *                         PathTracing::TraceMIS/Trace pt.cpp:98-311)
+ *   ajg_submit/poll/...  (no counterpart: the request loop that keeps scenes
+ *                         resident and batches jobs on one GPU)
+ *
+ * Ownership: the caller owns every host array it passes and may free it when
+ * the call returns; the library owns its device copies.  A scene is
+ * immutable after creation and may be traced and rendered concurrently from
+ * several host threads of one context (calls on one context serialise on an
+ * internal mutex).  Errors: every call returns AJG_OK or an AJG_ERR_* code
+ * and leaves a message for ajg_last_error().
+ */
+#ifndef AJISAI_GPU_H
+#define AJISAI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AJG_API __attribute__((visibility("default")))
+#define AJG_ABI_VERSION 1
+
+enum ajg_status {
+  AJG_OK = 0,
+  AJG_ERR_INVALID = 1,     /* bad argument or scene description */
+  AJG_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  AJG_ERR_OOM = 3,         /* device allocation or HBM budget exceeded */
+  AJG_ERR_UNSUPPORTED = 4, /* valid input the library does not implement */
+  AJG_ERR_DEVICE = 5,      /* a kernel's own guard tripped (stack depth,
+                              queue capacity, iteration bound); the context
+                              stays usable */
+  AJG_ERR_NOT_FOUND = 6,   /* unknown job id */
+  AJG_ERR_CANCELLED = 7
+};
+
+/* Per-triangle PostIntersect rules, one set per mesh. */
+enum {
+  AJG_MESH_TWO_SIDED = 1,   /* TwoSided (core/geometry/two_sided.cpp:44-53) */
+  AJG_MESH_NG_REVERSED = 2, /* Cube: normal from (c,b,a) (core/geometry/cube.cpp:96-108) */
+  AJG_MESH_HAS_NORMALS = 4  /* MeshGeo shading normals (core/geometry/mesh.cpp:183-204) */
+};
+enum { AJG_MAT_DIFFUSE = 0, AJG_MAT_DISNEY = 1 };
+enum { AJG_LIGHT_DIRECTIONAL = 0, AJG_LIGHT_ENV = 1 };
+enum { AJG_TRI_MOLLER_TRUMBORE = 0, AJG_TRI_WATERTIGHT = 1 };
+
+typedef struct ajg_ctx ajg_ctx;
+typedef struct ajg_scene ajg_scene;
+
+typedef struct ajg_config {
+  int32_t device;            /* CUDA device ordinal */
+  uint32_t wave_paths;       /* paths in flight per wave (0: default 4 Mi) */
+  uint64_t hbm_budget_bytes; /* admission budget for resident scenes and
+                                films (0: no limit) */
+} ajg_config;
+
+/* One triangle mesh as the reference's PLOC aggregate gathers it: the
+ * triangles of every mesh in order, each in MeshView index order
+ * (ploc_aggregate.cpp:259-285).  Global primitive index = position in that
+ * concatenation. */
+typedef struct ajg_mesh_desc {
+  const float* positions;  /* [num_vertices][3] */
+  const float* normals;    /* [num_vertices][3], read with HAS_NORMALS */
+  const uint32_t* indices; /* [num_triangles][3] */
+  uint32_t num_vertices;
+  uint32_t num_triangles;
+  uint32_t material;       /* index into the material array */
+  uint32_t flags;          /* AJG_MESH_* */
+} ajg_mesh_desc;
+
+/* Constant-texture material (Diffuse: base_color is the albedo). */
+typedef struct ajg_material {
+  uint32_t type; /* AJG_MAT_* */
+  float base_color[3];
+  float subsurface, metallic, specular, specular_tint, roughness,
+      anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss;
+  float pad[2];
+} ajg_material; /* 64 bytes, the [16]-float record of the flat layout */
+
+/* Lights in scene order (YAML order; default_scene.cpp:41-48). */
+typedef struct ajg_light {
+  uint32_t type;       /* AJG_LIGHT_* */
+  float rgb[3];        /* directional radiance, or the env texel */
+  float direction[3];  /* directional: toward the light (YAML `direction`) */
+  float cos_angle;     /* directional: cos of the cone half-angle */
+  float scaler;        /* env: radiance scale */
+  float rot_deg;       /* env: rotation about y */
+  float pad[2];
+} ajg_light; /* 48 bytes */
+
+typedef struct ajg_scene_opts {
+  uint32_t search_radius; /* PLOC neighbour radius (reference default 14) */
+  uint32_t tri_test;      /* AJG_TRI_*; Moller-Trumbore matches the reference */
+  uint32_t radix_compat;  /* 1: reproduce the reference's Morton radix sort,
+                             including its stale digit-0 offset
+                             (ploc_aggregate.cpp:97-130), so the tree is the
+                             reference's own; 0: correct stable sort */
+  uint32_t reserved;
+} ajg_scene_opts;
+
+/* Thin-lens camera: the two matrices ThinLensCamera keeps
+ * (thin_lens.cpp:40-54), column-major, plus lens and film size. */
+typedef struct ajg_camera {
+  float raster2camera[16];
+  float camera2world[16];
+  float lens_radius;
+  float focal_distance;
+  uint32_t width;
+  uint32_t height;
+} ajg_camera;
+
+/* PTRendererArgs (renderer.h:37-45) plus the counter-sampler seed. */
+typedef struct ajg_render_params {
+  uint32_t spp;
+  int32_t min_bounces;
+  int32_t max_bounces;
+  float cont_prob;
+  uint32_t use_mis;
+  uint32_t flags;  /* AJG_RENDER_* */
+  uint64_t seed;
+} ajg_render_params;
+
+enum {
+  AJG_RENDER_FP64_FILM = 1,      /* accumulate the film in FP64 (oracle
+                                    renders and error references) */
+  AJG_RENDER_DROP_NONFINITE = 2  /* leave samples whose radiance is NaN or
+                                    inf out of the film (radiance and
+                                    weight).  Off by default: the reference
+                                    keeps them -- its Disney pdf is 0 for a
+                                    half vector with no positive component
+                                    (disney.cpp:190-191) while the path
+                                    continues on pdf == 0 (pt.cpp:217) */
+};
+
+typedef struct ajg_ray {
+  float o[3], d[3];
+  float t_min, t_max;
+} ajg_ray; /* the Ray's fields after its constructor (ray.h:28-45) */
+
+typedef struct ajg_hit {
+  float t, u, v; /* u, v: Moller-Trumbore barycentrics of b and c */
+  int32_t prim;  /* global primitive index, -1 on a miss */
+} ajg_hit;
+
+typedef struct ajg_scene_info {
+  uint64_t num_triangles;
+  uint64_t num_nodes;      /* 2n-1 PLOC nodes */
+  uint64_t device_bytes;   /* resident bytes of the scene */
+  uint32_t ploc_iterations;
+  float build_ms;          /* GPU time of the last PLOC build */
+} ajg_scene_info;
+
+typedef struct ajg_stats {
+  uint64_t closest_rays, any_rays;
+  uint64_t nodes_visited, tris_tested; /* summed over both ray kinds */
+  uint64_t closest_nodes, closest_tris, any_nodes, any_tris;
+  uint64_t paths;
+} ajg_stats;
+
+/* ---- context --------------------------------------------------------- */
+AJG_API int ajg_abi_version(void);
+AJG_API int ajg_create_context(const ajg_config* cfg, ajg_ctx** out);
+AJG_API int ajg_destroy_context(ajg_ctx* ctx);
+AJG_API const char* ajg_last_error(ajg_ctx* ctx);
+AJG_API int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset);
+
+/* ---- scenes (PLOCAggregate::Build + DefaultScene) --------------------- */
+AJG_API int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
+                             uint32_t num_meshes,
+                             const ajg_material* materials,
+                             uint32_t num_materials, const ajg_light* lights,
+                             uint32_t num_lights, const ajg_scene_opts* opts,
+                             ajg_scene** out);
+/* The same from the flat per-triangle layout: tris [n][9] (a,b,c),
+ * corner_normals [n][9] (read where flags has HAS_NORMALS, may be NULL),
+ * tri_material [n], tri_flags [n], world [6] = Join of the primitives'
+ * AABBs (lo, hi). */
+AJG_API int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
+                                  const float* corner_normals,
+                                  const int32_t* tri_material,
+                                  const int32_t* tri_flags, uint64_t n,
+                                  const float* world,
+                                  const ajg_material* materials,
+                                  uint32_t num_materials,
+                                  const ajg_light* lights, uint32_t num_lights,
+                                  const ajg_scene_opts* opts, ajg_scene** out);
+AJG_API int ajg_scene_release(ajg_scene* scene);
+AJG_API int ajg_scene_get_info(ajg_scene* scene, ajg_scene_info* out);
+/* The built tree in the reference's layout (ploc_aggregate.cpp:146-152):
+ * node_bounds [2n-1][6], node_count_first [2n-1][2], perm [n]. */
+AJG_API int ajg_scene_download_bvh(ajg_scene* scene, float* node_bounds,
+                                   int64_t* node_count_first, int64_t* perm);
+
+/* ---- ray queries (Aggregate::Intersect / Occlude) ---------------------- */
+/* Host arrays.  Closest hit: ties in t go to the lowest primitive index. */
+AJG_API int ajg_trace_closest(ajg_scene* scene, const ajg_ray* rays,
+                              uint64_t n, ajg_hit* hits);
+AJG_API int ajg_trace_any(ajg_scene* scene, const ajg_ray* rays, uint64_t n,
+                          uint8_t* occluded);
+/* Device arrays, asynchronous on `stream` (a cudaStream_t, or NULL). */
+AJG_API int ajg_trace_closest_device(ajg_scene* scene, const ajg_ray* d_rays,
+                                     uint64_t n, ajg_hit* d_hits,
+                                     void* stream);
+AJG_API int ajg_trace_any_device(ajg_scene* scene, const ajg_ray* d_rays,
+                                 uint64_t n, uint8_t* d_occluded, void* stream);
+
+/* ---- shading and camera queries (golden-vector entry points) ---------- */
+/* n queries; op[i] 0: eval+pdf of (wi, wo), 1: sample(wo, sam).
+ * ng, ns, wo, wi, sam: [n][3]; out [n][8]: f rgb, pdf, wi xyz, valid. */
+AJG_API int ajg_bsdf_query(ajg_ctx* ctx, const ajg_material* materials,
+                           const float* ng, const float* ns, const float* wo,
+                           const float* wi, const float* sam,
+                           const int32_t* op, uint64_t n, float* out);
+/* raster [n][4] (x, y, lens u, lens v) -> rays [n][6] (o, d) after the Ray
+ * constructor. */
+AJG_API int ajg_camera_rays(ajg_ctx* ctx, const ajg_camera* cam,
+                            const float* raster, uint64_t n, float* rays);
+
+/* ---- rendering (Renderer::Render) -------------------------------------- */
+/* Blocking.  out_rgbw: host [height][width][4] = (sum of radiance, sum of
+ * weights) per pixel in the reference's film convention: each sample lands
+ * on the 2x2 box footprint (x-1..x, y-1..y) with row/column -1 folded into 0
+ * (film.cpp:27-63, film.h:119-129, image.h:38-42).  image = rgb / w. */
+AJG_API int ajg_render(ajg_scene* scene, const ajg_camera* cam,
+                       const ajg_render_params* params, float* out_rgbw);
+/* Same into device memory (float [h][w][4]), asynchronous on `stream`. */
+AJG_API int ajg_render_device(ajg_scene* scene, const ajg_camera* cam,
+                              const ajg_render_params* params,
+                              float* d_out_rgbw, void* stream);
+/* Per-sample radiance of pixels [pixel_begin, pixel_end): host
+ * out_li [count][spp][3], for parity checks on small renders. */
+AJG_API int ajg_render_samples(ajg_scene* scene, const ajg_camera* cam,
+                               const ajg_render_params* params,
+                               uint64_t pixel_begin, uint64_t pixel_end,
+                               float* out_li);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AJISAI_GPU_H */

@@ -1,0 +1,71 @@
+"""The C-ABI library builds, loads and exports every entry point the header
+declares; host-side argument checks work without a GPU.  CPU only."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from ajisai_render_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "ajisai_gpu.h").read_text()
+    return sorted(set(re.findall(r"AJG_API\s+[\w\s\*]+?\b(ajg_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_symbols()
+    for n in ("ajg_create_context", "ajg_scene_create", "ajg_trace_closest",
+              "ajg_trace_any", "ajg_render", "ajg_bsdf_query", "ajg_last_error"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for n in declared_symbols():
+        assert hasattr(lib, n), n
+
+
+def test_exports_nothing_else():
+    import subprocess
+    from ajisai_render_gb300 import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.LIB_PATH)],
+                         capture_output=True, text=True).stdout
+    exported = sorted({l.split()[-1] for l in out.splitlines() if " T " in l})
+    assert exported == declared_symbols()
+
+
+def test_struct_layouts_match_header(lib):
+    from ajisai_render_gb300 import _lib
+    assert C.sizeof(_lib.Material) == 64
+    assert C.sizeof(_lib.Light) == 48
+    assert C.sizeof(_lib.Camera) == 144
+    assert C.sizeof(_lib.MeshDesc) == 40
+    assert C.sizeof(_lib.RenderParams) == 32
+
+
+def test_null_arguments_are_rejected_without_a_gpu(lib):
+    assert lib.ajg_abi_version() == 1
+    assert lib.ajg_create_context(None, None) == 1          # AJG_ERR_INVALID
+    assert b"NULL" in lib.ajg_last_error(None)
+    assert lib.ajg_trace_closest(None, None, 0, None) == 1
+    assert lib.ajg_render(None, None, None, None) == 1
+    assert lib.ajg_scene_release(None) == 1
+
+
+def test_context_creation_reports_missing_device(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    rc = lib.ajg_create_context(None, C.byref(h))
+    assert rc == 2 and not h.value                            # AJG_ERR_CUDA
+    assert lib.ajg_last_error(None)

@@ -1,0 +1,334 @@
+"""GPU parity through the C ABI: PLOC trees, ray hits, BSDF values, camera
+rays and renders against the reference's golden vectors and the oracle."""
+import numpy as np
+import pytest
+
+from ajisai_render_gb300 import api
+from ajisai_render_gb300 import scenes as S
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = api.Context(0)
+    yield c
+    c.close()
+
+
+def geometry_scene(ctx, tris, world, radius=14, tri_test=0, compat=False):
+    tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
+    n = tris.shape[0]
+    flat = S.FlatScene(tris, np.zeros((n, 9), np.float32), np.zeros(n, np.int32),
+                       np.zeros(n, np.int32), np.asarray(world, np.float32),
+                       S.Diffuse((0.5, 0.5, 0.5)).pack()[None],
+                       np.zeros((0, 12), np.float32), None)
+    return api.GpuScene(ctx, flat, api.CreatePLOCAggregate(radius, tri_test, compat))
+
+
+def same_bits(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+
+# ------------------------------------------------------------------ PLOC --
+@pytest.mark.parametrize("case", ["ploc_cornell.npz", "ploc_ico4.npz",
+                                  "ploc_soup.npz", "ploc_flat.npz"])
+def test_ploc_reference_tree_bit_exact(ctx, golden, case):
+    """radix_compat: the GPU builds the reference's own tree, node for node."""
+    g = golden(case)
+    sc = geometry_scene(ctx, g["tris"], g["world"], int(g["radius"]), compat=True)
+    nb, ncf, perm = sc.download_bvh()
+    assert np.array_equal(perm, g["perm"])
+    assert np.array_equal(ncf, g["node_count_first"])
+    assert same_bits(nb, g["node_bounds"])
+
+
+@pytest.mark.parametrize("case", ["ploc_cornell.npz", "ploc_ico4.npz",
+                                  "ploc_soup.npz", "ploc_flat.npz"])
+def test_ploc_default_matches_oracle(ctx, golden, case):
+    g = golden(case)
+    sc = geometry_scene(ctx, g["tris"], g["world"], int(g["radius"]))
+    nb, ncf, perm = sc.download_bvh()
+    onb, oncf, operm = O.ploc_build(g["tris"], g["world"], int(g["radius"]))
+    assert np.array_equal(perm, operm)
+    assert np.array_equal(ncf, oncf)
+    assert same_bits(nb, onb)
+
+
+def test_ploc_large_matches_oracle(ctx):
+    """327,680 triangles (icosphere subdivision 7), radius 16."""
+    fl = S.flatten(S.icosphere_scene(subdiv=7, seed=2, width=8, height=8))
+    sc = geometry_scene(ctx, fl.tris, fl.world, 16)
+    nb, ncf, perm = sc.download_bvh()
+    onb, oncf, operm = O.ploc_build(fl.tris, fl.world, 16)
+    assert np.array_equal(perm, operm)
+    assert np.array_equal(ncf, oncf)
+    assert same_bits(nb, onb)
+
+
+def check_tree_properties(nb, ncf, perm, n):
+    assert np.array_equal(np.sort(perm), np.arange(n))
+    leaf = ncf[:, 0] == 1
+    assert leaf.sum() == n and np.array_equal(np.sort(ncf[leaf, 1]), np.arange(n))
+    inner = np.where(~leaf)[0]
+    assert inner.size == n - 1
+    c = ncf[inner, 1]
+    for ch in (c, c + 1):
+        solid = ~np.all(nb[ch, :3] == nb[ch, 3:], axis=1)
+        assert np.all(nb[inner[solid], :3] <= nb[ch[solid], :3])
+        assert np.all(nb[inner[solid], 3:] >= nb[ch[solid], 3:])
+    # every node but the root is some node's child, exactly once
+    kids = np.concatenate([c, c + 1])
+    assert np.array_equal(np.sort(kids), np.arange(1, 2 * n - 1))
+
+
+def test_ploc_full_size_properties(ctx):
+    """The single-job workload's 1,310,722 triangles: a valid PLOC tree."""
+    fl = S.flatten(S.icosphere_scene(subdiv=8, seed=0, width=8, height=8))
+    sc = geometry_scene(ctx, fl.tris, fl.world, 16)
+    nb, ncf, perm = sc.download_bvh()
+    check_tree_properties(nb, ncf, perm, fl.n_tris)
+    info = sc.info()
+    assert info["num_triangles"] == fl.n_tris and info["ploc_iterations"] > 0
+
+
+def test_single_and_two_triangle_scenes(ctx):
+    t1 = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    sc = geometry_scene(ctx, t1, [0, 0, 0, 1, 1, 0])
+    rays = np.array([[0.2, 0.2, 1, 0, 0, -1, 1e-4, np.inf],
+                     [2, 2, 1, 0, 0, -1, 1e-4, np.inf]], np.float32)
+    t, p, u, v = sc.Intersect(rays)
+    assert list(p) == [0, -1] and t[0] == np.float32(1.0)
+    assert list(sc.Occlude(rays)) == [True, False]
+    t2 = np.concatenate([t1, t1 + np.float32(2.0)])
+    sc2 = geometry_scene(ctx, t2, [0, 0, 0, 3, 3, 2])
+    t, p, _, _ = sc2.Intersect(rays)
+    assert list(p) == [0, -1]
+
+
+def test_reference_sort_overflow_is_refused(ctx):
+    """Two triangles whose Morton digits make the reference's sort write past
+    its arrays: the compatible build refuses instead of corrupting memory."""
+    quad = S.flatten(S.Scene([S.Quad((-1, -1, 0), (1, -1, 0), (1, 1, 0), (-1, 1, 0))],
+                             [S.Diffuse((0.5, 0.5, 0.5))], [], None))
+    try:
+        O.ploc_build(quad.tris, quad.world, 14, radix_compat=True)
+        overflow = False
+    except RuntimeError:
+        overflow = True
+    if not overflow:
+        pytest.skip("this input does not overflow the reference's sort")
+    from ajisai_render_gb300._lib import AjgError
+    with pytest.raises(AjgError) as e:
+        geometry_scene(ctx, quad.tris, quad.world, compat=True)
+    assert e.value.code == 1
+    # the default build handles it
+    sc = geometry_scene(ctx, quad.tris, quad.world)
+    assert sc.info()["num_triangles"] == 2
+
+
+# ----------------------------------------------------------------- trace --
+@pytest.mark.parametrize("case", ["trace_ico4.npz", "trace_soup.npz"])
+def test_closest_hit_matches_reference(ctx, golden, case):
+    g = golden(case)
+    sc = geometry_scene(ctx, g["tris"], g["world"], int(g["radius"]), compat=True)
+    t, p, u, v = sc.Intersect(g["rays"])
+    hit = g["prim"] >= 0
+    assert np.array_equal(p, g["prim"])
+    assert same_bits(t[hit], g["t"][hit])
+    assert same_bits(u[hit], g["u"][hit]) and same_bits(v[hit], g["v"][hit])
+    occ = sc.Occlude(g["rays"])
+    assert np.array_equal(occ, g["occluded"] == 1)
+
+
+def random_rays(rng, n, spread=2.0):
+    o = rng.uniform(-spread, spread, (n, 3))
+    d = rng.uniform(-1, 1, (n, 3)) - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tmax = np.where(rng.uniform(size=n) < 0.3, rng.uniform(0.2, 3, n), np.inf)
+    return np.concatenate([o, d, np.full((n, 1), 1e-4), tmax[:, None]], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("tri_test", [0, 1])
+def test_closest_and_any_match_oracle_large(ctx, tri_test):
+    rng = np.random.default_rng(5)
+    fl = S.flatten(S.icosphere_scene(subdiv=6, seed=4, width=8, height=8))
+    sc = geometry_scene(ctx, fl.tris, fl.world, 16, tri_test=tri_test)
+    rays = random_rays(rng, 200_000)
+    t, p, u, v = sc.Intersect(rays)
+    bvh = O.ploc_build(fl.tris, fl.world, 16)
+    ot, op, ou, ov = O.trace(fl.tris, rays, bvh=bvh, tri_test=tri_test)
+    assert np.array_equal(p, op)
+    hit = op >= 0
+    assert hit.mean() > 0.3
+    assert same_bits(t[hit], ot[hit]) and same_bits(u[hit], ou[hit])
+    assert same_bits(v[hit], ov[hit])
+    occ = sc.Occlude(rays)
+    _, oocc, _, _ = O.trace(fl.tris, rays, any_hit=True, bvh=bvh, tri_test=tri_test)
+    assert np.array_equal(occ, oocc == 1)
+    # brute force over every triangle agrees on a subsample
+    sub = rays[:1500]
+    bt, bp, _, _ = O.trace(fl.tris, sub, bvh=None, tri_test=tri_test)
+    assert np.array_equal(p[:1500], bp)
+
+
+def test_axis_aligned_and_degenerate_rays(ctx):
+    fl = S.flatten(S.cornell_box(8, 8))
+    sc = geometry_scene(ctx, fl.tris, fl.world)
+    rays = np.array([
+        [0, 0, 0, 1, 0, 0, 1e-4, np.inf],        # axis aligned
+        [0, 0, 0, 0, -1, 0, 1e-4, np.inf],
+        [0.5, 0, 0, 1, 0, 0, 1e-4, np.inf],      # origin on a wall plane
+        [0, 0, 0, 0, 0, 1, 1e-4, np.inf],        # out through the open front
+        [0, 0, 0, 1, 0, 0, 2.0, 1.0],            # empty interval
+        [0, 0, 0, 0.6, 0.8, 0, 1e-4, 0.1],       # short ray
+    ], np.float32)
+    t, p, u, v = sc.Intersect(rays)
+    bvh = O.ploc_build(fl.tris, fl.world, 14)
+    ot, op, _, _ = O.trace(fl.tris, rays, bvh=bvh)
+    bt, bp, _, _ = O.trace(fl.tris, rays, bvh=None)
+    assert np.array_equal(p, op) and np.array_equal(p, bp)
+    assert p[4] == -1 and p[5] == -1 and p[3] == -1
+
+
+def test_empty_batch(ctx):
+    fl = S.flatten(S.cornell_box(8, 8))
+    sc = geometry_scene(ctx, fl.tris, fl.world)
+    t, p, u, v = sc.Intersect(np.zeros((0, 8), np.float32))
+    assert p.size == 0
+
+
+# ------------------------------------------------------------------ BSDF --
+def test_bsdf_eval_pdf_matches_reference(ctx, golden):
+    """EvalAll / PdfAll within the stated 1e-5 relative bar."""
+    g = golden("bsdf.npz")
+    e = g["op"] == 0
+    out = ctx.bsdf_query(g["material"][e], g["ng"][e], g["ns"][e], g["wo"][e],
+                         g["wi"][e], g["sam"][e], g["op"][e])
+    np.testing.assert_allclose(out[:, :4], g["out"][e][:, :4], rtol=1e-5, atol=1e-30)
+
+
+def test_bsdf_sample_matches_reference(ctx, golden):
+    """SampleAll: the same validity and the sampled direction within 2e-5
+    (sampling goes through CUDA's acos/atan2/sin/cos/tan).  Lambertian f and
+    pdf within 1e-5; Disney f and pdf within 1e-5 once evaluated at the
+    reference's direction (Disney's Sample returns EvalAll/PdfAll there,
+    disney.cpp:141-145; the Lambertian sample carries the shading-normal
+    factor instead, aggregate_bsdf.cpp:81-87)."""
+    g = golden("bsdf.npz")
+    s = g["op"] == 1
+    args = [g[k][s] for k in ("material", "ng", "ns", "wo", "wi", "sam")]
+    out = ctx.bsdf_query(*args, g["op"][s])
+    ref = g["out"][s]
+    assert np.array_equal(out[:, 7], ref[:, 7])
+    ok = ref[:, 7] == 1
+    np.testing.assert_allclose(out[ok, 4:7], ref[ok, 4:7], rtol=0, atol=2e-5)
+    lam = ok & (args[0][:, 0] == 0)
+    dis = ok & (args[0][:, 0] == 1)
+    np.testing.assert_allclose(out[lam, :4], ref[lam, :4], rtol=1e-5, atol=1e-30)
+    ev = ctx.bsdf_query(args[0][dis], args[1][dis], args[2][dis], args[3][dis],
+                        ref[dis, 4:7], args[5][dis], np.zeros(dis.sum(), np.int32))
+    np.testing.assert_allclose(ev[:, :4], ref[dis, :4], rtol=1e-5, atol=1e-30)
+    close = np.isclose(out[dis, :4], ref[dis, :4], rtol=1e-5, atol=1e-30).all(1)
+    assert close.mean() > 0.98
+
+
+# ---------------------------------------------------------------- camera --
+def test_camera_rays_match_reference(ctx, golden):
+    g = golden("camera.npz")
+    pin = ctx.camera_rays(g["pinhole_camera"], g["pinhole_raster"])
+    assert same_bits(pin, g["pinhole_rays"])  # no transcendental: bit-exact
+    lens = ctx.camera_rays(g["lens_camera"], g["lens_raster"])
+    np.testing.assert_allclose(lens, g["lens_rays"], rtol=2e-6, atol=2e-7)
+
+
+# ---------------------------------------------------------------- render --
+def flat_of(g):
+    return S.FlatScene(g["tris"], g["corner_n"], g["tri_mat"], g["tri_flags"],
+                       g["world"], g["materials"], g["lights"], g["camera"])
+
+
+def params_of(g):
+    p = g["params"]
+    return api.PTRendererArgs(spp=int(p[0]), min_bounces=int(p[1]),
+                              max_bounces=int(p[2]), cont_prob=float(p[3]),
+                              use_mis=bool(p[4]))
+
+
+@pytest.mark.parametrize("case", ["render_cornell.npz", "render_ico.npz",
+                                  "render_cornell_nomis.npz"])
+def test_render_per_sample_matches_reference(ctx, golden, case):
+    """Shared counter sampler: each sample's radiance equals the reference's
+    within float32 tolerance, apart from rare paths that a last-ulp
+    difference of CUDA's transcendentals sends another way."""
+    g = golden(case)
+    flat = flat_of(g)
+    sc = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, 0, True))
+    r = api.PTRenderer(params_of(g), seed=int(g["seed"]))
+    li = r.RenderSamples(sc, flat.camera)
+    ref = g["li"]
+    close = np.isclose(li, ref, rtol=1e-4, atol=1e-6).all(axis=-1)
+    assert close.mean() > 0.99, close.mean()
+    # per-pixel means agree within 3 sigma of the sample spread
+    H, W = g["film"].shape[:2]
+    spp = ref.shape[1]
+    m_gpu, m_ref = li.mean(1), ref.mean(1)
+    sigma = np.maximum(ref.std(1), 1e-3) / np.sqrt(spp)
+    within = (np.abs(m_gpu - m_ref) <= 3 * sigma + 1e-5).all(axis=-1)
+    assert within.mean() > 0.99
+    # the film from Render() is the footprint sum of the same samples
+    film = r.Render(sc, flat.camera)
+    np.testing.assert_allclose(film.rgbw[..., :3], g["film"][..., :3],
+                               rtol=1e-3, atol=1e-3 * spp)
+    assert np.array_equal(film.rgbw[..., 3], g["film"][..., 3])
+
+
+def test_render_matches_oracle_film_and_is_deterministic(ctx):
+    sc_spec = S.cornell_box(48, 40)
+    flat = S.flatten(sc_spec)
+    sc = api.GpuScene(ctx, flat)
+    args = api.PTRendererArgs(spp=16, min_bounces=3, max_bounces=8)
+    r = api.PTRenderer(args, seed=3)
+    f1 = r.Render(sc, flat.camera).rgbw.copy()
+    f2 = r.Render(sc, flat.camera).rgbw.copy()
+    assert same_bits(f1, f2)
+    li_o, film_o = O.render(flat, dict(spp=16, min_bounces=3, max_bounces=8), seed=3)
+    assert np.array_equal(f1[..., 3], film_o[..., 3].astype(np.float32))
+    np.testing.assert_allclose(f1[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
+
+
+def test_wave_splitting_does_not_change_results():
+    """A render split into many small waves gives the same samples."""
+    flat = S.flatten(S.cornell_box(24, 24))
+    big = api.Context(0)
+    small = api.Context(0, wave_paths=1000)
+    args = api.PTRendererArgs(spp=8, min_bounces=3, max_bounces=8)
+    a = api.PTRenderer(args, seed=9).RenderSamples(api.GpuScene(big, flat), flat.camera)
+    b = api.PTRenderer(args, seed=9).RenderSamples(api.GpuScene(small, flat), flat.camera)
+    assert same_bits(a, b)
+    fa = api.PTRenderer(args, seed=9).Render(api.GpuScene(big, flat), flat.camera)
+    fb = api.PTRenderer(args, seed=9).Render(api.GpuScene(small, flat), flat.camera)
+    np.testing.assert_allclose(fa.rgbw, fb.rgbw, rtol=1e-6, atol=1e-6)
+    big.close()
+    small.close()
+
+
+def test_invalid_scene_is_rejected(ctx):
+    from ajisai_render_gb300._lib import AjgError
+    fl = S.flatten(S.cornell_box(8, 8))
+    fl.tri_mat = fl.tri_mat.copy()
+    fl.tri_mat[0] = 99
+    with pytest.raises(AjgError) as e:
+        api.GpuScene(ctx, fl)
+    assert e.value.code == 1
+
+
+def test_trace_counters(ctx):
+    ctx.stats(reset=True)
+    fl = S.flatten(S.cornell_box(8, 8))
+    sc = geometry_scene(ctx, fl.tris, fl.world)
+    rays = random_rays(np.random.default_rng(1), 1000, 0.4)
+    sc.Intersect(rays)
+    st = ctx.stats()
+    assert st["closest_rays"] == 1000 and st["closest_nodes"] >= 1000
