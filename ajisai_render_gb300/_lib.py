@@ -6,6 +6,7 @@ fallback: if the shared library is missing, every entry point raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
@@ -74,7 +75,10 @@ class SceneInfo(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "closest_rays", "any_rays", "nodes_visited", "tris_tested",
-        "closest_nodes", "closest_tris", "any_nodes", "any_tris", "paths")]
+        "closest_nodes", "closest_tris", "any_nodes", "any_tris", "paths",
+        "kernel_launches", "closest_launches", "any_launches",
+        "shade_launches")] + [(n, C.c_double) for n in (
+            "closest_ms", "any_ms", "shade_ms")]
 
 
 assert C.sizeof(Material) == 64 and C.sizeof(Light) == 48
@@ -87,6 +91,7 @@ SIGNATURES = {
     "ajg_destroy_context": ([_P], C.c_int),
     "ajg_last_error": ([_P], C.c_char_p),
     "ajg_get_stats": ([_P, C.POINTER(Stats), C.c_int], C.c_int),
+    "ajg_set_profiling": ([_P, C.c_int], C.c_int),
     "ajg_scene_create": ([_P, C.POINTER(MeshDesc), C.c_uint32, C.POINTER(Material),
                           C.c_uint32, C.POINTER(Light), C.c_uint32,
                           C.POINTER(SceneOpts), C.POINTER(_P)], C.c_int),
@@ -118,7 +123,7 @@ def load(path: Path | None = None):
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else Path(os.environ.get("AJG_LIB", LIB_PATH))
     if not p.exists():
         raise RuntimeError(
             f"{p} is missing: build it with `python -m ajisai_render_gb300.build`"

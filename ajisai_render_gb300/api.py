@@ -52,6 +52,9 @@ class Context:
     def check(self, rc):
         _lib.check(rc, self.h)
 
+    def set_profiling(self, enable: bool):
+        self.check(self.lib.ajg_set_profiling(self.h, int(enable)))
+
     def stats(self, reset: bool = False) -> dict:
         s = _lib.Stats()
         self.check(self.lib.ajg_get_stats(self.h, C.byref(s), int(reset)))
@@ -245,6 +248,16 @@ class PTRenderer:
         flags = (1 if self.fp64_film else 0) | (2 if self.drop_nonfinite else 0)
         return _lib.RenderParams(a.spp, a.min_bounces, a.max_bounces, a.cont_prob,
                                  int(a.use_mis), flags, self.seed)
+
+    def render_device(self, scene: GpuScene, camera, out_ptr: int, stream_ptr: int = 0):
+        """Render into device memory (float [h][w][4] at out_ptr), ordered on
+        the given CUDA stream (a cudaStream_t as an integer)."""
+        cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+        cam = camera_struct(cam36)
+        p = self.params()
+        scene.ctx.check(scene.ctx.lib.ajg_render_device(
+            scene.h, C.byref(cam), C.byref(p), C.c_void_p(out_ptr),
+            C.c_void_p(stream_ptr) if stream_ptr else None))
 
     def Render(self, scene: GpuScene, camera, film: Film | None = None) -> Film:
         cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()

@@ -21,6 +21,10 @@ CSRC = HERE / "csrc"
 INCLUDE = HERE.parent / "include"
 BUILD = HERE / "_build"
 LIB = BUILD / "libajisai_gpu.so"
+# Tuning builds: AJG_BUILD_TAG=<tag> AJG_EXTRA_NVCC="-DAJG_...=..." writes
+# _build/libajisai_gpu_<tag>.so; AJG_LIB=<path> makes the loader use it.
+TAG = os.environ.get("AJG_BUILD_TAG", "")
+EXTRA = os.environ.get("AJG_EXTRA_NVCC", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,15 +59,16 @@ def _stale(out: Path, deps) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     srcs = sources()
-    if not force and not _stale(LIB, srcs + headers() + [Path(__file__)]):
-        return LIB
-    obj = BUILD / "obj"
+    lib = BUILD / f"libajisai_gpu_{TAG}.so" if TAG else LIB
+    if not force and not _stale(lib, srcs + headers() + [Path(__file__)]):
+        return lib
+    obj = BUILD / (f"obj_{TAG}" if TAG else "obj")
     obj.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
     procs = []
     for s in srcs:
         o = obj / (s.stem + ".o")
-        cmd = [cc, *flags(), "-c", str(s), "-o", str(o)]
+        cmd = [cc, *flags(EXTRA), "-c", str(s), "-o", str(o)]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         procs.append((s, o, subprocess.Popen(cmd, stdout=subprocess.PIPE,
@@ -78,13 +83,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         objs.append(o)
     if errs:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errs))
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     r = subprocess.run([cc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp),
                         *map(str, objs)], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -86,17 +86,17 @@ __global__ void k_bsdf_query(const ajg_material* __restrict__ mats,
                              float* __restrict__ out) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
+    // the record in global memory; its first word is the uint32 type, which
+    // the BSDF routines do not read
     const float* m = reinterpret_cast<const float*>(mats + i);
-    float rec[16];
-    for (int k = 0; k < 16; ++k) rec[k] = m[k];
-    rec[0] = (float)mats[i].type;
-    const float lum = (float)(0.2126 * (double)rec[1] + 0.7152 * (double)rec[2] +
-                              0.0722 * (double)rec[3]);
+    const float lum = (float)(0.2126 * (double)m[1] + 0.7152 * (double)m[2] +
+                              0.0722 * (double)m[3]);
     Bsdf f;
     f.type = (int)mats[i].type;
     f.ng = ld3(ng + 3 * i);
     f.ns = ld3(ns + 3 * i);
-    f.m = load_material(rec, lum);
+    f.m = m;
+    f.lum = lum;
     float* o = out + 8 * i;
     if (op[i] == 0) {
       const F3 v = f.eval(ld3(wi + 3 * i), ld3(wo + 3 * i));
@@ -189,6 +189,7 @@ int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) !=
           cudaSuccess ||
       cudaMalloc(&ctx->d_error, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_fetch, sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&ctx->d_counters, 2 * sizeof(TraceCounters)) != cudaSuccess) {
     delete ctx;
     return fail(nullptr, AJG_ERR_CUDA, "context allocation failed");
@@ -203,8 +204,13 @@ int ajg_destroy_context(ajg_ctx* ctx) {
   if (!ctx) return AJG_ERR_INVALID;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  for (auto& p : ctx->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
   for (auto& b : ctx->arena) cudaFree(b.ptr);
   cudaFree(ctx->d_error);
+  cudaFree(ctx->d_fetch);
   cudaFree(ctx->d_counters);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -228,10 +234,37 @@ int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset) {
   out->nodes_visited = c[0].nodes + c[1].nodes;
   out->tris_tested = c[0].tris + c[1].tris;
   out->paths = ctx->paths_total;
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    ctx->kind_ms[p.kind] += ms;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  ctx->pending.clear();
+  out->kernel_launches = ctx->kernel_launches;
+  out->closest_launches = ctx->kind_launches[kKindClosest];
+  out->any_launches = ctx->kind_launches[kKindAny];
+  out->shade_launches = ctx->kind_launches[kKindShade];
+  out->closest_ms = ctx->kind_ms[kKindClosest];
+  out->any_ms = ctx->kind_ms[kKindAny];
+  out->shade_ms = ctx->kind_ms[kKindShade];
   if (reset) {
     CK(cudaMemset(ctx->d_counters, 0, sizeof(c)), "stats");
     ctx->paths_total = 0;
+    ctx->kernel_launches = 0;
+    for (int k = 0; k < kKinds; ++k) {
+      ctx->kind_ms[k] = 0;
+      ctx->kind_launches[k] = 0;
+    }
   }
+  return AJG_OK;
+}
+
+int ajg_set_profiling(ajg_ctx* ctx, int enable) {
+  if (!ctx) return fail(nullptr, AJG_ERR_INVALID, "NULL context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->profiling = enable != 0;
   return AJG_OK;
 }
 
@@ -463,6 +496,8 @@ static int trace_host(ajg_scene* s, const ajg_ray* rays, uint64_t n,
                       void* out, bool any) {
   if (!s || (n && (!rays || !out))) return AJG_ERR_INVALID;
   ajg_ctx* ctx = s->ctx;
+  if (n > (1ull << 31))
+    return fail(ctx, AJG_ERR_INVALID, "at most 2^31 rays per call");
   if (n == 0) return AJG_OK;
   std::lock_guard<std::mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
@@ -471,16 +506,19 @@ static int trace_host(ajg_scene* s, const ajg_ray* rays, uint64_t n,
   CK(dr.alloc(n, st), "trace: alloc");
   CK(cudaMemcpyAsync(dr.p, rays, n * sizeof(ajg_ray), cudaMemcpyHostToDevice, st),
      "trace: copy in");
+  CK(cudaMemsetAsync(ctx->d_fetch, 0, sizeof(uint32_t), st), "trace");
+  KernelTimer tm(ctx, st, any ? kKindAny : kKindClosest);
   if (any) {
     DevBuf<uint8_t> dh;
     CK(dh.alloc(n, st), "trace: alloc");
-    launch_trace_any(s->d, dr.p, n, dh.p, &ctx->d_counters[1], ctx->d_error, st);
+    launch_trace_any(s->d, dr.p, n, dh.p, ctx->d_fetch, &ctx->d_counters[1],
+                     ctx->d_error, st);
     CK(cudaMemcpyAsync(out, dh.p, n, cudaMemcpyDeviceToHost, st), "trace: copy out");
   } else {
     DevBuf<ajg_hit> dh;
     CK(dh.alloc(n, st), "trace: alloc");
-    launch_trace_closest(s->d, dr.p, n, dh.p, &ctx->d_counters[0], ctx->d_error,
-                         st);
+    launch_trace_closest(s->d, dr.p, n, dh.p, ctx->d_fetch, &ctx->d_counters[0],
+                         ctx->d_error, st);
     CK(cudaMemcpyAsync(out, dh.p, n * sizeof(ajg_hit), cudaMemcpyDeviceToHost, st),
        "trace: copy out");
   }
@@ -502,11 +540,16 @@ int ajg_trace_closest_device(ajg_scene* s, const ajg_ray* d_rays, uint64_t n,
                              ajg_hit* d_hits, void* stream) {
   if (!s || (n && (!d_rays || !d_hits))) return AJG_ERR_INVALID;
   ajg_ctx* ctx = s->ctx;
+  if (n > (1ull << 31))
+    return fail(ctx, AJG_ERR_INVALID, "at most 2^31 rays per call");
   std::lock_guard<std::mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
   StreamJoin j(ctx->stream, (cudaStream_t)stream);
-  launch_trace_closest(s->d, d_rays, n, d_hits, &ctx->d_counters[0],
-                       ctx->d_error, ctx->stream);
+  CK(cudaMemsetAsync(ctx->d_fetch, 0, sizeof(uint32_t), ctx->stream),
+     "trace_closest_device");
+  KernelTimer tm(ctx, ctx->stream, kKindClosest);
+  launch_trace_closest(s->d, d_rays, n, d_hits, ctx->d_fetch,
+                       &ctx->d_counters[0], ctx->d_error, ctx->stream);
   CK(cudaGetLastError(), "trace_closest_device");
   return AJG_OK;
 }
@@ -515,11 +558,16 @@ int ajg_trace_any_device(ajg_scene* s, const ajg_ray* d_rays, uint64_t n,
                          uint8_t* d_occluded, void* stream) {
   if (!s || (n && (!d_rays || !d_occluded))) return AJG_ERR_INVALID;
   ajg_ctx* ctx = s->ctx;
+  if (n > (1ull << 31))
+    return fail(ctx, AJG_ERR_INVALID, "at most 2^31 rays per call");
   std::lock_guard<std::mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
   StreamJoin j(ctx->stream, (cudaStream_t)stream);
-  launch_trace_any(s->d, d_rays, n, d_occluded, &ctx->d_counters[1],
-                   ctx->d_error, ctx->stream);
+  CK(cudaMemsetAsync(ctx->d_fetch, 0, sizeof(uint32_t), ctx->stream),
+     "trace_any_device");
+  KernelTimer tm(ctx, ctx->stream, kKindAny);
+  launch_trace_any(s->d, d_rays, n, d_occluded, ctx->d_fetch,
+                   &ctx->d_counters[1], ctx->d_error, ctx->stream);
   CK(cudaGetLastError(), "trace_any_device");
   return AJG_OK;
 }

@@ -31,6 +31,15 @@ namespace ajg {
 namespace {
 
 constexpr int kShadeThreads = 128;
+#ifndef AJG_SHADE_MIN_BLOCKS
+#define AJG_SHADE_MIN_BLOCKS 8
+#endif
+#ifndef AJG_TRACE_MIN_BLOCKS
+#define AJG_TRACE_MIN_BLOCKS 1
+#endif
+#ifndef AJG_TRACE_BLOCKS_PER_SM
+#define AJG_TRACE_BLOCKS_PER_SM 10
+#endif
 constexpr int kMaxLights = 15;
 
 struct WaveArgs {
@@ -61,7 +70,10 @@ struct WaveBufs {
   uint8_t* term_vis;
   float4* sq_o;  // o.xyz, t_max
   float4* sq_d;  // d.xyz, slot bits
-  uint32_t* counts;  // [0],[1] path queues, [2] shadow queue
+  uint32_t* lists;   // [3][P]: queue slots of misses, Lambertian and
+                     // Disney hits
+  uint32_t* counts;  // [0],[1] path queues, [2] shadow queue, [3] shadow
+                     // fetch, [4..6] lists, [7] extend fetch
 };
 
 __device__ __forceinline__ int dim_base(const WaveArgs& a, int b) {
@@ -107,46 +119,81 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
+// Closest hits of the path queue.
 template <int TEST>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, AJG_TRACE_MIN_BLOCKS)
     k_extend(DeviceScene s, const float4* __restrict__ ro,
              const float4* __restrict__ rd, const uint32_t* __restrict__ count,
-             ajg_hit* __restrict__ hits, TraceCounters* ctr, uint32_t* err) {
+             uint32_t* fetch_next, ajg_hit* __restrict__ hits,
+             TraceCounters* ctr, uint32_t* err) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += gridDim.x * blockDim.x) {
+  auto fetch = [&](uint32_t k) {
     const float4 o = ro[k], d = rd[k];
-    RayQ r = make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
-    Hit h;
-    traverse<TEST, false>(s, r, h, nn, nt, err);
-    ++nr;
+    return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
+  };
+  auto finish = [&](uint32_t k, const Hit& h, bool) {
     ajg_hit o2;
     o2.t = h.t;
     o2.u = h.u;
     o2.v = h.v;
     o2.prim = h.prim;
     hits[k] = o2;
-  }
+  };
+  trace_persistent<TEST, false>(s, n, fetch_next, fetch, finish, nr, nn, nt,
+                                err);
   flush_counters(ctr, nr, nn, nt);
 }
 
+// Files every queue slot under its hit's material type (or as a miss), so
+// that shading runs in material-specialised kernels; warps stay converged,
+// so each list append is one atomic per warp.
+__global__ void k_classify(DeviceScene s, const uint32_t* __restrict__ count,
+                           const ajg_hit* __restrict__ hits,
+                           uint32_t* __restrict__ lists,
+                           uint32_t* __restrict__ list_counts,
+                           uint32_t list_cap) {
+  const uint32_t n = *count;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t wb = blockIdx.x * blockDim.x + (threadIdx.x - lane); wb < n;
+       wb += stride) {
+    const uint32_t k = wb + lane;
+    int cls = -1;
+    if (k < n) {
+      const int prim = hits[k].prim;
+      cls = 0;
+      if (prim >= 0) {
+        const uint32_t mat =
+            __float_as_uint(__ldg(&s.shade[prim].w)) & 0xffffffu;
+        cls = 1 + ((int)__ldg(s.materials + 16 * mat) == AJG_MAT_DISNEY);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const uint32_t j = warp_append(&list_counts[c], cls == c);
+      if (cls == c) lists[(uint64_t)c * list_cap + j] = k;
+    }
+  }
+}
+
 template <int TEST>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, AJG_TRACE_MIN_BLOCKS)
     k_shadow(DeviceScene s, const float4* __restrict__ sq_o,
              const float4* __restrict__ sq_d, const uint32_t* __restrict__ count,
-             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err) {
+             uint32_t* fetch_next, uint8_t* __restrict__ vis,
+             TraceCounters* ctr, uint32_t* err) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += gridDim.x * blockDim.x) {
+  auto fetch = [&](uint32_t k) {
     const float4 o = sq_o[k], d = sq_d[k];
-    RayQ r = make_query(xyz(o), xyz(d), kRayEps, o.w);
-    Hit h;
-    const bool occ = traverse<TEST, true>(s, r, h, nn, nt, err);
-    ++nr;
-    if (!occ) vis[__float_as_uint(d.w)] = 1;
-  }
+    return make_query(xyz(o), xyz(d), kRayEps, o.w);
+  };
+  auto finish = [&](uint32_t k, const Hit&, bool occ) {
+    if (!occ) vis[__float_as_uint(sq_d[k].w)] = 1;
+  };
+  trace_persistent<TEST, true>(s, n, fetch_next, fetch, finish, nr, nn, nt,
+                               err);
   flush_counters(ctr, nr, nn, nt);
 }
 
@@ -164,11 +211,34 @@ __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
   w.sq_d[k] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
 }
 
-__global__ void __launch_bounds__(kShadeThreads)
-    k_shade(WaveArgs a, WaveBufs w, int b, int cur, uint32_t shadow_cap,
+// Escaped paths: the environment counts only for camera rays
+// (pt.cpp:114-121), or on every bounce without MIS (pt.cpp:245-249).
+__global__ void k_shade_miss(WaveArgs a, WaveBufs w, int cur,
+                             const uint32_t* __restrict__ list,
+                             const uint32_t* __restrict__ count) {
+  const uint32_t n = *count;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += gridDim.x * blockDim.x) {
+    const uint32_t p = w.qpath[cur][list[j]];
+    float4 L = w.rad[p];
+    L.x += a.env_rgb.x;
+    L.y += a.env_rgb.y;
+    L.z += a.env_rgb.z;
+    w.rad[p] = L;
+  }
+}
+
+// Shading of the hits on one material type: NEE to every light
+// (helper.h:100-133), the MIS BSDF sample (helper.h:209-265), the
+// continuation sample (pt.cpp:215-223) and the next bounce's roulette.
+template <int MAT>
+__global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
+    k_shade(WaveArgs a, WaveBufs w, int b, int cur,
+            const uint32_t* __restrict__ list,
+            const uint32_t* __restrict__ list_count, uint32_t shadow_cap,
             uint32_t* err) {
   const DeviceScene& s = a.s;
-  const uint32_t n = w.counts[cur];
+  const uint32_t n = *list_count;
   const int nt = (int)s.num_lights + 1;
   const int nxt = cur ^ 1;
   // warp-uniform loop: every lane of a warp runs the same iterations, so the
@@ -177,51 +247,32 @@ __global__ void __launch_bounds__(kShadeThreads)
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t wb = blockIdx.x * blockDim.x + (threadIdx.x - lane); wb < n;
        wb += stride) {
-    const uint32_t k = wb + lane;
-    const bool valid = k < n;
+    const uint32_t j = wb + lane;
+    const bool hit = j < n;
     uint32_t p = 0;
-    ajg_hit h;
-    h.prim = -1;
-    F3 ro = mk3(0, 0, 0), rd = mk3(0, 0, 1);
-    if (valid) {
-      p = w.qpath[cur][k];
-      h = w.hits[k];
-      ro = xyz(w.ro[cur][k]);
-      rd = xyz(w.rd[cur][k]);
-    }
-    const bool hit = valid && h.prim >= 0;
-    uint32_t pixel = 0, sample = 0;
-    if (valid) path_id(a, p, pixel, sample);
-    const uint64_t key = path_key(a.seed, pixel, sample);
-    F3 T = valid ? xyz(w.thr[p]) : mk3(0, 0, 0);
-
-    if (valid && !hit) {
-      // escaped: the environment counts only for camera rays (pt.cpp:114-121)
-      // or on every bounce without MIS (pt.cpp:245-249)
-      if ((b == 0 || !a.use_mis) && s.env >= 0) {
-        float4 L = w.rad[p];
-        L.x += a.env_rgb.x;
-        L.y += a.env_rgb.y;
-        L.z += a.env_rgb.z;
-        w.rad[p] = L;
-      }
-    }
-
     HitInfo hi;
-    Bsdf f;
+    BsdfT<MAT> f;
+    F3 T = mk3(0, 0, 0);
+    uint64_t key = 0;
     if (hit) {
+      const uint32_t k = list[j];
+      p = w.qpath[cur][k];
+      const ajg_hit h = w.hits[k];
+      const F3 ro = xyz(w.ro[cur][k]), rd = xyz(w.rd[cur][k]);
+      uint32_t pixel, sample;
+      path_id(a, p, pixel, sample);
+      key = path_key(a.seed, pixel, sample);
+      T = xyz(w.thr[p]);
       hi = complete_hit(s, ro, rd, h.t, h.u, h.v, h.prim);
-      f.type = (int)s.materials[16 * hi.mat];
+      f.m = s.materials + 16 * hi.mat;
       f.ng = hi.ng;
       f.ns = hi.ns;
-      f.m = load_material(s.materials + 16 * hi.mat, s.mat_lum[hi.mat].x);
+      f.lum = __ldg(&s.mat_lum[hi.mat].x);
       w.thr_shade[p] = make_float4(T.x, T.y, T.z, 0.f);
     }
     int dim = dim_base(a, b) + (b > a.min_b ? 1 : 0);
 
     if (a.use_mis) {
-      // NEE to every light (helper.h:100-133); the term's value is kept and
-      // its shadow ray queued, the sum is formed once visibility is known
       for (int l = 0; l < (int)s.num_lights; ++l) {
         const float* L = s.lights + 12 * l;
         bool emit = false;
@@ -240,6 +291,8 @@ __global__ void __launch_bounds__(kShadeThreads)
             lpos = hi.pos + 2.f * s.radius * r2l;
             lrad = mk3(L[1], L[2], L[3]);
           } else {
+            // g++ evaluates SampleContinuous's two Next1D() arguments right
+            // to left: the first draw is v (env_light.cpp:71-72)
             const float v = key_float(key, dim);
             float u = key_float(key, dim + 1);
             lrad = mk3(L[1], L[2], L[3]);
@@ -257,8 +310,7 @@ __global__ void __launch_bounds__(kShadeThreads)
               const float theta = v * kPi;
               const float st = sinf(theta);
               lpdf = st != 0.f ? 1.f / (2.f * kPi * kPi * st) : 0.f;
-              const F3 dir = mk3(-sinf(theta) * cosf(phi), cosf(theta),
-                                 -sinf(theta) * sinf(phi));
+              const F3 dir = mk3(-st * cosf(phi), cosf(theta), -st * sinf(phi));
               lpos = hi.pos + 2.f * s.radius * dir;
             }
           }
@@ -266,15 +318,16 @@ __global__ void __launch_bounds__(kShadeThreads)
             const float len = len3(lpos - hi.pos) - kRayEps;
             if (!(len < kRayEps)) {
               const F3 wl = normalize3(lpos - hi.pos);
-              const F3 bf = f.eval(wl, hi.wr);
+              F3 bf;
+              float bp;
+              f.eval_pdf(wl, hi.wr, bf, bp);
               if (!black3(bf)) {
-                const F3 n = normalize3(hi.ns);
+                const F3 nn = normalize3(hi.ns);
                 F3 fv;
                 if (type == AJG_LIGHT_DIRECTIONAL)
-                  fv = mk3(1.f, 1.f, 1.f) * lrad * bf * fabsf(dot3(wl, n));
+                  fv = mk3(1.f, 1.f, 1.f) * lrad * bf * fabsf(dot3(wl, nn));
                 else
-                  fv = lrad * bf * fabsf(dot3(wl, n));
-                const float bp = f.pdf(wl, hi.wr);
+                  fv = lrad * bf * fabsf(dot3(wl, nn));
                 fo = fv / lpdf * power_heuristic(lpdf, bp);
                 make_ray(hi.pos, wl, so, sd);
                 tmax = 0.99f * len;
@@ -282,17 +335,13 @@ __global__ void __launch_bounds__(kShadeThreads)
               }
             }
           }
-        }
-        const uint32_t slot = p * nt + l;
-        if (hit) {
+          const uint32_t slot = p * nt + l;
           w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
           w.term_vis[slot] = 0;
         }
-        emit_shadow(w, so, sd, tmax, slot, emit, shadow_cap, err);
+        emit_shadow(w, so, sd, tmax, p * nt + l, emit, shadow_cap, err);
         dim += 2;
       }
-      // MISSampleBsdf (helper.h:209-265): nothing emits, so only a ray that
-      // escapes to the environment contributes
       {
         bool emit = false;
         F3 fo = mk3(0, 0, 0), so = mk3(0, 0, 0), sd = mk3(0, 0, 1);
@@ -311,19 +360,16 @@ __global__ void __launch_bounds__(kShadeThreads)
               emit = true;
             }
           }
-        }
-        const uint32_t slot = p * nt + (nt - 1);
-        if (hit) {
+          const uint32_t slot = p * nt + (nt - 1);
           w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
           w.term_vis[slot] = 0;
         }
-        emit_shadow(w, so, sd, __int_as_float(0x7f800000), slot, emit,
-                    shadow_cap, err);
+        emit_shadow(w, so, sd, __int_as_float(0x7f800000), p * nt + (nt - 1),
+                    emit, shadow_cap, err);
         dim += 3;
       }
     }
 
-    // continuation (pt.cpp:215-223) and the next bounce's roulette
     bool alive = false;
     F3 nro = mk3(0, 0, 0), nrd = mk3(0, 0, 1);
     if (hit && b + 1 < a.max_b) {
@@ -508,7 +554,8 @@ uint64_t wave_bytes(uint64_t P, int nt) {
   add(slots * 16);             // term_f
   add(slots);                  // term_vis
   add(slots * 16); add(slots * 16);  // shadow queue
-  add(16);                     // counts
+  add(P * 4 * 3);              // material lists
+  add(32);                     // counts
   return b;
 }
 
@@ -568,7 +615,8 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
   w.term_vis = carve<uint8_t>(cur, P * nt);
   w.sq_o = carve<float4>(cur, P * nt);
   w.sq_d = carve<float4>(cur, P * nt);
-  w.counts = carve<uint32_t>(cur, 4);
+  w.lists = carve<uint32_t>(cur, P * 3);
+  w.counts = carve<uint32_t>(cur, 8);
 
   // film
   const bool fp64 = (prm.flags & AJG_RENDER_FP64_FILM) != 0;
@@ -613,6 +661,8 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
   const uint64_t chunk = std::min<uint64_t>(npix, P / S);
   const uint32_t shadow_cap = (uint32_t)(P * nt);
   const int gs = kSMs * 8;
+  // persistent traversal: resident blocks only (occupancy-limited)
+  const int trace_grid = kSMs * AJG_TRACE_BLOCKS_PER_SM;
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);
     for (uint64_t p0 = pb; p0 < pe; p0 += chunk) {
@@ -621,46 +671,77 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
       a.S = (uint32_t)Sw;
       a.s0 = (uint32_t)s0;
       a.n_paths = (uint32_t)(n_pix * Sw);
-      cudaMemsetAsync(w.counts, 0, 16, st);
+      cudaMemsetAsync(w.counts, 0, 32, st);
+      KernelTimer{ctx, st, -1};
       k_raygen<<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads, 0,
                  st>>>(a, w);
       int q = 0;
       for (int b = 0; b < a.max_b; ++b) {
-        k_set<<<1, 1, 0, st>>>(&w.counts[q ^ 1], 0u);
-        k_set<<<1, 1, 0, st>>>(&w.counts[2], 0u);
-        if (s.tri_test == AJG_TRI_WATERTIGHT)
-          k_extend<AJG_TRI_WATERTIGHT><<<kSMs * 16, 128, 0, st>>>(
-              s, w.ro[q], w.rd[q], &w.counts[q], w.hits, &ctx->d_counters[0],
-              ctx->d_error);
-        else
-          k_extend<AJG_TRI_MOLLER_TRUMBORE><<<kSMs * 16, 128, 0, st>>>(
-              s, w.ro[q], w.rd[q], &w.counts[q], w.hits, &ctx->d_counters[0],
-              ctx->d_error);
-        k_shade<<<gs, kShadeThreads, 0, st>>>(a, w, b, q, shadow_cap,
-                                               ctx->d_error);
-        if (a.use_mis) {
+        // next queue, shadow queue, fetch counters and material lists
+        cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
+        cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
+        {
+          KernelTimer tm(ctx, st, kKindClosest);
           if (s.tri_test == AJG_TRI_WATERTIGHT)
-            k_shadow<AJG_TRI_WATERTIGHT><<<kSMs * 16, 128, 0, st>>>(
-                s, w.sq_o, w.sq_d, &w.counts[2], w.term_vis,
-                &ctx->d_counters[1], ctx->d_error);
+            k_extend<AJG_TRI_WATERTIGHT><<<trace_grid, 128, 0, st>>>(
+                s, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
+                &ctx->d_counters[0], ctx->d_error);
           else
-            k_shadow<AJG_TRI_MOLLER_TRUMBORE><<<kSMs * 16, 128, 0, st>>>(
-                s, w.sq_o, w.sq_d, &w.counts[2], w.term_vis,
-                &ctx->d_counters[1], ctx->d_error);
+            k_extend<AJG_TRI_MOLLER_TRUMBORE><<<trace_grid, 128, 0, st>>>(
+                s, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
+                &ctx->d_counters[0], ctx->d_error);
+        }
+        {
+          KernelTimer tm(ctx, st, -1);
+          k_classify<<<gs, 256, 0, st>>>(s, &w.counts[q], w.hits, w.lists,
+                                         &w.counts[4], (uint32_t)P);
+        }
+        if ((b == 0 || !a.use_mis) && s.env >= 0) {
+          KernelTimer tm(ctx, st, kKindShade);
+          k_shade_miss<<<gs, kShadeThreads, 0, st>>>(a, w, q, w.lists,
+                                                     &w.counts[4]);
+        }
+        {
+          KernelTimer tm(ctx, st, kKindShade);
+          k_shade<AJG_MAT_DIFFUSE><<<gs, kShadeThreads, 0, st>>>(
+              a, w, b, q, w.lists + P, &w.counts[5], shadow_cap, ctx->d_error);
+        }
+        {
+          KernelTimer tm(ctx, st, kKindShade);
+          k_shade<AJG_MAT_DISNEY><<<gs, kShadeThreads, 0, st>>>(
+              a, w, b, q, w.lists + 2 * P, &w.counts[6], shadow_cap,
+              ctx->d_error);
+        }
+        if (a.use_mis) {
+          {
+            KernelTimer tm(ctx, st, kKindAny);
+            if (s.tri_test == AJG_TRI_WATERTIGHT)
+              k_shadow<AJG_TRI_WATERTIGHT><<<trace_grid, 128, 0, st>>>(
+                  s, w.sq_o, w.sq_d, &w.counts[2], &w.counts[3], w.term_vis,
+                  &ctx->d_counters[1], ctx->d_error);
+            else
+              k_shadow<AJG_TRI_MOLLER_TRUMBORE><<<trace_grid, 128, 0, st>>>(
+                  s, w.sq_o, w.sq_d, &w.counts[2], &w.counts[3], w.term_vis,
+                  &ctx->d_counters[1], ctx->d_error);
+          }
+          KernelTimer{ctx, st, -1};
           k_accumulate<<<gs, kShadeThreads, 0, st>>>(a, w, q);
         }
         q ^= 1;
       }
+      if (want_film) KernelTimer{ctx, st, -1};
       if (want_film)
         k_film_add<<<grid_for(n_pix, 256, gs), 256, 0, st>>>(
             a, w.rad, fsum, fcomp, fsum64, (uint32_t)n_pix,
             (prm.flags & AJG_RENDER_DROP_NONFINITE) ? 1 : 0);
+      if (d_li) KernelTimer{ctx, st, -1};
       if (d_li)
         k_copy_li<<<grid_for(a.n_paths, 256, gs), 256, 0, st>>>(
             a, w.rad, li_begin, prm.spp, d_li);
     }
   }
   if (want_film) {
+    KernelTimer{ctx, st, -1};
     k_resolve<<<grid_for(npix_all, 256, gs), 256, 0, st>>>(
         fsum, fcomp, fsum64, cam.width, cam.height, d_out);
     if (fsum) cudaFreeAsync(fsum, st);

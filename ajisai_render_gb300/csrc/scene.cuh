@@ -50,6 +50,14 @@ struct Buffer {
   size_t bytes = 0;
 };
 
+// Event pairs recorded around launches while profiling is on; resolved into
+// milliseconds when the stats are read.
+enum KernelKind { kKindClosest = 0, kKindAny = 1, kKindShade = 2, kKinds = 3 };
+struct PendingTiming {
+  cudaEvent_t a, b;
+  int kind;
+};
+
 }  // namespace ajg
 
 struct ajg_ctx {
@@ -61,8 +69,14 @@ struct ajg_ctx {
   std::mutex mu;
   std::string last_error;
   uint32_t* d_error = nullptr;            // device error flag
+  uint32_t* d_fetch = nullptr;            // ray counter of query launches
   ajg::TraceCounters* d_counters = nullptr;  // [2]: closest, any
   unsigned long long paths_total = 0;
+  unsigned long long kernel_launches = 0;
+  bool profiling = false;
+  std::vector<ajg::PendingTiming> pending;
+  double kind_ms[ajg::kKinds] = {0, 0, 0};
+  unsigned long long kind_launches[ajg::kKinds] = {0, 0, 0};
   // wavefront arena (grown on demand, reused across renders)
   std::vector<ajg::Buffer> arena;
   uint64_t arena_paths = 0;
@@ -81,6 +95,28 @@ struct ajg_scene {
 };
 
 namespace ajg {
+// Brackets one launch of a given kind with events when profiling.
+struct KernelTimer {
+  ajg_ctx* ctx;
+  cudaStream_t st;
+  int kind;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelTimer(ajg_ctx* c, cudaStream_t s, int k) : ctx(c), st(s), kind(k) {
+    ++ctx->kernel_launches;
+    if (kind >= 0) ++ctx->kind_launches[kind];
+    if (ctx->profiling && kind >= 0) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, st);
+    }
+  }
+  ~KernelTimer() {
+    if (a) {
+      cudaEventRecord(b, st);
+      ctx->pending.push_back(PendingTiming{a, b, kind});
+    }
+  }
+};
 // ploc.cu
 int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
                 const float* h_corner, const int32_t* h_mat,
@@ -93,9 +129,9 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
                 cudaStream_t st);
 // trace.cu
 void launch_trace_closest(const DeviceScene& s, const ajg_ray* rays,
-                          uint64_t n, ajg_hit* hits, TraceCounters* ctr,
-                          uint32_t* err, cudaStream_t st);
+                          uint64_t n, ajg_hit* hits, uint32_t* next,
+                          TraceCounters* ctr, uint32_t* err, cudaStream_t st);
 void launch_trace_any(const DeviceScene& s, const ajg_ray* rays, uint64_t n,
-                      uint8_t* occluded, TraceCounters* ctr, uint32_t* err,
-                      cudaStream_t st);
+                      uint8_t* occluded, uint32_t* next, TraceCounters* ctr,
+                      uint32_t* err, cudaStream_t st);
 }  // namespace ajg

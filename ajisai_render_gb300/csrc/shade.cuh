@@ -143,7 +143,7 @@ struct Lambert {
   __device__ __forceinline__ bool fringes(F3 w) const {
     return (dot3(ng, w) > 0) != (dot3(ns, w) > 0);
   }
-  __device__ BsdfSample sample(F3 wo, F3 sam) const {
+  __device__ __forceinline__ BsdfSample sample(F3 wo, F3 sam) const {
     if (fringes(wo)) {
       if (dot3(ng, wo) <= 0.f) return invalid_sample();
       float pdf;
@@ -162,7 +162,10 @@ struct Lambert {
     if (lwo.z <= 0.f) return invalid_sample();
     float pdf;
     F3 lwi = cosine_hemisphere(sam.y, sam.z, &pdf);
-    if ((double)pdf < 1e-3) return invalid_sample();
+    // pdf < 1e-3 compares in double in the reference
+    // (diffuse_component.cpp:39); for a float pdf that is pdf < 1e-3f
+    // exactly, as no float lies in [1e-3, 1e-3f)
+    if (pdf < 1e-3f) return invalid_sample();
     lwi = normalize3(lwi);
     pdf *= 1.f;
     const F3 wi = sf.to_world(lwi);
@@ -200,6 +203,76 @@ struct Lambert {
     return wsum > 0 ? p / wsum : 0;
   }
 };
+
+// ----------------------------------------------------- float-float helpers --
+// The reference evaluates the VNDF slope fit in double (disney.cpp:400-407).
+// GB300 issues FP64 at a small fraction of the FP32 rate, so the fit is
+// evaluated in float-float arithmetic (unevaluated sums hi + lo; Dekker's
+// and Knuth's error-free transformations, FMA-based products): about 48
+// significant bits, against the fit's denominator cancelling to ~2e-5 near
+// u2 = 1, so the result rounds to the same float as the double evaluation
+// except when that lands within ~2^-32 relative of a rounding boundary.
+struct FF {
+  float hi, lo;
+};
+__host__ __device__ __forceinline__ float fma_rn(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+__host__ __device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return FF{s, (a - (s - bb)) + (b - bb)};
+}
+__host__ __device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return FF{s, b - (s - a)};
+}
+__host__ __device__ __forceinline__ FF ff_add(FF x, FF y) {
+  FF s = ff_two_sum(x.hi, y.hi);
+  const FF t = ff_two_sum(x.lo, y.lo);
+  s.lo += t.hi;
+  s = ff_fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return ff_fast_two_sum(s.hi, s.lo);
+}
+__host__ __device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  float e = fma_rn(x.hi, y.hi, -p);
+  e = fma_rn(x.hi, y.lo, e);
+  e = fma_rn(x.lo, y.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ FF ff_div(FF x, FF y) {
+  const float q1 = x.hi / y.hi;
+  const FF r = ff_add(x, ff_mul(FF{-q1, 0.f}, y));
+  const float q2 = r.hi / y.hi;
+  const FF q = ff_fast_two_sum(q1, q2);
+  const FF r2 = ff_add(x, ff_mul(FF{-q.hi, -q.lo}, y));
+  return ff_add(q, FF{r2.hi / y.hi, 0.f});
+}
+#define AJG_FF_CONST(c) FF{(float)(c), (float)((c) - (double)(float)(c))}
+// rounds hi + lo to the nearest float (hi is already the nearest float to
+// the unevaluated sum after the final renormalisation)
+__host__ __device__ __forceinline__ float ff_round(FF x) { return x.hi + x.lo; }
+
+// z(u2) of the VNDF slope fit (disney.cpp:400-407)
+__host__ __device__ __forceinline__ float vndf_fit_z(float u2f) {
+  const FF u = FF{u2f, 0.f};
+  FF num = ff_add(ff_mul(u, AJG_FF_CONST(-0.365728915865723)),
+                  AJG_FF_CONST(0.790235037209296));
+  num = ff_add(ff_mul(u, num), AJG_FF_CONST(-0.424965825137544));
+  num = ff_add(ff_mul(u, num), AJG_FF_CONST(0.000152998850436920));
+  FF den = ff_add(ff_mul(u, AJG_FF_CONST(0.169507819808272)),
+                  AJG_FF_CONST(-0.397203533833404));
+  den = ff_add(ff_mul(u, den), AJG_FF_CONST(-0.232500544458471));
+  den = ff_add(ff_mul(u, den), FF{1.f, 0.f});
+  den = ff_add(ff_mul(u, den), AJG_FF_CONST(-0.539825872510702));
+  return ff_round(ff_div(num, den));
+}
 
 // --------------------------------------------------------------- Disney --
 // DisneyBSDF (core/material/disney.cpp:58-473)
@@ -274,20 +347,13 @@ struct DisneyB {
       S = -1.0f;
       u2 = 2.0f * (0.5f - u2);
     }
-    // the published rational fit of the slope distribution, in double as
-    // written (disney.cpp:400-407)
-    const double d2 = u2;
-    const float z =
-        (float)((d2 * (d2 * (d2 * (-0.365728915865723) + 0.790235037209296) -
-                       0.424965825137544) +
-                 0.000152998850436920) /
-                (d2 * (d2 * (d2 * (d2 * 0.169507819808272 - 0.397203533833404) -
-                             0.232500544458471) +
-                       1) -
-                 0.539825872510702));
+    // the published rational fit of the slope distribution, which the
+    // reference evaluates in double (disney.cpp:400-407): float-float here
+    const float z = vndf_fit_z(u2);
     sy = S * z * sqrtf(1.0f + sx * sx);
   }
-  __device__ static F3 sample_vn(F3 wi_in, float u1, float u2, float Alpha) {
+  __device__ static __forceinline__ F3 sample_vn(F3 wi_in, float u1, float u2,
+                                                float Alpha) {
     const F3 wi = normalize3(mk3(Alpha * wi_in.x, Alpha * wi_in.y, wi_in.z));
     float Theta = 0, Phi = 0;
     if (wi.z < 0.99999f) {
@@ -365,7 +431,7 @@ struct DisneyB {
     const float G = ggx_g(wo, wi, wh, 0.25f);
     return m.clearcoat * D * F * G / (4.0f * fabsf(wi.z) * fabsf(wo.z));
   }
-  __device__ F3 eval(F3 wi, F3 wo) const {
+  __device__ __forceinline__ F3 eval(F3 wi, F3 wo) const {
     const F3 lwi = normalize3(sf.to_local(wi));
     const F3 lwo = normalize3(sf.to_local(wo));
     if (fabsf(lwi.z) < FLT_EPSILON || fabsf(lwo.z) < FLT_EPSILON)
@@ -389,7 +455,7 @@ struct DisneyB {
     const float cc = clearcoat_term(lwi, lwo, wh, idh, m.clearcoat_gloss);
     return t1 + t2 + mk3(cc, cc, cc);
   }
-  __device__ float pdf(F3 wi, F3 wo) const {
+  __device__ __forceinline__ float pdf(F3 wi, F3 wo) const {
     const F3 lwi = normalize3(sf.to_local(wi));
     const F3 lwo = normalize3(sf.to_local(wo));
     const F3 wh = normalize3(lwo + lwi);
@@ -417,7 +483,60 @@ struct DisneyB {
     }
     return p;
   }
-  __device__ BsdfSample sample(F3 wo, F3 sam) const {
+  // eval() and pdf() of the same (wi, wo) with their common
+  // subexpressions computed once (the same operations, so bit-identical).
+  // pdf is left at 0 when f is black unless pdf_if_black.
+  __device__ __forceinline__ void eval_pdf(F3 wi, F3 wo, F3& f, float& pdf,
+                                           bool pdf_if_black) const {
+    const F3 lwi = normalize3(sf.to_local(wi));
+    const F3 lwo = normalize3(sf.to_local(wo));
+    const float rough = clampf(m.roughness, 0.02f, 1.f);
+    const F3 wh = normalize3(lwo + lwi);
+    f = mk3(0, 0, 0);
+    if (!(fabsf(lwi.z) < FLT_EPSILON || fabsf(lwo.z) < FLT_EPSILON)) {
+      const F3 untinted = mk3(m.lum, m.lum, m.lum);
+      F3 spec_alb = dlerp(dlerp(m.base, untinted, 1.0f - m.specular_tint),
+                          m.base, m.metallic);
+      const F3 sheen_alb = dlerp(untinted, m.base, m.sheen_tint);
+      const float odh = dot3(lwo, wh);
+      const float idh = dot3(lwi, wh);
+      const float omo = 1.f - odh;
+      spec_alb = dlerp(spec_alb, untinted, omo * omo * omo);
+      const float F = fresnel_schlick(odh, 0.0f);
+      const F3 sheen_term = F * m.sheen * sheen_alb;
+      const float dl =
+          dlerp(diffuse_term(lwi, lwo, idh, rough),
+                subsurface_term(lwi, lwo, idh, rough), m.subsurface);
+      const F3 t1 = (1.0f - m.metallic) * (m.base * dl + sheen_term);
+      const F3 t2 = spec_alb * specular_term(lwi, lwo, wh, odh, rough);
+      const float cc = clearcoat_term(lwi, lwo, wh, idh, m.clearcoat_gloss);
+      f = t1 + t2 + mk3(cc, cc, cc);
+    }
+    pdf = 0.f;
+    if (!pdf_if_black && black3(f)) return;
+    if (maxc3(wh) <= 0.f) return;
+    const float mpdf = pdf_vn(lwo, wh, rough * rough);
+    float p = 0.f;
+    const float dwhdwi = 1.f / (4.f * fabsf(dot3(lwi, wh)));
+    const float spec_pdf = mpdf * dwhdwi;
+    const float nr = std_lerp(0.f, 0.08f, m.specular);
+    const float odh = dot3(lwo, wh);
+    const float ps = fresnel_schlick(odh, nr);
+    p += spec_pdf * ps;
+    p += fabsf(lwi.z) * kInvPi * (1.f - ps);
+    if (m.clearcoat > 0.f) {
+      const float cw = m.clearcoat / (m.clearcoat + m.lum);
+      const float fc = fresnel_coat(fabsf(wo.z));
+      const float pc = (fc * cw) / (fc * cw + (1 - fc) * (1 - cw));
+      const float cr = std_lerp(0.005f, 0.10f, m.clearcoat_gloss);
+      const float chp = pdf_vn(wo, wh, cr);
+      const float cp = chp * dwhdwi;
+      p *= 1.0f - pc;
+      p += cp * pc;
+    }
+    pdf = p;
+  }
+  __device__ __forceinline__ BsdfSample sample(F3 wo, F3 sam) const {
     const F3 lwo = normalize3(sf.to_local(wo));
     F3 lwi, lwh;
     bool coat = false;
@@ -453,27 +572,93 @@ struct DisneyB {
     if (lwi.z <= 0.0f) return invalid_sample();
     BsdfSample s;
     s.dir = sf.to_world(lwi);
-    s.f = eval(s.dir, wo);
-    s.pdf = pdf(s.dir, wo);
+    eval_pdf(s.dir, wo, s.f, s.pdf, true);
     return s;
   }
 };
 
+// One out-of-line copy of each BSDF routine: the path kernel calls them from
+// ten sites per hit, and inlining them all overflows the instruction cache.
+static __device__ __noinline__ F3 disney_eval(const float* __restrict__ m, float lum,
+                                       F3 ns, F3 wi, F3 wo) {
+  const MatParams p = load_material(m, lum);
+  return DisneyB(p, ns).eval(wi, wo);
+}
+static __device__ __noinline__ float disney_pdf(const float* __restrict__ m,
+                                         float lum, F3 ns, F3 wi, F3 wo) {
+  const MatParams p = load_material(m, lum);
+  return DisneyB(p, ns).pdf(wi, wo);
+}
+static __device__ __noinline__ BsdfSample disney_sample(const float* __restrict__ m,
+                                                 float lum, F3 ns, F3 wo,
+                                                 F3 sam) {
+  const MatParams p = load_material(m, lum);
+  return DisneyB(p, ns).sample(wo, sam);
+}
+static __device__ __noinline__ void disney_eval_pdf(const float* __restrict__ m,
+                                                    float lum, F3 ns, F3 wi,
+                                                    F3 wo, F3& f, float& pdf,
+                                                    bool pdf_if_black) {
+  const MatParams p = load_material(m, lum);
+  DisneyB(p, ns).eval_pdf(wi, wo, f, pdf, pdf_if_black);
+}
+static __device__ __noinline__ BsdfSample lambert_sample(F3 ng, F3 ns, F3 alb,
+                                                  F3 wo, F3 sam) {
+  return Lambert(ng, ns, alb).sample(wo, sam);
+}
+static __device__ __noinline__ F3 lambert_eval(F3 ng, F3 ns, F3 alb, F3 wi, F3 wo) {
+  return Lambert(ng, ns, alb).eval(wi, wo);
+}
+static __device__ __noinline__ float lambert_pdf(F3 ng, F3 ns, F3 alb, F3 wi, F3 wo) {
+  return Lambert(ng, ns, alb).pdf(wi, wo);
+}
+
+// The BSDF at a hit: material record (in global memory) and the two normals.
 struct Bsdf {
   int type;
   F3 ng, ns;
-  MatParams m;
+  const float* m;  // [16] record
+  float lum;
+  __device__ __forceinline__ F3 albedo() const {
+    return mk3(m[1], m[2], m[3]);
+  }
   __device__ __forceinline__ BsdfSample sample(F3 wo, F3 s) const {
-    if (type == AJG_MAT_DIFFUSE) return Lambert(ng, ns, m.base).sample(wo, s);
-    return DisneyB(m, ns).sample(wo, s);
+    if (type == AJG_MAT_DIFFUSE) return lambert_sample(ng, ns, albedo(), wo, s);
+    return disney_sample(m, lum, ns, wo, s);
   }
   __device__ __forceinline__ F3 eval(F3 wi, F3 wo) const {
-    if (type == AJG_MAT_DIFFUSE) return Lambert(ng, ns, m.base).eval(wi, wo);
-    return DisneyB(m, ns).eval(wi, wo);
+    if (type == AJG_MAT_DIFFUSE) return lambert_eval(ng, ns, albedo(), wi, wo);
+    return disney_eval(m, lum, ns, wi, wo);
   }
   __device__ __forceinline__ float pdf(F3 wi, F3 wo) const {
-    if (type == AJG_MAT_DIFFUSE) return Lambert(ng, ns, m.base).pdf(wi, wo);
-    return DisneyB(m, ns).pdf(wi, wo);
+    if (type == AJG_MAT_DIFFUSE) return lambert_pdf(ng, ns, albedo(), wi, wo);
+    return disney_pdf(m, lum, ns, wi, wo);
+  }
+};
+
+// The same with the material type fixed at compile time (the specialised
+// shading kernels): NEE needs f and, when f is not black, the pdf.
+template <int MAT>
+struct BsdfT {
+  F3 ng, ns;
+  const float* m;
+  float lum;
+  __device__ __forceinline__ F3 albedo() const {
+    return mk3(m[1], m[2], m[3]);
+  }
+  __device__ __forceinline__ BsdfSample sample(F3 wo, F3 s) const {
+    if (MAT == AJG_MAT_DIFFUSE) return Lambert(ng, ns, albedo()).sample(wo, s);
+    return disney_sample(m, lum, ns, wo, s);
+  }
+  __device__ __forceinline__ void eval_pdf(F3 wi, F3 wo, F3& f,
+                                           float& pdf) const {
+    if (MAT == AJG_MAT_DIFFUSE) {
+      const Lambert l(ng, ns, albedo());
+      f = l.eval(wi, wo);
+      pdf = black3(f) ? 0.f : l.pdf(wi, wo);
+      return;
+    }
+    disney_eval_pdf(m, lum, ns, wi, wo, f, pdf, false);
   }
 };
 

@@ -10,70 +10,71 @@ constexpr int kTraceThreads = 128;
 template <int TEST>
 __global__ void __launch_bounds__(kTraceThreads)
     k_trace_closest(DeviceScene s, const ajg_ray* __restrict__ rays,
-                    uint64_t n, ajg_hit* __restrict__ hits,
+                    uint64_t n, uint32_t* next, ajg_hit* __restrict__ hits,
                     TraceCounters* ctr, uint32_t* err) {
   uint32_t nn = 0, nt = 0, nr = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  auto fetch = [&](uint32_t i) {
     const ajg_ray q = rays[i];
-    RayQ r = make_query(mk3(q.o[0], q.o[1], q.o[2]),
-                        mk3(q.d[0], q.d[1], q.d[2]), q.t_min, q.t_max);
-    Hit h;
-    traverse<TEST, false>(s, r, h, nn, nt, err);
-    ++nr;
+    return make_query(mk3(q.o[0], q.o[1], q.o[2]), mk3(q.d[0], q.d[1], q.d[2]),
+                      q.t_min, q.t_max);
+  };
+  auto finish = [&](uint32_t i, const Hit& h, bool) {
     ajg_hit o;
     o.t = h.t;
     o.u = h.u;
     o.v = h.v;
     o.prim = h.prim;
     hits[i] = o;
-  }
+  };
+  trace_persistent<TEST, false>(s, (uint32_t)n, next, fetch, finish, nr, nn,
+                                nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
 template <int TEST>
 __global__ void __launch_bounds__(kTraceThreads)
     k_trace_any(DeviceScene s, const ajg_ray* __restrict__ rays, uint64_t n,
-                uint8_t* __restrict__ occ, TraceCounters* ctr, uint32_t* err) {
+                uint32_t* next, uint8_t* __restrict__ occ, TraceCounters* ctr,
+                uint32_t* err) {
   uint32_t nn = 0, nt = 0, nr = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  auto fetch = [&](uint32_t i) {
     const ajg_ray q = rays[i];
-    RayQ r = make_query(mk3(q.o[0], q.o[1], q.o[2]),
-                        mk3(q.d[0], q.d[1], q.d[2]), q.t_min, q.t_max);
-    Hit h;
-    occ[i] = traverse<TEST, true>(s, r, h, nn, nt, err) ? 1 : 0;
-    ++nr;
-  }
+    return make_query(mk3(q.o[0], q.o[1], q.o[2]), mk3(q.d[0], q.d[1], q.d[2]),
+                      q.t_min, q.t_max);
+  };
+  auto finish = [&](uint32_t i, const Hit&, bool o) { occ[i] = o ? 1 : 0; };
+  trace_persistent<TEST, true>(s, (uint32_t)n, next, fetch, finish, nr, nn, nt,
+                               err);
   flush_counters(ctr, nr, nn, nt);
 }
 
 }  // namespace
 
+// `next` is a zeroed device word (the persistent lanes' ray counter).
 void launch_trace_closest(const DeviceScene& s, const ajg_ray* rays,
-                          uint64_t n, ajg_hit* hits, TraceCounters* ctr,
-                          uint32_t* err, cudaStream_t st) {
+                          uint64_t n, ajg_hit* hits, uint32_t* next,
+                          TraceCounters* ctr, uint32_t* err, cudaStream_t st) {
   if (!n) return;
-  const int g = grid_for(n, kTraceThreads, kSMs * 16);
+  const int g = grid_for(n, kTraceThreads, kSMs * 10);
   if (s.tri_test == AJG_TRI_WATERTIGHT)
     k_trace_closest<AJG_TRI_WATERTIGHT>
-        <<<g, kTraceThreads, 0, st>>>(s, rays, n, hits, ctr, err);
+        <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, hits, ctr, err);
   else
     k_trace_closest<AJG_TRI_MOLLER_TRUMBORE>
-        <<<g, kTraceThreads, 0, st>>>(s, rays, n, hits, ctr, err);
+        <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, hits, ctr, err);
 }
 
 void launch_trace_any(const DeviceScene& s, const ajg_ray* rays, uint64_t n,
-                      uint8_t* occluded, TraceCounters* ctr, uint32_t* err,
-                      cudaStream_t st) {
+                      uint8_t* occluded, uint32_t* next, TraceCounters* ctr,
+                      uint32_t* err, cudaStream_t st) {
   if (!n) return;
-  const int g = grid_for(n, kTraceThreads, kSMs * 16);
+  const int g = grid_for(n, kTraceThreads, kSMs * 10);
   if (s.tri_test == AJG_TRI_WATERTIGHT)
     k_trace_any<AJG_TRI_WATERTIGHT>
-        <<<g, kTraceThreads, 0, st>>>(s, rays, n, occluded, ctr, err);
+        <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, occluded, ctr, err);
   else
     k_trace_any<AJG_TRI_MOLLER_TRUMBORE>
-        <<<g, kTraceThreads, 0, st>>>(s, rays, n, occluded, ctr, err);
+        <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, occluded, ctr, err);
 }
 
 }  // namespace ajg

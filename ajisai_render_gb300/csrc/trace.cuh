@@ -231,6 +231,159 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, const RayQ& r,
   return hit.prim >= 0;
 }
 
+// Persistent-lane traversal.  Each lane owns one ray at a time and runs one
+// node visit per loop iteration; lanes whose ray finished take new rays from
+// a shared counter (warp-aggregated, once at least kRefill lanes of the warp
+// are idle), so lanes are not left idle at ray boundaries waiting for the
+// warp's slowest ray.  FETCH(k) returns the k-th ray; FINISH(k, hit, occluded)
+// stores its result.
+#ifndef AJG_REFILL
+#define AJG_REFILL 16
+#endif
+constexpr int kRefill = AJG_REFILL;
+
+template <int TEST, bool ANY, class FETCH, class FINISH>
+__device__ __forceinline__ void trace_persistent(
+    const DeviceScene& s, uint32_t n, uint32_t* next, FETCH fetch,
+    FINISH finish, uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris,
+    uint32_t* err) {
+  constexpr int kIdle = -1, kDone = 0x7fffffff;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  int k = kIdle;
+  RayQ r;
+  WtSetup w;
+  Hit hit;
+  int node = 0, sp = 0;
+  uint32_t visits = 0;
+  // a ray visits each node of the tree at most once
+  const uint32_t max_visits = s.num_inner + 1;
+  int stack_node[kStackSize];
+  float stack_t[kStackSize];
+  const float4* __restrict__ bvh = s.bvh;
+  const float4* __restrict__ tris = s.tris;
+  for (;;) {
+    const unsigned idle = __ballot_sync(full, k == kIdle);
+    const unsigned done = __ballot_sync(full, k == kDone);
+    if (idle && (__popc(idle) >= kRefill || (idle | done) == full)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(idle));
+      base = __shfl_sync(full, base, leader);
+      if (k == kIdle) {
+        const uint32_t kk = base + __popc(idle & lt);
+        if (kk < n) {
+          k = (int)kk;
+          r = fetch(kk);
+          if (TEST == AJG_TRI_WATERTIGHT) w = wt_setup(r);
+          hit.t = __int_as_float(0x7f800000);
+          hit.prim = -1;
+          hit.u = hit.v = 0.f;
+          node = 0;
+          sp = 0;
+          visits = 0;
+        } else {
+          k = kDone;
+        }
+      }
+    }
+    if (__all_sync(full, k == kDone)) break;
+    if (k < 0 || k == kDone) continue;
+
+    // one node visit
+    bool finished = false;
+    ++n_nodes;
+    if (++visits > max_visits) {
+      raise_device_error(err, kDevIterationBound);
+      finish((uint32_t)k, hit, hit.prim >= 0);
+      k = kIdle;
+      continue;
+    }
+    const float4 n0 = __ldg(bvh + 4 * node + 0);
+    const float4 n1 = __ldg(bvh + 4 * node + 1);
+    const float4 n2 = __ldg(bvh + 4 * node + 2);
+    const float4 n3 = __ldg(bvh + 4 * node + 3);
+    const float lim = ANY ? r.tmax : fminf(hit.t, r.tmax);
+    float tn0, tn1;
+    bool h0 = slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
+    bool h1 = slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
+    const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const bool hc = c == 0 ? h0 : h1;
+      const int rc = c == 0 ? r0 : r1;
+      if (hc && rc < 0 && !finished) {
+        const int slot = ~rc;
+        ++n_tris;
+        const float4 A = __ldg(tris + 3 * slot + 0);
+        const float4 B = __ldg(tris + 3 * slot + 1);
+        const float4 C = __ldg(tris + 3 * slot + 2);
+        float t, u, v;
+        const bool ok = TEST == AJG_TRI_WATERTIGHT
+                            ? wt_test(r, w, A, B, C, t, u, v)
+                            : mt_test(r, A, B, C, t, u, v);
+        if (ok) {
+          const int prim = __float_as_int(A.w);
+          if (ANY) {
+            hit.t = t;
+            hit.u = u;
+            hit.v = v;
+            hit.prim = prim;
+            finished = true;
+          } else if (t < hit.t || (t == hit.t && prim < hit.prim)) {
+            hit.t = t;
+            hit.u = u;
+            hit.v = v;
+            hit.prim = prim;
+          }
+        }
+      }
+      if (hc && rc < 0) {
+        if (c == 0)
+          h0 = false;
+        else
+          h1 = false;
+      }
+    }
+    if (!finished) {
+      if (h0 && h1) {
+        const bool first0 = tn0 <= tn1;
+        if (sp >= kStackSize) {
+          raise_device_error(err, kDevStackOverflow);
+          finished = true;
+        } else {
+          stack_node[sp] = first0 ? r1 : r0;
+          stack_t[sp] = first0 ? tn1 : tn0;
+          ++sp;
+          node = first0 ? r0 : r1;
+        }
+      } else if (h0) {
+        node = r0;
+      } else if (h1) {
+        node = r1;
+      } else {
+        // pop, skipping boxes a closer hit has since excluded
+        finished = true;
+        while (sp > 0) {
+          --sp;
+          const float lim2 = ANY ? r.tmax : fminf(hit.t, r.tmax);
+          if (stack_t[sp] <= lim2) {
+            node = stack_node[sp];
+            finished = false;
+            break;
+          }
+        }
+      }
+    }
+    if (finished) {
+      ++n_rays;
+      finish((uint32_t)k, hit, hit.prim >= 0);
+      k = kIdle;
+    }
+  }
+}
+
 __device__ __forceinline__ void flush_counters(TraceCounters* c, uint32_t rays,
                                                uint32_t nodes, uint32_t tris) {
   if (!c) return;

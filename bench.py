@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark of the PT-MIS / PLOC hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step" = one render job): the single-job plain GPU
+configuration -- a procedural icosphere at subdivision 8 (1,310,720
+triangles) radially displaced by 4-octave fBm of amplitude 0.15, on a
+2-triangle ground plane, seeded Disney parameters on the sphere and a
+Lambertian ground, a constant environment of 0.5 plus a directional light of
+2.0, 1024x1024, 256 samples per pixel, depth 16 (Russian roulette after
+bounce 5), PLOC search radius 16 with the tree built on the GPU.  The scene
+is synthetic and seeded.
+
+Printed on one JSON line:
+  value       Msamples/s of the job with the scene resident in HBM (the
+              BVH built once), timed with CUDA events on the launching
+              stream; the L2 is flushed (256 MiB write) between steps
+  e2e         the same metric through the C ABI with host buffers: every
+              step uploads the triangles, builds the PLOC tree on the GPU,
+              renders and copies the film back
+  roofline    the dominant traversal kernel: algorithmic bytes (nodes
+              visited x 64 B + triangles tested x 48 B, counted in-kernel)
+              per launch over its CUDA-event duration, against the measured
+              HBM copy bandwidth
+  cpu_baseline  the oracle (a C++ restatement of the reference's CPU path)
+              on the host cores, on a bounded sample of the same job
+With --gpus N (torchrun), every rank renders its own job (replicas: the path
+shards by job with no exchange), and value is the sum over ranks over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Msamples/s + p99 job latency, 1 GB300, batched/served vs plain at equal RMSE"
+WORKLOAD = ("single-job plain GPU: displaced icosphere subdiv 8 (1,310,720 tris) "
+            "+ 2-tri ground, Disney, 1024x1024, 256 spp, depth 16, PLOC r=16 built on the GPU")
+SPP, RES, DEPTH, MIN_B, RADIUS = 256, 1024, 16, 5, 16
+NODE_BYTES, TRI_BYTES = 64, 48
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--spp", type=int, default=SPP)
+    ap.add_argument("--res", type=int, default=RES)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload_scene(res):
+    from ajisai_render_gb300 import scenes as S
+    return S.flatten(S.icosphere_scene(subdiv=8, seed=0, width=res, height=res))
+
+
+def config(args):
+    return {"workload": WORKLOAD, "resolution": f"{args.res}x{args.res}", "spp": args.spp,
+            "max_depth": DEPTH, "min_bounces": MIN_B, "cont_prob": 0.9,
+            "ploc_search_radius": RADIUS, "triangles": 1310722, "sampler": "counter (seeded)",
+            "l2": "flushed between steps (256 MiB write)", "tri_test": "moller-trumbore"}
+
+
+# ----------------------------------------------------------------- clocks --
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names[1:], f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(kernel):
+    """DRAM bytes per launch of the kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    k = d.get(kernel)
+    return float(k["dram_bytes_per_launch"]) if k else None
+
+
+# ------------------------------------------------------------- CPU side --
+def cpu_sample(flat, seconds, threads, spp):
+    """Time the oracle on a bounded sample of the job: whole image rows spread
+    evenly over the film, as many as fit the time budget."""
+    from oracle import pyoracle as O
+    sc = O.OracleScene(flat, RADIUS)
+    W = int(flat.camera[34])
+    H = int(flat.camera[35])
+    params = dict(spp=spp, min_bounces=MIN_B, max_bounces=DEPTH)
+    # calibrate on one row through the middle, then size the sample
+    t = time.perf_counter()
+    sc.render(flat.camera, params, seed=1, pixel_range=((H // 2) * W, (H // 2 + 1) * W),
+              threads=threads)
+    per_row = time.perf_counter() - t
+    nrows = int(max(1, min(H, seconds / max(per_row, 1e-6))))
+    rows = np.linspace(0, H - 1, nrows).round().astype(int)
+    t = time.perf_counter()
+    for y in rows:
+        sc.render(flat.camera, params, seed=1, pixel_range=(y * W, (y + 1) * W),
+                  threads=threads)
+    dt = time.perf_counter() - t
+    samples = len(rows) * W * spp
+    sc.close()
+    return samples / dt / 1e6, len(rows), dt
+
+
+def run_reference(args):
+    """The reference's CPU path on the host cores: the oracle port (the
+    reference's own build needs its x86 toolchain setup and sources, which
+    the GPU host does not have), all host threads, a bounded pixel sample of
+    the same job per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    flat = workload_scene(args.res)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_sample(flat, 0.5, threads, args.spp)
+    vals, npxs, secs = [], [], []
+    for _ in range(args.steps):
+        v, npx, dt = cpu_sample(flat, per_step, threads, args.spp)
+        vals.append(v)
+        npxs.append(npx)
+        secs.append(dt)
+    value = float(np.sum(np.array(npxs) * args.res * args.spp) / np.sum(secs) / 1e6)
+    sample = (f"{int(np.mean(npxs))} image rows spread over the film x {args.res} px x "
+              f"{args.spp} spp per step (about {per_step:.0f} s of CPU work), oracle port "
+              "of the reference path")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Msamples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(secs) * 1e3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)", "config": config(args),
+        "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}))
+
+
+# ------------------------------------------------------------- GPU side --
+def run_ours(args):
+    import torch
+
+    from ajisai_render_gb300 import api
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    flat = workload_scene(args.res)
+    W = H = args.res
+    samples_per_step = W * H * args.spp
+    ctx = api.Context(local)
+    scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
+    rend = api.PTRenderer(api.PTRendererArgs(spp=args.spp, min_bounces=MIN_B,
+                                             max_bounces=DEPTH), seed=1 + rank)
+    out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        rend.render_device(scene, flat.camera, out.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+
+    # timed region: exactly K steps
+    ctx.set_profiling(True)
+    ctx.stats(reset=True)
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        rend.render_device(scene, flat.camera, out.data_ptr(), stream.cuda_stream)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(np.sum(step_ms))
+    st = ctx.stats()
+    ctx.set_profiling(False)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * samples_per_step * args.steps / (total_ms / 1e3) / 1e6
+
+    # roofline of the dominant traversal kernel
+    kinds = {"closest": ("closest_ms", "closest_launches", "closest_nodes", "closest_tris",
+                         "k_extend"),
+             "any": ("any_ms", "any_launches", "any_nodes", "any_tris", "k_shadow")}
+    dom = max(kinds, key=lambda k: st[kinds[k][0]])
+    ms_k, l_k, n_k, t_k, kname = kinds[dom]
+    launches = max(1, st[l_k])
+    bytes_per_launch = (st[n_k] * NODE_BYTES + st[t_k] * TRI_BYTES) / launches
+    avg_ms = st[ms_k] / launches
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
+    peak, peak_kind = peaks()
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                "traffic": traffic_per_launch(kname),
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "avg_launch_ms": avg_ms, "launches": int(st[l_k]),
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel_time_share": st[ms_k] / max(1e-9, total_ms),
+                "rays_per_s": (st["closest_rays"] + st["any_rays"]) / (total_ms / 1e3)}
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h2d = (flat.tris.nbytes + flat.corner_n.nbytes + flat.tri_mat.nbytes +
+               flat.tri_flags.nbytes + flat.world.nbytes + flat.materials.nbytes +
+               flat.lights.nbytes)
+        d2h = W * H * 16
+        film = api.Film(W, H)
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s2 = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
+            rend.Render(s2, flat.camera, film)
+            s2.release()
+        dt = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": world * samples_per_step * args.steps / dt / 1e6,
+               "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": dt / args.steps * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, npx, dt = cpu_sample(flat, args.cpu_seconds, threads, args.spp)
+        cpu = {"value": v, "unit": "Msamples/s", "cores": threads, "kind": "port",
+               "sample": f"{npx} image rows spread over the film x {args.res} px x "
+                         f"{args.spp} spp ({dt:.1f} s), oracle port of the reference "
+                         "path, all host threads"}
+
+    img = out.float().cpu().numpy()
+    nonfinite = int((~np.isfinite(img)).any(-1).sum())
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene, no dataset)",
+            "config": config(args), "clocks": clk, "e2e": e2e, "roofline": roofline,
+            "cpu_baseline": cpu, "gpu_launches": int(st["kernel_launches"]),
+            "ploc_build_ms": scene.info()["build_ms"],
+            "kernel_ms_per_step": {"k_extend": st["closest_ms"] / args.steps,
+                                   "k_shadow": st["any_ms"] / args.steps,
+                                   "k_shade": st["shade_ms"] / args.steps},
+            "step_ms": step_ms, "nonfinite_pixels": nonfinite,
+            "impl": "ours"}))
+    scene.release()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

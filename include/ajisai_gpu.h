@@ -175,6 +175,11 @@ typedef struct ajg_stats {
   uint64_t nodes_visited, tris_tested; /* summed over both ray kinds */
   uint64_t closest_nodes, closest_tris, any_nodes, any_tris;
   uint64_t paths;
+  uint64_t kernel_launches;  /* kernels the library launched */
+  /* with ajg_set_profiling(ctx, 1): launches and summed device time
+   * (CUDA events on the launching stream) per kernel kind */
+  uint64_t closest_launches, any_launches, shade_launches;
+  double closest_ms, any_ms, shade_ms;
 } ajg_stats;
 
 /* ---- context --------------------------------------------------------- */
@@ -183,6 +188,9 @@ AJG_API int ajg_create_context(const ajg_config* cfg, ajg_ctx** out);
 AJG_API int ajg_destroy_context(ajg_ctx* ctx);
 AJG_API const char* ajg_last_error(ajg_ctx* ctx);
 AJG_API int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset);
+/* Time every traversal and shading launch with CUDA events (for roofline
+ * measurements; adds two event records per launch). */
+AJG_API int ajg_set_profiling(ajg_ctx* ctx, int enable);
 
 /* ---- scenes (PLOCAggregate::Build + DefaultScene) --------------------- */
 AJG_API int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,

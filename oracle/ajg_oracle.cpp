@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -503,14 +504,13 @@ bool trace_any(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
 }
 
 template <class F>
-void parallel_rows(int64_t n, int threads, F&& f) {
-  if (threads <= 1 || n < 64) {
+void parallel_rows(int64_t n, int threads, F&& f, int64_t chunk = 64) {
+  if (threads <= 1 || n < 2) {
     for (int64_t i = 0; i < n; ++i) f(i);
     return;
   }
   std::atomic<int64_t> next{0};
   std::vector<std::thread> pool;
-  const int64_t chunk = 64;
   for (int t = 0; t < threads; ++t)
     pool.emplace_back([&]() {
       for (;;) {
@@ -1311,28 +1311,32 @@ float orc_rng(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) {
   return key_float(path_key(seed, pixel, sample), dim);
 }
 
-int orc_render(const float* tris, const float* corner_n,
-               const int32_t* tri_mat, const int32_t* tri_flags, int64_t n_tris,
-               const float* materials, int32_t n_materials,
-               const float* lights, int32_t n_lights, const float* world,
-               const float* camera, const double* params, uint64_t seed,
-               int64_t pixel_begin, int64_t pixel_end, float* out_li,
-               double* out_film, int threads) {
-  if (n_tris < 1) return -1;
-  const int spp = (int)params[0];
-  const int min_b = (int)params[1], max_b = (int)params[2];
-  const float cont = (float)params[3];
-  const bool use_mis = params[4] != 0;
-  const int mode = (int)params[5];
-  const int64_t r = (int64_t)params[6];
-  const int W = (int)camera[34], H = (int)camera[35];
-
+struct OrcScene {
   std::vector<Node> nodes;
   std::vector<int64_t> perm;
-  if (!ploc_build(tris, n_tris, world, r, params[7] != 0, nodes, perm))
-    return -2;
   Scene s;
-  s.acc = Accel{tris, n_tris, nodes.data(), perm.data()};
+  double build_seconds = 0;
+};
+
+void* orc_scene_create(const float* tris, const float* corner_n,
+                       const int32_t* tri_mat, const int32_t* tri_flags,
+                       int64_t n_tris, const float* materials,
+                       int32_t n_materials, const float* lights,
+                       int32_t n_lights, const float* world,
+                       int64_t search_radius, int radix_compat, int tri_test) {
+  if (n_tris < 1) return nullptr;
+  auto* o = new OrcScene();
+  auto t0 = std::chrono::steady_clock::now();
+  if (!ploc_build(tris, n_tris, world, search_radius, radix_compat != 0,
+                  o->nodes, o->perm)) {
+    delete o;
+    return nullptr;
+  }
+  o->build_seconds = std::chrono::duration<double>(
+                         std::chrono::steady_clock::now() - t0)
+                         .count();
+  Scene& s = o->s;
+  s.acc = Accel{tris, n_tris, o->nodes.data(), o->perm.data()};
   s.corner_n = corner_n;
   s.tri_mat = tri_mat;
   s.tri_flags = tri_flags;
@@ -1344,33 +1348,53 @@ int orc_render(const float* tris, const float* corner_n,
   }
   Box wb = world_box(world);
   s.radius = length(wb.hi - box_center(wb));
-  s.mode = mode;
+  s.mode = tri_test;
+  return o;
+}
 
+void orc_scene_destroy(void* h) { delete static_cast<OrcScene*>(h); }
+
+double orc_scene_build_seconds(void* h) {
+  return static_cast<OrcScene*>(h)->build_seconds;
+}
+
+int orc_scene_render(void* h, const float* camera, const double* params,
+                     uint64_t seed, int64_t pixel_begin, int64_t pixel_end,
+                     float* out_li, double* out_film, int threads) {
+  const Scene& s = static_cast<OrcScene*>(h)->s;
+  const int spp = (int)params[0];
+  const int min_b = (int)params[1], max_b = (int)params[2];
+  const float cont = (float)params[3];
+  const bool use_mis = params[4] != 0;
+  const int W = (int)camera[34], H = (int)camera[35];
   const int64_t npix = (int64_t)W * H;
   if (pixel_end > npix) pixel_end = npix;
   const int64_t count = pixel_end - pixel_begin;
   std::vector<double> src(count > 0 ? 3 * count : 0, 0.0);
-  parallel_rows(count, threads, [&](int64_t k) {
-    int64_t p = pixel_begin + k;
-    int x = (int)(p % W), y = (int)(p / W);
-    double acc[3] = {0, 0, 0};
-    for (int smp = 0; smp < spp; ++smp) {
-      Rng rng{path_key(seed, (uint32_t)p, (uint32_t)smp)};
-      const float u = x + rng.next();
-      const float v = y + rng.next();
-      float l0 = rng.next(), l1 = rng.next();
-      Ray ray = camera_ray(camera, u, v, l0, l1);
-      V3 L = trace_path(s, ray, rng, min_b, max_b, cont, use_mis);
-      if (out_li) {
-        float* o = out_li + 3 * ((p - pixel_begin) * (int64_t)spp + smp);
-        o[0] = L.x; o[1] = L.y; o[2] = L.z;
-      }
-      acc[0] += L.x; acc[1] += L.y; acc[2] += L.z;
-    }
-    src[3 * k] = acc[0];
-    src[3 * k + 1] = acc[1];
-    src[3 * k + 2] = acc[2];
-  });
+  parallel_rows(
+      count, threads,
+      [&](int64_t k) {
+        int64_t p = pixel_begin + k;
+        int x = (int)(p % W), y = (int)(p / W);
+        double acc[3] = {0, 0, 0};
+        for (int smp = 0; smp < spp; ++smp) {
+          Rng rng{path_key(seed, (uint32_t)p, (uint32_t)smp)};
+          const float u = x + rng.next();
+          const float v = y + rng.next();
+          float l0 = rng.next(), l1 = rng.next();
+          Ray ray = camera_ray(camera, u, v, l0, l1);
+          V3 L = trace_path(s, ray, rng, min_b, max_b, cont, use_mis);
+          if (out_li) {
+            float* o = out_li + 3 * ((p - pixel_begin) * (int64_t)spp + smp);
+            o[0] = L.x; o[1] = L.y; o[2] = L.z;
+          }
+          acc[0] += L.x; acc[1] += L.y; acc[2] += L.z;
+        }
+        src[3 * k] = acc[0];
+        src[3 * k + 1] = acc[1];
+        src[3 * k + 2] = acc[2];
+      },
+      1);
   if (out_film) {
     /* Tile::AddSample's 2x2 footprint with the clamping merge: a sample at
      * (x, y) lands on (x-1..x, y-1..y), row/column -1 folding into 0. */
@@ -1390,6 +1414,24 @@ int orc_render(const float* tris, const float* corner_n,
     }
   }
   return 0;
+}
+
+int orc_render(const float* tris, const float* corner_n,
+               const int32_t* tri_mat, const int32_t* tri_flags, int64_t n_tris,
+               const float* materials, int32_t n_materials,
+               const float* lights, int32_t n_lights, const float* world,
+               const float* camera, const double* params, uint64_t seed,
+               int64_t pixel_begin, int64_t pixel_end, float* out_li,
+               double* out_film, int threads) {
+  void* h = orc_scene_create(tris, corner_n, tri_mat, tri_flags, n_tris,
+                             materials, n_materials, lights, n_lights, world,
+                             (int64_t)params[6], params[7] != 0,
+                             (int)params[5]);
+  if (!h) return -2;
+  int rc = orc_scene_render(h, camera, params, seed, pixel_begin, pixel_end,
+                            out_li, out_film, threads);
+  orc_scene_destroy(h);
+  return rc;
 }
 
 }  // extern "C"

@@ -102,6 +102,20 @@ int orc_render(const float* tris, const float* corner_n,
                int64_t pixel_begin, int64_t pixel_end, float* out_li,
                double* out_film, int threads);
 
+/* The same split in two: build once (PLOC tree), render many times.  The
+ * arrays passed to orc_scene_create must outlive the handle. */
+void* orc_scene_create(const float* tris, const float* corner_n,
+                       const int32_t* tri_mat, const int32_t* tri_flags,
+                       int64_t n_tris, const float* materials,
+                       int32_t n_materials, const float* lights,
+                       int32_t n_lights, const float* world,
+                       int64_t search_radius, int radix_compat, int tri_test);
+int orc_scene_render(void* scene, const float* camera, const double* params,
+                     uint64_t seed, int64_t pixel_begin, int64_t pixel_end,
+                     float* out_li, double* out_film, int threads);
+double orc_scene_build_seconds(void* scene);
+void orc_scene_destroy(void* scene);
+
 #ifdef __cplusplus
 }
 #endif

@@ -47,8 +47,63 @@ def lib():
                                  _f32p, C.c_int32, _f32p, C.c_int32, _f32p,
                                  _f32p, _f64p, C.c_uint64, C.c_int64,
                                  C.c_int64, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_scene_create.restype = C.c_void_p
+        L.orc_scene_create.argtypes = [_f32p, _f32p, _i32p, _i32p, C.c_int64, _f32p,
+                                       C.c_int32, _f32p, C.c_int32, _f32p,
+                                       C.c_int64, C.c_int, C.c_int]
+        L.orc_scene_render.argtypes = [C.c_void_p, _f32p, _f64p, C.c_uint64,
+                                       C.c_int64, C.c_int64, C.c_void_p,
+                                       C.c_void_p, C.c_int]
+        L.orc_scene_build_seconds.argtypes = [C.c_void_p]
+        L.orc_scene_build_seconds.restype = C.c_double
+        L.orc_scene_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
+
+
+class OracleScene:
+    """Oracle scene built once (PLOC on the CPU) and rendered many times."""
+
+    def __init__(self, flat, search_radius=14, radix_compat=False, tri_test=0):
+        self._keep = [_c(flat.tris, np.float32), _c(flat.corner_n, np.float32),
+                      _c(flat.tri_mat, np.int32), _c(flat.tri_flags, np.int32),
+                      _c(flat.materials, np.float32), _c(flat.lights, np.float32),
+                      _c(flat.world, np.float32)]
+        k = self._keep
+        self.h = lib().orc_scene_create(k[0], k[1], k[2], k[3], flat.n_tris, k[4],
+                                        k[4].shape[0], k[5], k[5].shape[0], k[6],
+                                        search_radius, int(radix_compat), tri_test)
+        if not self.h:
+            raise RuntimeError("orc_scene_create failed")
+        self.build_seconds = lib().orc_scene_build_seconds(self.h)
+
+    def render(self, camera, params, seed=0, pixel_range=None, per_sample=False,
+               threads=None):
+        cam = _c(camera, np.float32)
+        W, H = int(cam[34]), int(cam[35])
+        spp = int(params["spp"])
+        p = np.array([spp, params.get("min_bounces", 5), params.get("max_bounces", 10),
+                      params.get("cont_prob", 0.9), params.get("use_mis", 1), 0, 0, 0],
+                     np.float64)
+        b, e = pixel_range if pixel_range else (0, W * H)
+        li = np.zeros((e - b, spp, 3), np.float32) if per_sample else None
+        film = np.zeros((H, W, 4), np.float64)
+        rc = lib().orc_scene_render(self.h, cam, p, seed, b, e,
+                                    li.ctypes.data if li is not None else None,
+                                    film.ctypes.data, threads or threads_default())
+        assert rc == 0
+        return li, film
+
+    def close(self):
+        if self.h:
+            lib().orc_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def threads_default():

@@ -226,7 +226,19 @@ def test_bsdf_sample_matches_reference(ctx, golden):
     np.testing.assert_allclose(out[ok, 4:7], ref[ok, 4:7], rtol=0, atol=2e-5)
     lam = ok & (args[0][:, 0] == 0)
     dis = ok & (args[0][:, 0] == 1)
-    np.testing.assert_allclose(out[lam, :4], ref[lam, :4], rtol=1e-5, atol=1e-30)
+    # Lambertian: f = albedo/pi * |ns.wi|/|ng.wi| of each side's own sampled
+    # direction; the factor's 1/|ng.wi| amplifies the ulp-level direction
+    # differences, so compare after dividing the factor out
+    def factor(ng, ns, wi):
+        a = np.abs(np.sum(ng.astype(np.float64) * wi, axis=1))
+        b = np.abs(np.sum(ns.astype(np.float64) * wi, axis=1))
+        return np.where(a == 0, 1.0, b / np.where(a == 0, 1, a))
+    fg = factor(args[1][lam], args[2][lam], out[lam, 4:7])[:, None]
+    fr = factor(args[1][lam], args[2][lam], ref[lam, 4:7])[:, None]
+    np.testing.assert_allclose(out[lam, :3] / fg, ref[lam, :3] / fr, rtol=1e-5)
+    np.testing.assert_allclose(out[lam, 3], ref[lam, 3], rtol=1e-5)
+    close_l = np.isclose(out[lam, :4], ref[lam, :4], rtol=1e-5, atol=1e-30).all(1)
+    assert close_l.mean() > 0.98
     ev = ctx.bsdf_query(args[0][dis], args[1][dis], args[2][dis], args[3][dis],
                         ref[dis, 4:7], args[5][dis], np.zeros(dis.sum(), np.int32))
     np.testing.assert_allclose(ev[:, :4], ref[dis, :4], rtol=1e-5, atol=1e-30)
