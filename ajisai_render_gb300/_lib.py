@@ -111,6 +111,8 @@ SIGNATURES = {
     "ajg_render": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P], C.c_int),
     "ajg_render_device": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P, _P],
                           C.c_int),
+    "ajg_render_static": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P, _P],
+                          C.c_int),
     "ajg_render_samples": ([_P, C.POINTER(Camera), C.POINTER(RenderParams),
                             C.c_uint64, C.c_uint64, _P], C.c_int),
 }

@@ -578,27 +578,20 @@ static int ensure_arena(ajg_ctx* ctx, uint64_t P, int nt, char** base) {
   return AJG_OK;
 }
 
-int render_impl(ajg_scene* sc, const ajg_camera& cam,
-                const ajg_render_params& prm, float4* d_out,
-                uint64_t li_begin, uint64_t li_end, float* d_li,
-                cudaStream_t st) {
-  ajg_ctx* ctx = sc->ctx;
-  const DeviceScene& s = sc->d;
+static int check_render(ajg_ctx* ctx, const DeviceScene& s,
+                        const ajg_camera& cam, const ajg_render_params& prm) {
   if (cam.width == 0 || cam.height == 0 || prm.spp == 0)
     return fail(ctx, AJG_ERR_INVALID, "empty film or zero spp");
   if (prm.max_bounces < 0 || prm.max_bounces > 1024)
     return fail(ctx, AJG_ERR_INVALID, "max_bounces must be in [0, 1024]");
   if (s.num_lights > kMaxLights)
     return fail(ctx, AJG_ERR_UNSUPPORTED, "at most 15 lights");
-  const uint64_t npix_all = (uint64_t)cam.width * cam.height;
-  if (npix_all > (1ull << 31))
+  if ((uint64_t)cam.width * cam.height > (1ull << 31))
     return fail(ctx, AJG_ERR_INVALID, "film too large");
-  const int nt = (int)s.num_lights + 1;
-  const uint64_t P = ctx->wave_paths;
+  return AJG_OK;
+}
 
-  char* base = nullptr;
-  int rc = ensure_arena(ctx, P, nt, &base);
-  if (rc) return rc;
+static WaveBufs carve_wave(char* base, uint64_t P, int nt) {
   char* cur = base;
   WaveBufs w;
   w.thr = carve<float4>(cur, P);
@@ -617,24 +610,26 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
   w.sq_d = carve<float4>(cur, P * nt);
   w.lists = carve<uint32_t>(cur, P * 3);
   w.counts = carve<uint32_t>(cur, 8);
+  return w;
+}
 
-  // film
-  const bool fp64 = (prm.flags & AJG_RENDER_FP64_FILM) != 0;
-  float4 *fsum = nullptr, *fcomp = nullptr;
-  double* fsum64 = nullptr;
+// The sample loop of one render over zeroed film accumulators: waves of S
+// samples of a pixel range, the bounce loop per wave, the film update per
+// wave and the footprint resolve at the end.  `timers` enables the
+// profiling events of the traversal and shading launches.
+static void run_waves(ajg_scene* sc, const ajg_camera& cam,
+                      const ajg_render_params& prm, const WaveBufs& w,
+                      uint64_t P, float4* fsum, float4* fcomp, double* fsum64,
+                      float4* d_out, uint64_t li_begin, uint64_t li_end,
+                      float* d_li, cudaStream_t st, bool timers) {
+  ajg_ctx* ctx = sc->ctx;
+  const DeviceScene& s = sc->d;
+  const int nt = (int)s.num_lights + 1;
+  const uint64_t npix_all = (uint64_t)cam.width * cam.height;
   const bool want_film = d_out != nullptr;
-  if (want_film) {
-    if (fp64) {
-      if (cudaMallocAsync((void**)&fsum64, npix_all * 32, st) != cudaSuccess)
-        return fail(ctx, AJG_ERR_OOM, "device allocation failed (film)");
-      cudaMemsetAsync(fsum64, 0, npix_all * 32, st);
-    } else {
-      if (cudaMallocAsync((void**)&fsum, npix_all * 32, st) != cudaSuccess)
-        return fail(ctx, AJG_ERR_OOM, "device allocation failed (film)");
-      fcomp = fsum + npix_all;
-      cudaMemsetAsync(fsum, 0, npix_all * 32, st);
-    }
-  }
+  const int kc = timers ? kKindClosest : -1;
+  const int ka = timers ? kKindAny : -1;
+  const int ks = timers ? kKindShade : -1;
 
   WaveArgs a;
   a.s = s;
@@ -681,7 +676,7 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
         cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
         cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
         {
-          KernelTimer tm(ctx, st, kKindClosest);
+          KernelTimer tm(ctx, st, kc);
           if (s.tri_test == AJG_TRI_WATERTIGHT)
             k_extend<AJG_TRI_WATERTIGHT><<<trace_grid, 128, 0, st>>>(
                 s, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
@@ -697,24 +692,24 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
                                          &w.counts[4], (uint32_t)P);
         }
         if ((b == 0 || !a.use_mis) && s.env >= 0) {
-          KernelTimer tm(ctx, st, kKindShade);
+          KernelTimer tm(ctx, st, ks);
           k_shade_miss<<<gs, kShadeThreads, 0, st>>>(a, w, q, w.lists,
                                                      &w.counts[4]);
         }
         {
-          KernelTimer tm(ctx, st, kKindShade);
+          KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DIFFUSE><<<gs, kShadeThreads, 0, st>>>(
               a, w, b, q, w.lists + P, &w.counts[5], shadow_cap, ctx->d_error);
         }
         {
-          KernelTimer tm(ctx, st, kKindShade);
+          KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DISNEY><<<gs, kShadeThreads, 0, st>>>(
               a, w, b, q, w.lists + 2 * P, &w.counts[6], shadow_cap,
               ctx->d_error);
         }
         if (a.use_mis) {
           {
-            KernelTimer tm(ctx, st, kKindAny);
+            KernelTimer tm(ctx, st, ka);
             if (s.tri_test == AJG_TRI_WATERTIGHT)
               k_shadow<AJG_TRI_WATERTIGHT><<<trace_grid, 128, 0, st>>>(
                   s, w.sq_o, w.sq_d, &w.counts[2], &w.counts[3], w.term_vis,
@@ -744,10 +739,84 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
     KernelTimer{ctx, st, -1};
     k_resolve<<<grid_for(npix_all, 256, gs), 256, 0, st>>>(
         fsum, fcomp, fsum64, cam.width, cam.height, d_out);
-    if (fsum) cudaFreeAsync(fsum, st);
-    if (fsum64) cudaFreeAsync(fsum64, st);
   }
   ctx->paths_total += (unsigned long long)npix * prm.spp;
+}
+
+int render_impl(ajg_scene* sc, const ajg_camera& cam,
+                const ajg_render_params& prm, float4* d_out,
+                uint64_t li_begin, uint64_t li_end, float* d_li,
+                cudaStream_t st) {
+  ajg_ctx* ctx = sc->ctx;
+  const DeviceScene& s = sc->d;
+  int rc = check_render(ctx, s, cam, prm);
+  if (rc) return rc;
+  const int nt = (int)s.num_lights + 1;
+  const uint64_t P = ctx->wave_paths;
+  const uint64_t npix_all = (uint64_t)cam.width * cam.height;
+  char* base = nullptr;
+  rc = ensure_arena(ctx, P, nt, &base);
+  if (rc) return rc;
+  const WaveBufs w = carve_wave(base, P, nt);
+
+  // film accumulators: per pixel a float32 sum and Kahan compensation, or a
+  // float64 sum
+  const bool fp64 = (prm.flags & AJG_RENDER_FP64_FILM) != 0;
+  float4 *fsum = nullptr, *fcomp = nullptr;
+  double* fsum64 = nullptr;
+  if (d_out) {
+    if (fp64) {
+      if (cudaMallocAsync((void**)&fsum64, npix_all * 32, st) != cudaSuccess)
+        return fail(ctx, AJG_ERR_OOM, "device allocation failed (film)");
+      cudaMemsetAsync(fsum64, 0, npix_all * 32, st);
+    } else {
+      if (cudaMallocAsync((void**)&fsum, npix_all * 32, st) != cudaSuccess)
+        return fail(ctx, AJG_ERR_OOM, "device allocation failed (film)");
+      fcomp = fsum + npix_all;
+      cudaMemsetAsync(fsum, 0, npix_all * 32, st);
+    }
+  }
+  run_waves(sc, cam, prm, w, P, fsum, fcomp, fsum64, d_out, li_begin, li_end,
+            d_li, st, true);
+  if (fsum) cudaFreeAsync(fsum, st);
+  if (fsum64) cudaFreeAsync(fsum64, st);
+  return AJG_OK;
+}
+
+int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
+                      const ajg_render_params& prm, float4* d_out,
+                      cudaStream_t st, char* scratch, uint64_t bytes) {
+  ajg_ctx* ctx = sc->ctx;
+  const DeviceScene& s = sc->d;
+  int rc = check_render(ctx, s, cam, prm);
+  if (rc) return rc;
+  const int nt = (int)s.num_lights + 1;
+  const uint64_t npix = (uint64_t)cam.width * cam.height;
+  const uint64_t film_bytes = ((npix * 32 + 255) / 256) * 256;
+  const uint64_t min_wave = wave_bytes(1024, nt);
+  if (film_bytes + min_wave > bytes)
+    return fail(ctx, AJG_ERR_INVALID,
+                "film of " + std::to_string(npix) + " pixels needs " +
+                    std::to_string(film_bytes + min_wave) +
+                    " bytes of scratch; the static scratch holds " +
+                    std::to_string(bytes) + " (at most " +
+                    std::to_string((bytes - min_wave) / 32) + " pixels)");
+  uint64_t P = 1024;
+  while (wave_bytes(P + 1024, nt) + film_bytes <= bytes) P += 1024;
+  float4* fsum = nullptr;
+  float4* fcomp = nullptr;
+  double* fsum64 = nullptr;
+  // the scratch keeps the previous call's contents: zero the film
+  if (prm.flags & AJG_RENDER_FP64_FILM) {
+    fsum64 = reinterpret_cast<double*>(scratch);
+  } else {
+    fsum = reinterpret_cast<float4*>(scratch);
+    fcomp = fsum + npix;
+  }
+  cudaMemsetAsync(scratch, 0, npix * 32, st);
+  const WaveBufs w = carve_wave(scratch + film_bytes, P, nt);
+  run_waves(sc, cam, prm, w, P, fsum, fcomp, fsum64, d_out, 0, 0, nullptr, st,
+            false);
   return AJG_OK;
 }
 

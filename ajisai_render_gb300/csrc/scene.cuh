@@ -127,6 +127,11 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
                 const ajg_render_params& prm, float4* d_out,
                 uint64_t li_begin, uint64_t li_end, float* d_li,
                 cudaStream_t st);
+// The same render over caller-provided scratch (film accumulators first,
+// then one wave); allocates nothing.  Runs on `st`; no profiling events.
+int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
+                      const ajg_render_params& prm, float4* d_out,
+                      cudaStream_t st, char* scratch, uint64_t bytes);
 // trace.cu
 void launch_trace_closest(const DeviceScene& s, const ajg_ray* rays,
                           uint64_t n, ajg_hit* hits, uint32_t* next,

@@ -255,6 +255,21 @@ AJG_API int ajg_render(ajg_scene* scene, const ajg_camera* cam,
 AJG_API int ajg_render_device(ajg_scene* scene, const ajg_camera* cam,
                               const ajg_render_params* params,
                               float* d_out_rgbw, void* stream);
+/* Rendering that allocates nothing, for callers that cannot call cudaMalloc
+ * (device memory owned by another allocator or a fixed budget, or code that
+ * must not allocate while it runs).  No counterpart in the reference.
+ * Same result as ajg_render_device, asynchronous on `stream`, but the film
+ * accumulators and the wave state live in a 32 MiB static device array that
+ * every GPU loading this library keeps until exit: a film needs 32 bytes per
+ * pixel of it next to a wave of at least 1,024 paths, so films above about
+ * 1,000,000 pixels (1024x1024 does not fit; 512x512 does) are rejected with
+ * AJG_ERR_INVALID.  The first call on a device looks the array's address up
+ * and should come before any stream capture.  All calls on a device share
+ * the array: each clears what it needs, and calls whose GPU work overlaps
+ * (other streams, other contexts) race on it. */
+AJG_API int ajg_render_static(ajg_scene* scene, const ajg_camera* cam,
+                              const ajg_render_params* params,
+                              float* d_out_rgbw, void* stream);
 /* Per-sample radiance of pixels [pixel_begin, pixel_end): host
  * out_li [count][spp][3], for parity checks on small renders. */
 AJG_API int ajg_render_samples(ajg_scene* scene, const ajg_camera* cam,
