@@ -412,14 +412,16 @@ inline bool wt_test(const Ray& r, const WtRay& w, const float* tri,
  * 3.9.2), and an inclusive comparison against the current best t so that an
  * equal-t hit on a lower primitive index is never culled. */
 constexpr float kSlabWiden = 1.0000003576278687f; /* 1 + 2 * 3u/(1-3u) */
+/* fminf / fmaxf semantics (a NaN operand yields the other one), inline; the
+ * sign of a zero result may differ, which no comparison below can see */
+inline float nmin(float a, float b) { return (b < a || a != a) ? b : a; }
+inline float nmax(float a, float b) { return (a < b || a != a) ? b : a; }
 inline bool slab(const Box& b, const Ray& r, V3 inv, float tlimit) {
   float tx0 = (b.lo.x - r.o.x) * inv.x, tx1 = (b.hi.x - r.o.x) * inv.x;
   float ty0 = (b.lo.y - r.o.y) * inv.y, ty1 = (b.hi.y - r.o.y) * inv.y;
   float tz0 = (b.lo.z - r.o.z) * inv.z, tz1 = (b.hi.z - r.o.z) * inv.z;
-  float tn = std::fmax(std::fmax(std::fmin(tx0, tx1), std::fmin(ty0, ty1)),
-                       std::fmin(tz0, tz1));
-  float tf = std::fmin(std::fmin(std::fmax(tx0, tx1), std::fmax(ty0, ty1)),
-                       std::fmax(tz0, tz1));
+  float tn = nmax(nmax(nmin(tx0, tx1), nmin(ty0, ty1)), nmin(tz0, tz1));
+  float tf = nmin(nmin(nmax(tx0, tx1), nmax(ty0, ty1)), nmax(tz0, tz1));
   tf = tf * kSlabWiden;
   return tn <= tf && tn <= tlimit && tf >= r.tmin;
 }
@@ -427,6 +429,29 @@ inline bool slab(const Box& b, const Ray& r, V3 inv, float tlimit) {
 struct Hit {
   float t, u, v;
   int32_t prim;
+};
+
+/* Traversal stack: 256 entries inline, growing on the heap only for
+ * pathologically deep trees. */
+struct SmallStack {
+  int64_t inl[256];
+  std::vector<int64_t> heap;
+  int n = 0;
+  void push(int64_t v) {
+    if (n < 256)
+      inl[n] = v;
+    else
+      heap.push_back(v);
+    ++n;
+  }
+  int64_t pop() {
+    --n;
+    if (n < 256) return inl[n];
+    int64_t v = heap.back();
+    heap.pop_back();
+    return v;
+  }
+  bool empty() const { return n == 0; }
 };
 
 struct Accel {
@@ -456,20 +481,18 @@ Hit trace_closest(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
     return h;
   }
   V3 inv = mk(1.f / r.d.x, 1.f / r.d.y, 1.f / r.d.z);
-  std::vector<int64_t> st;
-  st.reserve(128);
-  st.push_back(0);
+  SmallStack st;
+  st.push(0);
   while (!st.empty()) {
-    int64_t k = st.back();
-    st.pop_back();
+    int64_t k = st.pop();
     const Node& nd = acc.nodes[k];
-    float lim = std::fmin(h.t, r.tmax);
+    float lim = nmin(h.t, r.tmax);
     if (!slab(nd.b, r, inv, lim)) continue;
     if (nd.count) {
       consider((int32_t)acc.perm[nd.first]);
     } else {
-      st.push_back(nd.first + 1);
-      st.push_back(nd.first);
+      st.push(nd.first + 1);
+      st.push(nd.first);
     }
   }
   return h;
@@ -484,20 +507,18 @@ bool trace_any(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
     return false;
   }
   V3 inv = mk(1.f / r.d.x, 1.f / r.d.y, 1.f / r.d.z);
-  std::vector<int64_t> st;
-  st.reserve(128);
-  st.push_back(0);
+  SmallStack st;
+  st.push(0);
   while (!st.empty()) {
-    int64_t k = st.back();
-    st.pop_back();
+    int64_t k = st.pop();
     const Node& nd = acc.nodes[k];
     if (!slab(nd.b, r, inv, r.tmax)) continue;
     if (nd.count) {
       if (tri_test(mode, r, w, acc.tris + 9 * acc.perm[nd.first], &t, &u, &v))
         return true;
     } else {
-      st.push_back(nd.first + 1);
-      st.push_back(nd.first);
+      st.push(nd.first + 1);
+      st.push(nd.first);
     }
   }
   return false;

@@ -23,7 +23,7 @@ ORACLE_SO = BUILD / "libajg_oracle.so"
 REF_SO = REF_OUT / "libajref.so"
 REFERENCE_ROOT = Path(os.environ.get("AJG_REFERENCE_ROOT", "/root/reference"))
 
-CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
+CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off",
             "-fno-fast-math", "-pthread"]
 
 
