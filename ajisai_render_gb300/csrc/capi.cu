@@ -48,11 +48,14 @@ int check_device(ajg_ctx* ctx) {
 }
 
 // Run work on the context stream ordered after `user`, and make `user` wait
-// for it: one arena per context, so work of a context never overlaps.
+// for it: one arena per context, so work of a context never overlaps.  A
+// NULL `user` is the legacy default stream (the context stream is
+// non-blocking, so it has to be joined explicitly like any other).
 struct StreamJoin {
   cudaStream_t ctx_s, user;
-  StreamJoin(cudaStream_t c, cudaStream_t u) : ctx_s(c), user(u) {
-    if (user && user != ctx_s) {
+  StreamJoin(cudaStream_t c, cudaStream_t u)
+      : ctx_s(c), user(u ? u : cudaStreamLegacy) {
+    if (user != ctx_s) {
       cudaEvent_t e;
       cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
       cudaEventRecord(e, user);
@@ -61,7 +64,7 @@ struct StreamJoin {
     }
   }
   ~StreamJoin() {
-    if (user && user != ctx_s) {
+    if (user != ctx_s) {
       cudaEvent_t e;
       cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
       cudaEventRecord(e, ctx_s);

@@ -225,7 +225,8 @@ AJG_API int ajg_trace_closest(ajg_scene* scene, const ajg_ray* rays,
                               uint64_t n, ajg_hit* hits);
 AJG_API int ajg_trace_any(ajg_scene* scene, const ajg_ray* rays, uint64_t n,
                           uint8_t* occluded);
-/* Device arrays, asynchronous on `stream` (a cudaStream_t, or NULL). */
+/* Device arrays, asynchronous on `stream` (a cudaStream_t; NULL is the legacy
+ * default stream). */
 AJG_API int ajg_trace_closest_device(ajg_scene* scene, const ajg_ray* d_rays,
                                      uint64_t n, ajg_hit* d_hits,
                                      void* stream);
