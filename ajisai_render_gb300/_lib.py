@@ -15,7 +15,11 @@ LIB_PATH = HERE / "_build" / "libajisai_gpu.so"
 AJG_OK = 0
 STATUS = {0: "AJG_OK", 1: "AJG_ERR_INVALID", 2: "AJG_ERR_CUDA", 3: "AJG_ERR_OOM",
           4: "AJG_ERR_UNSUPPORTED", 5: "AJG_ERR_DEVICE", 6: "AJG_ERR_NOT_FOUND",
-          7: "AJG_ERR_CANCELLED"}
+          7: "AJG_ERR_CANCELLED", 8: "AJG_ERR_TIMEOUT"}
+AJG_ERR_CANCELLED = 7
+AJG_ERR_TIMEOUT = 8
+JOB_STATES = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
+SCHED_FAIR, SCHED_FIFO = 0, 1
 
 
 class AjgError(RuntimeError):
@@ -81,6 +85,33 @@ class Stats(C.Structure):
             "closest_ms", "any_ms", "shade_ms")]
 
 
+class JobDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("params", RenderParams),
+                ("window", C.c_uint32 * 4), ("progress_spp", C.c_uint32),
+                ("reserved", C.c_uint32), ("out_rgbw", C.c_void_p),
+                ("d_out_rgbw", C.c_void_p)]
+
+
+class JobStatus(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("spp_done", C.c_uint32),
+                ("spp_total", C.c_uint32), ("updates", C.c_uint32),
+                ("error", C.c_int32), ("reserved", C.c_uint32),
+                ("submit_ms", C.c_double), ("start_ms", C.c_double),
+                ("first_result_ms", C.c_double), ("done_ms", C.c_double)]
+
+
+class ServeOpts(C.Structure):
+    _fields_ = [("policy", C.c_uint32), ("max_active_jobs", C.c_uint32),
+                ("inflight_waves", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "jobs_submitted", "jobs_done", "jobs_cancelled", "jobs_failed", "waves",
+        "paths", "results_delivered", "graph_builds", "kernel_launches",
+        "active_bytes")]
+
+
 assert C.sizeof(Material) == 64 and C.sizeof(Light) == 48
 assert C.sizeof(Camera) == 144 and C.sizeof(RenderParams) == 32
 
@@ -115,6 +146,18 @@ SIGNATURES = {
                           C.c_int),
     "ajg_render_samples": ([_P, C.POINTER(Camera), C.POINTER(RenderParams),
                             C.c_uint64, C.c_uint64, _P], C.c_int),
+    "ajg_serve_configure": ([_P, C.POINTER(ServeOpts)], C.c_int),
+    "ajg_submit": ([_P, C.POINTER(JobDesc), C.POINTER(C.c_uint64)], C.c_int),
+    "ajg_poll": ([_P, C.c_uint64, C.POINTER(JobStatus)], C.c_int),
+    "ajg_wait": ([_P, C.c_uint64, C.c_int32, C.POINTER(JobStatus)], C.c_int),
+    "ajg_job_read": ([_P, C.c_uint64, _P, C.POINTER(JobStatus)], C.c_int),
+    "ajg_cancel": ([_P, C.c_uint64], C.c_int),
+    "ajg_job_release": ([_P, C.c_uint64], C.c_int),
+    "ajg_render_batch": ([_P, C.POINTER(JobDesc), C.c_uint32, C.POINTER(JobStatus)],
+                         C.c_int),
+    "ajg_serve_get_stats": ([_P, C.POINTER(ServeStats)], C.c_int),
+    "ajg_image_rmse": ([_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, C.c_uint32,
+                        C.POINTER(C.c_double), C.POINTER(C.c_uint64)], C.c_int),
 }
 
 _lib = None

@@ -77,6 +77,55 @@ class Context:
                                            n, _ptr(out)))
         return out
 
+    # ---- request loop (ajg_submit / ajg_poll / ajg_wait / ajg_cancel) ----
+    def configure_serving(self, policy: str = "fair", max_active_jobs: int = 0,
+                          inflight_waves: int = 0):
+        pol = {"fair": _lib.SCHED_FAIR, "fifo": _lib.SCHED_FIFO}[policy]
+        o = _lib.ServeOpts(pol, max_active_jobs, inflight_waves, 0)
+        self.check(self.lib.ajg_serve_configure(self.h, C.byref(o)))
+
+    def submit(self, scene: "GpuScene", camera, renderer: "PTRenderer",
+               window=None, progress_spp: int = 0, host: bool = True,
+               d_out_ptr: int = 0) -> "RenderJob":
+        """Queue a render job; its result (window-sized Film) fills in as the
+        request loop delivers progressive and final results."""
+        desc, film = _job_desc(scene, camera, renderer, window, progress_spp, host,
+                               d_out_ptr)
+        jid = C.c_uint64()
+        self.check(self.lib.ajg_submit(self.h, C.byref(desc), C.byref(jid)))
+        return RenderJob(self, jid.value, film)
+
+    def render_batch(self, jobs) -> list:
+        """Blocking batch of (scene, camera, renderer[, window]) tuples; returns
+        [(Film, status dict)] in order."""
+        descs = (_lib.JobDesc * len(jobs))()
+        films = []
+        for i, j in enumerate(jobs):
+            scene, camera, renderer = j[:3]
+            window = j[3] if len(j) > 3 else None
+            d, film = _job_desc(scene, camera, renderer, window, 0, True, 0)
+            descs[i] = d
+            films.append(film)
+        st = (_lib.JobStatus * len(jobs))()
+        self.check(self.lib.ajg_render_batch(self.h, descs, len(jobs), st))
+        return [(films[i], _status(st[i])) for i in range(len(jobs))]
+
+    def serve_stats(self) -> dict:
+        s = _lib.ServeStats()
+        self.check(self.lib.ajg_serve_get_stats(self.h, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in s._fields_}
+
+    def image_rmse(self, d_a: int, d_b: int, width: int, height: int,
+                   stride_a: int | None = None, stride_b: int | None = None):
+        """FP64 RMSE of rgb / w between two device rgbw images (pointers);
+        returns (rmse, pixels compared)."""
+        r = C.c_double()
+        n = C.c_uint64()
+        self.check(self.lib.ajg_image_rmse(
+            self.h, C.c_void_p(d_a), stride_a or width, C.c_void_p(d_b),
+            stride_b or width, width, height, C.byref(r), C.byref(n)))
+        return r.value, n.value
+
     def camera_rays(self, camera36, raster):
         cam = camera_struct(camera36)
         r = np.ascontiguousarray(raster, F32).reshape(-1, 4)
@@ -282,3 +331,64 @@ class PTRenderer:
 
 def CreatePTRenderer(args: PTRendererArgs, seed: int = 0) -> PTRenderer:
     return PTRenderer(args, seed)
+
+
+def _status(st: _lib.JobStatus) -> dict:
+    d = {n: getattr(st, n) for n, _ in st._fields_}
+    d["state_name"] = _lib.JOB_STATES.get(st.state, str(st.state))
+    return d
+
+
+def _job_desc(scene: GpuScene, camera, renderer: PTRenderer, window, progress_spp,
+              host, d_out_ptr):
+    cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+    cam = camera_struct(cam36)
+    x0, y0, w, h = window if window else (0, 0, cam.width, cam.height)
+    d = _lib.JobDesc()
+    d.scene = scene.h.value if isinstance(scene.h, C.c_void_p) else scene.h
+    d.camera = cam
+    d.params = renderer.params()
+    d.window[:] = [x0, y0, w, h]
+    d.progress_spp = progress_spp
+    film = Film(w, h) if host else None
+    d.out_rgbw = film.rgbw.ctypes.data if film is not None else None
+    d.d_out_rgbw = d_out_ptr or None
+    return d, film
+
+
+class RenderJob:
+    """A job of the context's request loop.  `film` (host results) is
+    rewritten in place with every delivered result."""
+
+    def __init__(self, ctx: Context, job_id: int, film: Film | None):
+        self.ctx, self.id, self.film = ctx, job_id, film
+
+    def poll(self) -> dict:
+        st = _lib.JobStatus()
+        self.ctx.check(self.ctx.lib.ajg_poll(self.ctx.h, self.id, C.byref(st)))
+        return _status(st)
+
+    def wait(self, timeout_ms: int = -1) -> dict:
+        """Block until the job ends; returns its status (state_name 'done',
+        'cancelled' or 'failed'), or the running status on a timeout."""
+        st = _lib.JobStatus()
+        rc = self.ctx.lib.ajg_wait(self.ctx.h, self.id, timeout_ms, C.byref(st))
+        if rc not in (_lib.AJG_OK, _lib.AJG_ERR_CANCELLED, _lib.AJG_ERR_TIMEOUT) and \
+                st.state != 4:
+            self.ctx.check(rc)
+        return _status(st)
+
+    def read(self):
+        """(rgbw copy of the latest delivered result, status): consistent
+        with each other even while the job runs."""
+        st = _lib.JobStatus()
+        out = np.zeros_like(self.film.rgbw)
+        self.ctx.check(self.ctx.lib.ajg_job_read(self.ctx.h, self.id, _ptr(out),
+                                                 C.byref(st)))
+        return out, _status(st)
+
+    def cancel(self):
+        self.ctx.check(self.ctx.lib.ajg_cancel(self.ctx.h, self.id))
+
+    def release(self):
+        self.ctx.check(self.ctx.lib.ajg_job_release(self.ctx.h, self.id))

@@ -206,6 +206,7 @@ int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
 int ajg_destroy_context(ajg_ctx* ctx) {
   if (!ctx) return AJG_ERR_INVALID;
   cudaSetDevice(ctx->device);
+  server_shutdown(ctx);
   cudaStreamSynchronize(ctx->stream);
   for (auto& p : ctx->pending) {
     cudaEventDestroy(p.a);
@@ -451,8 +452,11 @@ int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
 int ajg_scene_release(ajg_scene* s) {
   if (!s) return AJG_ERR_INVALID;
   ajg_ctx* ctx = s->ctx;
+  if (s->jobs.load() > 0)
+    return fail(ctx, AJG_ERR_INVALID, "scene has unfinished jobs");
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  server_sync(ctx);
   for (void* p : s->allocations) cudaFree(p);
   if (ctx->resident_bytes >= s->info.device_bytes)
     ctx->resident_bytes -= s->info.device_bytes;

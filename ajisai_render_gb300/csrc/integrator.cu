@@ -2,16 +2,21 @@
 // (core/renderer/pt.cpp:98-311) split into per-bounce kernels over SoA
 // queues, driven by TiledIntegrator::Render's sample loop (pt.cpp:40-73).
 //
-// A wave holds S samples of a range of pixels (path p -> pixel pix0 + p / S,
-// sample s0 + p % S).  Per bounce:
+// A single-job wave holds S samples of a range of pixels (path p -> pixel
+// pix0 + p / S, sample s0 + p % S).  A multi-job wave holds chunks of many
+// jobs (each its own scene, camera, film and parameters; see Chunk); every
+// kernel exists in both forms (template flag MJ), and the multi-job form
+// reads the per-path job, scene and sampler key from the wave's tables.
+// Per bounce:
 //   trace_closest(queue) -> shade (NEE candidates, MIS-BSDF escape ray,
 //   continuation, Russian roulette for the next bounce) -> trace_any(shadow
 //   queue) -> accumulate (the direct-lighting sum in the reference's order)
 // Queues are compacted with warp-ballot appends; every kernel is a
 // grid-stride loop that reads its queue length from device memory, so a wave
-// needs no host synchronisation.  After the last bounce each pixel adds its
-// S samples to a Kahan-compensated float32 film (or a float64 one), and a
-// resolve pass applies the reference's 2x2 box footprint.
+// needs no host synchronisation and a multi-job wave is one captured graph.
+// After the last bounce each pixel adds its S samples to a Kahan-compensated
+// float32 film (or a float64 one), and a resolve pass applies the
+// reference's 2x2 box footprint.
 //
 // Sampler dimensions per path (the reference's draw order, pt.cpp:58-61,
 // 107-108, 203-216, helper.h, directional_light.cpp:46, env_light.cpp:71):
@@ -22,6 +27,8 @@
 //   3 for the MIS BSDF sample, 3 for the continuation sample.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "shade.cuh"
@@ -31,54 +38,55 @@ namespace ajg {
 namespace {
 
 constexpr int kShadeThreads = 128;
+constexpr int kTraceThreads = 128;
 #ifndef AJG_SHADE_MIN_BLOCKS
 #define AJG_SHADE_MIN_BLOCKS 8
 #endif
 #ifndef AJG_TRACE_MIN_BLOCKS
 #define AJG_TRACE_MIN_BLOCKS 1
 #endif
-#ifndef AJG_TRACE_BLOCKS_PER_SM
-#define AJG_TRACE_BLOCKS_PER_SM 10
-#endif
 constexpr int kMaxLights = 15;
+constexpr unsigned kFull = 0xffffffffu;
 
 struct WaveArgs {
   DeviceScene s;
   ajg_camera cam;
-  uint64_t seed;
+  JobParams j;
   uint32_t pix0, S, s0, n_paths;
-  int32_t min_b, max_b;
-  float cont;
-  int use_mis;
-  int nd;  // draws per bounce without the roulette draw
-  float4 env_rgb;  // scaler * texel of the scene's env light
-  int env_mass;    // the env light's Distribution2D::Pdf is nonzero
 };
 
-struct WaveBufs {
-  // by path
-  float4* thr;
-  float4* thr_shade;
-  float4* rad;
-  // by queue slot (double buffered)
-  uint32_t* qpath[2];
-  float4* ro[2];
-  float4* rd[2];
-  ajg_hit* hits;
-  // shadow terms: slot = path * (lights + 1) + term
-  float4* term_f;
-  uint8_t* term_vis;
-  float4* sq_o;  // o.xyz, t_max
-  float4* sq_d;  // d.xyz, slot bits
-  uint32_t* lists;   // [3][P]: queue slots of misses, Lambertian and
-                     // Disney hits
-  uint32_t* counts;  // [0],[1] path queues, [2] shadow queue, [3] shadow
-                     // fetch, [4..6] lists, [7] extend fetch
+// Where a kernel finds the job and the scene of a path: the kernel
+// arguments (single job) or the wave tables (multi-job).
+template <bool MJ>
+struct Src;
+template <>
+struct Src<false> {
+  static __device__ __forceinline__ const JobParams& job(const WaveArgs& a,
+                                                         const MJTables&,
+                                                         uint32_t) {
+    return a.j;
+  }
+  static __device__ __forceinline__ const DeviceScene& scene(
+      const WaveArgs& a, const MJTables&, uint32_t) {
+    return a.s;
+  }
+};
+template <>
+struct Src<true> {
+  static __device__ __forceinline__ const JobParams& job(const WaveArgs&,
+                                                         const MJTables& t,
+                                                         uint32_t jid) {
+    return t.jobs[jid].j;
+  }
+  static __device__ __forceinline__ const DeviceScene& scene(
+      const WaveArgs&, const MJTables& t, uint32_t jid) {
+    return t.scenes[t.jobs[jid].scene];
+  }
 };
 
-__device__ __forceinline__ int dim_base(const WaveArgs& a, int b) {
-  const int rr = b - a.min_b - 1;
-  return 4 + b * a.nd + (rr > 0 ? rr : 0);
+__device__ __forceinline__ int dim_base(const JobParams& J, int b) {
+  const int rr = b - J.min_b - 1;
+  return 4 + b * J.nd + (rr > 0 ? rr : 0);
 }
 
 __device__ __forceinline__ void path_id(const WaveArgs& a, uint32_t p,
@@ -87,49 +95,107 @@ __device__ __forceinline__ void path_id(const WaveArgs& a, uint32_t p,
   sample = a.s0 + p % a.S;
 }
 
-__global__ void k_set(uint32_t* c, uint32_t v) { *c = v; }
+// Last index c in [0, n) with off[c] <= v (off ascending, off[0] == 0).
+__device__ __forceinline__ uint32_t find_le(const uint32_t* off, uint32_t n,
+                                            uint32_t v) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (off[mid] <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
 
+// The camera sample of one path (pt.cpp:58-61) and the roulette before
+// bounce 0.
+__device__ __forceinline__ void raygen_path(const ajg_camera& cam,
+                                            const JobParams& J, uint64_t key,
+                                            int x, int y, F3& ro, F3& rd,
+                                            F3& T, bool& alive) {
+  const float u = x + key_float(key, 0);
+  const float v = y + key_float(key, 1);
+  const float l0 = key_float(key, 2), l1 = key_float(key, 3);
+  camera_ray(cam, u, v, l0, l1, ro, rd);
+  T = mk3(1.f, 1.f, 1.f);
+  alive = J.max_b > 0;
+  if (alive && 0 > J.min_b) {  // roulette before bounce 0
+    if (key_float(key, dim_base(J, 0)) > J.cont) alive = false;
+    T = T / J.cont;
+  }
+}
+
+template <bool MJ>
 __global__ void __launch_bounds__(kShadeThreads)
-    k_raygen(WaveArgs a, WaveBufs w) {
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n_paths;
+    k_raygen(WaveArgs a, MJTables t, WaveBufs w) {
+  __shared__ uint32_t s_off[MJ ? kMaxWaveChunks : 1];
+  uint32_t n_paths = a.n_paths, n_chunks = 0;
+  if constexpr (MJ) {
+    n_paths = t.hdr->n_paths;
+    n_chunks = t.hdr->n_chunks;
+    for (uint32_t c = threadIdx.x; c < n_chunks; c += blockDim.x)
+      s_off[c] = t.chunks[c].path_off;
+    __syncthreads();
+  }
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_paths;
        p += gridDim.x * blockDim.x) {
-    uint32_t pixel, sample;
-    path_id(a, p, pixel, sample);
-    const uint64_t key = path_key(a.seed, pixel, sample);
-    const int x = (int)(pixel % a.cam.width), y = (int)(pixel / a.cam.width);
-    const float u = x + key_float(key, 0);
-    const float v = y + key_float(key, 1);
-    const float l0 = key_float(key, 2), l1 = key_float(key, 3);
-    F3 ro, rd;
-    camera_ray(a.cam, u, v, l0, l1, ro, rd);
-    F3 T = mk3(1.f, 1.f, 1.f);
-    bool alive = a.max_b > 0;
-    if (alive && 0 > a.min_b) {  // roulette before bounce 0
-      if (key_float(key, dim_base(a, 0)) > a.cont) alive = false;
-      T = T / a.cont;
+    F3 ro, rd, T;
+    bool alive;
+    uint32_t sid = 0;
+    if constexpr (MJ) {
+      const Chunk C = t.chunks[find_le(s_off, n_chunks, p)];
+      const uint32_t q = p - C.path_off;
+      const uint32_t i = C.pix0 + q / C.S;
+      const uint32_t sample = C.s0 + q % C.S;
+      const JobRec& R = t.jobs[C.job];
+      const int x = (int)(R.j.x0 + i % R.j.win_w);
+      const int y = (int)(R.j.y0 + i / R.j.win_w);
+      const uint64_t key =
+          path_key(R.j.seed, (uint32_t)y * R.j.film_w + (uint32_t)x, sample);
+      w.pjob[p] = C.job;
+      w.pkey[p] = key;
+      sid = R.scene;
+      raygen_path(R.cam, R.j, key, x, y, ro, rd, T, alive);
+    } else {
+      uint32_t pixel, sample;
+      path_id(a, p, pixel, sample);
+      const uint64_t key = path_key(a.j.seed, pixel, sample);
+      const int x = (int)(pixel % a.cam.width), y = (int)(pixel / a.cam.width);
+      raygen_path(a.cam, a.j, key, x, y, ro, rd, T, alive);
     }
     w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
     w.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t k = warp_append(&w.counts[0], alive);
     if (alive) {
       w.qpath[0][k] = p;
-      w.ro[0][k] = make_float4(ro.x, ro.y, ro.z, 0.f);
+      w.ro[0][k] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(sid));
       w.rd[0][k] = make_float4(rd.x, rd.y, rd.z, 0.f);
     }
   }
 }
 
+__device__ __forceinline__ void retarget(TraceScene& ts, const MJTables& t,
+                                         uint32_t sid) {
+  const DeviceScene& sc = t.scenes[sid];
+  ts.bvh = sc.bvh;
+  ts.tris = sc.tris;
+  ts.max_visits = sc.num_inner + 1;
+}
+
 // Closest hits of the path queue.
-template <int TEST>
-__global__ void __launch_bounds__(128, AJG_TRACE_MIN_BLOCKS)
-    k_extend(DeviceScene s, const float4* __restrict__ ro,
+template <int TEST, bool MJ>
+__global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
+    k_extend(DeviceScene s, MJTables t, const float4* __restrict__ ro,
              const float4* __restrict__ rd, const uint32_t* __restrict__ count,
              uint32_t* fetch_next, ajg_hit* __restrict__ hits,
              TraceCounters* ctr, uint32_t* err) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k) {
+  auto fetch = [&](uint32_t k, TraceScene& ts) {
     const float4 o = ro[k], d = rd[k];
+    if constexpr (MJ) retarget(ts, t, __float_as_uint(o.w));
     return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
   };
   auto finish = [&](uint32_t k, const Hit& h, bool) {
@@ -140,15 +206,18 @@ __global__ void __launch_bounds__(128, AJG_TRACE_MIN_BLOCKS)
     o2.prim = h.prim;
     hits[k] = o2;
   };
-  trace_persistent<TEST, false>(s, n, fetch_next, fetch, finish, nr, nn, nt,
-                                err);
+  trace_persistent<TEST, false>(trace_scene(s), n, fetch_next, fetch, finish,
+                                nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
 // Files every queue slot under its hit's material type (or as a miss), so
 // that shading runs in material-specialised kernels; warps stay converged,
 // so each list append is one atomic per warp.
-__global__ void k_classify(DeviceScene s, const uint32_t* __restrict__ count,
+template <bool MJ>
+__global__ void k_classify(DeviceScene s, MJTables t,
+                           const float4* __restrict__ ro,
+                           const uint32_t* __restrict__ count,
                            const ajg_hit* __restrict__ hits,
                            uint32_t* __restrict__ lists,
                            uint32_t* __restrict__ list_counts,
@@ -164,9 +233,16 @@ __global__ void k_classify(DeviceScene s, const uint32_t* __restrict__ count,
       const int prim = hits[k].prim;
       cls = 0;
       if (prim >= 0) {
+        const float4* shade = s.shade;
+        const float* materials = s.materials;
+        if constexpr (MJ) {
+          const DeviceScene& sc = t.scenes[__float_as_uint(ro[k].w)];
+          shade = sc.shade;
+          materials = sc.materials;
+        }
         const uint32_t mat =
-            __float_as_uint(__ldg(&s.shade[prim].w)) & 0xffffffu;
-        cls = 1 + ((int)__ldg(s.materials + 16 * mat) == AJG_MAT_DISNEY);
+            __float_as_uint(__ldg(&shade[prim].w)) & 0xffffffu;
+        cls = 1 + ((int)__ldg(materials + 16 * mat) == AJG_MAT_DISNEY);
       }
     }
 #pragma unroll
@@ -177,30 +253,33 @@ __global__ void k_classify(DeviceScene s, const uint32_t* __restrict__ count,
   }
 }
 
-template <int TEST>
-__global__ void __launch_bounds__(128, AJG_TRACE_MIN_BLOCKS)
-    k_shadow(DeviceScene s, const float4* __restrict__ sq_o,
-             const float4* __restrict__ sq_d, const uint32_t* __restrict__ count,
-             uint32_t* fetch_next, uint8_t* __restrict__ vis,
-             TraceCounters* ctr, uint32_t* err) {
+template <int TEST, bool MJ>
+__global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
+    k_shadow(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
+             const float4* __restrict__ sq_d,
+             const uint16_t* __restrict__ sq_scene,
+             const uint32_t* __restrict__ count, uint32_t* fetch_next,
+             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k) {
+  auto fetch = [&](uint32_t k, TraceScene& ts) {
     const float4 o = sq_o[k], d = sq_d[k];
+    if constexpr (MJ) retarget(ts, t, sq_scene[k]);
     return make_query(xyz(o), xyz(d), kRayEps, o.w);
   };
   auto finish = [&](uint32_t k, const Hit&, bool occ) {
     if (!occ) vis[__float_as_uint(sq_d[k].w)] = 1;
   };
-  trace_persistent<TEST, true>(s, n, fetch_next, fetch, finish, nr, nn, nt,
-                               err);
+  trace_persistent<TEST, true>(trace_scene(s), n, fetch_next, fetch, finish,
+                               nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
+template <bool MJ>
 __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
-                                            bool pred, uint32_t cap,
-                                            uint32_t* err) {
+                                            uint32_t sid, bool pred,
+                                            uint32_t cap, uint32_t* err) {
   const uint32_t k = warp_append(&w.counts[2], pred);
   if (!pred) return;
   if (k >= cap) {
@@ -209,21 +288,32 @@ __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
   }
   w.sq_o[k] = make_float4(o.x, o.y, o.z, tmax);
   w.sq_d[k] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
+  if constexpr (MJ) w.sq_scene[k] = (uint16_t)sid;
 }
 
 // Escaped paths: the environment counts only for camera rays
-// (pt.cpp:114-121), or on every bounce without MIS (pt.cpp:245-249).
-__global__ void k_shade_miss(WaveArgs a, WaveBufs w, int cur,
-                             const uint32_t* __restrict__ list,
+// (pt.cpp:114-121), or on every bounce without MIS (pt.cpp:245-249).  The
+// single-job launch is skipped on the host when neither applies.
+template <bool MJ>
+__global__ void k_shade_miss(WaveArgs a, MJTables t, WaveBufs w, int b,
+                             int cur, const uint32_t* __restrict__ list,
                              const uint32_t* __restrict__ count) {
   const uint32_t n = *count;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n;
        j += gridDim.x * blockDim.x) {
     const uint32_t p = w.qpath[cur][list[j]];
+    float4 env = a.j.env_rgb;
+    if constexpr (MJ) {
+      const uint32_t jid = w.pjob[p];
+      const JobParams& J = t.jobs[jid].j;
+      if (!(b == 0 || !J.use_mis) || Src<true>::scene(a, t, jid).env < 0)
+        continue;
+      env = J.env_rgb;
+    }
     float4 L = w.rad[p];
-    L.x += a.env_rgb.x;
-    L.y += a.env_rgb.y;
-    L.z += a.env_rgb.z;
+    L.x += env.x;
+    L.y += env.y;
+    L.z += env.z;
     w.rad[p] = L;
   }
 }
@@ -231,15 +321,13 @@ __global__ void k_shade_miss(WaveArgs a, WaveBufs w, int cur,
 // Shading of the hits on one material type: NEE to every light
 // (helper.h:100-133), the MIS BSDF sample (helper.h:209-265), the
 // continuation sample (pt.cpp:215-223) and the next bounce's roulette.
-template <int MAT>
+template <int MAT, bool MJ>
 __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
-    k_shade(WaveArgs a, WaveBufs w, int b, int cur,
+    k_shade(WaveArgs a, MJTables t, WaveBufs w, int b, int cur,
             const uint32_t* __restrict__ list,
-            const uint32_t* __restrict__ list_count, uint32_t shadow_cap,
-            uint32_t* err) {
-  const DeviceScene& s = a.s;
+            const uint32_t* __restrict__ list_count, uint32_t NT,
+            uint32_t shadow_cap, uint32_t* err) {
   const uint32_t n = *list_count;
-  const int nt = (int)s.num_lights + 1;
   const int nxt = cur ^ 1;
   // warp-uniform loop: every lane of a warp runs the same iterations, so the
   // warp-wide queue appends see all lanes
@@ -249,19 +337,29 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
        wb += stride) {
     const uint32_t j = wb + lane;
     const bool hit = j < n;
-    uint32_t p = 0;
+    uint32_t p = 0, k = 0, jid = 0;
+    if (hit) {
+      k = list[j];
+      p = w.qpath[cur][k];
+      if constexpr (MJ) jid = w.pjob[p];
+    }
+    const JobParams& J = Src<MJ>::job(a, t, jid);
+    const DeviceScene& s = Src<MJ>::scene(a, t, jid);
+    const uint32_t sid = MJ ? t.jobs[jid].scene : 0u;
     HitInfo hi;
     BsdfT<MAT> f;
     F3 T = mk3(0, 0, 0);
     uint64_t key = 0;
     if (hit) {
-      const uint32_t k = list[j];
-      p = w.qpath[cur][k];
       const ajg_hit h = w.hits[k];
       const F3 ro = xyz(w.ro[cur][k]), rd = xyz(w.rd[cur][k]);
-      uint32_t pixel, sample;
-      path_id(a, p, pixel, sample);
-      key = path_key(a.seed, pixel, sample);
+      if constexpr (MJ) {
+        key = w.pkey[p];
+      } else {
+        uint32_t pixel, sample;
+        path_id(a, p, pixel, sample);
+        key = path_key(a.j.seed, pixel, sample);
+      }
       T = xyz(w.thr[p]);
       hi = complete_hit(s, ro, rd, h.t, h.u, h.v, h.prim);
       f.m = s.materials + 16 * hi.mat;
@@ -270,15 +368,26 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
       f.lum = __ldg(&s.mat_lum[hi.mat].x);
       w.thr_shade[p] = make_float4(T.x, T.y, T.z, 0.f);
     }
-    int dim = dim_base(a, b) + (b > a.min_b ? 1 : 0);
+    int dim = dim_base(J, b) + (b > J.min_b ? 1 : 0);
+    // lanes of a multi-job warp differ in lights and MIS: loop over the
+    // warp's maximum with the lanes past their own count idle
+    const int nl = (int)s.num_lights;
+    const bool mis = hit && J.use_mis;
+    int nl_loop = nl;
+    bool any_mis = J.use_mis != 0;
+    if constexpr (MJ) {
+      nl_loop = (int)__reduce_max_sync(kFull, mis ? (unsigned)nl : 0u);
+      any_mis = __any_sync(kFull, mis);
+    }
 
-    if (a.use_mis) {
-      for (int l = 0; l < (int)s.num_lights; ++l) {
-        const float* L = s.lights + 12 * l;
+    if (any_mis) {
+      for (int l = 0; l < nl_loop; ++l) {
+        const bool on = MJ ? (mis && l < nl) : hit;
+        const float* L = s.lights + 12 * (MJ ? (l < nl ? l : 0) : l);
         bool emit = false;
         F3 fo = mk3(0, 0, 0), so = mk3(0, 0, 0), sd = mk3(0, 0, 1);
         float tmax = 0.f;
-        if (hit) {
+        if (on) {
           F3 lpos, lrad;
           float lpdf;
           const int type = (int)L[0];
@@ -335,44 +444,46 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
               }
             }
           }
-          const uint32_t slot = p * nt + l;
+          const uint32_t slot = p * NT + l;
           w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
           w.term_vis[slot] = 0;
         }
-        emit_shadow(w, so, sd, tmax, p * nt + l, emit, shadow_cap, err);
-        dim += 2;
+        emit_shadow<MJ>(w, so, sd, tmax, p * NT + l, sid, emit, shadow_cap,
+                        err);
+        if (on) dim += 2;
       }
       {
+        const bool on = MJ ? mis : hit;
         bool emit = false;
         F3 fo = mk3(0, 0, 0), so = mk3(0, 0, 0), sd = mk3(0, 0, 1);
-        if (hit) {
+        if (on) {
           const F3 sam = mk3(key_float(key, dim), key_float(key, dim + 1),
                              key_float(key, dim + 2));
           BsdfSample bs = f.sample(hi.wr, sam);
           if (!(black3(bs.f) || bs.pdf == 0.f) && s.env >= 0) {
             bs.dir = normalize3(bs.dir);
             make_ray(eps_offset(hi, bs.dir), bs.dir, so, sd);
-            const F3 rad = mk3(a.env_rgb.x, a.env_rgb.y, a.env_rgb.z);
+            const F3 rad = mk3(J.env_rgb.x, J.env_rgb.y, J.env_rgb.z);
             if (!black3(rad)) {
               const F3 fv = rad * bs.f * fabsf(dot3(hi.ns, sd));
-              const float lp = env_pdf(a.env_mass != 0, sd);
+              const float lp = env_pdf(J.env_mass != 0, sd);
               fo = mk3(0, 0, 0) + fv / bs.pdf * power_heuristic(bs.pdf, lp);
               emit = true;
             }
           }
-          const uint32_t slot = p * nt + (nt - 1);
+          const uint32_t slot = p * NT + (NT - 1);
           w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
           w.term_vis[slot] = 0;
+          dim += 3;
         }
-        emit_shadow(w, so, sd, __int_as_float(0x7f800000), p * nt + (nt - 1),
-                    emit, shadow_cap, err);
-        dim += 3;
+        emit_shadow<MJ>(w, so, sd, __int_as_float(0x7f800000),
+                        p * NT + (NT - 1), sid, emit, shadow_cap, err);
       }
     }
 
     bool alive = false;
     F3 nro = mk3(0, 0, 0), nrd = mk3(0, 0, 1);
-    if (hit && b + 1 < a.max_b) {
+    if (hit && b + 1 < J.max_b) {
       const F3 sam = mk3(key_float(key, dim), key_float(key, dim + 1),
                          key_float(key, dim + 2));
       const BsdfSample bs = f.sample(hi.wr, sam);
@@ -380,11 +491,11 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
         T = T * (bs.f * fabsf(dot3(hi.ng, bs.dir)) / bs.pdf);
         make_ray(eps_offset(hi, bs.dir), bs.dir, nro, nrd);
         alive = true;
-        if (b + 1 > a.min_b) {
-          if (key_float(key, dim_base(a, b + 1)) > a.cont)
+        if (b + 1 > J.min_b) {
+          if (key_float(key, dim_base(J, b + 1)) > J.cont)
             alive = false;
           else
-            T = T / a.cont;
+            T = T / J.cont;
         }
       }
       w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
@@ -392,7 +503,7 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
     const uint32_t kn = warp_append(&w.counts[nxt], alive);
     if (alive) {
       w.qpath[nxt][kn] = p;
-      w.ro[nxt][kn] = make_float4(nro.x, nro.y, nro.z, 0.f);
+      w.ro[nxt][kn] = make_float4(nro.x, nro.y, nro.z, __uint_as_float(sid));
       w.rd[nxt][kn] = make_float4(nrd.x, nrd.y, nrd.z, 0.f);
     }
   }
@@ -400,18 +511,24 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
 
 // direct_illum += throughput * MISSampleLight(...) for each light, then
 // += throughput * MISSampleBsdf(...); pixel.value += direct (pt.cpp:200-213)
+template <bool MJ>
 __global__ void __launch_bounds__(kShadeThreads)
-    k_accumulate(WaveArgs a, WaveBufs w, int cur) {
+    k_accumulate(WaveArgs a, MJTables t, WaveBufs w, int cur, uint32_t NT) {
   const uint32_t n = w.counts[cur];
-  const int nt = (int)a.s.num_lights + 1;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += gridDim.x * blockDim.x) {
     if (w.hits[k].prim < 0) continue;
     const uint32_t p = w.qpath[cur][k];
+    int nl = (int)a.s.num_lights;
+    if constexpr (MJ) {
+      const JobParams& J = t.jobs[w.pjob[p]].j;
+      if (!J.use_mis) continue;
+      nl = J.nl;
+    }
     const F3 T = xyz(w.thr_shade[p]);
     F3 direct = mk3(0.f, 0.f, 0.f);
-    for (int j = 0; j < nt; ++j) {
-      const uint32_t slot = p * nt + j;
+    for (int j = 0; j <= nl; ++j) {
+      const uint32_t slot = p * NT + (j < nl ? (uint32_t)j : NT - 1);
       const F3 fv = w.term_vis[slot] ? xyz(w.term_f[slot]) : mk3(0, 0, 0);
       direct = direct + T * fv;
     }
@@ -424,59 +541,89 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
-// Each pixel adds its S samples in sample order (Kahan-compensated float32,
-// or float64).
-__global__ void k_film_add(WaveArgs a, const float4* __restrict__ rad,
-                           float4* __restrict__ sum, float4* __restrict__ comp,
-                           double* __restrict__ sum64, uint32_t n_pix,
-                           int drop_nonfinite) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pix;
-       i += gridDim.x * blockDim.x) {
-    const uint32_t pixel = a.pix0 + i;
-    if (sum64) {
-      double* o = sum64 + 4 * (uint64_t)pixel;
-      double x = o[0], y = o[1], z = o[2], wsum = o[3];
-      for (uint32_t j = 0; j < a.S; ++j) {
-        const float4 L = rad[(uint64_t)i * a.S + j];
-        if (drop_nonfinite &&
-            !(isfinite(L.x) && isfinite(L.y) && isfinite(L.z)))
-          continue;
-        x += L.x;
-        y += L.y;
-        z += L.z;
-        wsum += 1.0;
-      }
-      o[0] = x;
-      o[1] = y;
-      o[2] = z;
-      o[3] = wsum;
-      continue;
-    }
-    float4 s4 = sum[pixel], c4 = comp[pixel];
-    for (uint32_t j = 0; j < a.S; ++j) {
-      const float4 L = rad[(uint64_t)i * a.S + j];
+// Adds S consecutive samples to one film pixel in sample order
+// (Kahan-compensated float32, or float64).
+__device__ __forceinline__ void film_pixel(const float4* __restrict__ rad,
+                                           uint64_t base, uint32_t S,
+                                           uint64_t pixel, float4* sum,
+                                           float4* comp, double* sum64,
+                                           bool drop_nonfinite) {
+  if (sum64) {
+    double* o = sum64 + 4 * pixel;
+    double x = o[0], y = o[1], z = o[2], wsum = o[3];
+    for (uint32_t j = 0; j < S; ++j) {
+      const float4 L = rad[base + j];
       if (drop_nonfinite &&
           !(isfinite(L.x) && isfinite(L.y) && isfinite(L.z)))
         continue;
-      s4.w += 1.f;
-      float y, t;
-      y = L.x - c4.x; t = s4.x + y; c4.x = (t - s4.x) - y; s4.x = t;
-      y = L.y - c4.y; t = s4.y + y; c4.y = (t - s4.y) - y; s4.y = t;
-      y = L.z - c4.z; t = s4.z + y; c4.z = (t - s4.z) - y; s4.z = t;
+      x += L.x;
+      y += L.y;
+      z += L.z;
+      wsum += 1.0;
     }
-    sum[pixel] = s4;
-    comp[pixel] = c4;
+    o[0] = x;
+    o[1] = y;
+    o[2] = z;
+    o[3] = wsum;
+    return;
+  }
+  float4 s4 = sum[pixel], c4 = comp[pixel];
+  for (uint32_t j = 0; j < S; ++j) {
+    const float4 L = rad[base + j];
+    if (drop_nonfinite && !(isfinite(L.x) && isfinite(L.y) && isfinite(L.z)))
+      continue;
+    s4.w += 1.f;
+    float y, t;
+    y = L.x - c4.x; t = s4.x + y; c4.x = (t - s4.x) - y; s4.x = t;
+    y = L.y - c4.y; t = s4.y + y; c4.y = (t - s4.y) - y; s4.y = t;
+    y = L.z - c4.z; t = s4.z + y; c4.z = (t - s4.z) - y; s4.z = t;
+  }
+  sum[pixel] = s4;
+  comp[pixel] = c4;
+}
+
+// Each pixel of the wave adds its S samples in sample order.
+template <bool MJ>
+__global__ void k_film_add(WaveArgs a, MJTables t,
+                           const float4* __restrict__ rad,
+                           float4* __restrict__ sum, float4* __restrict__ comp,
+                           double* __restrict__ sum64, uint32_t n_pix) {
+  __shared__ uint32_t s_off[MJ ? kMaxWaveChunks : 1];
+  uint32_t n_chunks = 0;
+  if constexpr (MJ) {
+    n_pix = t.hdr->n_pix;
+    n_chunks = t.hdr->n_chunks;
+    for (uint32_t c = threadIdx.x; c < n_chunks; c += blockDim.x)
+      s_off[c] = t.chunks[c].pix_off;
+    __syncthreads();
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pix;
+       i += gridDim.x * blockDim.x) {
+    if constexpr (MJ) {
+      const Chunk C = t.chunks[find_le(s_off, n_chunks, i)];
+      const JobRec& R = t.jobs[C.job];
+      const uint32_t li = i - C.pix_off;
+      film_pixel(rad, C.path_off + (uint64_t)li * C.S, C.S, C.pix0 + li,
+                 R.fsum, R.fcomp, R.fsum64, R.j.drop_nonfinite != 0);
+    } else {
+      film_pixel(rad, (uint64_t)i * a.S, a.S, a.pix0 + i, sum, comp, sum64,
+                 a.j.drop_nonfinite != 0);
+    }
   }
 }
 
 // The reference's film convention (film.cpp:27-63, film.h:119-129,
 // image.h:38-42): a sample at (x, y) lands on (x-1..x, y-1..y) with weight
 // 1, and row/column -1 folds into 0.  Target (tx, ty) thus sums sources
-// tx (twice when tx == 0) and tx + 1, likewise in y.
+// tx (twice when tx == 0) and tx + 1, likewise in y.  For a window of the
+// image the fold applies only where the window starts at row/column 0, and
+// sources past the window are absent.  The four terms are summed in
+// double: the compensated float32 film carries more than float precision.
 __global__ void k_resolve(const float4* __restrict__ sum,
                           const float4* __restrict__ comp,
                           const double* __restrict__ sum64, uint32_t W,
-                          uint32_t H, float4* __restrict__ out) {
+                          uint32_t H, int fold_x, int fold_y,
+                          float4* __restrict__ out) {
   const uint64_t npix = (uint64_t)W * H;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < npix;
        i += (uint64_t)gridDim.x * blockDim.x) {
@@ -485,11 +632,11 @@ __global__ void k_resolve(const float4* __restrict__ sum,
     for (int dy = 0; dy < 2; ++dy) {
       const uint32_t sy = ty + dy;
       if (sy >= H) continue;
-      const int my = (dy == 0 && ty == 0) ? 2 : 1;
+      const int my = (dy == 0 && ty == 0 && fold_y) ? 2 : 1;
       for (int dx = 0; dx < 2; ++dx) {
         const uint32_t sx = tx + dx;
         if (sx >= W) continue;
-        const int mx = (dx == 0 && tx == 0) ? 2 : 1;
+        const int mx = (dx == 0 && tx == 0 && fold_x) ? 2 : 1;
         const uint64_t src = (uint64_t)sy * W + sx;
         double x, y, z, ww;
         if (sum64) {
@@ -542,11 +689,39 @@ T* carve(char*& cur, uint64_t count) {
   return p;
 }
 
-uint64_t wave_bytes(uint64_t P, int nt) {
+// Blocks of `fn` (launched with `threads` threads) that are resident on the
+// device at once: the grid of a persistent kernel.
+int resident_grid(const void* fn, int threads) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(fn, dev);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int sms = kSMs, per_sm = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int g = sms * per_sm;
+  cache[key] = g;
+  return g;
+}
+
+}  // namespace
+
+uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   const uint64_t slots = P * nt;
   uint64_t b = 0;
   auto add = [&](uint64_t bytes) { b += ((bytes + 255) / 256) * 256; };
   add(P * 16); add(P * 16); add(P * 16);  // thr, thr_shade, rad
+  if (mj) {
+    add(P * 4);  // pjob
+    add(P * 8);  // pkey
+  }
   add(P * 4); add(P * 4);      // qpath
   add(P * 16); add(P * 16);    // ro
   add(P * 16); add(P * 16);    // rd
@@ -554,17 +729,43 @@ uint64_t wave_bytes(uint64_t P, int nt) {
   add(slots * 16);             // term_f
   add(slots);                  // term_vis
   add(slots * 16); add(slots * 16);  // shadow queue
+  if (mj) add(slots * 2);      // sq_scene
   add(P * 4 * 3);              // material lists
   add(32);                     // counts
   return b;
 }
 
-}  // namespace
+WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj) {
+  char* cur = base;
+  WaveBufs w{};
+  w.thr = carve<float4>(cur, P);
+  w.thr_shade = carve<float4>(cur, P);
+  w.rad = carve<float4>(cur, P);
+  if (mj) {
+    w.pjob = carve<uint32_t>(cur, P);
+    w.pkey = carve<uint64_t>(cur, P);
+  }
+  w.qpath[0] = carve<uint32_t>(cur, P);
+  w.qpath[1] = carve<uint32_t>(cur, P);
+  w.ro[0] = carve<float4>(cur, P);
+  w.ro[1] = carve<float4>(cur, P);
+  w.rd[0] = carve<float4>(cur, P);
+  w.rd[1] = carve<float4>(cur, P);
+  w.hits = carve<ajg_hit>(cur, P);
+  w.term_f = carve<float4>(cur, P * nt);
+  w.term_vis = carve<uint8_t>(cur, P * nt);
+  w.sq_o = carve<float4>(cur, P * nt);
+  w.sq_d = carve<float4>(cur, P * nt);
+  if (mj) w.sq_scene = carve<uint16_t>(cur, P * nt);
+  w.lists = carve<uint32_t>(cur, P * 3);
+  w.counts = carve<uint32_t>(cur, 8);
+  return w;
+}
 
 // The wave arena: one device allocation reused across renders of the
 // context, grown when a render needs more paths or light terms.
 static int ensure_arena(ajg_ctx* ctx, uint64_t P, int nt, char** base) {
-  const uint64_t need = wave_bytes(P, nt);
+  const uint64_t need = wave_bytes(P, nt, false);
   if (ctx->arena.empty() || ctx->arena[0].bytes < need) {
     for (auto& b : ctx->arena) cudaFree(b.ptr);
     ctx->arena.clear();
@@ -578,8 +779,8 @@ static int ensure_arena(ajg_ctx* ctx, uint64_t P, int nt, char** base) {
   return AJG_OK;
 }
 
-static int check_render(ajg_ctx* ctx, const DeviceScene& s,
-                        const ajg_camera& cam, const ajg_render_params& prm) {
+int check_render(ajg_ctx* ctx, const DeviceScene& s, const ajg_camera& cam,
+                 const ajg_render_params& prm) {
   if (cam.width == 0 || cam.height == 0 || prm.spp == 0)
     return fail(ctx, AJG_ERR_INVALID, "empty film or zero spp");
   if (prm.max_bounces < 0 || prm.max_bounces > 1024)
@@ -591,26 +792,32 @@ static int check_render(ajg_ctx* ctx, const DeviceScene& s,
   return AJG_OK;
 }
 
-static WaveBufs carve_wave(char* base, uint64_t P, int nt) {
-  char* cur = base;
-  WaveBufs w;
-  w.thr = carve<float4>(cur, P);
-  w.thr_shade = carve<float4>(cur, P);
-  w.rad = carve<float4>(cur, P);
-  w.qpath[0] = carve<uint32_t>(cur, P);
-  w.qpath[1] = carve<uint32_t>(cur, P);
-  w.ro[0] = carve<float4>(cur, P);
-  w.ro[1] = carve<float4>(cur, P);
-  w.rd[0] = carve<float4>(cur, P);
-  w.rd[1] = carve<float4>(cur, P);
-  w.hits = carve<ajg_hit>(cur, P);
-  w.term_f = carve<float4>(cur, P * nt);
-  w.term_vis = carve<uint8_t>(cur, P * nt);
-  w.sq_o = carve<float4>(cur, P * nt);
-  w.sq_d = carve<float4>(cur, P * nt);
-  w.lists = carve<uint32_t>(cur, P * 3);
-  w.counts = carve<uint32_t>(cur, 8);
-  return w;
+JobParams make_job_params(const ajg_scene* sc, const ajg_camera& cam,
+                          const ajg_render_params& prm) {
+  const DeviceScene& s = sc->d;
+  JobParams j{};
+  j.seed = prm.seed;
+  j.min_b = prm.min_bounces;
+  j.max_b = prm.max_bounces;
+  j.cont = prm.cont_prob;
+  j.use_mis = prm.use_mis ? 1 : 0;
+  j.nl = (int)s.num_lights;
+  j.nd = j.use_mis ? (2 * j.nl + 6) : 3;
+  j.env_rgb = make_float4(0, 0, 0, 0);
+  j.env_mass = 0;
+  if (s.env >= 0) {
+    const float* L = sc->host_lights.data() + 12 * s.env;
+    // EnvLight::Radiance = scaler * texel (env_light.cpp:65)
+    j.env_rgb = make_float4(L[8] * L[1], L[8] * L[2], L[8] * L[3], 0.f);
+    j.env_mass = L[11] != 0.f ? 1 : 0;
+  }
+  j.drop_nonfinite = (prm.flags & AJG_RENDER_DROP_NONFINITE) ? 1 : 0;
+  j.film_w = cam.width;
+  j.film_h = cam.height;
+  j.x0 = j.y0 = 0;
+  j.win_w = cam.width;
+  j.win_h = cam.height;
+  return j;
 }
 
 // The sample loop of one render over zeroed film accumulators: waves of S
@@ -630,24 +837,12 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const int kc = timers ? kKindClosest : -1;
   const int ka = timers ? kKindAny : -1;
   const int ks = timers ? kKindShade : -1;
+  const MJTables t{};
 
   WaveArgs a;
   a.s = s;
   a.cam = cam;
-  a.seed = prm.seed;
-  a.min_b = prm.min_bounces;
-  a.max_b = prm.max_bounces;
-  a.cont = prm.cont_prob;
-  a.use_mis = prm.use_mis ? 1 : 0;
-  a.nd = a.use_mis ? (2 * (int)s.num_lights + 6) : 3;
-  a.env_rgb = make_float4(0, 0, 0, 0);
-  a.env_mass = 0;
-  if (s.env >= 0) {
-    const float* L = sc->host_lights.data() + 12 * s.env;
-    // EnvLight::Radiance = scaler * texel (env_light.cpp:65)
-    a.env_rgb = make_float4(L[8] * L[1], L[8] * L[2], L[8] * L[3], 0.f);
-    a.env_mass = L[11] != 0.f ? 1 : 0;
-  }
+  a.j = make_job_params(sc, cam, prm);
 
   const uint64_t pb = d_li ? li_begin : 0;
   const uint64_t pe = d_li ? li_end : npix_all;
@@ -656,8 +851,16 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const uint64_t chunk = std::min<uint64_t>(npix, P / S);
   const uint32_t shadow_cap = (uint32_t)(P * nt);
   const int gs = kSMs * 8;
-  // persistent traversal: resident blocks only (occupancy-limited)
-  const int trace_grid = kSMs * AJG_TRACE_BLOCKS_PER_SM;
+  const bool wt = s.tri_test == AJG_TRI_WATERTIGHT;
+  // persistent traversal: resident blocks only
+  const int g_ext = resident_grid(
+      wt ? (const void*)k_extend<AJG_TRI_WATERTIGHT, false>
+         : (const void*)k_extend<AJG_TRI_MOLLER_TRUMBORE, false>,
+      kTraceThreads);
+  const int g_shw = resident_grid(
+      wt ? (const void*)k_shadow<AJG_TRI_WATERTIGHT, false>
+         : (const void*)k_shadow<AJG_TRI_MOLLER_TRUMBORE, false>,
+      kTraceThreads);
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);
     for (uint64_t p0 = pb; p0 < pe; p0 += chunk) {
@@ -668,67 +871,75 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       a.n_paths = (uint32_t)(n_pix * Sw);
       cudaMemsetAsync(w.counts, 0, 32, st);
       KernelTimer{ctx, st, -1};
-      k_raygen<<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads, 0,
-                 st>>>(a, w);
+      k_raygen<false><<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads,
+                        0, st>>>(a, t, w);
       int q = 0;
-      for (int b = 0; b < a.max_b; ++b) {
+      for (int b = 0; b < a.j.max_b; ++b) {
         // next queue, shadow queue, fetch counters and material lists
         cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
         cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
         {
           KernelTimer tm(ctx, st, kc);
-          if (s.tri_test == AJG_TRI_WATERTIGHT)
-            k_extend<AJG_TRI_WATERTIGHT><<<trace_grid, 128, 0, st>>>(
-                s, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
-                &ctx->d_counters[0], ctx->d_error);
+          if (wt)
+            k_extend<AJG_TRI_WATERTIGHT, false>
+                <<<g_ext, kTraceThreads, 0, st>>>(
+                    s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7],
+                    w.hits, &ctx->d_counters[0], ctx->d_error);
           else
-            k_extend<AJG_TRI_MOLLER_TRUMBORE><<<trace_grid, 128, 0, st>>>(
-                s, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
-                &ctx->d_counters[0], ctx->d_error);
+            k_extend<AJG_TRI_MOLLER_TRUMBORE, false>
+                <<<g_ext, kTraceThreads, 0, st>>>(
+                    s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7],
+                    w.hits, &ctx->d_counters[0], ctx->d_error);
         }
         {
           KernelTimer tm(ctx, st, -1);
-          k_classify<<<gs, 256, 0, st>>>(s, &w.counts[q], w.hits, w.lists,
-                                         &w.counts[4], (uint32_t)P);
+          k_classify<false><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q],
+                                                w.hits, w.lists, &w.counts[4],
+                                                (uint32_t)P);
         }
-        if ((b == 0 || !a.use_mis) && s.env >= 0) {
+        if ((b == 0 || !a.j.use_mis) && s.env >= 0) {
           KernelTimer tm(ctx, st, ks);
-          k_shade_miss<<<gs, kShadeThreads, 0, st>>>(a, w, q, w.lists,
-                                                     &w.counts[4]);
+          k_shade_miss<false><<<gs, kShadeThreads, 0, st>>>(
+              a, t, w, b, q, w.lists, &w.counts[4]);
         }
         {
           KernelTimer tm(ctx, st, ks);
-          k_shade<AJG_MAT_DIFFUSE><<<gs, kShadeThreads, 0, st>>>(
-              a, w, b, q, w.lists + P, &w.counts[5], shadow_cap, ctx->d_error);
+          k_shade<AJG_MAT_DIFFUSE, false><<<gs, kShadeThreads, 0, st>>>(
+              a, t, w, b, q, w.lists + P, &w.counts[5], (uint32_t)nt,
+              shadow_cap, ctx->d_error);
         }
         {
           KernelTimer tm(ctx, st, ks);
-          k_shade<AJG_MAT_DISNEY><<<gs, kShadeThreads, 0, st>>>(
-              a, w, b, q, w.lists + 2 * P, &w.counts[6], shadow_cap,
-              ctx->d_error);
+          k_shade<AJG_MAT_DISNEY, false><<<gs, kShadeThreads, 0, st>>>(
+              a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)nt,
+              shadow_cap, ctx->d_error);
         }
-        if (a.use_mis) {
+        if (a.j.use_mis) {
           {
             KernelTimer tm(ctx, st, ka);
-            if (s.tri_test == AJG_TRI_WATERTIGHT)
-              k_shadow<AJG_TRI_WATERTIGHT><<<trace_grid, 128, 0, st>>>(
-                  s, w.sq_o, w.sq_d, &w.counts[2], &w.counts[3], w.term_vis,
-                  &ctx->d_counters[1], ctx->d_error);
+            if (wt)
+              k_shadow<AJG_TRI_WATERTIGHT, false>
+                  <<<g_shw, kTraceThreads, 0, st>>>(
+                      s, t, w.sq_o, w.sq_d, nullptr, &w.counts[2],
+                      &w.counts[3], w.term_vis, &ctx->d_counters[1],
+                      ctx->d_error);
             else
-              k_shadow<AJG_TRI_MOLLER_TRUMBORE><<<trace_grid, 128, 0, st>>>(
-                  s, w.sq_o, w.sq_d, &w.counts[2], &w.counts[3], w.term_vis,
-                  &ctx->d_counters[1], ctx->d_error);
+              k_shadow<AJG_TRI_MOLLER_TRUMBORE, false>
+                  <<<g_shw, kTraceThreads, 0, st>>>(
+                      s, t, w.sq_o, w.sq_d, nullptr, &w.counts[2],
+                      &w.counts[3], w.term_vis, &ctx->d_counters[1],
+                      ctx->d_error);
           }
           KernelTimer{ctx, st, -1};
-          k_accumulate<<<gs, kShadeThreads, 0, st>>>(a, w, q);
+          k_accumulate<false><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
+                                                            (uint32_t)nt);
         }
         q ^= 1;
       }
       if (want_film) KernelTimer{ctx, st, -1};
       if (want_film)
-        k_film_add<<<grid_for(n_pix, 256, gs), 256, 0, st>>>(
-            a, w.rad, fsum, fcomp, fsum64, (uint32_t)n_pix,
-            (prm.flags & AJG_RENDER_DROP_NONFINITE) ? 1 : 0);
+        k_film_add<false><<<grid_for(n_pix, 256, gs), 256, 0, st>>>(
+            a, t, w.rad, fsum, fcomp, fsum64, (uint32_t)n_pix);
       if (d_li) KernelTimer{ctx, st, -1};
       if (d_li)
         k_copy_li<<<grid_for(a.n_paths, 256, gs), 256, 0, st>>>(
@@ -738,9 +949,81 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   if (want_film) {
     KernelTimer{ctx, st, -1};
     k_resolve<<<grid_for(npix_all, 256, gs), 256, 0, st>>>(
-        fsum, fcomp, fsum64, cam.width, cam.height, d_out);
+        fsum, fcomp, fsum64, cam.width, cam.height, 1, 1, d_out);
   }
   ctx->paths_total += (unsigned long long)npix * prm.spp;
+}
+
+void prepare_mj_kernels() {
+  resident_grid((const void*)k_extend<AJG_TRI_WATERTIGHT, true>, kTraceThreads);
+  resident_grid((const void*)k_extend<AJG_TRI_MOLLER_TRUMBORE, true>,
+                kTraceThreads);
+  resident_grid((const void*)k_shadow<AJG_TRI_WATERTIGHT, true>, kTraceThreads);
+  resident_grid((const void*)k_shadow<AJG_TRI_MOLLER_TRUMBORE, true>,
+                kTraceThreads);
+}
+
+void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
+                     int NT, int bounces, int tri_test, TraceCounters* ctr,
+                     uint32_t* err, cudaStream_t st) {
+  const DeviceScene s{};
+  WaveArgs a{};
+  const uint32_t shadow_cap = (uint32_t)(P * NT);
+  const int gs = kSMs * 8;
+  const bool wt = tri_test == AJG_TRI_WATERTIGHT;
+  const int g_ext = resident_grid(
+      wt ? (const void*)k_extend<AJG_TRI_WATERTIGHT, true>
+         : (const void*)k_extend<AJG_TRI_MOLLER_TRUMBORE, true>,
+      kTraceThreads);
+  const int g_shw = resident_grid(
+      wt ? (const void*)k_shadow<AJG_TRI_WATERTIGHT, true>
+         : (const void*)k_shadow<AJG_TRI_MOLLER_TRUMBORE, true>,
+      kTraceThreads);
+  cudaMemsetAsync(w.counts, 0, 32, st);
+  k_raygen<true><<<gs, kShadeThreads, 0, st>>>(a, t, w);
+  int q = 0;
+  for (int b = 0; b < bounces; ++b) {
+    cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
+    cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
+    if (wt)
+      k_extend<AJG_TRI_WATERTIGHT, true><<<g_ext, kTraceThreads, 0, st>>>(
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
+          ctr, err);
+    else
+      k_extend<AJG_TRI_MOLLER_TRUMBORE, true><<<g_ext, kTraceThreads, 0, st>>>(
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
+          ctr, err);
+    k_classify<true><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q], w.hits,
+                                         w.lists, &w.counts[4], (uint32_t)P);
+    k_shade_miss<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, b, q, w.lists,
+                                                     &w.counts[4]);
+    k_shade<AJG_MAT_DIFFUSE, true><<<gs, kShadeThreads, 0, st>>>(
+        a, t, w, b, q, w.lists + P, &w.counts[5], (uint32_t)NT, shadow_cap,
+        err);
+    k_shade<AJG_MAT_DISNEY, true><<<gs, kShadeThreads, 0, st>>>(
+        a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
+        shadow_cap, err);
+    if (wt)
+      k_shadow<AJG_TRI_WATERTIGHT, true><<<g_shw, kTraceThreads, 0, st>>>(
+          s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[2], &w.counts[3],
+          w.term_vis, ctr + 1, err);
+    else
+      k_shadow<AJG_TRI_MOLLER_TRUMBORE, true><<<g_shw, kTraceThreads, 0, st>>>(
+          s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[2], &w.counts[3],
+          w.term_vis, ctr + 1, err);
+    k_accumulate<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
+                                                     (uint32_t)NT);
+    q ^= 1;
+  }
+  k_film_add<true><<<gs, 256, 0, st>>>(a, t, w.rad, nullptr, nullptr, nullptr,
+                                       0);
+}
+
+void enqueue_resolve(const float4* fsum, const float4* fcomp,
+                     const double* fsum64, uint32_t w, uint32_t h,
+                     bool fold_x, bool fold_y, float4* out, cudaStream_t st) {
+  k_resolve<<<grid_for((uint64_t)w * h, 256, kSMs * 8), 256, 0, st>>>(
+      fsum, fcomp, fsum64, w, h, fold_x ? 1 : 0, fold_y ? 1 : 0, out);
 }
 
 int render_impl(ajg_scene* sc, const ajg_camera& cam,
@@ -757,7 +1040,7 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
   char* base = nullptr;
   rc = ensure_arena(ctx, P, nt, &base);
   if (rc) return rc;
-  const WaveBufs w = carve_wave(base, P, nt);
+  const WaveBufs w = carve_wave(base, P, nt, false);
 
   // film accumulators: per pixel a float32 sum and Kahan compensation, or a
   // float64 sum
@@ -793,7 +1076,7 @@ int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
   const int nt = (int)s.num_lights + 1;
   const uint64_t npix = (uint64_t)cam.width * cam.height;
   const uint64_t film_bytes = ((npix * 32 + 255) / 256) * 256;
-  const uint64_t min_wave = wave_bytes(1024, nt);
+  const uint64_t min_wave = wave_bytes(1024, nt, false);
   if (film_bytes + min_wave > bytes)
     return fail(ctx, AJG_ERR_INVALID,
                 "film of " + std::to_string(npix) + " pixels needs " +
@@ -802,7 +1085,7 @@ int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
                     std::to_string(bytes) + " (at most " +
                     std::to_string((bytes - min_wave) / 32) + " pixels)");
   uint64_t P = 1024;
-  while (wave_bytes(P + 1024, nt) + film_bytes <= bytes) P += 1024;
+  while (wave_bytes(P + 1024, nt, false) + film_bytes <= bytes) P += 1024;
   float4* fsum = nullptr;
   float4* fcomp = nullptr;
   double* fsum64 = nullptr;
@@ -814,7 +1097,7 @@ int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
     fcomp = fsum + npix;
   }
   cudaMemsetAsync(scratch, 0, npix * 32, st);
-  const WaveBufs w = carve_wave(scratch + film_bytes, P, nt);
+  const WaveBufs w = carve_wave(scratch + film_bytes, P, nt, false);
   run_waves(sc, cam, prm, w, P, fsum, fcomp, fsum64, d_out, 0, 0, nullptr, st,
             false);
   return AJG_OK;

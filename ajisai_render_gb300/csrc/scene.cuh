@@ -1,5 +1,7 @@
 // Device-resident scene and the host objects behind the C ABI handles.
 #pragma once
+#include <atomic>
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -37,6 +39,86 @@ struct DeviceScene {
   int32_t tri_test = 0;
 };
 
+// Per-job constants of the integrator, shared by the single-job and the
+// multi-job waves.  The film of a job covers the window (x0, y0, win_w,
+// win_h) of a film_w x film_h image; the sampler keys by the image pixel
+// y * film_w + x, so a window renders exactly the samples the whole image
+// would render there.
+struct JobParams {
+  uint64_t seed;
+  int32_t min_b, max_b;
+  float cont;
+  int32_t use_mis;
+  int32_t nd;   // sampler draws per bounce without the roulette draw
+  int32_t nl;   // lights of the job's scene
+  float4 env_rgb;  // scaler * texel of the scene's env light
+  int32_t env_mass;  // the env light's Distribution2D::Pdf is nonzero
+  int32_t drop_nonfinite;
+  uint32_t film_w, film_h;
+  uint32_t x0, y0, win_w, win_h;
+};
+
+// Device record of a job in a multi-job wave.
+struct JobRec {
+  JobParams j;
+  ajg_camera cam;
+  uint32_t scene;  // index into the wave's scene table
+  uint32_t pad;
+  float4* fsum;    // film (window-sized): float32 sum + Kahan compensation
+  float4* fcomp;
+  double* fsum64;  // or a float64 sum
+};
+
+// One job's share of a wave: window pixels [pix0, pix0 + n_pix), samples
+// [s0, s0 + S) each; its paths are [path_off, path_off + n_pix * S) of the
+// wave (pixel-major) and its pixels [pix_off, pix_off + n_pix) of the
+// wave's film pass.
+struct Chunk {
+  uint32_t job, pix0, n_pix, S, s0, path_off, pix_off, pad;
+};
+
+// Header of the per-wave tables in device memory.
+struct WaveHeader {
+  uint32_t n_chunks, n_paths, n_pix, n_jobs;
+};
+
+constexpr int kMaxWaveChunks = 1024;
+
+// Device state of one wave (carved from a wave arena).
+struct WaveBufs {
+  // by path
+  float4* thr;
+  float4* thr_shade;
+  float4* rad;
+  uint32_t* pjob;  // multi-job waves: the path's job
+  uint64_t* pkey;  // multi-job waves: the path's sampler key
+  // by queue slot (double buffered); ro.w carries the scene index in
+  // multi-job waves
+  uint32_t* qpath[2];
+  float4* ro[2];
+  float4* rd[2];
+  ajg_hit* hits;
+  // light terms: slot = path * NT + term (lights first, the MIS BSDF term
+  // last at NT - 1)
+  float4* term_f;
+  uint8_t* term_vis;
+  float4* sq_o;  // shadow queue: o.xyz, t_max
+  float4* sq_d;  // d.xyz, slot bits
+  uint16_t* sq_scene;  // multi-job waves: scene index per shadow ray
+  uint32_t* lists;   // [3][P]: queue slots of misses, Lambertian and
+                     // Disney hits
+  uint32_t* counts;  // [0],[1] path queues, [2] shadow queue, [3] shadow
+                     // fetch, [4..6] lists, [7] extend fetch
+};
+
+// Tables of a multi-job wave in device memory.
+struct MJTables {
+  const DeviceScene* scenes;
+  const JobRec* jobs;
+  const Chunk* chunks;
+  const WaveHeader* hdr;
+};
+
 // Counters the traversal kernels accumulate (algorithmic bytes for the
 // roofline: nodes * 64 B + triangles * 48 B).
 struct TraceCounters {
@@ -60,8 +142,15 @@ struct PendingTiming {
 
 }  // namespace ajg
 
+namespace ajg {
+struct Server;
+}
+
 struct ajg_ctx {
   int device = 0;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  ajg::Server* server = nullptr;  // the request loop, started on first use
+  std::mutex server_mu;
   uint32_t wave_paths = 1u << 22;
   uint64_t hbm_budget = 0;
   uint64_t resident_bytes = 0;
@@ -90,6 +179,7 @@ struct ajg_scene {
   float4* ploc_nodes = nullptr;  // [2n-1][2]
   int32_t* perm = nullptr;       // [n]
   ajg_scene_info info{};
+  std::atomic<int> jobs{0};  // unfinished jobs of the request loop
   std::vector<float> host_lights;
   std::vector<float> host_materials;
 };
@@ -123,6 +213,27 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
                 const int32_t* h_flags, uint64_t n, const float* world,
                 const ajg_scene_opts& opts);
 // integrator.cu
+uint64_t wave_bytes(uint64_t P, int nt, bool mj);
+WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj);
+// Enqueues one multi-job wave on `st` (capturable: fixed arguments, queue
+// lengths and table contents read on the device): raygen, `bounces` bounce
+// iterations, film update.  NT = light terms per path of the arena.
+void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
+                     int NT, int bounces, int tri_test, TraceCounters* ctr,
+                     uint32_t* err, cudaStream_t st);
+// Kernels of a multi-job wave launched per wave (for launch counts).
+inline int mj_wave_kernels(int bounces) { return 2 + 7 * bounces; }
+// Looks up the persistent grids of the multi-job kernels (call before a
+// stream capture).
+void prepare_mj_kernels();
+// Resolves a window-sized film into (sum rgb, sum w) per target pixel.
+void enqueue_resolve(const float4* fsum, const float4* fcomp,
+                     const double* fsum64, uint32_t w, uint32_t h,
+                     bool fold_x, bool fold_y, float4* out, cudaStream_t st);
+int check_render(ajg_ctx* ctx, const DeviceScene& s, const ajg_camera& cam,
+                 const ajg_render_params& prm);
+JobParams make_job_params(const ajg_scene* sc, const ajg_camera& cam,
+                          const ajg_render_params& prm);
 int render_impl(ajg_scene* sc, const ajg_camera& cam,
                 const ajg_render_params& prm, float4* d_out,
                 uint64_t li_begin, uint64_t li_end, float* d_li,
@@ -132,6 +243,9 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
 int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
                       const ajg_render_params& prm, float4* d_out,
                       cudaStream_t st, char* scratch, uint64_t bytes);
+// serve.cu
+void server_shutdown(ajg_ctx* ctx);
+void server_sync(ajg_ctx* ctx);
 // trace.cu
 void launch_trace_closest(const DeviceScene& s, const ajg_ray* rays,
                           uint64_t n, ajg_hit* hits, uint32_t* next,

@@ -13,7 +13,7 @@ __global__ void __launch_bounds__(kTraceThreads)
                     uint64_t n, uint32_t* next, ajg_hit* __restrict__ hits,
                     TraceCounters* ctr, uint32_t* err) {
   uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t i) {
+  auto fetch = [&](uint32_t i, TraceScene&) {
     const ajg_ray q = rays[i];
     return make_query(mk3(q.o[0], q.o[1], q.o[2]), mk3(q.d[0], q.d[1], q.d[2]),
                       q.t_min, q.t_max);
@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(kTraceThreads)
     o.prim = h.prim;
     hits[i] = o;
   };
-  trace_persistent<TEST, false>(s, (uint32_t)n, next, fetch, finish, nr, nn,
+  trace_persistent<TEST, false>(trace_scene(s), (uint32_t)n, next, fetch, finish, nr, nn,
                                 nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
@@ -37,13 +37,13 @@ __global__ void __launch_bounds__(kTraceThreads)
                 uint32_t* next, uint8_t* __restrict__ occ, TraceCounters* ctr,
                 uint32_t* err) {
   uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t i) {
+  auto fetch = [&](uint32_t i, TraceScene&) {
     const ajg_ray q = rays[i];
     return make_query(mk3(q.o[0], q.o[1], q.o[2]), mk3(q.d[0], q.d[1], q.d[2]),
                       q.t_min, q.t_max);
   };
   auto finish = [&](uint32_t i, const Hit&, bool o) { occ[i] = o ? 1 : 0; };
-  trace_persistent<TEST, true>(s, (uint32_t)n, next, fetch, finish, nr, nn, nt,
+  trace_persistent<TEST, true>(trace_scene(s), (uint32_t)n, next, fetch, finish, nr, nn, nt,
                                err);
   flush_counters(ctr, nr, nn, nt);
 }

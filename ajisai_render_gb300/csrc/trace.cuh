@@ -242,11 +242,25 @@ __device__ __forceinline__ bool traverse(const DeviceScene& s, const RayQ& r,
 #endif
 constexpr int kRefill = AJG_REFILL;
 
+// The tree a ray is traced against.  FETCH(k, ts) may retarget `ts` per
+// ray (waves that mix scenes); single-scene callers leave it untouched.
+struct TraceScene {
+  const float4* bvh;
+  const float4* tris;
+  uint32_t max_visits;  // a ray visits each node of the tree at most once
+};
+__device__ __forceinline__ TraceScene trace_scene(const DeviceScene& s) {
+  TraceScene t;
+  t.bvh = s.bvh;
+  t.tris = s.tris;
+  t.max_visits = s.num_inner + 1;
+  return t;
+}
+
 template <int TEST, bool ANY, class FETCH, class FINISH>
 __device__ __forceinline__ void trace_persistent(
-    const DeviceScene& s, uint32_t n, uint32_t* next, FETCH fetch,
-    FINISH finish, uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris,
-    uint32_t* err) {
+    TraceScene ts, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
+    uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris, uint32_t* err) {
   constexpr int kIdle = -1, kDone = 0x7fffffff;
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -257,12 +271,8 @@ __device__ __forceinline__ void trace_persistent(
   Hit hit;
   int node = 0, sp = 0;
   uint32_t visits = 0;
-  // a ray visits each node of the tree at most once
-  const uint32_t max_visits = s.num_inner + 1;
   int stack_node[kStackSize];
   float stack_t[kStackSize];
-  const float4* __restrict__ bvh = s.bvh;
-  const float4* __restrict__ tris = s.tris;
   for (;;) {
     const unsigned idle = __ballot_sync(full, k == kIdle);
     const unsigned done = __ballot_sync(full, k == kDone);
@@ -275,7 +285,7 @@ __device__ __forceinline__ void trace_persistent(
         const uint32_t kk = base + __popc(idle & lt);
         if (kk < n) {
           k = (int)kk;
-          r = fetch(kk);
+          r = fetch(kk, ts);
           if (TEST == AJG_TRI_WATERTIGHT) w = wt_setup(r);
           hit.t = __int_as_float(0x7f800000);
           hit.prim = -1;
@@ -294,12 +304,14 @@ __device__ __forceinline__ void trace_persistent(
     // one node visit
     bool finished = false;
     ++n_nodes;
-    if (++visits > max_visits) {
+    if (++visits > ts.max_visits) {
       raise_device_error(err, kDevIterationBound);
       finish((uint32_t)k, hit, hit.prim >= 0);
       k = kIdle;
       continue;
     }
+    const float4* __restrict__ bvh = ts.bvh;
+    const float4* __restrict__ tris = ts.tris;
     const float4 n0 = __ldg(bvh + 4 * node + 0);
     const float4 n1 = __ldg(bvh + 4 * node + 1);
     const float4 n2 = __ldg(bvh + 4 * node + 2);

@@ -513,3 +513,89 @@ def icosphere_scene(subdiv: int = 8, seed: int = 0, width: int = 1024,
     cam = Camera((0.0, 0.6, 3.6), (0.0, -0.1, 0.0), (0.0, 1.0, 0.0), 40.0,
                  width, height)
     return Scene(prims, mats, lights, cam)
+
+
+# ------------------------------------------------------- mixed workloads --
+def _orbit_camera(rng: np.random.Generator, width: int, height: int,
+                  target=(0.0, -0.1, 0.0), dist: float = 3.6) -> Camera:
+    """Pinhole camera on a seeded sphere around the scene, looking at its
+    centre (azimuth U[0, 360), elevation U[5, 45] degrees)."""
+    az = np.radians(rng.uniform(0.0, 360.0))
+    el = np.radians(rng.uniform(5.0, 45.0))
+    t = np.asarray(target, np.float64)
+    pos = t + dist * np.array([np.cos(el) * np.sin(az), np.sin(el),
+                               np.cos(el) * np.cos(az)])
+    return Camera(tuple(pos), tuple(t), (0.0, 1.0, 0.0), 40.0, width, height)
+
+
+def clutter_meshes(n_cubes: int, rng: np.random.Generator, groups: int,
+                   extent: float = 1.0):
+    """Random-box clutter: n_cubes boxes (12 triangles each) with random
+    centres in [-extent, extent]^3, sizes and rotations about y, split into
+    `groups` meshes (one material each).  Returns [(positions, indices)]."""
+    c = rng.uniform(-extent, extent, (n_cubes, 3))
+    size = rng.uniform(0.02, 0.25, (n_cubes, 3)) * extent
+    ang = rng.uniform(0.0, 2 * np.pi, n_cubes)
+    corners = np.array([[x, y, z] for x in (-.5, .5) for y in (-.5, .5)
+                        for z in (-.5, .5)])                       # [8, 3]
+    # outward-facing triangles of the 8-corner box
+    faces = np.array([[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5],
+                      [0, 4, 5], [0, 5, 1], [2, 3, 7], [2, 7, 6],
+                      [0, 2, 6], [0, 6, 4], [1, 5, 7], [1, 7, 3]], np.int64)
+    local = corners[None] * size[:, None, :]                        # [n, 8, 3]
+    ca, sa = np.cos(ang)[:, None], np.sin(ang)[:, None]
+    x = local[..., 0] * ca + local[..., 2] * sa
+    z = -local[..., 0] * sa + local[..., 2] * ca
+    pos = np.stack([x, local[..., 1], z], -1) + c[:, None, :]      # [n, 8, 3]
+    out = []
+    for g in range(groups):
+        sel = np.arange(g, n_cubes, groups)
+        if not len(sel):
+            continue
+        p = pos[sel].reshape(-1, 3).astype(F32)
+        idx = (faces[None] + 8 * np.arange(len(sel))[:, None, None]).reshape(-1, 3)
+        out.append((p, idx.astype(np.int32)))
+    return out
+
+
+def mixed_scene(seed: int, target_tris: int, width: int, height: int) -> Scene:
+    """A scene of the batched/served workload: either a displaced icosphere
+    at the smallest subdivision with at least `target_tris` triangles (at
+    most subdivision 8), or random-box clutter of target_tris / 12 boxes in 16
+    material groups; Disney parameters drawn per object, a 2-triangle
+    Lambertian ground, a constant environment of 0.5 and a directional light
+    of 2.0, and a camera on a seeded sphere around the scene."""
+    rng = np.random.default_rng(seed)
+    prims, mats = [], []
+    if rng.uniform() < 0.5:
+        s = 0
+        while 20 * 4 ** s < target_tris and s < 8:
+            s += 1
+        pos, nrm, idx = displaced_icosphere(s, seed)
+        mats.append(disney_params(rng))
+        prims.append(Mesh(pos, idx, nrm, 0, False))
+    else:
+        for k, (p, idx) in enumerate(clutter_meshes(max(1, target_tris // 12), rng, 16)):
+            mats.append(disney_params(rng))
+            prims.append(Mesh(p, idx, None, k, False))
+    mats.append(Diffuse((0.5, 0.5, 0.5)))
+    g, y = 8.0, -1.2
+    prims.append(Quad((-g, y, g), (g, y, g), (g, y, -g), (-g, y, -g), len(mats) - 1, True))
+    lights = [DirectionalLight((0.3, 1.0, 0.2), 2.0), EnvLight(0.5)]
+    return Scene(prims, mats, lights, _orbit_camera(rng, width, height))
+
+
+def batch_workload(n: int = 48, seed: int = 0, resolutions=(128, 256, 512, 1024),
+                   spp_range=(16, 256), tri_range=(1_000, 2_000_000)):
+    """Job list of the batched workload: per job a scene seed, a triangle
+    count log-uniform in tri_range, a square resolution drawn from
+    `resolutions` and spp log-uniform in spp_range."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(n):
+        tris = int(round(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1])))))
+        res = int(rng.choice(resolutions))
+        spp = int(round(np.exp(rng.uniform(np.log(spp_range[0]), np.log(spp_range[1])))))
+        jobs.append({"scene_seed": int(seed * 1000 + i), "tris": tris, "res": res,
+                     "spp": spp})
+    return jobs

@@ -51,7 +51,8 @@ enum ajg_status {
                               queue capacity, iteration bound); the context
                               stays usable */
   AJG_ERR_NOT_FOUND = 6,   /* unknown job id */
-  AJG_ERR_CANCELLED = 7
+  AJG_ERR_CANCELLED = 7,
+  AJG_ERR_TIMEOUT = 8      /* ajg_wait: the job is still running */
 };
 
 /* Per-triangle PostIntersect rules, one set per mesh. */
@@ -271,6 +272,111 @@ AJG_API int ajg_render_device(ajg_scene* scene, const ajg_camera* cam,
 AJG_API int ajg_render_static(ajg_scene* scene, const ajg_camera* cam,
                               const ajg_render_params* params,
                               float* d_out_rgbw, void* stream);
+/* ---- batched rendering and serving ------------------------------------
+ * No counterpart in the reference, whose renderer runs one job per process
+ * (main.cpp:84-112).  Jobs -- each a scene, camera, film window, spp and
+ * parameters -- go to a per-context request loop that keeps scenes and
+ * films resident, admits jobs as the HBM budget (ajg_config) allows, and
+ * fills every wave of paths from many jobs at once: a wave carries chunks
+ * (pixel range x sample range) of up to 1,024 jobs over their own scenes,
+ * and its bounce loop is one CUDA graph launch.  Each pixel receives its
+ * samples in sample order, so a job's film is bit-identical to the same job
+ * rendered alone (ajg_render) or in any mix.  Progressive results: every
+ * `progress_spp` samples per pixel the job's window is resolved and
+ * delivered (host buffer and/or device buffer). */
+enum {
+  AJG_JOB_QUEUED = 0,    /* waiting for admission (HBM budget, job slots) */
+  AJG_JOB_RUNNING = 1,
+  AJG_JOB_DONE = 2,
+  AJG_JOB_CANCELLED = 3,
+  AJG_JOB_FAILED = 4
+};
+enum {
+  AJG_SCHED_FAIR = 0,  /* every wave splits its paths evenly between the
+                          running jobs (processor sharing) */
+  AJG_SCHED_FIFO = 1   /* every wave takes the oldest jobs' work first */
+};
+
+typedef struct ajg_job_desc {
+  ajg_scene* scene;
+  ajg_camera camera;
+  ajg_render_params params;
+  uint32_t window[4];     /* x0, y0, w, h of the rendered part of the film;
+                             w == 0 or h == 0: the whole film.  Results cover
+                             the window; a target pixel equals the whole
+                             render's where its 2x2 footprint sources lie in
+                             the window (all but a last row/column that does
+                             not end at the film's edge) */
+  uint32_t progress_spp;  /* deliver a result every this many samples per
+                             pixel (0: the final result only) */
+  uint32_t reserved;
+  float* out_rgbw;        /* host [h][w][4] (window), or NULL */
+  float* d_out_rgbw;      /* device [h][w][4] (window), or NULL; written in
+                             the request loop's stream order before the
+                             result is reported */
+} ajg_job_desc;
+
+typedef struct ajg_job_status {
+  uint32_t state;      /* AJG_JOB_* */
+  uint32_t spp_done;   /* samples per pixel of the last delivered result */
+  uint32_t spp_total;
+  uint32_t updates;    /* results delivered so far */
+  int32_t error;       /* AJG_OK, or the failure's status code */
+  uint32_t reserved;
+  /* host clock, milliseconds since the context was created */
+  double submit_ms, start_ms, first_result_ms, done_ms;
+} ajg_job_status;
+
+typedef struct ajg_serve_opts {
+  uint32_t policy;          /* AJG_SCHED_* */
+  uint32_t max_active_jobs; /* jobs holding films at once (<= 1024; 0: 256) */
+  uint32_t inflight_waves;  /* waves queued on the GPU ahead of the host
+                               (0: 2) */
+  uint32_t reserved;
+} ajg_serve_opts;
+
+typedef struct ajg_serve_stats {
+  uint64_t jobs_submitted, jobs_done, jobs_cancelled, jobs_failed;
+  uint64_t waves, paths, results_delivered, graph_builds;
+  uint64_t kernel_launches;
+  uint64_t active_bytes;  /* films and result buffers held now */
+} ajg_serve_stats;
+
+/* Scheduling options; takes effect for the waves planned after the call. */
+AJG_API int ajg_serve_configure(ajg_ctx* ctx, const ajg_serve_opts* opts);
+/* Queue a job; returns at once.  The job keeps `scene` in use until it ends
+ * (ajg_scene_release refuses a scene with unfinished jobs). */
+AJG_API int ajg_submit(ajg_ctx* ctx, const ajg_job_desc* job,
+                       uint64_t* job_id);
+AJG_API int ajg_poll(ajg_ctx* ctx, uint64_t job_id, ajg_job_status* out);
+/* Block until the job ends (AJG_OK when done, AJG_ERR_CANCELLED, the
+ * failure's code) or `timeout_ms` passes (AJG_ERR_TIMEOUT; < 0: forever). */
+AJG_API int ajg_wait(ajg_ctx* ctx, uint64_t job_id, int32_t timeout_ms,
+                     ajg_job_status* out);
+/* The job's latest delivered result (a copy of its host result buffer,
+ * taken while no result is being written into it; out_rgbw may be NULL)
+ * together with the matching status. */
+AJG_API int ajg_job_read(ajg_ctx* ctx, uint64_t job_id, float* out_rgbw,
+                         ajg_job_status* out);
+/* Stop a job: no further waves take its work; state CANCELLED once the
+ * waves already on the GPU retire. */
+AJG_API int ajg_cancel(ajg_ctx* ctx, uint64_t job_id);
+/* Forget an ended job's record. */
+AJG_API int ajg_job_release(ajg_ctx* ctx, uint64_t job_id);
+/* Blocking batch: submits every job, waits for all; status[i] per job (may
+ * be NULL).  Returns the first failing job's code. */
+AJG_API int ajg_render_batch(ajg_ctx* ctx, const ajg_job_desc* jobs,
+                             uint32_t n, ajg_job_status* status);
+AJG_API int ajg_serve_get_stats(ajg_ctx* ctx, ajg_serve_stats* out);
+
+/* Image error in FP64 on the device: RMSE over the pixels where both
+ * weights are positive of rgb / w, all three channels, between two device
+ * images [h][stride][4] (strides in pixels).  Blocking. */
+AJG_API int ajg_image_rmse(ajg_ctx* ctx, const float* d_a, uint32_t stride_a,
+                           const float* d_b, uint32_t stride_b,
+                           uint32_t width, uint32_t height, double* rmse,
+                           uint64_t* pixels);
+
 /* Per-sample radiance of pixels [pixel_begin, pixel_end): host
  * out_li [count][spp][3], for parity checks on small renders. */
 AJG_API int ajg_render_samples(ajg_scene* scene, const ajg_camera* cam,
