@@ -741,6 +741,9 @@ __global__ void k_rmse_partial(const float4* __restrict__ a, uint32_t sa,
     const uint32_t x = (uint32_t)(i % w), y = (uint32_t)(i / w);
     const float4 pa = a[(uint64_t)y * sa + x], pb = b[(uint64_t)y * sb + x];
     if (!(pa.w > 0.f) || !(pb.w > 0.f)) continue;
+    if (!(isfinite(pa.x) && isfinite(pa.y) && isfinite(pa.z) &&
+          isfinite(pb.x) && isfinite(pb.y) && isfinite(pb.z)))
+      continue;  // pixels holding a NaN or inf sample
     const double ia = 1.0 / pa.w, ib = 1.0 / pb.w;
     const double dx = pa.x * ia - pb.x * ib;
     const double dy = pa.y * ia - pb.y * ib;

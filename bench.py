@@ -63,6 +63,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-jobs", type=int, default=48)
+    ap.add_argument("--serve-jobs", type=int, default=64)
+    ap.add_argument("--serve-load", type=float, default=0.8,
+                    help="arrival rate as a fraction of the batched throughput")
+    ap.add_argument("--rmse-crop", type=int, default=32)
+    ap.add_argument("--rmse-spp", type=int, default=4096)
     return ap.parse_args()
 
 
@@ -323,6 +331,15 @@ def run_ours(args):
 
     img = out.float().cpu().numpy()
     nonfinite = int((~np.isfinite(img)).any(-1).sum())
+
+    batched = served = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        bctx = api.Context(local, hbm_budget_bytes=150 << 30)
+        batched = run_batched(bctx, args)
+        if not args.no_serve:
+            served = run_served(bctx, args, batched["_capacity"])
+        batched.pop("_capacity")
+        bctx.close()
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "Msamples/s", "n_gpus": world,
@@ -337,11 +354,167 @@ def run_ours(args):
                                    "k_shadow": st["any_ms"] / args.steps,
                                    "k_shade": st["shade_ms"] / args.steps},
             "step_ms": step_ms, "nonfinite_pixels": nonfinite,
+            "batched": batched, "served": served,
             "impl": "ours"}))
     scene.release()
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------- batched and served --
+BATCH_DEPTH = 12
+
+
+def _same_bits(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+
+def _cam(camera, w, h):
+    from ajisai_render_gb300 import scenes as S
+    return S.Camera(camera.position, camera.look_at, camera.up, camera.fov, w, h)
+
+
+def build_mix(ctx, n, seed):
+    """Scenes of the batched workload, resident on the GPU."""
+    from ajisai_render_gb300 import api
+    from ajisai_render_gb300 import scenes as S
+    jobs = S.batch_workload(n, seed=seed)
+    built, tris = [], 0
+    for j in jobs:
+        sc = S.mixed_scene(j["scene_seed"], j["tris"], j["res"], j["res"])
+        g = api.GpuScene(ctx, sc, api.CreatePLOCAggregate(RADIUS))
+        tris += g.flat.n_tris
+        built.append((g, sc.camera))
+    return jobs, built, tris
+
+
+def run_batched(ctx, args):
+    """The batched workload: the same jobs rendered one by one through
+    ajg_render (the plain single-job tracer) and as one ajg_render_batch;
+    both with host results.  Films must be identical bit for bit; each
+    image's RMSE against an FP64-accumulated render of a central crop."""
+    import torch
+    from ajisai_render_gb300 import api
+    t0 = time.perf_counter()
+    jobs, built, tris = build_mix(ctx, args.batch_jobs, seed=1)
+    gen_s = time.perf_counter() - t0
+    descs = []
+    for j, (g, cam) in zip(jobs, built):
+        r = api.PTRenderer(api.PTRendererArgs(spp=j["spp"], min_bounces=MIN_B,
+                                              max_bounces=BATCH_DEPTH), seed=7)
+        descs.append((g, _cam(cam, j["res"], j["res"]), r))
+    samples = sum(j["res"] ** 2 * j["spp"] for j in jobs)
+    ctx.configure_serving("fifo")
+    # warm both paths (arenas, graphs) on a small job
+    descs[0][2].Render(descs[0][0], _cam(descs[0][1], 16, 16))
+    ctx.render_batch([(descs[0][0], _cam(descs[0][1], 16, 16), descs[0][2])])
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain = [r.Render(g, cam) for g, cam, r in descs]
+    t_plain = time.perf_counter() - t
+    t = time.perf_counter()
+    batched = ctx.render_batch(descs)
+    t_batch = time.perf_counter() - t
+    identical = all(_same_bits(f.rgbw, p.rgbw) for (f, _), p in zip(batched, plain))
+    # FP64 references of a central crop (+1 row/column of footprint sources)
+    c = args.rmse_crop
+    refs = []
+    for (g, cam, r), j in zip(descs, jobs):
+        res = j["res"]
+        x0 = y0 = max(0, (res - c) // 2 - 1)
+        rr = api.PTRenderer(api.PTRendererArgs(spp=args.rmse_spp, min_bounces=MIN_B,
+                                               max_bounces=BATCH_DEPTH), seed=1234,
+                            fp64_film=True)
+        refs.append((g, cam, rr, (x0, y0, min(c + 1, res - x0), min(c + 1, res - y0))))
+    t = time.perf_counter()
+    ref_out = ctx.render_batch(refs)
+    t_ref = time.perf_counter() - t
+    rmse = []
+    for (film, _), (ref, _), (_, _, _, win) in zip(batched, ref_out, refs):
+        x0, y0, w, h = win
+        cw, ch = min(c, w), min(c, h)
+        a = torch.from_numpy(np.ascontiguousarray(film.rgbw[y0:y0 + ch, x0:x0 + cw])).cuda()
+        b = torch.from_numpy(np.ascontiguousarray(ref.rgbw[:ch, :cw])).cuda()
+        e, _ = ctx.image_rmse(a.data_ptr(), b.data_ptr(), cw, ch)
+        rmse.append(e)
+    rmse = np.array(rmse)
+    return {
+        "workload": f"{len(jobs)} jobs over their own scenes ({tris:,} triangles in all, "
+                    "displaced icospheres or random-box clutter, 1k-2M each), "
+                    "res {128,256,512,1024}^2, spp log-uniform 16-256, depth 12, Disney",
+        "samples": int(samples),
+        "batched_msamples_s": samples / t_batch / 1e6,
+        "plain_msamples_s": samples / t_plain / 1e6,
+        "speedup_vs_plain": t_plain / t_batch,
+        "batched_s": t_batch, "plain_s": t_plain,
+        "films_bit_identical": bool(identical),
+        "rmse_vs_fp64": {"crop": c, "reference_spp": args.rmse_spp,
+                         "median": float(np.median(rmse)), "max": float(rmse.max()),
+                         "min": float(rmse.min()), "equal_for_both_arms": bool(identical)},
+        "results": "host buffers (device-to-host copy of every film inside the timing)",
+        "scene_generation_and_build_s": gen_s, "reference_render_s": t_ref,
+        "_capacity": samples / t_batch,
+    }
+
+
+def run_served(ctx, args, capacity_samples_s):
+    """Poisson arrivals of render jobs over 8 resident scenes; progressive
+    results every 16 spp; latency from submission to the final result."""
+    from ajisai_render_gb300 import api
+    from ajisai_render_gb300 import scenes as S
+    jobs8, built, tris = build_mix(ctx, 8, seed=2)
+    rng = np.random.default_rng(5)
+    n = args.serve_jobs
+    plan = []
+    for i in range(n):
+        k = int(rng.integers(0, 8))
+        res = int(rng.choice([256, 512, 1024]))
+        spp = int(round(np.exp(rng.uniform(np.log(4), np.log(1024)))))
+        cam = S._orbit_camera(rng, res, res)
+        plan.append((k, res, spp, cam))
+    mean_samples = np.mean([r * r * s for _, r, s, _ in plan])
+    rate = args.serve_load * capacity_samples_s / mean_samples  # jobs per second
+    gaps = rng.exponential(1.0 / rate, n)
+    ctx.configure_serving("fair")
+    submitted = []
+    t0 = time.perf_counter()
+    at = 0.0
+    for (k, res, spp, cam), gap in zip(plan, gaps):
+        at += gap
+        dt = t0 + at - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        r = api.PTRenderer(api.PTRendererArgs(spp=spp, min_bounces=MIN_B,
+                                              max_bounces=BATCH_DEPTH), seed=i_seed(k, res, spp))
+        submitted.append(ctx.submit(built[k][0], cam, r, progress_spp=16))
+    sts = [j.wait() for j in submitted]
+    t_end = time.perf_counter()
+    for j in submitted:
+        j.release()
+    lat = np.array([s["done_ms"] - s["submit_ms"] for s in sts])
+    first = np.array([s["first_result_ms"] - s["submit_ms"] for s in sts])
+    done = sum(1 for s in sts if s["state_name"] == "done")
+    samples = sum(r * r * s for _, r, s, _ in plan)
+    span_ms = max(s["done_ms"] for s in sts) - min(s["submit_ms"] for s in sts)
+    return {
+        "workload": f"{n} jobs, Poisson arrivals at {args.serve_load:.0%} of the batched "
+                    f"throughput ({rate:.2f} jobs/s), 8 resident scenes ({tris:,} triangles), "
+                    "res {256,512,1024}^2, spp log-uniform 4-1024, camera on a seeded sphere, "
+                    "depth 12, progressive results every 16 spp, fair scheduling, "
+                    "HBM budget 150 GB",
+        "jobs_done": done,
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "mean_ms": float(lat.mean()),
+        "first_result_p50_ms": float(np.percentile(first, 50)),
+        "first_result_p99_ms": float(np.percentile(first, 99)),
+        "msamples_s": samples / (span_ms / 1e3) / 1e6,
+        "wall_s": t_end - t0,
+    }
+
+
+def i_seed(k, res, spp):
+    return (k * 1_000_003 + res * 101 + spp) & 0xffffffff
 
 
 def main():

@@ -369,9 +369,10 @@ AJG_API int ajg_render_batch(ajg_ctx* ctx, const ajg_job_desc* jobs,
                              uint32_t n, ajg_job_status* status);
 AJG_API int ajg_serve_get_stats(ajg_ctx* ctx, ajg_serve_stats* out);
 
-/* Image error in FP64 on the device: RMSE over the pixels where both
- * weights are positive of rgb / w, all three channels, between two device
- * images [h][stride][4] (strides in pixels).  Blocking. */
+/* Image error in FP64 on the device: RMSE of rgb / w, all three channels,
+ * between two device images [h][stride][4] (strides in pixels), over the
+ * pixels where both weights are positive and both sums finite (`pixels`
+ * returns how many; a pixel holding a NaN sample is left out).  Blocking. */
 AJG_API int ajg_image_rmse(ajg_ctx* ctx, const float* d_a, uint32_t stride_a,
                            const float* d_b, uint32_t stride_b,
                            uint32_t width, uint32_t height, double* rmse,

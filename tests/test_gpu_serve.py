@@ -277,9 +277,12 @@ def test_image_rmse_fp64(ctx):
     b = rng.uniform(0, 2, (37, 53, 4)).astype(np.float32)
     a[..., 3] = rng.integers(0, 3, (37, 53))
     b[..., 3] = rng.integers(1, 3, (37, 53))
+    a[3, 4, 1] = np.nan
+    b[9, 9, 0] = np.inf
     ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
     r, n = ctx.image_rmse(ta.data_ptr(), tb.data_ptr(), 53, 37)
-    m = (a[..., 3] > 0) & (b[..., 3] > 0)
+    m = (a[..., 3] > 0) & (b[..., 3] > 0) & np.isfinite(a[..., :3]).all(-1) & \
+        np.isfinite(b[..., :3]).all(-1)
     ia = a[..., :3].astype(np.float64) / np.where(m, a[..., 3], 1)[..., None]
     ib = b[..., :3].astype(np.float64) / np.where(m, b[..., 3], 1)[..., None]
     ref = np.sqrt(((ia - ib)[m] ** 2).mean())
