@@ -54,7 +54,7 @@ class Light(C.Structure):
 
 class SceneOpts(C.Structure):
     _fields_ = [("search_radius", C.c_uint32), ("tri_test", C.c_uint32),
-                ("radix_compat", C.c_uint32), ("reserved", C.c_uint32)]
+                ("radix_compat", C.c_uint32), ("bvh_width", C.c_uint32)]
 
 
 class Camera(C.Structure):
@@ -73,7 +73,8 @@ class RenderParams(C.Structure):
 class SceneInfo(C.Structure):
     _fields_ = [("num_triangles", C.c_uint64), ("num_nodes", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("ploc_iterations", C.c_uint32),
-                ("build_ms", C.c_float)]
+                ("build_ms", C.c_float), ("bvh_width", C.c_uint32),
+                ("bvh_node_bytes", C.c_uint32), ("bvh_nodes", C.c_uint64)]
 
 
 class Stats(C.Structure):

@@ -140,11 +140,12 @@ class AggregateOptions:
     search_radius: int = 14
     tri_test: int = 0          # 0 Moller-Trumbore (as the reference), 1 watertight
     radix_compat: bool = False  # reproduce the reference's Morton sort exactly
+    bvh_width: int = 0         # 2 binary PLOC tree, 4/8 collapsed; 0 default
 
 
 def CreatePLOCAggregate(search_radius: int = 14, tri_test: int = 0,
-                        radix_compat: bool = False) -> AggregateOptions:
-    return AggregateOptions(search_radius, tri_test, radix_compat)
+                        radix_compat: bool = False, bvh_width: int = 0) -> AggregateOptions:
+    return AggregateOptions(search_radius, tri_test, radix_compat, bvh_width)
 
 
 def camera_struct(camera36) -> _lib.Camera:
@@ -187,7 +188,8 @@ class GpuScene:
         agg = aggregate or AggregateOptions()
         flat = scene if isinstance(scene, FlatScene) else flatten(scene)
         self.flat = flat
-        opts = _lib.SceneOpts(agg.search_radius, agg.tri_test, int(agg.radix_compat), 0)
+        opts = _lib.SceneOpts(agg.search_radius, agg.tri_test, int(agg.radix_compat),
+                              agg.bvh_width)
         mats = _materials(flat.materials)
         lights = _lights(flat.lights)
         tris = np.ascontiguousarray(flat.tris, F32)

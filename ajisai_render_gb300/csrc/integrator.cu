@@ -185,7 +185,7 @@ __device__ __forceinline__ void retarget(TraceScene& ts, const MJTables& t,
 }
 
 // Closest hits of the path queue.
-template <int TEST, bool MJ>
+template <int TEST, bool MJ, int W>
 __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
     k_extend(DeviceScene s, MJTables t, const float4* __restrict__ ro,
              const float4* __restrict__ rd, const uint32_t* __restrict__ count,
@@ -206,8 +206,8 @@ __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
     o2.prim = h.prim;
     hits[k] = o2;
   };
-  trace_persistent<TEST, false>(trace_scene(s), n, fetch_next, fetch, finish,
-                                nr, nn, nt, err);
+  trace_persistent<TEST, false, W>(trace_scene(s), n, fetch_next, fetch,
+                                   finish, nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
@@ -253,7 +253,7 @@ __global__ void k_classify(DeviceScene s, MJTables t,
   }
 }
 
-template <int TEST, bool MJ>
+template <int TEST, bool MJ, int W>
 __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
     k_shadow(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
              const float4* __restrict__ sq_d,
@@ -270,8 +270,8 @@ __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
   auto finish = [&](uint32_t k, const Hit&, bool occ) {
     if (!occ) vis[__float_as_uint(sq_d[k].w)] = 1;
   };
-  trace_persistent<TEST, true>(trace_scene(s), n, fetch_next, fetch, finish,
-                               nr, nn, nt, err);
+  trace_persistent<TEST, true, W>(trace_scene(s), n, fetch_next, fetch,
+                                  finish, nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
@@ -851,16 +851,27 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const uint64_t chunk = std::min<uint64_t>(npix, P / S);
   const uint32_t shadow_cap = (uint32_t)(P * nt);
   const int gs = kSMs * 8;
-  const bool wt = s.tri_test == AJG_TRI_WATERTIGHT;
   // persistent traversal: resident blocks only
-  const int g_ext = resident_grid(
-      wt ? (const void*)k_extend<AJG_TRI_WATERTIGHT, false>
-         : (const void*)k_extend<AJG_TRI_MOLLER_TRUMBORE, false>,
-      kTraceThreads);
-  const int g_shw = resident_grid(
-      wt ? (const void*)k_shadow<AJG_TRI_WATERTIGHT, false>
-         : (const void*)k_shadow<AJG_TRI_MOLLER_TRUMBORE, false>,
-      kTraceThreads);
+  auto extend = [&](int q) {
+    dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
+      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+      const int g = resident_grid((const void*)k_extend<TT, false, WW>,
+                                  kTraceThreads);
+      k_extend<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
+          &ctx->d_counters[0], ctx->d_error);
+    });
+  };
+  auto shadow = [&]() {
+    dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
+      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+      const int g = resident_grid((const void*)k_shadow<TT, false, WW>,
+                                  kTraceThreads);
+      k_shadow<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
+          s, t, w.sq_o, w.sq_d, nullptr, &w.counts[2], &w.counts[3],
+          w.term_vis, &ctx->d_counters[1], ctx->d_error);
+    });
+  };
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);
     for (uint64_t p0 = pb; p0 < pe; p0 += chunk) {
@@ -880,16 +891,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
         cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
         {
           KernelTimer tm(ctx, st, kc);
-          if (wt)
-            k_extend<AJG_TRI_WATERTIGHT, false>
-                <<<g_ext, kTraceThreads, 0, st>>>(
-                    s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7],
-                    w.hits, &ctx->d_counters[0], ctx->d_error);
-          else
-            k_extend<AJG_TRI_MOLLER_TRUMBORE, false>
-                <<<g_ext, kTraceThreads, 0, st>>>(
-                    s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7],
-                    w.hits, &ctx->d_counters[0], ctx->d_error);
+          extend(q);
         }
         {
           KernelTimer tm(ctx, st, -1);
@@ -917,18 +919,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
         if (a.j.use_mis) {
           {
             KernelTimer tm(ctx, st, ka);
-            if (wt)
-              k_shadow<AJG_TRI_WATERTIGHT, false>
-                  <<<g_shw, kTraceThreads, 0, st>>>(
-                      s, t, w.sq_o, w.sq_d, nullptr, &w.counts[2],
-                      &w.counts[3], w.term_vis, &ctx->d_counters[1],
-                      ctx->d_error);
-            else
-              k_shadow<AJG_TRI_MOLLER_TRUMBORE, false>
-                  <<<g_shw, kTraceThreads, 0, st>>>(
-                      s, t, w.sq_o, w.sq_d, nullptr, &w.counts[2],
-                      &w.counts[3], w.term_vis, &ctx->d_counters[1],
-                      ctx->d_error);
+            shadow();
           }
           KernelTimer{ctx, st, -1};
           k_accumulate<false><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
@@ -955,44 +946,36 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
 }
 
 void prepare_mj_kernels() {
-  resident_grid((const void*)k_extend<AJG_TRI_WATERTIGHT, true>, kTraceThreads);
-  resident_grid((const void*)k_extend<AJG_TRI_MOLLER_TRUMBORE, true>,
-                kTraceThreads);
-  resident_grid((const void*)k_shadow<AJG_TRI_WATERTIGHT, true>, kTraceThreads);
-  resident_grid((const void*)k_shadow<AJG_TRI_MOLLER_TRUMBORE, true>,
-                kTraceThreads);
+  for (int tt = 0; tt < 2; ++tt)
+    for (int wd : {2, 4, 8})
+      dispatch_trace(tt, wd, [&](auto T, auto Wd) {
+        constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+        resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
+        resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
+      });
 }
 
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
-                     int NT, int bounces, int tri_test, TraceCounters* ctr,
-                     uint32_t* err, cudaStream_t st) {
+                     int NT, int bounces, int tri_test, int width,
+                     TraceCounters* ctr, uint32_t* err, cudaStream_t st) {
   const DeviceScene s{};
   WaveArgs a{};
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
-  const bool wt = tri_test == AJG_TRI_WATERTIGHT;
-  const int g_ext = resident_grid(
-      wt ? (const void*)k_extend<AJG_TRI_WATERTIGHT, true>
-         : (const void*)k_extend<AJG_TRI_MOLLER_TRUMBORE, true>,
-      kTraceThreads);
-  const int g_shw = resident_grid(
-      wt ? (const void*)k_shadow<AJG_TRI_WATERTIGHT, true>
-         : (const void*)k_shadow<AJG_TRI_MOLLER_TRUMBORE, true>,
-      kTraceThreads);
   cudaMemsetAsync(w.counts, 0, 32, st);
   k_raygen<true><<<gs, kShadeThreads, 0, st>>>(a, t, w);
   int q = 0;
   for (int b = 0; b < bounces; ++b) {
     cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
     cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
-    if (wt)
-      k_extend<AJG_TRI_WATERTIGHT, true><<<g_ext, kTraceThreads, 0, st>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
-          ctr, err);
-    else
-      k_extend<AJG_TRI_MOLLER_TRUMBORE, true><<<g_ext, kTraceThreads, 0, st>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
-          ctr, err);
+    dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
+      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+      const int g =
+          resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
+      k_extend<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits, ctr,
+          err);
+    });
     k_classify<true><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q], w.hits,
                                          w.lists, &w.counts[4], (uint32_t)P);
     k_shade_miss<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, b, q, w.lists,
@@ -1003,14 +986,14 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
     k_shade<AJG_MAT_DISNEY, true><<<gs, kShadeThreads, 0, st>>>(
         a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
         shadow_cap, err);
-    if (wt)
-      k_shadow<AJG_TRI_WATERTIGHT, true><<<g_shw, kTraceThreads, 0, st>>>(
+    dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
+      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+      const int g =
+          resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
+      k_shadow<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
           s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[2], &w.counts[3],
           w.term_vis, ctr + 1, err);
-    else
-      k_shadow<AJG_TRI_MOLLER_TRUMBORE, true><<<g_shw, kTraceThreads, 0, st>>>(
-          s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[2], &w.counts[3],
-          w.term_vis, ctr + 1, err);
+    });
     k_accumulate<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
                                                      (uint32_t)NT);
     q ^= 1;

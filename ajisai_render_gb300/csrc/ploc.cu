@@ -347,6 +347,90 @@ __global__ void k_bvh2_single(const PNode* __restrict__ nodes,
   bvh[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
 }
 
+// Collapse of the binary tree into W-wide nodes, top down, one level of
+// wide nodes per launch: a wide node takes its binary node and expands the
+// interior child with the largest surface area until it has W children (or
+// only leaves); its interior children become the wide nodes of the next
+// level, allocated contiguously.  Node layout (2W float4, 32W bytes): the
+// children's lo.x, hi.x, lo.y, hi.y, lo.z, hi.z in groups of four, then the
+// references (>= 0 wide node, ~slot leaf, kEmptyRef unused), then padding.
+constexpr int kWideEmpty = (int)0x80000000;
+
+template <int W>
+__global__ void k_collapse(const PNode* __restrict__ nodes,
+                           const uint2* __restrict__ fin, uint32_t n_in,
+                           uint2* __restrict__ fout,
+                           uint32_t* __restrict__ counters,
+                           float4* __restrict__ wide) {
+  constexpr int G = W / 4;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in;
+       i += gridDim.x * blockDim.x) {
+    const uint2 e = fin[i];  // (binary node, wide slot)
+    uint32_t ch[W];
+    int nc = 1;
+    ch[0] = e.x;
+    while (nc < W) {
+      int best = -1;
+      float ba = 0.f;
+      for (int c = 0; c < nc; ++c) {
+        const PNode x = nodes[ch[c]];
+        if (__float_as_int(x.b.w) != 0) continue;  // leaf
+        const float a = area(xyz(x.a), xyz(x.b));
+        if (best < 0 || a > ba) {
+          best = c;
+          ba = a;
+        }
+      }
+      if (best < 0) break;
+      const uint32_t f = (uint32_t)__float_as_int(nodes[ch[best]].a.w);
+      ch[best] = f;
+      ch[nc++] = f + 1;
+    }
+    int ni = 0;
+    for (int c = 0; c < nc; ++c)
+      ni += __float_as_int(nodes[ch[c]].b.w) == 0 ? 1 : 0;
+    uint32_t base = 0, fo = 0;
+    if (ni) {
+      base = atomicAdd(&counters[1], (uint32_t)ni);
+      fo = atomicAdd(&counters[0], (uint32_t)ni);
+    }
+    float pl[6][W];
+    int rf[W];
+    int j = 0;
+    for (int c = 0; c < W; ++c) {
+      if (c < nc) {
+        const PNode x = nodes[ch[c]];
+        pl[0][c] = x.a.x;
+        pl[1][c] = x.b.x;
+        pl[2][c] = x.a.y;
+        pl[3][c] = x.b.y;
+        pl[4][c] = x.a.z;
+        pl[5][c] = x.b.z;
+        if (__float_as_int(x.b.w) != 0) {
+          rf[c] = ~__float_as_int(x.a.w);
+        } else {
+          rf[c] = (int)(base + j);
+          fout[fo + j] = make_uint2(ch[c], base + j);
+          ++j;
+        }
+      } else {
+        for (int k = 0; k < 6; ++k) pl[k][c] = 0.f;
+        rf[c] = kWideEmpty;
+      }
+    }
+    float4* o = wide + (uint64_t)e.y * (2 * W);
+    for (int g = 0; g < G; ++g) {
+      for (int k = 0; k < 6; ++k)
+        o[k * G + g] = make_float4(pl[k][4 * g], pl[k][4 * g + 1],
+                                   pl[k][4 * g + 2], pl[k][4 * g + 3]);
+      o[6 * G + g] = make_float4(
+          __int_as_float(rf[4 * g]), __int_as_float(rf[4 * g + 1]),
+          __int_as_float(rf[4 * g + 2]), __int_as_float(rf[4 * g + 3]));
+      o[7 * G + g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
 __global__ void k_slot_tris(const float* __restrict__ tris,
                             const int32_t* __restrict__ perm, uint64_t n,
                             float4* __restrict__ out) {
@@ -441,13 +525,20 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     return p;
   };
   const uint64_t inner = n > 1 ? n - 1 : 1;
-  float4* bvh = (float4*)keep(inner * 4 * sizeof(float4));
+  // default: the 4-wide tree (the fastest measured on GB300 for the
+  // workloads here; 8-wide nodes cost occupancy)
+  const int width = opts.bvh_width ? (int)opts.bvh_width : 4;
+  if (width != 2 && width != 4 && width != 8)
+    return set_err(ctx, AJG_ERR_INVALID, "bvh_width must be 0, 2, 4 or 8");
+  float4* bvh =
+      width == 2 ? (float4*)keep(inner * 4 * sizeof(float4)) : nullptr;
   float4* slot_tris = (float4*)keep(n * 3 * sizeof(float4));
   float4* shade = (float4*)keep(n * sizeof(float4));
   float* corner = any_normals ? (float*)keep(n * 9 * sizeof(float)) : nullptr;
   float4* ploc_nodes = (float4*)keep(m * sizeof(PNode));
   int32_t* perm_keep = (int32_t*)keep(n * sizeof(int32_t));
-  if (!bvh || !slot_tris || !shade || (any_normals && !corner) ||
+  if ((width == 2 && !bvh) || !slot_tris || !shade ||
+      (any_normals && !corner) ||
       !ploc_nodes || !perm_keep)
     return set_err(ctx, AJG_ERR_OOM, "device allocation failed (scene)");
 
@@ -583,12 +674,54 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
                   cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(perm_keep, perm, n * sizeof(int32_t),
                   cudaMemcpyDeviceToDevice, st);
-  if (n > 1) {
-    k_inner_flags<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, flags);
-    device_scan(flags, mi, m, true, scratch, st);
-    k_bvh2<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, mi, bvh);
+  uint32_t num_nodes = (uint32_t)inner;
+  if (width == 2) {
+    if (n > 1) {
+      k_inner_flags<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, flags);
+      device_scan(flags, mi, m, true, scratch, st);
+      k_bvh2<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, mi, bvh);
+    } else {
+      k_bvh2_single<<<1, 1, 0, st>>>(nodes, bvh);
+    }
   } else {
-    k_bvh2_single<<<1, 1, 0, st>>>(nodes, bvh);
+    // wide layout: collapse level by level into a worst-case buffer, then
+    // keep the nodes made
+    const uint64_t node_f4 = 2 * (uint64_t)width;
+    float4* wtmp = tmp.get<float4>(inner * node_f4);
+    uint2* fa = tmp.get<uint2>(inner);
+    uint2* fb = tmp.get<uint2>(inner);
+    uint32_t* wc = tmp.get<uint32_t>(2);
+    if (tmp.err != cudaSuccess)
+      return set_err(ctx, AJG_ERR_OOM, "device allocation failed (wide BVH)");
+    const uint32_t init[2] = {0u, 1u};
+    cudaMemcpyAsync(wc, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    const uint2 root = make_uint2(0u, 0u);
+    cudaMemcpyAsync(fa, &root, sizeof(root), cudaMemcpyHostToDevice, st);
+    uint32_t n_in = 1, levels = 0;
+    while (n_in) {
+      cudaMemsetAsync(wc, 0, sizeof(uint32_t), st);
+      if (width == 4)
+        k_collapse<4><<<grid_for(n_in, 128), 128, 0, st>>>(nodes, fa, n_in,
+                                                           fb, wc, wtmp);
+      else
+        k_collapse<8><<<grid_for(n_in, 128), 128, 0, st>>>(nodes, fa, n_in,
+                                                           fb, wc, wtmp);
+      uint32_t h[2] = {0, 0};
+      if (cudaMemcpyAsync(h, wc, sizeof(h), cudaMemcpyDeviceToHost, st) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return set_err(ctx, AJG_ERR_CUDA, "wide BVH collapse failed");
+      n_in = h[0];
+      num_nodes = h[1];
+      std::swap(fa, fb);
+      if (++levels > inner + 1)
+        return set_err(ctx, AJG_ERR_DEVICE, "wide BVH collapse did not end");
+    }
+    bvh = (float4*)keep((uint64_t)num_nodes * node_f4 * sizeof(float4));
+    if (!bvh)
+      return set_err(ctx, AJG_ERR_OOM, "device allocation failed (wide BVH)");
+    cudaMemcpyAsync(bvh, wtmp, (uint64_t)num_nodes * node_f4 * sizeof(float4),
+                    cudaMemcpyDeviceToDevice, st);
   }
   k_slot_tris<<<gb, 256, 0, st>>>(d_tris, perm, n, slot_tris);
   k_shade_data<<<gb, 256, 0, st>>>(d_tris, d_mat, d_flags, n, shade);
@@ -617,7 +750,8 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   s->d.shade = shade;
   s->d.corner = corner;
   s->d.n = n;
-  s->d.num_inner = (uint32_t)inner;
+  s->d.num_inner = num_nodes;
+  s->d.width = width;
   s->d.tri_test = (int32_t)opts.tri_test;
   s->ploc_nodes = ploc_nodes;
   s->perm = perm_keep;
@@ -625,6 +759,9 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   s->info.num_nodes = m;
   s->info.ploc_iterations = iters;
   s->info.build_ms = ms;
+  s->info.bvh_width = (uint32_t)width;
+  s->info.bvh_node_bytes = width == 2 ? 64u : 32u * (uint32_t)width;
+  s->info.bvh_nodes = num_nodes;
   // lights are fitted to the world bounds (default_scene.cpp:41-48)
   const F3 center = (whi + wlo) / 2.f;
   const F3 half = whi - center;

@@ -11,10 +11,12 @@
 namespace ajg {
 
 // HBM layout of a built scene (all arrays are device pointers):
-//   bvh    [inner][4] float4  two child boxes per interior node:
+//   bvh    width 2: [inner][4] float4, two child boxes per interior node:
 //          (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y), (c1 ... same),
 //          (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z), (ref0, ref1, -, -) where a
-//          ref >= 0 is an interior node and ~slot a leaf
+//          ref >= 0 is an interior node and ~slot a leaf;
+//          width W = 4, 8: [nodes][2W] float4 of the collapsed tree (see
+//          k_collapse in ploc.cu)
 //   tris   [slots][3] float4  vertices a, b, c of the triangle in each leaf
 //          slot (Morton order); a.w carries the primitive index
 //   shade  [n] float4         per primitive: geometric normal, w = material |
@@ -37,6 +39,7 @@ struct DeviceScene {
   int32_t env = -1;      // the scene's environment light (the last one)
   float radius = 0.f;    // (world.max - world.center).length()
   int32_t tri_test = 0;
+  int32_t width = 2;     // node width of `bvh`: 2 (binary PLOC tree), 4, 8
 };
 
 // Per-job constants of the integrator, shared by the single-job and the
@@ -219,8 +222,8 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj);
 // lengths and table contents read on the device): raygen, `bounces` bounce
 // iterations, film update.  NT = light terms per path of the arena.
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
-                     int NT, int bounces, int tri_test, TraceCounters* ctr,
-                     uint32_t* err, cudaStream_t st);
+                     int NT, int bounces, int tri_test, int width,
+                     TraceCounters* ctr, uint32_t* err, cudaStream_t st);
 // Kernels of a multi-job wave launched per wave (for launch counts).
 inline int mj_wave_kernels(int bounces) { return 2 + 7 * bounces; }
 // Looks up the persistent grids of the multi-job kernels (call before a

@@ -21,6 +21,7 @@
 #include <deque>
 #include <map>
 #include <thread>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -140,7 +141,7 @@ struct Server {
   std::vector<char*> h_tables;  // pinned, one per in-flight slot + 1
   size_t table_bytes = 0;
   uint64_t wave_no = 0;
-  std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
   std::deque<InFlight> inflight;
   std::vector<uint32_t*> err_words;  // pinned, recycled
   uint32_t* d_err = nullptr;
@@ -155,7 +156,7 @@ struct Server {
   void retire_oldest();
   void end_job_locked(Job* j, uint32_t state, int err);
   int ensure_arena(int nt);
-  cudaGraphExec_t graph_for(int bounces, int tri_test);
+  cudaGraphExec_t graph_for(int bounces, int tri_test, int width);
 };
 
 namespace {
@@ -191,8 +192,8 @@ int Server::ensure_arena(int nt) {
   return AJG_OK;
 }
 
-cudaGraphExec_t Server::graph_for(int bounces, int tri_test) {
-  const auto key = std::make_pair(bounces, tri_test);
+cudaGraphExec_t Server::graph_for(int bounces, int tri_test, int width) {
+  const auto key = std::make_tuple(bounces, tri_test, width);
   auto it = graphs.find(key);
   if (it != graphs.end()) return it->second;
   prepare_mj_kernels();
@@ -201,7 +202,7 @@ cudaGraphExec_t Server::graph_for(int bounces, int tri_test) {
   if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) !=
       cudaSuccess)
     return nullptr;
-  enqueue_mj_wave(t, w, P, NT, bounces, tri_test, d_ctr, d_err, st);
+  enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, d_ctr, d_err, st);
   if (cudaStreamEndCapture(st, &g) != cudaSuccess || !g) return nullptr;
   if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
   cudaGraphDestroy(g);
@@ -363,12 +364,15 @@ uint64_t remaining_paths(const Job* j) {
 // is no work to launch.
 bool Server::plan_and_launch() {
   std::vector<Plan> plan;
-  int bounces = 0, tri_test = -1, nt_max = 1;
+  int bounces = 0, tri_test = -1, width = 0, nt_max = 1;
   {
     std::lock_guard<std::mutex> lk(mu);
     for (Job* j : active) {
       if (j->cancel || j->s_cur >= j->prm.spp) continue;
-      if (tri_test < 0) tri_test = (int)j->scene->d.tri_test;
+      if (tri_test < 0) {
+        tri_test = (int)j->scene->d.tri_test;
+        width = (int)j->scene->d.width;
+      }
       nt_max = std::max(nt_max, (int)j->jp.nl + 1);
     }
     if (tri_test < 0) return false;
@@ -386,8 +390,11 @@ bool Server::plan_and_launch() {
     std::vector<Job*> cand;
     for (Job* j : active) {
       if (j->cancel || j->s_cur >= j->prm.spp) continue;
-      // one triangle test per wave (the oldest job's); arena light terms
-      if ((int)j->scene->d.tri_test != tri_test) continue;
+      // one triangle test and node width per wave (the oldest job's);
+      // arena light terms
+      if ((int)j->scene->d.tri_test != tri_test ||
+          (int)j->scene->d.width != width)
+        continue;
       if ((int)j->jp.nl + 1 > NT) continue;
       cand.push_back(j);
     }
@@ -486,12 +493,12 @@ bool Server::plan_and_launch() {
   cudaMemcpyAsync(d_tables, h, table_bytes, cudaMemcpyHostToDevice, st);
 
   InFlight f{};
-  cudaGraphExec_t g = graph_for(bounces, tri_test);
+  cudaGraphExec_t g = graph_for(bounces, tri_test, width);
   if (g) {
     cudaGraphLaunch(g, st);
   } else {  // capture unavailable: the same launches on the stream
     cudaGetLastError();
-    enqueue_mj_wave(t, w, P, NT, bounces, tri_test, d_ctr, d_err, st);
+    enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, d_ctr, d_err, st);
   }
   // results this wave completes
   for (const Plan& p : plan) {

@@ -7,7 +7,7 @@ namespace {
 
 constexpr int kTraceThreads = 128;
 
-template <int TEST>
+template <int TEST, int W>
 __global__ void __launch_bounds__(kTraceThreads)
     k_trace_closest(DeviceScene s, const ajg_ray* __restrict__ rays,
                     uint64_t n, uint32_t* next, ajg_hit* __restrict__ hits,
@@ -26,12 +26,12 @@ __global__ void __launch_bounds__(kTraceThreads)
     o.prim = h.prim;
     hits[i] = o;
   };
-  trace_persistent<TEST, false>(trace_scene(s), (uint32_t)n, next, fetch, finish, nr, nn,
-                                nt, err);
+  trace_persistent<TEST, false, W>(trace_scene(s), (uint32_t)n, next, fetch,
+                                   finish, nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
-template <int TEST>
+template <int TEST, int W>
 __global__ void __launch_bounds__(kTraceThreads)
     k_trace_any(DeviceScene s, const ajg_ray* __restrict__ rays, uint64_t n,
                 uint32_t* next, uint8_t* __restrict__ occ, TraceCounters* ctr,
@@ -43,8 +43,8 @@ __global__ void __launch_bounds__(kTraceThreads)
                       q.t_min, q.t_max);
   };
   auto finish = [&](uint32_t i, const Hit&, bool o) { occ[i] = o ? 1 : 0; };
-  trace_persistent<TEST, true>(trace_scene(s), (uint32_t)n, next, fetch, finish, nr, nn, nt,
-                               err);
+  trace_persistent<TEST, true, W>(trace_scene(s), (uint32_t)n, next, fetch,
+                                  finish, nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
@@ -56,12 +56,10 @@ void launch_trace_closest(const DeviceScene& s, const ajg_ray* rays,
                           TraceCounters* ctr, uint32_t* err, cudaStream_t st) {
   if (!n) return;
   const int g = grid_for(n, kTraceThreads, kSMs * 10);
-  if (s.tri_test == AJG_TRI_WATERTIGHT)
-    k_trace_closest<AJG_TRI_WATERTIGHT>
+  dispatch_trace(s.tri_test, s.width, [&](auto T, auto W) {
+    k_trace_closest<decltype(T)::value, decltype(W)::value>
         <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, hits, ctr, err);
-  else
-    k_trace_closest<AJG_TRI_MOLLER_TRUMBORE>
-        <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, hits, ctr, err);
+  });
 }
 
 void launch_trace_any(const DeviceScene& s, const ajg_ray* rays, uint64_t n,
@@ -69,12 +67,10 @@ void launch_trace_any(const DeviceScene& s, const ajg_ray* rays, uint64_t n,
                       uint32_t* err, cudaStream_t st) {
   if (!n) return;
   const int g = grid_for(n, kTraceThreads, kSMs * 10);
-  if (s.tri_test == AJG_TRI_WATERTIGHT)
-    k_trace_any<AJG_TRI_WATERTIGHT>
+  dispatch_trace(s.tri_test, s.width, [&](auto T, auto W) {
+    k_trace_any<decltype(T)::value, decltype(W)::value>
         <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, occluded, ctr, err);
-  else
-    k_trace_any<AJG_TRI_MOLLER_TRUMBORE>
-        <<<g, kTraceThreads, 0, st>>>(s, rays, n, next, occluded, ctr, err);
+  });
 }
 
 }  // namespace ajg

@@ -11,11 +11,12 @@
 // passes.  The per-thread stack lives in registers/local memory and is
 // guarded: overflow sets the device error word and ends the ray.
 #pragma once
+#include <type_traits>
+
 #include "scene.cuh"
 
 namespace ajg {
 
-constexpr int kStackSize = 96;
 constexpr float kSlabWiden = 1.0000003576278687f;  // 1 + 2*gamma(3)
 
 struct Hit {
@@ -132,116 +133,6 @@ __device__ __forceinline__ RayQ make_query(F3 o, F3 d, float tmin,
   return r;
 }
 
-// TEST: AJG_TRI_*; ANY: occlusion query (returns at the first hit).
-template <int TEST, bool ANY>
-__device__ __forceinline__ bool traverse(const DeviceScene& s, const RayQ& r,
-                                         Hit& hit, uint32_t& n_nodes,
-                                         uint32_t& n_tris, uint32_t* err) {
-  WtSetup w;
-  if (TEST == AJG_TRI_WATERTIGHT) w = wt_setup(r);
-  hit.t = __int_as_float(0x7f800000);  // +inf
-  hit.prim = -1;
-  hit.u = hit.v = 0.f;
-  int stack_node[kStackSize];
-  float stack_t[kStackSize];
-  int sp = 0;
-  int node = 0;
-  const float4* __restrict__ bvh = s.bvh;
-  const float4* __restrict__ tris = s.tris;
-  for (;;) {
-    ++n_nodes;
-    const float4 n0 = __ldg(bvh + 4 * node + 0);
-    const float4 n1 = __ldg(bvh + 4 * node + 1);
-    const float4 n2 = __ldg(bvh + 4 * node + 2);
-    const float4 n3 = __ldg(bvh + 4 * node + 3);
-    const float lim = ANY ? r.tmax : fminf(hit.t, r.tmax);
-    float tn0, tn1;
-    bool h0 = slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
-    bool h1 = slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
-    const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const bool hc = c == 0 ? h0 : h1;
-      const int rc = c == 0 ? r0 : r1;
-      if (hc && rc < 0) {
-        const int slot = ~rc;
-        ++n_tris;
-        const float4 A = __ldg(tris + 3 * slot + 0);
-        const float4 B = __ldg(tris + 3 * slot + 1);
-        const float4 C = __ldg(tris + 3 * slot + 2);
-        float t, u, v;
-        const bool ok = TEST == AJG_TRI_WATERTIGHT
-                            ? wt_test(r, w, A, B, C, t, u, v)
-                            : mt_test(r, A, B, C, t, u, v);
-        if (ok) {
-          const int prim = __float_as_int(A.w);
-          if (ANY) {
-            hit.t = t;
-            hit.u = u;
-            hit.v = v;
-            hit.prim = prim;
-            return true;
-          }
-          if (t < hit.t || (t == hit.t && prim < hit.prim)) {
-            hit.t = t;
-            hit.u = u;
-            hit.v = v;
-            hit.prim = prim;
-          }
-        }
-        if (c == 0)
-          h0 = false;
-        else
-          h1 = false;
-      }
-    }
-    if (h0 && h1) {
-      const bool first0 = tn0 <= tn1;
-      if (sp >= kStackSize) {
-        raise_device_error(err, kDevStackOverflow);
-        return hit.prim >= 0;
-      }
-      stack_node[sp] = first0 ? r1 : r0;
-      stack_t[sp] = first0 ? tn1 : tn0;
-      ++sp;
-      node = first0 ? r0 : r1;
-      continue;
-    }
-    if (h0) {
-      node = r0;
-      continue;
-    }
-    if (h1) {
-      node = r1;
-      continue;
-    }
-    // pop, skipping boxes a closer hit has since excluded
-    bool found = false;
-    while (sp > 0) {
-      --sp;
-      const float lim2 = ANY ? r.tmax : fminf(hit.t, r.tmax);
-      if (stack_t[sp] <= lim2) {
-        node = stack_node[sp];
-        found = true;
-        break;
-      }
-    }
-    if (!found) break;
-  }
-  return hit.prim >= 0;
-}
-
-// Persistent-lane traversal.  Each lane owns one ray at a time and runs one
-// node visit per loop iteration; lanes whose ray finished take new rays from
-// a shared counter (warp-aggregated, once at least kRefill lanes of the warp
-// are idle), so lanes are not left idle at ray boundaries waiting for the
-// warp's slowest ray.  FETCH(k) returns the k-th ray; FINISH(k, hit, occluded)
-// stores its result.
-#ifndef AJG_REFILL
-#define AJG_REFILL 16
-#endif
-constexpr int kRefill = AJG_REFILL;
-
 // The tree a ray is traced against.  FETCH(k, ts) may retarget `ts` per
 // ray (waves that mix scenes); single-scene callers leave it untouched.
 struct TraceScene {
@@ -257,11 +148,61 @@ __device__ __forceinline__ TraceScene trace_scene(const DeviceScene& s) {
   return t;
 }
 
-template <int TEST, bool ANY, class FETCH, class FINISH>
+// Stack depth per lane: a node visit pushes at most W-1 siblings.
+template <int W>
+struct StackDepth {
+  static constexpr int value = W == 2 ? 96 : (W == 4 ? 128 : 192);
+};
+
+// Tests one triangle of a leaf slot against the ray and keeps the closest
+// hit (ties in t to the lowest primitive index); any-hit queries stop at the
+// first accepted triangle.
+template <int TEST, bool ANY>
+__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
+                                          int slot, const RayQ& r,
+                                          const WtSetup& w, Hit& hit) {
+  const float4 A = __ldg(tris + 3 * slot + 0);
+  const float4 B = __ldg(tris + 3 * slot + 1);
+  const float4 C = __ldg(tris + 3 * slot + 2);
+  float t, u, v;
+  const bool ok = TEST == AJG_TRI_WATERTIGHT ? wt_test(r, w, A, B, C, t, u, v)
+                                             : mt_test(r, A, B, C, t, u, v);
+  if (!ok) return false;
+  const int prim = __float_as_int(A.w);
+  if (ANY || t < hit.t || (t == hit.t && prim < hit.prim)) {
+    hit.t = t;
+    hit.u = u;
+    hit.v = v;
+    hit.prim = prim;
+  }
+  return ANY;
+}
+
+// Persistent-lane traversal.  Each lane owns one ray at a time and runs one
+// node visit per loop iteration; lanes whose ray finished take new rays from
+// a shared counter (warp-aggregated, once at least kRefill lanes of the warp
+// are idle), so lanes are not left idle at ray boundaries waiting for the
+// warp's slowest ray.  FETCH(k, ts) returns the k-th ray; FINISH(k, hit,
+// occluded) stores its result.
+//
+// W is the node width: 2 is the binary PLOC tree (64-byte nodes holding both
+// children's boxes); 4 and 8 are the collapsed wide trees (32*W-byte nodes:
+// the children's boxes as lo.x, hi.x, lo.y, hi.y, lo.z, hi.z groups of four,
+// then the child references).  In a wide node the boxes that pass are
+// visited nearest first: leaf children are tested at once, the nearest
+// interior child is visited next and the others are pushed farthest first.
+#ifndef AJG_REFILL
+#define AJG_REFILL 16
+#endif
+constexpr int kRefill = AJG_REFILL;
+constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
+
+template <int TEST, bool ANY, int W, class FETCH, class FINISH>
 __device__ __forceinline__ void trace_persistent(
     TraceScene ts, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
     uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris, uint32_t* err) {
   constexpr int kIdle = -1, kDone = 0x7fffffff;
+  constexpr int kStack = StackDepth<W>::value;
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -271,8 +212,8 @@ __device__ __forceinline__ void trace_persistent(
   Hit hit;
   int node = 0, sp = 0;
   uint32_t visits = 0;
-  int stack_node[kStackSize];
-  float stack_t[kStackSize];
+  int stack_node[kStack];
+  float stack_t[kStack];
   for (;;) {
     const unsigned idle = __ballot_sync(full, k == kIdle);
     const unsigned done = __ballot_sync(full, k == kDone);
@@ -312,79 +253,166 @@ __device__ __forceinline__ void trace_persistent(
     }
     const float4* __restrict__ bvh = ts.bvh;
     const float4* __restrict__ tris = ts.tris;
-    const float4 n0 = __ldg(bvh + 4 * node + 0);
-    const float4 n1 = __ldg(bvh + 4 * node + 1);
-    const float4 n2 = __ldg(bvh + 4 * node + 2);
-    const float4 n3 = __ldg(bvh + 4 * node + 3);
     const float lim = ANY ? r.tmax : fminf(hit.t, r.tmax);
-    float tn0, tn1;
-    bool h0 = slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
-    bool h1 = slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
-    const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
+    bool descend = false;  // `node` holds the next node to visit
+    if constexpr (W == 2) {
+      const float4 n0 = __ldg(bvh + 4 * node + 0);
+      const float4 n1 = __ldg(bvh + 4 * node + 1);
+      const float4 n2 = __ldg(bvh + 4 * node + 2);
+      const float4 n3 = __ldg(bvh + 4 * node + 3);
+      float tn0, tn1;
+      bool h0 = slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
+      bool h1 = slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
+      const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
 #pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const bool hc = c == 0 ? h0 : h1;
-      const int rc = c == 0 ? r0 : r1;
-      if (hc && rc < 0 && !finished) {
-        const int slot = ~rc;
-        ++n_tris;
-        const float4 A = __ldg(tris + 3 * slot + 0);
-        const float4 B = __ldg(tris + 3 * slot + 1);
-        const float4 C = __ldg(tris + 3 * slot + 2);
-        float t, u, v;
-        const bool ok = TEST == AJG_TRI_WATERTIGHT
-                            ? wt_test(r, w, A, B, C, t, u, v)
-                            : mt_test(r, A, B, C, t, u, v);
-        if (ok) {
-          const int prim = __float_as_int(A.w);
-          if (ANY) {
-            hit.t = t;
-            hit.u = u;
-            hit.v = v;
-            hit.prim = prim;
+      for (int c = 0; c < 2; ++c) {
+        const bool hc = c == 0 ? h0 : h1;
+        const int rc = c == 0 ? r0 : r1;
+        if (hc && rc < 0 && !finished) {
+          ++n_tris;
+          finished = leaf_test<TEST, ANY>(tris, ~rc, r, w, hit);
+        }
+        if (hc && rc < 0) {
+          if (c == 0)
+            h0 = false;
+          else
+            h1 = false;
+        }
+      }
+      if (!finished) {
+        if (h0 && h1) {
+          const bool first0 = tn0 <= tn1;
+          if (sp >= kStack) {
+            raise_device_error(err, kDevStackOverflow);
             finished = true;
-          } else if (t < hit.t || (t == hit.t && prim < hit.prim)) {
-            hit.t = t;
-            hit.u = u;
-            hit.v = v;
-            hit.prim = prim;
+          } else {
+            stack_node[sp] = first0 ? r1 : r0;
+            stack_t[sp] = first0 ? tn1 : tn0;
+            ++sp;
+            node = first0 ? r0 : r1;
+            descend = true;
           }
+        } else if (h0) {
+          node = r0;
+          descend = true;
+        } else if (h1) {
+          node = r1;
+          descend = true;
         }
       }
-      if (hc && rc < 0) {
-        if (c == 0)
-          h0 = false;
-        else
-          h1 = false;
-      }
-    }
-    if (!finished) {
-      if (h0 && h1) {
-        const bool first0 = tn0 <= tn1;
-        if (sp >= kStackSize) {
-          raise_device_error(err, kDevStackOverflow);
-          finished = true;
-        } else {
-          stack_node[sp] = first0 ? r1 : r0;
-          stack_t[sp] = first0 ? tn1 : tn0;
-          ++sp;
-          node = first0 ? r0 : r1;
+    } else {
+      constexpr int G = W / 4;  // float4 groups per plane
+      const float4* nd = bvh + (uint64_t)node * (2 * W);
+      float tn[W];
+      int ref[W];
+      unsigned inner = 0;  // interior children whose box passed
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const float4 lx = __ldg(nd + 0 * G + g), hx = __ldg(nd + 1 * G + g);
+        const float4 ly = __ldg(nd + 2 * G + g), hy = __ldg(nd + 3 * G + g);
+        const float4 lz = __ldg(nd + 4 * G + g), hz = __ldg(nd + 5 * G + g);
+        const float4 rf = __ldg(nd + 6 * G + g);
+        const float* plx = &lx.x;
+        const float* phx = &hx.x;
+        const float* ply = &ly.x;
+        const float* phy = &hy.x;
+        const float* plz = &lz.x;
+        const float* phz = &hz.x;
+        const float* prf = &rf.x;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int c = 4 * g + j;
+          ref[c] = __float_as_int(prf[j]);
+          float t0;
+          const bool h = ref[c] != kEmptyRef &&
+                         slab2(plx[j], phx[j], ply[j], phy[j], plz[j], phz[j],
+                               r, lim, t0);
+          tn[c] = t0;
+          if (h && ref[c] < 0 && !finished) {
+            ++n_tris;
+            finished = leaf_test<TEST, ANY>(tris, ~ref[c], r, w, hit);
+          }
+          if (h && ref[c] >= 0) inner |= 1u << c;
         }
-      } else if (h0) {
-        node = r0;
-      } else if (h1) {
-        node = r1;
-      } else {
-        // pop, skipping boxes a closer hit has since excluded
-        finished = true;
-        while (sp > 0) {
-          --sp;
-          const float lim2 = ANY ? r.tmax : fminf(hit.t, r.tmax);
-          if (stack_t[sp] <= lim2) {
-            node = stack_node[sp];
-            finished = false;
+      }
+      if (!finished && inner && ANY) {
+        // occlusion: any order will do -- visit the first, push the rest
+        const int c0 = __ffs(inner) - 1;
+        inner &= inner - 1;
+        while (inner && !finished) {
+          const int c = __ffs(inner) - 1;
+          inner &= inner - 1;
+          if (sp >= kStack) {
+            raise_device_error(err, kDevStackOverflow);
+            finished = true;
             break;
           }
+          int fr = 0;
+          float ft = 0.f;
+#pragma unroll
+          for (int cc = 0; cc < W; ++cc)
+            if (cc == c) {
+              fr = ref[cc];
+              ft = tn[cc];
+            }
+          stack_node[sp] = fr;
+          stack_t[sp] = ft;
+          ++sp;
+        }
+        if (!finished) {
+          int nr = 0;
+#pragma unroll
+          for (int cc = 0; cc < W; ++cc)
+            if (cc == c0) nr = ref[cc];
+          node = nr;
+          descend = true;
+        }
+      } else if (!finished && inner) {
+        // push all but the nearest, farthest first
+        while (__popc(inner) > 1) {
+          int far_c = -1;
+          float far_t = -__int_as_float(0x7f800000);
+#pragma unroll
+          for (int c = 0; c < W; ++c)
+            if (((inner >> c) & 1u) && (far_c < 0 || tn[c] > far_t)) {
+              far_c = c;
+              far_t = tn[c];
+            }
+          if (sp >= kStack) {
+            raise_device_error(err, kDevStackOverflow);
+            finished = true;
+            break;
+          }
+          int fr = 0;
+#pragma unroll
+          for (int c = 0; c < W; ++c)
+            if (c == far_c) fr = ref[c];
+          stack_node[sp] = fr;
+          stack_t[sp] = far_t;
+          ++sp;
+          inner &= ~(1u << far_c);
+        }
+        if (!finished) {
+          const int c = __ffs(inner) - 1;
+          int nr = 0;
+#pragma unroll
+          for (int cc = 0; cc < W; ++cc)
+            if (cc == c) nr = ref[cc];
+          node = nr;
+          descend = true;
+        }
+      }
+    }
+    if (!finished && !descend) {
+      // pop, skipping boxes a closer hit has since excluded
+      finished = true;
+      while (sp > 0) {
+        --sp;
+        const float lim2 = ANY ? r.tmax : fminf(hit.t, r.tmax);
+        if (stack_t[sp] <= lim2) {
+          node = stack_node[sp];
+          finished = false;
+          break;
         }
       }
     }
@@ -393,6 +421,32 @@ __device__ __forceinline__ void trace_persistent(
       finish((uint32_t)k, hit, hit.prim >= 0);
       k = kIdle;
     }
+  }
+}
+
+// Calls f(TEST, W) with the triangle test and node width as compile-time
+// constants (std::integral_constant), for launching the matching kernel.
+template <class F>
+inline void dispatch_trace(int tri_test, int width, F&& f) {
+  using MT = std::integral_constant<int, AJG_TRI_MOLLER_TRUMBORE>;
+  using WT = std::integral_constant<int, AJG_TRI_WATERTIGHT>;
+  using W2 = std::integral_constant<int, 2>;
+  using W4 = std::integral_constant<int, 4>;
+  using W8 = std::integral_constant<int, 8>;
+  if (tri_test == AJG_TRI_WATERTIGHT) {
+    if (width == 8)
+      f(WT{}, W8{});
+    else if (width == 4)
+      f(WT{}, W4{});
+    else
+      f(WT{}, W2{});
+  } else {
+    if (width == 8)
+      f(MT{}, W8{});
+    else if (width == 4)
+      f(MT{}, W4{});
+    else
+      f(MT{}, W2{});
   }
 }
 

@@ -20,7 +20,8 @@ Printed on one JSON line:
               step uploads the triangles, builds the PLOC tree on the GPU,
               renders and copies the film back
   roofline    the dominant traversal kernel: algorithmic bytes (nodes
-              visited x 64 B + triangles tested x 48 B, counted in-kernel)
+              visited x node size -- 64 B binary, 32*W B for W-wide nodes --
+              + triangles tested x 48 B, counted in-kernel)
               per launch over its CUDA-event duration, against the measured
               HBM copy bandwidth
   cpu_baseline  the oracle (a C++ restatement of the reference's CPU path)
@@ -49,7 +50,7 @@ METRIC = "Msamples/s + p99 job latency, 1 GB300, batched/served vs plain at equa
 WORKLOAD = ("single-job plain GPU: displaced icosphere subdiv 8 (1,310,720 tris) "
             "+ 2-tri ground, Disney, 1024x1024, 256 spp, depth 16, PLOC r=16 built on the GPU")
 SPP, RES, DEPTH, MIN_B, RADIUS = 256, 1024, 16, 5, 16
-NODE_BYTES, TRI_BYTES = 64, 48
+TRI_BYTES = 48
 
 
 def parse():
@@ -71,6 +72,8 @@ def parse():
                     help="arrival rate as a fraction of the batched throughput")
     ap.add_argument("--rmse-crop", type=int, default=32)
     ap.add_argument("--rmse-spp", type=int, default=4096)
+    ap.add_argument("--bvh-width", type=int, default=0,
+                    help="traversal tree: 2 binary, 4/8 collapsed, 0 library default")
     return ap.parse_args()
 
 
@@ -236,7 +239,7 @@ def run_ours(args):
     W = H = args.res
     samples_per_step = W * H * args.spp
     ctx = api.Context(local)
-    scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
+    scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS, bvh_width=args.bvh_width))
     rend = api.PTRenderer(api.PTRendererArgs(spp=args.spp, min_bounces=MIN_B,
                                              max_bounces=DEPTH), seed=1 + rank)
     out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
@@ -282,7 +285,8 @@ def run_ours(args):
     dom = max(kinds, key=lambda k: st[kinds[k][0]])
     ms_k, l_k, n_k, t_k, kname = kinds[dom]
     launches = max(1, st[l_k])
-    bytes_per_launch = (st[n_k] * NODE_BYTES + st[t_k] * TRI_BYTES) / launches
+    node_bytes = scene.info()["bvh_node_bytes"]
+    bytes_per_launch = (st[n_k] * node_bytes + st[t_k] * TRI_BYTES) / launches
     avg_ms = st[ms_k] / launches
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     peak, peak_kind = peaks()
@@ -308,7 +312,8 @@ def run_ours(args):
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            s2 = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
+            s2 = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS,
+                                                                  bvh_width=args.bvh_width))
             rend.Render(s2, flat.camera, film)
             s2.release()
         dt = time.perf_counter() - t0
@@ -347,7 +352,8 @@ def run_ours(args):
             "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene, no dataset)",
-            "config": config(args), "clocks": clk, "e2e": e2e, "roofline": roofline,
+            "config": {**config(args), "bvh_width": scene.info()["bvh_width"]},
+            "clocks": clk, "e2e": e2e, "roofline": roofline,
             "cpu_baseline": cpu, "gpu_launches": int(st["kernel_launches"]),
             "ploc_build_ms": scene.info()["build_ms"],
             "kernel_ms_per_step": {"k_extend": st["closest_ms"] / args.steps,

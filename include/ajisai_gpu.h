@@ -116,7 +116,10 @@ typedef struct ajg_scene_opts {
                              including its stale digit-0 offset
                              (ploc_aggregate.cpp:97-130), so the tree is the
                              reference's own; 0: correct stable sort */
-  uint32_t reserved;
+  uint32_t bvh_width;     /* traversal tree: 2 the binary PLOC tree, 4 or 8
+                             the tree collapsed into 4/8-wide nodes (same
+                             hits: the traversal result does not depend on
+                             the tree); 0: the library's default, 4 */
 } ajg_scene_opts;
 
 /* Thin-lens camera: the two matrices ThinLensCamera keeps
@@ -169,6 +172,9 @@ typedef struct ajg_scene_info {
   uint64_t device_bytes;   /* resident bytes of the scene */
   uint32_t ploc_iterations;
   float build_ms;          /* GPU time of the last PLOC build */
+  uint32_t bvh_width;      /* node width of the traversal tree */
+  uint32_t bvh_node_bytes; /* bytes per traversal node */
+  uint64_t bvh_nodes;      /* traversal nodes */
 } ajg_scene_info;
 
 typedef struct ajg_stats {

@@ -17,14 +17,14 @@ def ctx():
     c.close()
 
 
-def geometry_scene(ctx, tris, world, radius=14, tri_test=0, compat=False):
+def geometry_scene(ctx, tris, world, radius=14, tri_test=0, compat=False, width=0):
     tris = np.ascontiguousarray(tris, np.float32).reshape(-1, 9)
     n = tris.shape[0]
     flat = S.FlatScene(tris, np.zeros((n, 9), np.float32), np.zeros(n, np.int32),
                        np.zeros(n, np.int32), np.asarray(world, np.float32),
                        S.Diffuse((0.5, 0.5, 0.5)).pack()[None],
                        np.zeros((0, 12), np.float32), None)
-    return api.GpuScene(ctx, flat, api.CreatePLOCAggregate(radius, tri_test, compat))
+    return api.GpuScene(ctx, flat, api.CreatePLOCAggregate(radius, tri_test, compat, width))
 
 
 def same_bits(a, b):
@@ -93,16 +93,17 @@ def test_ploc_full_size_properties(ctx):
     assert info["num_triangles"] == fl.n_tris and info["ploc_iterations"] > 0
 
 
-def test_single_and_two_triangle_scenes(ctx):
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_single_and_two_triangle_scenes(ctx, width):
     t1 = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
-    sc = geometry_scene(ctx, t1, [0, 0, 0, 1, 1, 0])
+    sc = geometry_scene(ctx, t1, [0, 0, 0, 1, 1, 0], width=width)
     rays = np.array([[0.2, 0.2, 1, 0, 0, -1, 1e-4, np.inf],
                      [2, 2, 1, 0, 0, -1, 1e-4, np.inf]], np.float32)
     t, p, u, v = sc.Intersect(rays)
     assert list(p) == [0, -1] and t[0] == np.float32(1.0)
     assert list(sc.Occlude(rays)) == [True, False]
     t2 = np.concatenate([t1, t1 + np.float32(2.0)])
-    sc2 = geometry_scene(ctx, t2, [0, 0, 0, 3, 3, 2])
+    sc2 = geometry_scene(ctx, t2, [0, 0, 0, 3, 3, 2], width=width)
     t, p, _, _ = sc2.Intersect(rays)
     assert list(p) == [0, -1]
 
@@ -129,10 +130,14 @@ def test_reference_sort_overflow_is_refused(ctx):
 
 
 # ----------------------------------------------------------------- trace --
+@pytest.mark.parametrize("width", [2, 4, 8])
 @pytest.mark.parametrize("case", ["trace_ico4.npz", "trace_soup.npz"])
-def test_closest_hit_matches_reference(ctx, golden, case):
+def test_closest_hit_matches_reference(ctx, golden, case, width):
+    """The reference's own tree (radix_compat), traversed as built or
+    collapsed 4/8-wide: the reference's hits bit for bit."""
     g = golden(case)
-    sc = geometry_scene(ctx, g["tris"], g["world"], int(g["radius"]), compat=True)
+    sc = geometry_scene(ctx, g["tris"], g["world"], int(g["radius"]), compat=True,
+                        width=width)
     t, p, u, v = sc.Intersect(g["rays"])
     hit = g["prim"] >= 0
     assert np.array_equal(p, g["prim"])
@@ -150,11 +155,12 @@ def random_rays(rng, n, spread=2.0):
     return np.concatenate([o, d, np.full((n, 1), 1e-4), tmax[:, None]], 1).astype(np.float32)
 
 
+@pytest.mark.parametrize("width", [2, 4, 8])
 @pytest.mark.parametrize("tri_test", [0, 1])
-def test_closest_and_any_match_oracle_large(ctx, tri_test):
+def test_closest_and_any_match_oracle_large(ctx, tri_test, width):
     rng = np.random.default_rng(5)
     fl = S.flatten(S.icosphere_scene(subdiv=6, seed=4, width=8, height=8))
-    sc = geometry_scene(ctx, fl.tris, fl.world, 16, tri_test=tri_test)
+    sc = geometry_scene(ctx, fl.tris, fl.world, 16, tri_test=tri_test, width=width)
     rays = random_rays(rng, 200_000)
     t, p, u, v = sc.Intersect(rays)
     bvh = O.ploc_build(fl.tris, fl.world, 16)
@@ -173,9 +179,10 @@ def test_closest_and_any_match_oracle_large(ctx, tri_test):
     assert np.array_equal(p[:1500], bp)
 
 
-def test_axis_aligned_and_degenerate_rays(ctx):
+@pytest.mark.parametrize("width", [2, 4, 8])
+def test_axis_aligned_and_degenerate_rays(ctx, width):
     fl = S.flatten(S.cornell_box(8, 8))
-    sc = geometry_scene(ctx, fl.tris, fl.world)
+    sc = geometry_scene(ctx, fl.tris, fl.world, width=width)
     rays = np.array([
         [0, 0, 0, 1, 0, 0, 1e-4, np.inf],        # axis aligned
         [0, 0, 0, 0, -1, 0, 1e-4, np.inf],
@@ -308,6 +315,22 @@ def test_render_matches_oracle_film_and_is_deterministic(ctx):
     li_o, film_o = O.render(flat, dict(spp=16, min_bounces=3, max_bounces=8), seed=3)
     assert np.array_equal(f1[..., 3], film_o[..., 3].astype(np.float32))
     np.testing.assert_allclose(f1[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
+
+
+@pytest.mark.parametrize("width", [4, 8])
+def test_wide_tree_renders_the_same_film(ctx, width):
+    """The traversal result does not depend on the tree: a render over the
+    collapsed tree equals the binary tree's bit for bit."""
+    spec = S.icosphere_scene(5, 3, 40, 32)
+    flat = S.flatten(spec)
+    r = api.PTRenderer(api.PTRendererArgs(spp=8, min_bounces=2, max_bounces=10), seed=5)
+    a = r.Render(api.GpuScene(ctx, flat, api.CreatePLOCAggregate(16, bvh_width=2)),
+                 flat.camera).rgbw
+    wide = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(16, bvh_width=width))
+    b = r.Render(wide, flat.camera).rgbw
+    assert same_bits(a, b)
+    info = wide.info()
+    assert 0 < info["device_bytes"]
 
 
 def test_wave_splitting_does_not_change_results():

@@ -45,6 +45,10 @@ def scenes(ctx):
         "three": (api.GpuScene(ctx, three), three.camera),
         "ico_wt": (api.GpuScene(ctx, ico, api.CreatePLOCAggregate(14, tri_test=1)),
                    ico.camera),
+        "ico_w8": (api.GpuScene(ctx, ico, api.CreatePLOCAggregate(14, bvh_width=8)),
+                   ico.camera),
+        "clutter_w4": (api.GpuScene(ctx, clutter, api.CreatePLOCAggregate(14, bvh_width=4)),
+                       clutter.camera),
     }
     return out
 
@@ -71,6 +75,8 @@ def job_list(scenes):
         ("ico_wt", 32, 48, renderer(12, seed=2)),
         ("box", 16, 16, renderer(64, fp64=True)),
         ("ico", 20, 20, renderer(20, drop=True, max_b=16)),
+        ("ico_w8", 24, 40, renderer(10, seed=6)),
+        ("clutter_w4", 40, 24, renderer(6, seed=8, mis=False)),
     ]
 
 
