@@ -947,7 +947,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
 
 void prepare_mj_kernels() {
   for (int tt = 0; tt < 2; ++tt)
-    for (int wd : {2, 4, 8})
+    for (int wd : {2, 4, 8, 4 | (int)kBvhCompressed, 8 | (int)kBvhCompressed})
       dispatch_trace(tt, wd, [&](auto T, auto Wd) {
         constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
         resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);

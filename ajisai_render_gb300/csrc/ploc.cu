@@ -431,6 +431,137 @@ __global__ void k_collapse(const PNode* __restrict__ nodes,
   }
 }
 
+// The same collapse into compressed nodes (layout in scene.cuh), moving the
+// leaf triangles of every node next to each other in `tris_new`.
+template <int W>
+__global__ void k_collapse_c(const PNode* __restrict__ nodes,
+                             const float4* __restrict__ tris_old,
+                             const uint2* __restrict__ fin, uint32_t n_in,
+                             uint2* __restrict__ fout,
+                             uint32_t* __restrict__ counters,
+                             float4* __restrict__ wide,
+                             float4* __restrict__ tris_new) {
+  constexpr int NF = CwLayout<W>::kFloat4;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in;
+       i += gridDim.x * blockDim.x) {
+    const uint2 e = fin[i];
+    uint32_t ch[W];
+    int nc = 1;
+    ch[0] = e.x;
+    while (nc < W) {
+      int best = -1;
+      float ba = 0.f;
+      for (int c = 0; c < nc; ++c) {
+        const PNode x = nodes[ch[c]];
+        if (__float_as_int(x.b.w) != 0) continue;
+        const float a = area(xyz(x.a), xyz(x.b));
+        if (best < 0 || a > ba) {
+          best = c;
+          ba = a;
+        }
+      }
+      if (best < 0) break;
+      const uint32_t f = (uint32_t)__float_as_int(nodes[ch[best]].a.w);
+      ch[best] = f;
+      ch[nc++] = f + 1;
+    }
+    // quantisation grid: origin = lo of the union, 255 steps of 2^e cover
+    // the union's extent per axis
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+    float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int c = 0; c < nc; ++c) {
+      const PNode x = nodes[ch[c]];
+      lo[0] = fminf(lo[0], x.a.x);
+      lo[1] = fminf(lo[1], x.a.y);
+      lo[2] = fminf(lo[2], x.a.z);
+      hi[0] = fmaxf(hi[0], x.b.x);
+      hi[1] = fmaxf(hi[1], x.b.y);
+      hi[2] = fmaxf(hi[2], x.b.z);
+    }
+    uint32_t eb[3];
+    float sc[3];
+    double step[3];
+    for (int a = 0; a < 3; ++a) {
+      const double ext = (double)hi[a] - (double)lo[a];
+      int ex = -126;
+      if (ext > 0.0) {
+        int k = 0;
+        frexp(ext / 255.0, &k);  // ext / 255 < 2^k
+        ex = k;
+      }
+      ex = ex < -126 ? -126 : (ex > 127 ? 127 : ex);
+      eb[a] = (uint32_t)(ex + 127);
+      sc[a] = cw_scale(eb[a]);
+      step[a] = ldexp(1.0, ex);
+    }
+    uint32_t vmask = 0, imask = 0;
+    uint8_t q[6][W];
+    for (int c = 0; c < W; ++c) {
+      if (c >= nc) {
+        for (int k = 0; k < 6; ++k) q[k][c] = 0;
+        continue;
+      }
+      const PNode x = nodes[ch[c]];
+      vmask |= 1u << c;
+      if (__float_as_int(x.b.w) == 0) imask |= 1u << c;
+      const float cl[3] = {x.a.x, x.a.y, x.a.z};
+      const float chh[3] = {x.b.x, x.b.y, x.b.z};
+      for (int a = 0; a < 3; ++a) {
+        double fl = floor(((double)cl[a] - (double)lo[a]) / step[a]);
+        double fh = ceil(((double)chh[a] - (double)lo[a]) / step[a]);
+        uint32_t ql = fl < 0.0 ? 0u : (fl > 255.0 ? 255u : (uint32_t)fl);
+        uint32_t qh = fh < 0.0 ? 0u : (fh > 255.0 ? 255u : (uint32_t)fh);
+        // the decoded planes must enclose the child's box
+        while (ql > 0 &&
+               cw_decode(lo[a], cw_qfloat(0x4B000000u | ql), sc[a]) > cl[a])
+          --ql;
+        while (qh < 255 &&
+               cw_decode(lo[a], cw_qfloat(0x4B000000u | qh), sc[a]) < chh[a])
+          ++qh;
+        q[2 * a][c] = (uint8_t)ql;
+        q[2 * a + 1][c] = (uint8_t)qh;
+      }
+    }
+    const int ni = __popc(imask), nl = __popc(vmask & ~imask);
+    uint32_t base = 0, fo = 0, tb = 0;
+    if (ni) {
+      base = atomicAdd(&counters[1], (uint32_t)ni);
+      fo = atomicAdd(&counters[0], (uint32_t)ni);
+    }
+    if (nl) tb = atomicAdd(&counters[2], (uint32_t)nl);
+    int ji = 0, jl = 0;
+    for (int c = 0; c < nc; ++c) {
+      const PNode x = nodes[ch[c]];
+      if ((imask >> c) & 1u) {
+        fout[fo + ji] = make_uint2(ch[c], base + ji);
+        ++ji;
+      } else {
+        const uint32_t slot = (uint32_t)__float_as_int(x.a.w);
+        for (int k = 0; k < 3; ++k)
+          tris_new[3 * (uint64_t)(tb + jl) + k] = tris_old[3 * (uint64_t)slot + k];
+        ++jl;
+      }
+    }
+    float4* o = wide + (uint64_t)e.y * NF;
+    o[0] = make_float4(lo[0], lo[1], lo[2],
+                       __uint_as_float(eb[0] | (eb[1] << 8) | (eb[2] << 16) |
+                                       (imask << 24)));
+    o[1] = make_float4(__uint_as_float(base), __uint_as_float(tb),
+                       __uint_as_float(vmask), 0.f);
+    uint32_t words[4 * (NF - 2)];
+    for (int k = 0; k < 4 * (NF - 2); ++k) words[k] = 0;
+    for (int k = 0; k < 6; ++k)
+      for (int c = 0; c < W; ++c) {
+        const int byte = k * W + c;
+        words[byte >> 2] |= (uint32_t)q[k][c] << (8 * (byte & 3));
+      }
+    for (int f = 0; f < NF - 2; ++f)
+      o[2 + f] = make_float4(
+          __uint_as_float(words[4 * f]), __uint_as_float(words[4 * f + 1]),
+          __uint_as_float(words[4 * f + 2]), __uint_as_float(words[4 * f + 3]));
+  }
+}
+
 __global__ void k_slot_tris(const float* __restrict__ tris,
                             const int32_t* __restrict__ perm, uint64_t n,
                             float4* __restrict__ out) {
@@ -528,8 +659,12 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   // default: the 4-wide tree (the fastest measured on GB300 for the
   // workloads here; 8-wide nodes cost occupancy)
   const int width = opts.bvh_width ? (int)opts.bvh_width : 4;
-  if (width != 2 && width != 4 && width != 8)
-    return set_err(ctx, AJG_ERR_INVALID, "bvh_width must be 0, 2, 4 or 8");
+  const bool compressed = (width & kBvhCompressed) != 0;
+  const int wn = width & 0xff;  // children per node
+  if (!(width == 2 || wn == 4 || wn == 8) || (width & ~0x1ff))
+    return set_err(ctx, AJG_ERR_INVALID,
+                   "bvh_width must be 0, 2, 4 or 8 (4 and 8 optionally "
+                   "| AJG_BVH_COMPRESSED)");
   float4* bvh =
       width == 2 ? (float4*)keep(inner * 4 * sizeof(float4)) : nullptr;
   float4* slot_tris = (float4*)keep(n * 3 * sizeof(float4));
@@ -686,26 +821,36 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   } else {
     // wide layout: collapse level by level into a worst-case buffer, then
     // keep the nodes made
-    const uint64_t node_f4 = 2 * (uint64_t)width;
+    const uint64_t node_f4 =
+        compressed ? (wn == 8 ? CwLayout<8>::kFloat4 : CwLayout<4>::kFloat4)
+                   : 2 * (uint64_t)wn;
+    // the triangles move into node order for compressed nodes
+    k_slot_tris<<<gb, 256, 0, st>>>(d_tris, perm, n, slot_tris);
     float4* wtmp = tmp.get<float4>(inner * node_f4);
+    float4* tri_tmp = compressed ? tmp.get<float4>(3 * n) : nullptr;
     uint2* fa = tmp.get<uint2>(inner);
     uint2* fb = tmp.get<uint2>(inner);
-    uint32_t* wc = tmp.get<uint32_t>(2);
+    uint32_t* wc = tmp.get<uint32_t>(3);
     if (tmp.err != cudaSuccess)
       return set_err(ctx, AJG_ERR_OOM, "device allocation failed (wide BVH)");
-    const uint32_t init[2] = {0u, 1u};
+    const uint32_t init[3] = {0u, 1u, 0u};
     cudaMemcpyAsync(wc, init, sizeof(init), cudaMemcpyHostToDevice, st);
     const uint2 root = make_uint2(0u, 0u);
     cudaMemcpyAsync(fa, &root, sizeof(root), cudaMemcpyHostToDevice, st);
     uint32_t n_in = 1, levels = 0;
     while (n_in) {
       cudaMemsetAsync(wc, 0, sizeof(uint32_t), st);
-      if (width == 4)
-        k_collapse<4><<<grid_for(n_in, 128), 128, 0, st>>>(nodes, fa, n_in,
-                                                           fb, wc, wtmp);
+      const int g = grid_for(n_in, 128);
+      if (compressed && wn == 4)
+        k_collapse_c<4><<<g, 128, 0, st>>>(nodes, slot_tris, fa, n_in, fb, wc,
+                                           wtmp, tri_tmp);
+      else if (compressed)
+        k_collapse_c<8><<<g, 128, 0, st>>>(nodes, slot_tris, fa, n_in, fb, wc,
+                                           wtmp, tri_tmp);
+      else if (wn == 4)
+        k_collapse<4><<<g, 128, 0, st>>>(nodes, fa, n_in, fb, wc, wtmp);
       else
-        k_collapse<8><<<grid_for(n_in, 128), 128, 0, st>>>(nodes, fa, n_in,
-                                                           fb, wc, wtmp);
+        k_collapse<8><<<g, 128, 0, st>>>(nodes, fa, n_in, fb, wc, wtmp);
       uint32_t h[2] = {0, 0};
       if (cudaMemcpyAsync(h, wc, sizeof(h), cudaMemcpyDeviceToHost, st) !=
               cudaSuccess ||
@@ -722,8 +867,11 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
       return set_err(ctx, AJG_ERR_OOM, "device allocation failed (wide BVH)");
     cudaMemcpyAsync(bvh, wtmp, (uint64_t)num_nodes * node_f4 * sizeof(float4),
                     cudaMemcpyDeviceToDevice, st);
+    if (compressed)
+      cudaMemcpyAsync(slot_tris, tri_tmp, 3 * n * sizeof(float4),
+                      cudaMemcpyDeviceToDevice, st);
   }
-  k_slot_tris<<<gb, 256, 0, st>>>(d_tris, perm, n, slot_tris);
+  if (width == 2) k_slot_tris<<<gb, 256, 0, st>>>(d_tris, perm, n, slot_tris);
   k_shade_data<<<gb, 256, 0, st>>>(d_tris, d_mat, d_flags, n, shade);
   cudaEventRecord(e1, st);
   cudaError_t ce = cudaStreamSynchronize(st);
@@ -760,7 +908,11 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   s->info.ploc_iterations = iters;
   s->info.build_ms = ms;
   s->info.bvh_width = (uint32_t)width;
-  s->info.bvh_node_bytes = width == 2 ? 64u : 32u * (uint32_t)width;
+  s->info.bvh_node_bytes =
+      width == 2 ? 64u
+                 : (compressed ? 16u * (wn == 8 ? CwLayout<8>::kFloat4
+                                                : CwLayout<4>::kFloat4)
+                               : 32u * (uint32_t)wn);
   s->info.bvh_nodes = num_nodes;
   // lights are fitted to the world bounds (default_scene.cpp:41-48)
   const F3 center = (whi + wlo) / 2.f;

@@ -39,7 +39,8 @@ struct DeviceScene {
   int32_t env = -1;      // the scene's environment light (the last one)
   float radius = 0.f;    // (world.max - world.center).length()
   int32_t tri_test = 0;
-  int32_t width = 2;     // node width of `bvh`: 2 (binary PLOC tree), 4, 8
+  int32_t width = 2;     // layout of `bvh`: 2 (binary PLOC tree), 4, 8, or
+                         // 4 / 8 | kBvhCompressed
 };
 
 // Per-job constants of the integrator, shared by the single-job and the
@@ -121,6 +122,35 @@ struct MJTables {
   const Chunk* chunks;
   const WaveHeader* hdr;
 };
+
+// Compressed wide nodes (bvh_width W | kBvhCompressed, W = 4 or 8; 80 bytes
+// for W = 8, 64 for W = 4):
+//   float4 0: node origin (lo corner of the children's union), and
+//             e_x | e_y << 8 | e_z << 16 | imask << 24 (e biased by 127)
+//   float4 1: child_base, tri_base, vmask (uint bits)
+//   then six planes (lo.x, hi.x, lo.y, hi.y, lo.z, hi.z) of W bytes each
+// Child c is valid when vmask bit c is set; an interior child is the wide
+// node child_base + (interior children before c), a leaf the triangle
+// tri_base + (leaf children before c).  A plane decodes as
+// origin + q * 2^e with exactly one rounding (cw_decode); the build picks q
+// so that the decoded box contains the child's box, so the box test stays
+// conservative and the hits are the same as over the binary tree.
+constexpr uint32_t kBvhCompressed = 0x100;
+template <int W>
+struct CwLayout {
+  static constexpr int kFloat4 = (32 + 6 * W + 15) / 16;
+};
+__device__ __forceinline__ float cw_scale(uint32_t eb) {
+  return __uint_as_float(eb << 23);
+}
+__device__ __forceinline__ float cw_qfloat(uint32_t q_bits) {
+  // q_bits = 0x4B000000 | q: the float 2^23 + q, minus 2^23 is exactly q
+  return __uint_as_float(q_bits) - 8388608.f;
+}
+__device__ __forceinline__ float cw_decode(float origin, float fq,
+                                           float scale) {
+  return origin + fq * scale;
+}
 
 // Counters the traversal kernels accumulate (algorithmic bytes for the
 // roofline: nodes * 64 B + triangles * 48 B).

@@ -185,22 +185,25 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 // warp's slowest ray.  FETCH(k, ts) returns the k-th ray; FINISH(k, hit,
 // occluded) stores its result.
 //
-// W is the node width: 2 is the binary PLOC tree (64-byte nodes holding both
-// children's boxes); 4 and 8 are the collapsed wide trees (32*W-byte nodes:
-// the children's boxes as lo.x, hi.x, lo.y, hi.y, lo.z, hi.z groups of four,
-// then the child references).  In a wide node the boxes that pass are
-// visited nearest first: leaf children are tested at once, the nearest
-// interior child is visited next and the others are pushed farthest first.
+// L is the tree layout: 2 is the binary PLOC tree (64-byte nodes holding
+// both children's boxes); 4 and 8 are the collapsed wide trees (32*W-byte
+// nodes: the children's boxes as lo.x, hi.x, lo.y, hi.y, lo.z, hi.z groups
+// of four, then the child references); 4 or 8 | kBvhCompressed the
+// quantised wide nodes (scene.cuh).  In a wide node the leaf children whose
+// box passes are tested at once; for closest hits the nearest interior
+// child is visited next and the others are pushed farthest first.
 #ifndef AJG_REFILL
 #define AJG_REFILL 16
 #endif
 constexpr int kRefill = AJG_REFILL;
 constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
 
-template <int TEST, bool ANY, int W, class FETCH, class FINISH>
+template <int TEST, bool ANY, int L, class FETCH, class FINISH>
 __device__ __forceinline__ void trace_persistent(
     TraceScene ts, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
     uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris, uint32_t* err) {
+  constexpr int W = L & 0xff;  // children per node
+  constexpr bool CMP = (L & (int)kBvhCompressed) != 0;
   constexpr int kIdle = -1, kDone = 0x7fffffff;
   constexpr int kStack = StackDepth<W>::value;
   const unsigned full = 0xffffffffu;
@@ -301,38 +304,91 @@ __device__ __forceinline__ void trace_persistent(
         }
       }
     } else {
-      constexpr int G = W / 4;  // float4 groups per plane
-      const float4* nd = bvh + (uint64_t)node * (2 * W);
       float tn[W];
       int ref[W];
       unsigned inner = 0;  // interior children whose box passed
+      if constexpr (!CMP) {
+        constexpr int G = W / 4;  // float4 groups per plane
+        const float4* nd = bvh + (uint64_t)node * (2 * W);
 #pragma unroll
-      for (int g = 0; g < G; ++g) {
-        const float4 lx = __ldg(nd + 0 * G + g), hx = __ldg(nd + 1 * G + g);
-        const float4 ly = __ldg(nd + 2 * G + g), hy = __ldg(nd + 3 * G + g);
-        const float4 lz = __ldg(nd + 4 * G + g), hz = __ldg(nd + 5 * G + g);
-        const float4 rf = __ldg(nd + 6 * G + g);
-        const float* plx = &lx.x;
-        const float* phx = &hx.x;
-        const float* ply = &ly.x;
-        const float* phy = &hy.x;
-        const float* plz = &lz.x;
-        const float* phz = &hz.x;
-        const float* prf = &rf.x;
+        for (int g = 0; g < G; ++g) {
+          const float4 lx = __ldg(nd + 0 * G + g), hx = __ldg(nd + 1 * G + g);
+          const float4 ly = __ldg(nd + 2 * G + g), hy = __ldg(nd + 3 * G + g);
+          const float4 lz = __ldg(nd + 4 * G + g), hz = __ldg(nd + 5 * G + g);
+          const float4 rf = __ldg(nd + 6 * G + g);
+          const float* plx = &lx.x;
+          const float* phx = &hx.x;
+          const float* ply = &ly.x;
+          const float* phy = &hy.x;
+          const float* plz = &lz.x;
+          const float* phz = &hz.x;
+          const float* prf = &rf.x;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int c = 4 * g + j;
-          ref[c] = __float_as_int(prf[j]);
-          float t0;
-          const bool h = ref[c] != kEmptyRef &&
-                         slab2(plx[j], phx[j], ply[j], phy[j], plz[j], phz[j],
-                               r, lim, t0);
-          tn[c] = t0;
-          if (h && ref[c] < 0 && !finished) {
-            ++n_tris;
-            finished = leaf_test<TEST, ANY>(tris, ~ref[c], r, w, hit);
+          for (int j = 0; j < 4; ++j) {
+            const int c = 4 * g + j;
+            ref[c] = __float_as_int(prf[j]);
+            float t0;
+            const bool h = ref[c] != kEmptyRef &&
+                           slab2(plx[j], phx[j], ply[j], phy[j], plz[j],
+                                 phz[j], r, lim, t0);
+            tn[c] = t0;
+            if (h && ref[c] < 0 && !finished) {
+              ++n_tris;
+              finished = leaf_test<TEST, ANY>(tris, ~ref[c], r, w, hit);
+            }
+            if (h && ref[c] >= 0) inner |= 1u << c;
           }
-          if (h && ref[c] >= 0) inner |= 1u << c;
+        }
+      } else {
+        constexpr int NF = CwLayout<W>::kFloat4;
+        const float4* nd = bvh + (uint64_t)node * NF;
+        const float4 h0 = __ldg(nd), h1 = __ldg(nd + 1);
+        uint32_t qw[4 * (NF - 2)];
+#pragma unroll
+        for (int f = 0; f < NF - 2; ++f) {
+          const float4 v = __ldg(nd + 2 + f);
+          qw[4 * f] = __float_as_uint(v.x);
+          qw[4 * f + 1] = __float_as_uint(v.y);
+          qw[4 * f + 2] = __float_as_uint(v.z);
+          qw[4 * f + 3] = __float_as_uint(v.w);
+        }
+        const uint32_t hb = __float_as_uint(h0.w);
+        const float sx = cw_scale(hb & 0xffu);
+        const float sy = cw_scale((hb >> 8) & 0xffu);
+        const float sz = cw_scale((hb >> 16) & 0xffu);
+        const uint32_t imask = hb >> 24;
+        const uint32_t cbase = __float_as_uint(h1.x);
+        const uint32_t tbase = __float_as_uint(h1.y);
+        const uint32_t vmask = __float_as_uint(h1.z);
+        const uint32_t lmask = vmask & ~imask;
+#pragma unroll
+        for (int c = 0; c < W; ++c) {
+          tn[c] = 0.f;
+          ref[c] = 0;
+          if (!((vmask >> c) & 1u)) continue;
+          // plane k of child c: byte c of the plane's W bytes, decoded
+          // exactly as the build checked it
+          auto plane = [&](int k, float origin, float sc) {
+            const uint32_t word = qw[k * (W / 4) + (c >> 2)];
+            const uint32_t bits =
+                __byte_perm(word, 0x4B000000u, (uint32_t)(c & 3) | 0x7540u);
+            return cw_decode(origin, cw_qfloat(bits), sc);
+          };
+          float t0;
+          if (!slab2(plane(0, h0.x, sx), plane(1, h0.x, sx),
+                     plane(2, h0.y, sy), plane(3, h0.y, sy),
+                     plane(4, h0.z, sz), plane(5, h0.z, sz), r, lim, t0))
+            continue;
+          tn[c] = t0;
+          const uint32_t below = (1u << c) - 1u;
+          if ((imask >> c) & 1u) {
+            ref[c] = (int)(cbase + __popc(imask & below));
+            inner |= 1u << c;
+          } else if (!finished) {
+            ++n_tris;
+            finished = leaf_test<TEST, ANY>(
+                tris, (int)(tbase + __popc(lmask & below)), r, w, hit);
+          }
         }
       }
       if (!finished && inner && ANY) {
@@ -424,30 +480,32 @@ __device__ __forceinline__ void trace_persistent(
   }
 }
 
-// Calls f(TEST, W) with the triangle test and node width as compile-time
-// constants (std::integral_constant), for launching the matching kernel.
-template <class F>
-inline void dispatch_trace(int tri_test, int width, F&& f) {
-  using MT = std::integral_constant<int, AJG_TRI_MOLLER_TRUMBORE>;
-  using WT = std::integral_constant<int, AJG_TRI_WATERTIGHT>;
-  using W2 = std::integral_constant<int, 2>;
-  using W4 = std::integral_constant<int, 4>;
-  using W8 = std::integral_constant<int, 8>;
-  if (tri_test == AJG_TRI_WATERTIGHT) {
-    if (width == 8)
-      f(WT{}, W8{});
-    else if (width == 4)
-      f(WT{}, W4{});
-    else
-      f(WT{}, W2{});
-  } else {
-    if (width == 8)
-      f(MT{}, W8{});
-    else if (width == 4)
-      f(MT{}, W4{});
-    else
-      f(MT{}, W2{});
+// Calls f(TEST, L) with the triangle test and the tree layout as
+// compile-time constants (std::integral_constant), for launching the
+// matching kernel.
+template <class F, class T>
+inline void dispatch_layout(int layout, F&& f, T test) {
+  using L2 = std::integral_constant<int, 2>;
+  using L4 = std::integral_constant<int, 4>;
+  using L8 = std::integral_constant<int, 8>;
+  using C4 = std::integral_constant<int, 4 | (int)kBvhCompressed>;
+  using C8 = std::integral_constant<int, 8 | (int)kBvhCompressed>;
+  switch (layout) {
+    case 4: f(test, L4{}); break;
+    case 8: f(test, L8{}); break;
+    case 4 | (int)kBvhCompressed: f(test, C4{}); break;
+    case 8 | (int)kBvhCompressed: f(test, C8{}); break;
+    default: f(test, L2{}); break;
   }
+}
+template <class F>
+inline void dispatch_trace(int tri_test, int layout, F&& f) {
+  if (tri_test == AJG_TRI_WATERTIGHT)
+    dispatch_layout(layout, f,
+                    std::integral_constant<int, AJG_TRI_WATERTIGHT>{});
+  else
+    dispatch_layout(layout, f,
+                    std::integral_constant<int, AJG_TRI_MOLLER_TRUMBORE>{});
 }
 
 __device__ __forceinline__ void flush_counters(TraceCounters* c, uint32_t rays,

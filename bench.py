@@ -72,8 +72,10 @@ def parse():
                     help="arrival rate as a fraction of the batched throughput")
     ap.add_argument("--rmse-crop", type=int, default=32)
     ap.add_argument("--rmse-spp", type=int, default=4096)
-    ap.add_argument("--bvh-width", type=int, default=0,
-                    help="traversal tree: 2 binary, 4/8 collapsed, 0 library default")
+    ap.add_argument("--bvh-width", type=lambda v: (int(v[:-1]) | 0x100) if v.endswith("c")
+                    else int(v), default=0,
+                    help="traversal tree: 2 binary, 4/8 collapsed, 4c/8c collapsed with "
+                         "quantised boxes, 0 library default")
     return ap.parse_args()
 
 
@@ -359,6 +361,11 @@ def run_ours(args):
             "kernel_ms_per_step": {"k_extend": st["closest_ms"] / args.steps,
                                    "k_shadow": st["any_ms"] / args.steps,
                                    "k_shade": st["shade_ms"] / args.steps},
+            "trace_stats": {
+                kind: {"rays_per_step": st[f"{kind}_rays"] / args.steps,
+                       "nodes_per_ray": st[f"{kind}_nodes"] / max(1, st[f"{kind}_rays"]),
+                       "tris_per_ray": st[f"{kind}_tris"] / max(1, st[f"{kind}_rays"])}
+                for kind in ("closest", "any")},
             "step_ms": step_ms, "nonfinite_pixels": nonfinite,
             "batched": batched, "served": served,
             "impl": "ours"}))

@@ -64,6 +64,7 @@ enum {
 enum { AJG_MAT_DIFFUSE = 0, AJG_MAT_DISNEY = 1 };
 enum { AJG_LIGHT_DIRECTIONAL = 0, AJG_LIGHT_ENV = 1 };
 enum { AJG_TRI_MOLLER_TRUMBORE = 0, AJG_TRI_WATERTIGHT = 1 };
+#define AJG_BVH_COMPRESSED 0x100 /* ajg_scene_opts.bvh_width flag */
 
 typedef struct ajg_ctx ajg_ctx;
 typedef struct ajg_scene ajg_scene;
@@ -117,9 +118,12 @@ typedef struct ajg_scene_opts {
                              (ploc_aggregate.cpp:97-130), so the tree is the
                              reference's own; 0: correct stable sort */
   uint32_t bvh_width;     /* traversal tree: 2 the binary PLOC tree, 4 or 8
-                             the tree collapsed into 4/8-wide nodes (same
-                             hits: the traversal result does not depend on
-                             the tree); 0: the library's default, 4 */
+                             the tree collapsed into 4/8-wide nodes, either
+                             | AJG_BVH_COMPRESSED for nodes with 8-bit
+                             quantised child boxes (same hits: the traversal
+                             result does not depend on the tree and the
+                             quantised boxes enclose the exact ones); 0: the
+                             library's default, 4 */
 } ajg_scene_opts;
 
 /* Thin-lens camera: the two matrices ThinLensCamera keeps

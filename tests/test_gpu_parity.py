@@ -9,6 +9,9 @@ from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
 
+# traversal trees: binary, 4/8-wide, and 4/8-wide with quantised boxes
+LAYOUTS = [2, 4, 8, 4 | 0x100, 8 | 0x100]
+
 
 @pytest.fixture(scope="module")
 def ctx():
@@ -93,7 +96,7 @@ def test_ploc_full_size_properties(ctx):
     assert info["num_triangles"] == fl.n_tris and info["ploc_iterations"] > 0
 
 
-@pytest.mark.parametrize("width", [2, 4, 8])
+@pytest.mark.parametrize("width", LAYOUTS)
 def test_single_and_two_triangle_scenes(ctx, width):
     t1 = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
     sc = geometry_scene(ctx, t1, [0, 0, 0, 1, 1, 0], width=width)
@@ -130,7 +133,7 @@ def test_reference_sort_overflow_is_refused(ctx):
 
 
 # ----------------------------------------------------------------- trace --
-@pytest.mark.parametrize("width", [2, 4, 8])
+@pytest.mark.parametrize("width", LAYOUTS)
 @pytest.mark.parametrize("case", ["trace_ico4.npz", "trace_soup.npz"])
 def test_closest_hit_matches_reference(ctx, golden, case, width):
     """The reference's own tree (radix_compat), traversed as built or
@@ -155,7 +158,7 @@ def random_rays(rng, n, spread=2.0):
     return np.concatenate([o, d, np.full((n, 1), 1e-4), tmax[:, None]], 1).astype(np.float32)
 
 
-@pytest.mark.parametrize("width", [2, 4, 8])
+@pytest.mark.parametrize("width", LAYOUTS)
 @pytest.mark.parametrize("tri_test", [0, 1])
 def test_closest_and_any_match_oracle_large(ctx, tri_test, width):
     rng = np.random.default_rng(5)
@@ -179,7 +182,7 @@ def test_closest_and_any_match_oracle_large(ctx, tri_test, width):
     assert np.array_equal(p[:1500], bp)
 
 
-@pytest.mark.parametrize("width", [2, 4, 8])
+@pytest.mark.parametrize("width", LAYOUTS)
 def test_axis_aligned_and_degenerate_rays(ctx, width):
     fl = S.flatten(S.cornell_box(8, 8))
     sc = geometry_scene(ctx, fl.tris, fl.world, width=width)
@@ -317,7 +320,7 @@ def test_render_matches_oracle_film_and_is_deterministic(ctx):
     np.testing.assert_allclose(f1[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
 
 
-@pytest.mark.parametrize("width", [4, 8])
+@pytest.mark.parametrize("width", LAYOUTS[1:])
 def test_wide_tree_renders_the_same_film(ctx, width):
     """The traversal result does not depend on the tree: a render over the
     collapsed tree equals the binary tree's bit for bit."""

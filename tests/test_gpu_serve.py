@@ -49,6 +49,10 @@ def scenes(ctx):
                    ico.camera),
         "clutter_w4": (api.GpuScene(ctx, clutter, api.CreatePLOCAggregate(14, bvh_width=4)),
                        clutter.camera),
+        "ico_c8": (api.GpuScene(ctx, ico, api.CreatePLOCAggregate(14, bvh_width=0x108)),
+                   ico.camera),
+        "box_c4": (api.GpuScene(ctx, box, api.CreatePLOCAggregate(14, bvh_width=0x104)),
+                   box.camera),
     }
     return out
 
@@ -77,6 +81,8 @@ def job_list(scenes):
         ("ico", 20, 20, renderer(20, drop=True, max_b=16)),
         ("ico_w8", 24, 40, renderer(10, seed=6)),
         ("clutter_w4", 40, 24, renderer(6, seed=8, mis=False)),
+        ("ico_c8", 32, 32, renderer(9, seed=11)),
+        ("box_c4", 24, 32, renderer(7, seed=12)),
     ]
 
 
