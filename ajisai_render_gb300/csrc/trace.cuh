@@ -40,7 +40,7 @@ __device__ __forceinline__ bool mt_test(const RayQ& r, float4 A, float4 B,
   const F3 h = cross3(r.d, e1);
   const float a = dot3f(e0, h);
   if (a > -1e-6f && a < 1e-6f) return false;
-  const float f = 1.f / a;
+  const float f = __frcp_rn(a);  // == 1.f / a, correctly rounded
   const F3 s = r.o - v0;
   const float u = f * dot3f(s, h);
   if (u < 0.f || u > 1.f) return false;
@@ -101,7 +101,7 @@ __device__ __forceinline__ bool wt_test(const RayQ& r, const WtSetup& w,
   const float det = U + V + W;
   if (det == 0.f) return false;
   const float T = U * (w.sz * Az0) + V * (w.sz * Bz0) + W * (w.sz * Cz0);
-  const float rcp = 1.f / det;
+  const float rcp = __frcp_rn(det);
   const float t = T * rcp;
   if (!(t > r.tmin && t < r.tmax)) return false;
   t_out = t;
