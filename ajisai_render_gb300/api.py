@@ -16,6 +16,7 @@ Everything runs in libajisai_gpu.so; this module only packs arguments.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -37,9 +38,13 @@ class Context:
         h = C.c_void_p()
         _lib.check(self.lib.ajg_create_context(C.byref(cfg), C.byref(h)))
         self.h = h
+        self._scenes = weakref.WeakSet()
 
     def close(self):
+        """Destroy the context; its scenes still alive are released first."""
         if self.h:
+            for sc in list(self._scenes):
+                sc.release()
             self.lib.ajg_destroy_context(self.h)
             self.h = None
 
@@ -203,11 +208,12 @@ class GpuScene:
             _ptr(world), mats, flat.materials.shape[0], lights,
             flat.lights.shape[0], C.byref(opts), C.byref(h)))
         self.h = h
+        ctx._scenes.add(self)
 
     def release(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.ctx.lib.ajg_scene_release(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
