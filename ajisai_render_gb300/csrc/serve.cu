@@ -27,6 +27,13 @@
 
 #include "scene.cuh"
 
+// the layouts the ctypes binding and the header comments state
+static_assert(sizeof(ajg_job_desc) == 224, "ajg_job_desc layout");
+static_assert(sizeof(ajg_job_status) == 56, "ajg_job_status layout");
+static_assert(sizeof(ajg_serve_opts) == 16, "ajg_serve_opts layout");
+static_assert(sizeof(ajg_serve_stats) == 80, "ajg_serve_stats layout");
+static_assert(sizeof(ajg_scene_info) == 48, "ajg_scene_info layout");
+
 namespace ajg {
 namespace {
 

@@ -599,3 +599,56 @@ def batch_workload(n: int = 48, seed: int = 0, resolutions=(128, 256, 512, 1024)
         jobs.append({"scene_seed": int(seed * 1000 + i), "tris": tris, "res": res,
                      "spp": spp})
     return jobs
+
+
+def _rotation(rng: np.random.Generator) -> np.ndarray:
+    """A uniformly random 3x3 rotation (QR of a Gaussian matrix)."""
+    q, r = np.linalg.qr(rng.normal(size=(3, 3)))
+    q *= np.sign(np.diag(r))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def project(camera: Camera, points: np.ndarray) -> np.ndarray:
+    """Raster coordinates (x, y) of world points through the camera's
+    matrices (the inverse of the ray generation's mapping)."""
+    m = np.asarray(camera.pack(), np.float64)
+    r2c = m[0:16].reshape(4, 4).T
+    c2w = m[16:32].reshape(4, 4).T
+    w2r = np.linalg.inv(r2c) @ np.linalg.inv(c2w)
+    p = np.concatenate([points, np.ones((len(points), 1))], 1) @ w2r.T
+    return p[:, :2] / p[:, 3:4]
+
+
+def large_scene(seed: int = 0, width: int = 1920, height: int = 1080,
+                copies: int = 20, subdiv: int = 8, box: float = 100.0) -> Scene:
+    """The precision-stress workload: `copies` copies of the single-job
+    displaced icosphere (subdivision 8: 26,214,400 triangles for 20), each
+    with a random rotation, a uniform scale U[0.5, 2] and a position inside
+    a box^3 cube, flattened into one tree, each with its own Disney
+    parameters; a constant environment of 0.5 and a directional light of
+    2.0; a pinhole camera outside the cube looking at its centre."""
+    rng = np.random.default_rng(seed)
+    pos0, nrm0, idx = displaced_icosphere(subdiv, seed)
+    pos0 = pos0.astype(np.float64)
+    nrm0 = nrm0.astype(np.float64)
+    prims, mats, centers, scales = [], [], [], []
+    half = box / 2.0
+    for k in range(copies):
+        rot = _rotation(rng)
+        scale = rng.uniform(0.5, 2.0)
+        t = rng.uniform(-half + 2.5 * scale, half - 2.5 * scale, 3)
+        pos = (pos0 @ rot.T) * scale + t
+        nrm = nrm0 @ rot.T
+        mats.append(disney_params(rng))
+        prims.append(Mesh(pos.astype(F32), idx, nrm.astype(F32), k, False))
+        centers.append(t)
+        scales.append(scale)
+    lights = [DirectionalLight((0.3, 1.0, 0.2), 2.0), EnvLight(0.5)]
+    cam = Camera((0.0, 0.35 * box, 1.55 * box), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0,
+                 width, height)
+    scene = Scene(prims, mats, lights, cam)
+    scene.copy_centers = np.array(centers)
+    scene.copy_scales = np.array(scales)
+    return scene

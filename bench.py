@@ -72,6 +72,10 @@ def parse():
                     help="arrival rate as a fraction of the batched throughput")
     ap.add_argument("--rmse-crop", type=int, default=32)
     ap.add_argument("--rmse-spp", type=int, default=4096)
+    ap.add_argument("--large", action="store_true",
+                    help="also run the large-scene workload (26.2 M triangles, "
+                         "1920x1080, 1024 spp, depth 32, FP64 crop reference)")
+    ap.add_argument("--large-ref-spp", type=int, default=65536)
     ap.add_argument("--bvh-width", type=lambda v: (int(v[:-1]) | 0x100) if v.endswith("c")
                     else int(v), default=0,
                     help="traversal tree: 2 binary, 4/8 collapsed, 4c/8c collapsed with "
@@ -351,7 +355,9 @@ def run_ours(args):
     img = out.float().cpu().numpy()
     nonfinite = int((~np.isfinite(img)).any(-1).sum())
 
-    batched = served = None
+    batched = served = large = None
+    if rank == 0 and world == 1 and args.large:
+        large = run_large(args, local)
     if rank == 0 and world == 1 and not args.no_batch:
         bctx = api.Context(local, hbm_budget_bytes=150 << 30)
         batched = run_batched(bctx, args)
@@ -380,7 +386,7 @@ def run_ours(args):
                        "tris_per_ray": st[f"{kind}_tris"] / max(1, st[f"{kind}_rays"])}
                 for kind in ("closest", "any")},
             "step_ms": step_ms, "nonfinite_pixels": nonfinite,
-            "batched": batched, "served": served,
+            "batched": batched, "served": served, "large": large,
             "impl": "ours"}))
     scene.release()
     ctx.close()
@@ -537,6 +543,69 @@ def run_served(ctx, args, capacity_samples_s):
         "msamples_s": samples / (span_ms / 1e3) / 1e6,
         "wall_s": t_end - t0,
     }
+
+
+def run_large(args, local):
+    """The large-scene workload: one job over 20 transformed copies of the
+    displaced icosphere in one tree, its time and its RMSE against an
+    FP64-accumulated render of a 128x128 crop."""
+    import torch
+    from ajisai_render_gb300 import api
+    from ajisai_render_gb300 import scenes as S
+    t0 = time.perf_counter()
+    spec = S.large_scene(seed=3)
+    flat = S.flatten(spec)
+    gen_s = time.perf_counter() - t0
+    ctx = api.Context(local)
+    try:
+        scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
+        info = scene.info()
+        args_r = api.PTRendererArgs(spp=1024, min_bounces=MIN_B, max_bounces=32)
+        rend = api.PTRenderer(args_r, seed=21)
+        W, H = spec.camera.width, spec.camera.height
+        out = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+        stream = torch.cuda.current_stream()
+        warm = api.PTRenderer(api.PTRendererArgs(spp=1, min_bounces=MIN_B, max_bounces=32))
+        warm.render_device(scene, flat.camera, out.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        rend.render_device(scene, flat.camera, out.data_ptr(), stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        # the crop: centred on the copy that looks largest on the film
+        c = 128
+        cam_pos = np.asarray(spec.camera.position)
+        px = S.project(spec.camera, spec.copy_centers)
+        size = spec.copy_scales / np.linalg.norm(spec.copy_centers - cam_pos, axis=1)
+        inside = (px[:, 0] >= c // 2) & (px[:, 0] < W - c // 2 - 1) & \
+                 (px[:, 1] >= c // 2) & (px[:, 1] < H - c // 2 - 1)
+        k = int(np.argmax(np.where(inside, size, -1.0)))
+        x0, y0 = int(px[k, 0]) - c // 2, int(px[k, 1]) - c // 2
+        ref_r = api.PTRenderer(api.PTRendererArgs(spp=args.large_ref_spp, min_bounces=MIN_B,
+                                                  max_bounces=32), seed=99, fp64_film=True)
+        t = time.perf_counter()
+        (ref, st), = ctx.render_batch([(scene, flat.camera, ref_r, (x0, y0, c + 1, c + 1))])
+        ref_s = time.perf_counter() - t
+        crop = out[y0:y0 + c, x0:x0 + c].contiguous()
+        refd = torch.from_numpy(np.ascontiguousarray(ref.rgbw[:c, :c])).cuda()
+        e, npx = ctx.image_rmse(crop.data_ptr(), refd.data_ptr(), c, c)
+        img = out.cpu().numpy()
+        samples = W * H * 1024
+        return {"workload": f"{flat.n_tris:,} triangles (20 copies of the displaced "
+                            "icosphere, random rotation, scale U[0.5,2], in a 100^3 box, "
+                            "one tree), 1920x1080, 1024 spp, depth 32, Disney per copy",
+                "msamples_s": samples / (ms / 1e3) / 1e6, "render_s": ms / 1e3,
+                "ploc_build_ms": info["build_ms"], "bvh_width": info["bvh_width"],
+                "device_bytes": info["device_bytes"],
+                "rmse_vs_fp64_crop": {"crop": f"{c}x{c} at ({x0},{y0})",
+                                      "reference_spp": args.large_ref_spp, "rmse": e,
+                                      "pixels": npx, "reference_s": ref_s},
+                "nonfinite_pixels": int((~np.isfinite(img)).any(-1).sum()),
+                "scene_generation_s": gen_s}
+    finally:
+        ctx.close()
 
 
 def i_seed(k, res, spp):

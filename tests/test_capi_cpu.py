@@ -61,6 +61,33 @@ def test_null_arguments_are_rejected_without_a_gpu(lib):
     assert lib.ajg_scene_release(None) == 1
 
 
+def test_serving_entry_points_reject_null_arguments(lib):
+    """The request loop's entry points check their arguments before they
+    touch a device."""
+    from ajisai_render_gb300 import _lib
+    st = _lib.JobStatus()
+    jid = C.c_uint64()
+    assert lib.ajg_submit(None, None, C.byref(jid)) == 1
+    assert lib.ajg_poll(None, 1, C.byref(st)) == 1
+    assert lib.ajg_wait(None, 1, 0, C.byref(st)) == 1
+    assert lib.ajg_job_read(None, 1, None, C.byref(st)) == 1
+    assert lib.ajg_cancel(None, 1) == 1
+    assert lib.ajg_job_release(None, 1) == 1
+    assert lib.ajg_render_batch(None, None, 0, None) == 1
+    assert lib.ajg_serve_configure(None, None) == 1
+    assert lib.ajg_serve_get_stats(None, None) == 1
+    assert lib.ajg_image_rmse(None, None, 0, None, 0, 0, 0, None, None) == 1
+
+
+def test_serving_structs_match_header(lib):
+    from ajisai_render_gb300 import _lib
+    assert C.sizeof(_lib.JobDesc) == 8 + 144 + 32 + 16 + 8 + 16
+    assert C.sizeof(_lib.JobStatus) == 24 + 32
+    assert C.sizeof(_lib.ServeOpts) == 16
+    assert C.sizeof(_lib.ServeStats) == 80
+    assert C.sizeof(_lib.SceneInfo) == 48
+
+
 def test_context_creation_reports_missing_device(lib):
     import torch
     if torch.cuda.is_available():
