@@ -161,6 +161,46 @@ SIGNATURES = {
                         C.POINTER(C.c_double), C.POINTER(C.c_uint64)], C.c_int),
 }
 
+class HostSceneView(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint64), ("tris", C.c_void_p),
+                ("corner_normals", C.c_void_p), ("tri_material", C.c_void_p),
+                ("tri_flags", C.c_void_p), ("world", C.c_float * 6),
+                ("num_materials", C.c_uint32), ("num_lights", C.c_uint32),
+                ("materials", C.c_void_p), ("lights", C.c_void_p),
+                ("opts", SceneOpts), ("camera", Camera), ("params", RenderParams),
+                ("num_outputs", C.c_uint32), ("reserved", C.c_uint32),
+                ("outputs", C.POINTER(C.c_char_p))]
+
+
+HOST_LIB_PATH = HERE / "_build" / "libajisai_host.so"
+HOST_SIGNATURES = {
+    "ajh_load_scene": ([C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t],
+                       C.c_int),
+    "ajh_scene_view_get": ([C.c_void_p, C.POINTER(HostSceneView)], C.c_int),
+    "ajh_scene_free": ([C.c_void_p], None),
+    "ajh_write_image": ([C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_char_p,
+                         C.c_size_t], C.c_int),
+}
+_host = None
+
+
+def load_host():
+    """The host library (scene files, image output; no CUDA)."""
+    global _host
+    if _host is not None:
+        return _host
+    if not HOST_LIB_PATH.exists():
+        raise RuntimeError(f"{HOST_LIB_PATH} is missing: build it with "
+                           "`python -m ajisai_render_gb300.build`")
+    lib = C.CDLL(str(HOST_LIB_PATH))
+    for name, (args, res) in HOST_SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _host = lib
+    return lib
+
+
 _lib = None
 
 

@@ -400,3 +400,78 @@ class RenderJob:
 
     def release(self):
         self.ctx.check(self.ctx.lib.ajg_job_release(self.ctx.h, self.id))
+
+
+# ---------------------------------------------------------- scene files --
+@dataclass
+class SceneFile:
+    """An Ajisai YAML scene file as the GPU path reads it (see
+    include/ajisai_host.h): the flat scene, the camera record, the
+    renderer's arguments and seed, the PLOC options and the files its
+    save_to_img post processors name."""
+    flat: FlatScene
+    camera: np.ndarray
+    args: PTRendererArgs
+    seed: int
+    aggregate: AggregateOptions
+    outputs: list
+
+
+def load_scene_file(path) -> SceneFile:
+    """Read a scene file (the reference's YAML format) with the host
+    library: main.cpp's scene, camera and renderer nodes."""
+    lib = _lib.load_host()
+    h = C.c_void_p()
+    err = C.create_string_buffer(1024)
+    if lib.ajh_load_scene(str(path).encode(), C.byref(h), err, len(err)) != 0:
+        raise ValueError(err.value.decode())
+    try:
+        v = _lib.HostSceneView()
+        lib.ajh_scene_view_get(h, C.byref(v))
+        n = v.num_triangles
+
+        def arr(ptr, count, dtype, shape):
+            if count == 0:
+                return np.zeros(shape, dtype)
+            buf = (C.c_char * (count * np.dtype(dtype).itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype).copy().reshape(shape)
+
+        mats = arr(v.materials, v.num_materials * 16, F32, (v.num_materials, 16))
+        mats[:, 0] = arr(v.materials, v.num_materials * 16, np.uint32,
+                         (v.num_materials, 16))[:, 0]
+        lights = arr(v.lights, v.num_lights * 12, F32, (v.num_lights, 12))
+        if v.num_lights:
+            lights[:, 0] = arr(v.lights, v.num_lights * 12, np.uint32,
+                               (v.num_lights, 12))[:, 0]
+        cam = np.zeros(36, F32)
+        cam[0:16] = np.array(v.camera.raster2camera, F32)
+        cam[16:32] = np.array(v.camera.camera2world, F32)
+        cam[32], cam[33] = v.camera.lens_radius, v.camera.focal_distance
+        cam[34], cam[35] = v.camera.width, v.camera.height
+        flat = FlatScene(
+            tris=arr(v.tris, n * 9, F32, (n, 9)),
+            corner_n=arr(v.corner_normals, n * 9, F32, (n, 9)),
+            tri_mat=arr(v.tri_material, n, np.int32, (n,)),
+            tri_flags=arr(v.tri_flags, n, np.int32, (n,)),
+            world=np.array(v.world, F32), materials=mats, lights=lights, camera=cam)
+        p = v.params
+        args = PTRendererArgs(spp=p.spp, min_bounces=p.min_bounces,
+                              max_bounces=p.max_bounces, cont_prob=p.cont_prob,
+                              use_mis=bool(p.use_mis))
+        agg = AggregateOptions(v.opts.search_radius, v.opts.tri_test,
+                               bool(v.opts.radix_compat), v.opts.bvh_width)
+        outs = [v.outputs[i].decode() for i in range(v.num_outputs)]
+        return SceneFile(flat, cam, args, int(p.seed), agg, outs)
+    finally:
+        lib.ajh_scene_free(h)
+
+
+def write_image(path, rgbw: np.ndarray):
+    """Write a film (rgbw [h, w, 4]) as .pfm (float) or .png (8-bit, the
+    reference's ImageWriter conversion)."""
+    lib = _lib.load_host()
+    a = np.ascontiguousarray(rgbw, F32)
+    err = C.create_string_buffer(1024)
+    if lib.ajh_write_image(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0],
+                           err, len(err)) != 0:
+        raise ValueError(err.value.decode())

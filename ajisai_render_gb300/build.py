@@ -92,5 +92,43 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return lib
 
 
+HOST = HERE / "host"
+HOST_LIB = BUILD / "libajisai_host.so"
+CLI = BUILD / "ajisai_gpu"
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(INCLUDE)]
+
+
+def build_host(force: bool = False) -> Path:
+    """The host side (g++, no CUDA): libajisai_host.so -- scene files and
+    image output -- and the ajisai_gpu command line, linked against
+    libajisai_gpu.so (run from _build/)."""
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    lib_srcs = [HOST / f for f in ("yaml_lite.cpp", "obj_lite.cpp", "scene_file.cpp",
+                                   "image_out.cpp", "host_capi.cpp")]
+    deps = sorted(HOST.glob("*.h")) + sorted(HOST.glob("*.cpp")) + headers() + \
+        [Path(__file__)]
+    BUILD.mkdir(parents=True, exist_ok=True)
+    if force or _stale(HOST_LIB, deps):
+        tmp = HOST_LIB.with_suffix(".so.tmp")
+        r = subprocess.run([cxx, *HOST_FLAGS, "-shared", "-fvisibility=hidden",
+                            "-o", str(tmp), *map(str, lib_srcs)],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("host library build failed:\n" + r.stderr)
+        os.replace(tmp, HOST_LIB)
+    if LIB.exists() and (force or _stale(CLI, deps + [LIB])):
+        srcs = [HOST / "cli.cpp"] + [x for x in lib_srcs if x.name != "host_capi.cpp"]
+        tmp = CLI.with_suffix(".tmp")
+        r = subprocess.run([cxx, *HOST_FLAGS, "-o", str(tmp), *map(str, srcs),
+                            "-L", str(BUILD), "-lajisai_gpu",
+                            "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("ajisai_gpu build failed:\n" + r.stderr)
+        os.replace(tmp, CLI)
+    return HOST_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if not TAG:
+        print(build_host(force="--force" in sys.argv))

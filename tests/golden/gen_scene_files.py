@@ -1,0 +1,83 @@
+"""Writes the scene-file fixtures in the reference's YAML format
+(factory/creator/*.cpp keys): the Cornell-style box of
+ajisai_render_gb300.scenes.cornell_box, block style, and the same scene in
+flow style.  The cube matrices are the float32 values scenes.py uses,
+printed so that they read back bit for bit.
+
+    python tests/golden/gen_scene_files.py
+"""
+from pathlib import Path
+
+import numpy as np
+
+import sys
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from ajisai_render_gb300 import scenes as S  # noqa: E402
+
+OUT = Path(__file__).resolve().parent / "scenes"
+
+
+def f32(v) -> str:
+    """Shortest decimal that reads back (decimal -> float) as the float32."""
+    x = np.float32(v)
+    return str(int(x)) if float(x).is_integer() else np.format_float_positional(
+        x, unique=True, trim="-")
+
+
+def vec(v) -> str:
+    return "[" + ", ".join(f32(x) for x in v) + "]"
+
+
+def cornell_yaml(flow: bool) -> str:
+    sc = S.cornell_box(256, 256)
+    mats = {0: (0.73, 0.73, 0.73), 1: (0.65, 0.05, 0.05), 2: (0.12, 0.45, 0.15)}
+    lines = ["# Cornell-style box: 5 walls (open front), two rotated boxes,",
+             "# a directional light and a constant environment.",
+             "scene:", "  type: default", "  primitives:"]
+    for p in sc.primitives:
+        if isinstance(p, S.Quad):
+            geo = (f"{{type: twosided, internal: {{type: quad, a: {vec(p.a)}, "
+                   f"b: {vec(p.b)}, c: {vec(p.c)}, d: {vec(p.d)}}}}}")
+        else:
+            geo = (f"{{type: cube, transform: {{type: matrix, matrix: "
+                   f"{vec(p.transform)}}}}}")
+        mat = f"{{type: diffuse, albedo: {{type: constant, texel: {vec(mats[p.material])}}}}}"
+        if flow:
+            lines.append(f"    - {{type: geometry, geometry: {geo}, material: {mat}}}")
+        else:
+            lines += ["    - type: geometry", f"      geometry: {geo}",
+                      "      material:", "        type: diffuse",
+                      f"        albedo: {{type: constant, texel: {vec(mats[p.material])}}}"]
+    lines += ["  lights:",
+              "    - type: directional",
+              "      direction: [0.3, 1.0, 0.2]   # toward the light",
+              "      emission: [3, 3, 3]",
+              "    - type: envmap",
+              "      texture:",
+              "        type: constant",
+              "        texel: 0.2",
+              "  aggregate: {type: ploc, search_radius: 14}",
+              "camera:",
+              "  type: thin_lens",
+              "  resolution: [256, 256]",
+              "  position: [0, 0, 1.9]",
+              "  look_at: [0, 0, 0]",
+              "  up: [0, 1, 0]",
+              "  fov: 40",
+              "renderer:",
+              "  type: pt",
+              "  spp: 64",
+              "  min_bounces: 3",
+              "  max_bounces: 8",
+              "post_processors:",
+              "  - type: save_to_img",
+              "    filename: cornell.png"]
+    return "\n".join(lines) + "\n"
+
+
+if __name__ == "__main__":
+    OUT.mkdir(exist_ok=True)
+    (OUT / "cornell_box.yaml").write_text(cornell_yaml(False))
+    (OUT / "cornell_box_flow.yaml").write_text(cornell_yaml(True))
+    print("wrote", OUT)
