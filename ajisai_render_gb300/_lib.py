@@ -103,7 +103,7 @@ class JobStatus(C.Structure):
 
 class ServeOpts(C.Structure):
     _fields_ = [("policy", C.c_uint32), ("max_active_jobs", C.c_uint32),
-                ("inflight_waves", C.c_uint32), ("reserved", C.c_uint32)]
+                ("inflight_waves", C.c_uint32), ("wave_paths", C.c_uint32)]
 
 
 class ServeStats(C.Structure):

@@ -84,9 +84,9 @@ class Context:
 
     # ---- request loop (ajg_submit / ajg_poll / ajg_wait / ajg_cancel) ----
     def configure_serving(self, policy: str = "fair", max_active_jobs: int = 0,
-                          inflight_waves: int = 0):
+                          inflight_waves: int = 0, wave_paths: int = 0):
         pol = {"fair": _lib.SCHED_FAIR, "fifo": _lib.SCHED_FIFO}[policy]
-        o = _lib.ServeOpts(pol, max_active_jobs, inflight_waves, 0)
+        o = _lib.ServeOpts(pol, max_active_jobs, inflight_waves, wave_paths)
         self.check(self.lib.ajg_serve_configure(self.h, C.byref(o)))
 
     def submit(self, scene: "GpuScene", camera, renderer: "PTRenderer",

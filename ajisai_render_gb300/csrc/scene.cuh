@@ -184,7 +184,9 @@ struct ajg_ctx {
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
   ajg::Server* server = nullptr;  // the request loop, started on first use
   std::mutex server_mu;
-  uint32_t wave_paths = 1u << 22;
+  // paths in flight per wave: big enough that the persistent traversal
+  // launches are long against their drain (~10 GB of wave state)
+  uint32_t wave_paths = 1u << 25;
   uint64_t hbm_budget = 0;
   uint64_t resident_bytes = 0;
   cudaStream_t stream = nullptr;

@@ -129,6 +129,7 @@ struct Server {
   std::condition_variable cv_work, cv_done;
   bool stop = false;
   ajg_serve_opts opts{AJG_SCHED_FAIR, 256, 2, 0};
+  uint64_t want_P = 0;  // wave size the next arena gets (0: the context's)
   uint64_t next_id = 1;
   std::deque<Job*> pending;
   std::vector<Job*> active;  // admitted, not ended (admission order)
@@ -162,7 +163,7 @@ struct Server {
   bool plan_and_launch();
   void retire_oldest();
   void end_job_locked(Job* j, uint32_t state, int err);
-  int ensure_arena(int nt);
+  int ensure_arena(int nt, uint64_t target_paths);
   cudaGraphExec_t graph_for(int bounces, int tri_test, int width);
 };
 
@@ -179,16 +180,16 @@ size_t tables_size() {
 
 }  // namespace
 
-int Server::ensure_arena(int nt) {
-  if (arena && nt <= NT) return AJG_OK;
+int Server::ensure_arena(int nt, uint64_t target) {
+  if (arena && nt <= NT && P == target) return AJG_OK;
   // a bigger light count needs a bigger arena: drain, then regrow
   while (!inflight.empty()) retire_oldest();
   for (auto& g : graphs) cudaGraphExecDestroy(g.second);
   graphs.clear();
   if (arena) cudaFree(arena);
   arena = nullptr;
-  P = ctx->wave_paths;
-  NT = std::max(nt, 3);
+  P = target;
+  NT = std::max(nt, NT > 0 ? NT : 3);
   arena_bytes = wave_bytes(P, NT, true);
   if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) {
     arena = nullptr;
@@ -259,7 +260,8 @@ bool Server::admit_locked() {
     // the wave arena counts from the first admission on, allocated or not
     const uint64_t arena_need = std::max<uint64_t>(
         arena_bytes,
-        wave_bytes(ctx->wave_paths, std::max(3, (int)j->jp.nl + 1), true));
+        wave_bytes(want_P ? want_P : ctx->wave_paths,
+                   std::max(3, (int)j->jp.nl + 1), true));
     const uint64_t held =
         ctx->resident_bytes + arena_need + stats.active_bytes;
     if (budget && held + j->bytes > budget) {
@@ -372,8 +374,10 @@ uint64_t remaining_paths(const Job* j) {
 bool Server::plan_and_launch() {
   std::vector<Plan> plan;
   int bounces = 0, tri_test = -1, width = 0, nt_max = 1;
+  uint64_t target_P = 0;
   {
     std::lock_guard<std::mutex> lk(mu);
+    target_P = want_P ? want_P : ctx->wave_paths;
     for (Job* j : active) {
       if (j->cancel || j->s_cur >= j->prm.spp) continue;
       if (tri_test < 0) {
@@ -384,7 +388,7 @@ bool Server::plan_and_launch() {
     }
     if (tri_test < 0) return false;
   }
-  if (ensure_arena(nt_max) != AJG_OK) {
+  if (ensure_arena(nt_max, target_P) != AJG_OK) {
     std::lock_guard<std::mutex> lk(mu);
     std::vector<Job*> fail_jobs;
     for (Job* j : active)
@@ -801,12 +805,15 @@ int ajg_serve_configure(ajg_ctx* ctx, const ajg_serve_opts* opts) {
     return ajg::fail(ctx, AJG_ERR_INVALID, "max_active_jobs above 1024");
   if (opts->inflight_waves > 8)
     return ajg::fail(ctx, AJG_ERR_INVALID, "inflight_waves above 8");
+  if (opts->wave_paths && (opts->wave_paths < 1024 || opts->wave_paths > (1u << 27)))
+    return ajg::fail(ctx, AJG_ERR_INVALID, "wave_paths must be in [1024, 2^27]");
   Server* s = nullptr;
   int rc = ensure_server(ctx, &s);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(s->mu);
   s->opts = *opts;
   if (!s->opts.inflight_waves) s->opts.inflight_waves = 2;
+  s->want_P = opts->wave_paths;
   return AJG_OK;
 }
 

@@ -72,6 +72,10 @@ def parse():
                     help="arrival rate as a fraction of the batched throughput")
     ap.add_argument("--rmse-crop", type=int, default=32)
     ap.add_argument("--rmse-spp", type=int, default=4096)
+    ap.add_argument("--wave-paths", type=int, default=0,
+                    help="paths in flight per wave (0: library default)")
+    ap.add_argument("--batch-wave-paths", type=int, default=0,
+                    help="paths per wave of the batched/served context (0: default)")
     ap.add_argument("--large", action="store_true",
                     help="also run the large-scene workload (26.2 M triangles, "
                          "1920x1080, 1024 spp, depth 32, FP64 crop reference)")
@@ -244,7 +248,7 @@ def run_ours(args):
     flat = workload_scene(args.res)
     W = H = args.res
     samples_per_step = W * H * args.spp
-    ctx = api.Context(local)
+    ctx = api.Context(local, wave_paths=args.wave_paths)
     scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS, bvh_width=args.bvh_width))
     rend = api.PTRenderer(api.PTRendererArgs(spp=args.spp, min_bounces=MIN_B,
                                              max_bounces=DEPTH), seed=1 + rank)
@@ -359,7 +363,8 @@ def run_ours(args):
     if rank == 0 and world == 1 and args.large:
         large = run_large(args, local)
     if rank == 0 and world == 1 and not args.no_batch:
-        bctx = api.Context(local, hbm_budget_bytes=150 << 30)
+        bctx = api.Context(local, wave_paths=args.batch_wave_paths,
+                           hbm_budget_bytes=150 << 30)
         batched = run_batched(bctx, args)
         if not args.no_serve:
             served = run_served(bctx, args, batched["_capacity"])
@@ -372,7 +377,8 @@ def run_ours(args):
             "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene, no dataset)",
-            "config": {**config(args), "bvh_width": scene.info()["bvh_width"]},
+            "config": {**config(args), "bvh_width": scene.info()["bvh_width"],
+                       "wave_paths": args.wave_paths or (1 << 22)},
             "clocks": clk, "e2e": e2e, "roofline": roofline,
             "cpu_baseline": cpu, "gpu_launches": launches_timed,
             "ploc_build_ms": scene.info()["build_ms"],

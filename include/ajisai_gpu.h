@@ -71,7 +71,8 @@ typedef struct ajg_scene ajg_scene;
 
 typedef struct ajg_config {
   int32_t device;            /* CUDA device ordinal */
-  uint32_t wave_paths;       /* paths in flight per wave (0: default 4 Mi) */
+  uint32_t wave_paths;       /* paths in flight per wave (0: default 32 Mi,
+                                ~10 GB of wave state) */
   uint64_t hbm_budget_bytes; /* admission budget for resident scenes and
                                 films (0: no limit) */
 } ajg_config;
@@ -342,7 +343,9 @@ typedef struct ajg_serve_opts {
   uint32_t max_active_jobs; /* jobs holding films at once (<= 1024; 0: 256) */
   uint32_t inflight_waves;  /* waves queued on the GPU ahead of the host
                                (0: 2) */
-  uint32_t reserved;
+  uint32_t wave_paths;      /* paths per wave of the request loop (0: the
+                               context's); smaller waves deliver results
+                               sooner, bigger ones run faster */
 } ajg_serve_opts;
 
 typedef struct ajg_serve_stats {

@@ -95,17 +95,19 @@ def alone(scenes, name, w, h, r):
     return r.Render(sc, cam_at(cam, w, h)).rgbw
 
 
-@pytest.mark.parametrize("policy", ["fair", "fifo"])
-def test_batch_equals_alone(ctx, scenes, policy):
+@pytest.mark.parametrize("policy,wave", [("fair", 0), ("fifo", 0), ("fair", 1 << 14)])
+def test_batch_equals_alone(ctx, scenes, policy, wave):
+    """Many waves of 16 Ki paths or few big ones: the same films."""
     jobs = job_list(scenes)
     ref = [alone(scenes, n, w, h, r) for n, w, h, r in jobs]
-    ctx.configure_serving(policy)
+    ctx.configure_serving(policy, wave_paths=wave)
     out = ctx.render_batch([(scenes[n][0], cam_at(scenes[n][1], w, h), r)
                             for n, w, h, r in jobs])
     for (film, st), r, j in zip(out, ref, jobs):
         assert st["state_name"] == "done", j[0]
         assert st["spp_done"] == j[3].args.spp
         assert same_bits(film.rgbw, r), j[0]
+    ctx.configure_serving("fair")
 
 
 def test_batch_of_many_small_jobs_shares_waves(ctx, scenes):
