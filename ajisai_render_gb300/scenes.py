@@ -129,6 +129,7 @@ class Quad:
     material: int = 0
     two_sided: bool = False
     kind: int = 0
+    emission: Optional[Sequence[float]] = None  # radiance: an area light
 
 
 @dataclass
@@ -139,6 +140,7 @@ class Cube:
     material: int = 0
     two_sided: bool = False
     kind: int = 1
+    emission: Optional[Sequence[float]] = None
 
 
 @dataclass
@@ -150,6 +152,7 @@ class Mesh:
     material: int = 0
     two_sided: bool = False
     kind: int = 2
+    emission: Optional[Sequence[float]] = None
 
 
 @dataclass
@@ -281,6 +284,11 @@ class FlatScene:
     materials: np.ndarray   # [m, 16] float32
     lights: np.ndarray      # [l, 12] float32
     camera: Optional[np.ndarray]  # [36] float32
+    # emissive primitives (area lights), in primitive order: radiance, and
+    # first triangle, triangle count, geometry kind (0 quad, 1 cube, 2 mesh),
+    # two_sided
+    emit_rad: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), F32))
+    emit_info: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int32))
 
     @property
     def n_tris(self) -> int:
@@ -289,10 +297,17 @@ class FlatScene:
 
 def flatten(scene: Scene) -> FlatScene:
     tris, cns, mats, flags = [], [], [], []
+    emit_rad, emit_info = [], []
+    n = 0
     world = (np.full(3, np.finfo(F32).max, F32),
              np.full(3, -np.finfo(F32).max, F32))
     for p in scene.primitives:
         t, cn, fl = _prim_triangles(p)
+        e = getattr(p, "emission", None)
+        if e is not None and np.any(np.asarray(e, F32) != 0):
+            emit_rad.append(np.broadcast_to(np.asarray(e, F32), 3))
+            emit_info.append([n, t.shape[0], p.kind, int(p.two_sided)])
+        n += t.shape[0]
         tris.append(t.reshape(-1, 9))
         cns.append(np.zeros((t.shape[0], 9), F32) if cn is None
                    else cn.reshape(-1, 9).astype(F32))
@@ -311,7 +326,9 @@ def flatten(scene: Scene) -> FlatScene:
         world=np.concatenate(world).astype(F32),
         materials=mat_arr.astype(F32),
         lights=light_arr.astype(F32),
-        camera=None if scene.camera is None else scene.camera.pack())
+        camera=None if scene.camera is None else scene.camera.pack(),
+        emit_rad=np.array(emit_rad, F32).reshape(-1, 3),
+        emit_info=np.array(emit_info, np.int32).reshape(-1, 4))
 
 
 # ----------------------------------------------------------------- camera --
@@ -391,6 +408,47 @@ def cornell_box(width: int = 256, height: int = 256) -> Scene:
         Cube(_rot_y_matrix_rowmajor((0.3, 0.3, 0.3), -18.0, (0.17, -0.35, 0.12)), white, False),
     ]
     lights = [DirectionalLight((0.3, 1.0, 0.2), 3.0), EnvLight(0.2)]
+    cam = Camera((0.0, 0.0, 1.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0,
+                 width, height)
+    return Scene(prims, mats, lights, cam)
+
+
+def cornell_area(width: int = 256, height: int = 256) -> Scene:
+    """The box of ``cornell_box`` lit by its emitters, one of each kind the
+    reference's area lights take: a one-sided ceiling quad facing down
+    (radiance (8,6,3)), a two-sided vertical quad near the left wall
+    (1,2,4), an emissive icosphere mesh of 80 triangles on the floor
+    (6,2,1) and an emissive cube under the ceiling (2,4,2); beside them a
+    directional light of radiance 1 and a constant environment of 0.05.
+    The tall inner box is a Disney material, the short one Lambertian."""
+    white, red, green, disney = 0, 1, 2, 3
+    mats = [Diffuse((0.73, 0.73, 0.73)), Diffuse((0.65, 0.05, 0.05)),
+            Diffuse((0.12, 0.45, 0.15)),
+            Disney((0.8, 0.6, 0.4), metallic=0.3, roughness=0.35,
+                   clearcoat=0.5, clearcoat_gloss=0.7)]
+    h = 0.5
+    v, f = icosphere(1)
+    ball = (v * 0.07 + np.array([0.3, -h + 0.07, 0.28])).astype(F32)
+    prims = [
+        Quad((-h, -h, h), (h, -h, h), (h, -h, -h), (-h, -h, -h), white, True),   # floor
+        Quad((-h, h, -h), (h, h, -h), (h, h, h), (-h, h, h), white, True),       # ceiling
+        Quad((-h, -h, -h), (h, -h, -h), (h, h, -h), (-h, h, -h), white, True),   # back
+        Quad((-h, -h, h), (-h, -h, -h), (-h, h, -h), (-h, h, h), red, True),     # left
+        Quad((h, -h, -h), (h, -h, h), (h, h, h), (h, h, -h), green, True),       # right
+        Cube(_rot_y_matrix_rowmajor((0.3, 0.6, 0.3), 15.0, (-0.17, -0.2, -0.12)), disney, False),
+        Cube(_rot_y_matrix_rowmajor((0.3, 0.3, 0.3), -18.0, (0.17, -0.35, 0.12)), white, False),
+        # emitters
+        Quad((-0.15, h - 1e-3, -0.15), (0.15, h - 1e-3, -0.15),
+             (0.15, h - 1e-3, 0.15), (-0.15, h - 1e-3, 0.15), white, False,
+             emission=(8.0, 6.0, 3.0)),
+        Quad((-0.42, -0.1, -0.25), (-0.42, -0.1, 0.0), (-0.42, 0.12, 0.0),
+             (-0.42, 0.12, -0.25), white, True, emission=(1.0, 2.0, 4.0)),
+        Mesh(ball, f.astype(np.int32), None, white, False,
+             emission=(6.0, 2.0, 1.0)),
+        Cube(_rot_y_matrix_rowmajor((0.08, 0.08, 0.08), 30.0, (0.25, 0.33, -0.3)),
+             white, False, emission=(2.0, 4.0, 2.0)),
+    ]
+    lights = [DirectionalLight((0.3, 1.0, 0.2), 1.0), EnvLight(0.05)]
     cam = Camera((0.0, 0.0, 1.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0,
                  width, height)
     return Scene(prims, mats, lights, cam)

@@ -988,6 +988,7 @@ struct Rng {
 /* ------------------------------------------------------------- lights --- */
 struct Light {
   int type;
+  int area = -1; /* index into Scene::areas for ORC_LIGHT_AREA */
   V3 rgb;      /* directional radiance / env texel */
   V3 dir;      /* normalised toward-light direction */
   float cosmax;
@@ -1006,7 +1007,135 @@ struct Light {
     float w = luminance(rgb) * std::sin(kPi * (0 + 0.5f) / float(1));
     env_ok = w * (1.f / float(1)) > 0.f;
   }
+  Light(int area_index, V3 radiance)
+      : type(ORC_LIGHT_AREA),
+        area(area_index),
+        rgb(radiance),
+        dir(mk(0, 1, 0)),
+        cosmax(1.f),
+        scaler(1.f),
+        rot(0.f),
+        frame(mk(0, 1, 0)),
+        env_ok(false) {}
 };
+
+/* AreaLight over an emissive primitive's geometry (area_light.cpp, with
+ * the geometry's Sample / Pdf: quad.cpp:128-171, cube.cpp:145-191,
+ * mesh.cpp:62-68,251-297, two_sided.cpp:65-114). */
+struct AreaL {
+  V3 rad;
+  int kind = ORC_GEOM_QUAD;
+  bool two_sided = false;
+  /* quad: a, b, c, d; mesh: its corners in index-buffer order; cube: each
+   * triangle's corners in the tuples' declared order */
+  std::vector<V3> pts;
+  int ntri = 0;
+  float area = 0.f, sample_prob = 0.f;
+  float pdf_const = 0.f; /* Geometry::Pdf (the same for every point) */
+};
+
+struct GeomSample {
+  V3 pos, ng;
+  float pdf;
+};
+
+GeomSample area_sample(const AreaL& A, float x, float y, float z) {
+  V3 sam = mk(x, y, z);
+  bool back = false;
+  if (A.two_sided) { /* TwoSided::Sample splits x between the faces */
+    back = sam.x < 0.5f;
+    if (back)
+      sam.x = 2 * x;
+    else
+      sam.x = 2 * (x - 0.5f);
+  }
+  V3 sn = sam;
+  if (sn.x + sn.y > 1.f) {
+    sn.x = 1.f - sn.x;
+    sn.y = 1.f - sn.y;
+  }
+  GeomSample g;
+  if (A.kind == ORC_GEOM_QUAD) {
+    const V3 &a = A.pts[0], &b = A.pts[1], &c = A.pts[2], &d = A.pts[3];
+    if (sam.z < A.sample_prob) {
+      g.pos = (1 - sn.x - sn.y) * a + sn.x * b + sn.y * c;
+      g.ng = normalized(cross(b - a, c - a));
+    } else {
+      g.pos = (1 - sn.x - sn.y) * a + sn.x * c + sn.y * d;
+      g.ng = normalized(cross(c - a, d - a));
+    }
+    g.pdf = 1.f / A.area;
+  } else if (A.kind == ORC_GEOM_MESH) {
+    /* the triangle index addresses the index buffer without the factor
+     * 3: corners idx, idx+1, idx+2 (mesh.cpp:260-262) */
+    const int idx = std::min(int(sam.z * (float)A.ntri), A.ntri - 1);
+    const V3 &pi = A.pts[idx], &pj = A.pts[idx + 1], &pk = A.pts[idx + 2];
+    g.pos = (1 - sn.x - sn.y) * pi + sn.x * pj + sn.y * pk;
+    g.ng = normalized(cross(pj - pi, pk - pi));
+    g.pdf = 1.f / A.area;
+  } else {
+    const int idx = std::min(int(sam.z * (float)12), 11);
+    const V3 &pa = A.pts[3 * idx], &pb = A.pts[3 * idx + 1],
+             &pc = A.pts[3 * idx + 2];
+    g.pos = (1 - sn.x - sn.y) * pa + sn.x * pb + sn.y * pc;
+    g.ng = normalized(cross(pb - pa, pc - pa));
+    g.pdf = 1.f / (12.f * length(cross(pb - pa, pc - pa)) * 0.5f);
+  }
+  if (A.two_sided) {
+    g.pdf = (float)((double)g.pdf * 0.5);
+    if (back) g.ng = g.ng * -1.f;
+  }
+  return g;
+}
+
+/* AreaLight::Pdf (area_light.cpp:68-79) */
+float area_pdf(const AreaL& A, V3 ref, V3 pos, V3 normal) {
+  if (dot(ref - pos, normal) <= 0.f) return 0.f;
+  const V3 l2r = ref - pos;
+  const float dist2 = dot(l2r, l2r);
+  const float abscos = std::fabs(dot(l2r, normal));
+  return A.pdf_const * (dist2 / abscos);
+}
+
+AreaL make_area(const float* tris, const float* rad, const int32_t* info) {
+  AreaL A;
+  A.rad = mk(rad[0], rad[1], rad[2]);
+  const int64_t first = info[0];
+  A.ntri = info[1];
+  A.kind = info[2];
+  A.two_sided = info[3] != 0;
+  auto corner = [&](int64_t t, int k) { return ld3(tris + 9 * (first + t) + 3 * k); };
+  if (A.kind == ORC_GEOM_QUAD) {
+    const V3 a = corner(0, 0), b = corner(0, 1), c = corner(0, 2),
+             d = corner(1, 2);
+    A.pts = {a, b, c, d};
+    const float abc = length(cross(b - a, c - a)) * 0.5f;
+    const float acd = length(cross(c - a, d - a)) * 0.5f;
+    A.area = abc + acd;
+    A.sample_prob = abc / A.area;
+    A.pdf_const = 1.f / A.area;
+  } else if (A.kind == ORC_GEOM_MESH) {
+    float area = 0.f;
+    for (int t = 0; t < A.ntri; ++t) {
+      const V3 pi = corner(t, 0), pj = corner(t, 1), pk = corner(t, 2);
+      A.pts.push_back(pi);
+      A.pts.push_back(pj);
+      A.pts.push_back(pk);
+      area = (float)((double)area +
+                     0.5 * (double)length(cross(pj - pi, pk - pi)));
+    }
+    A.area = area;
+    A.pdf_const = 1.f / area;
+  } else {
+    /* the MeshView sees each tuple reversed; Sample reads it as declared */
+    for (int t = 0; t < A.ntri; ++t)
+      for (int k = 2; k >= 0; --k) A.pts.push_back(corner(t, k));
+    const V3 &pa = A.pts[0], &pb = A.pts[1], &pc = A.pts[2];
+    A.pdf_const = 1.f / (12.f * length(cross(pb - pa, pc - pa)) * 0.5f);
+  }
+  if (A.two_sided) A.pdf_const = A.pdf_const * 0.5f;
+  return A;
+}
 
 struct LightSample {
   V3 pos, radiance;
@@ -1021,6 +1150,8 @@ struct Scene {
   const int32_t* tri_flags;
   std::vector<Mat> mats;
   std::vector<Light> lights;
+  std::vector<AreaL> areas;
+  std::vector<int> tri_light; /* light index of an emissive triangle, or -1 */
   int env = -1;
   float radius; /* (aabb.max - aabb.center).length() */
   int mode;
@@ -1085,7 +1216,17 @@ float env_pdf(const Light& L, V3 ref2light) {
 V3 mis_light(const Scene& s, const Light& L, const HitInfo& h, const Bsdf& f,
              Rng& rng) {
   LightSample ls;
-  if (L.type == ORC_LIGHT_DIRECTIONAL) {
+  if (L.type == ORC_LIGHT_AREA) { /* AreaLight::Sample (area_light.cpp:36-57) */
+    const float x = rng.next(), y = rng.next(), z = rng.next(); /* Next3D */
+    const AreaL& A = s.areas[L.area];
+    const GeomSample g = area_sample(A, x, y, z);
+    if (dot(g.ng, h.pos - g.pos) <= 0) return mk(0, 0, 0);
+    const V3 i2r = h.pos - g.pos;
+    const float dist2 = dot(i2r, i2r);
+    ls.pdf = g.pdf * dist2 / std::fabs(dot(g.ng, i2r));
+    ls.pos = g.pos;
+    ls.radiance = A.rad;
+  } else if (L.type == ORC_LIGHT_DIRECTIONAL) {
     float u0 = rng.next(), u1 = rng.next();
     V3 r2l = L.frame.to_world(uniform_cone(u0, u1, L.cosmax));
     ls.pdf = uniform_cone_pdf(L.cosmax);
@@ -1120,9 +1261,11 @@ V3 mis_light(const Scene& s, const Light& L, const HitInfo& h, const Bsdf& f,
   if (trace_any(s.acc, sr, s.mode, true)) return mk(0, 0, 0);
   const V3 bf = f.eval(w, h.wr);
   if (is_black(bf)) return mk(0, 0, 0);
-  const V3 n = normalized(h.ns);
+  /* MISSampleAreaLight takes the shading normal as it is; the others
+   * normalise it (helper.h:64, 91, 120) */
+  const V3 n = L.type == ORC_LIGHT_AREA ? h.ns : normalized(h.ns);
   V3 fv;
-  if (L.type == ORC_LIGHT_DIRECTIONAL)
+  if (L.type == ORC_LIGHT_DIRECTIONAL || L.type == ORC_LIGHT_AREA)
     fv = mk(1.f, 1.f, 1.f) * ls.radiance * bf * std::fabs(dot(w, n));
   else
     fv = ls.radiance * bf * std::fabs(dot(w, n));
@@ -1130,8 +1273,8 @@ V3 mis_light(const Scene& s, const Light& L, const HitInfo& h, const Bsdf& f,
   return fv / ls.pdf * power_heuristic(ls.pdf, bp);
 }
 
-/* MISSampleBsdf (helper.h:209-265).  No primitive emits, so only a ray
- * that escapes to the environment contributes. */
+/* MISSampleBsdf (helper.h:209-265): a ray that escapes sees the
+ * environment, one that hits an emissive primitive its area light. */
 V3 mis_bsdf(const Scene& s, const HitInfo& h, const Bsdf& f, Rng& rng) {
   float a = rng.next(), b = rng.next(), c = rng.next();
   Sample bs = f.sample(h.wr, mk(a, b, c));
@@ -1139,7 +1282,17 @@ V3 mis_bsdf(const Scene& s, const HitInfo& h, const Bsdf& f, Rng& rng) {
   bs.dir = normalized(bs.dir);
   Ray r = make_ray(eps_offset(h, bs.dir), bs.dir);
   Hit hh = trace_closest(s.acc, r, s.mode, true);
-  if (hh.prim >= 0) return mk(0, 0, 0);
+  if (hh.prim >= 0) {
+    const int li = s.tri_light.empty() ? -1 : s.tri_light[hh.prim];
+    if (li < 0) return mk(0, 0, 0);
+    const HitInfo lh = complete_hit(s, r, hh);
+    const AreaL& A = s.areas[s.lights[li].area];
+    const V3 le = dot(lh.ng, lh.wr) > 0 ? A.rad : mk(0, 0, 0);
+    if (is_black(le)) return mk(0, 0, 0);
+    const V3 fv = le * bs.f * std::fabs(dot(h.ns, r.d));
+    const float lp = area_pdf(A, r.o, lh.pos, lh.ng);
+    return fv / bs.pdf * power_heuristic(bs.pdf, lp);
+  }
   if (s.env < 0) return mk(0, 0, 0);
   const Light& L = s.lights[s.env];
   V3 rad = L.scaler * L.rgb;
@@ -1173,6 +1326,14 @@ V3 trace_path(const Scene& s, Ray ray, Rng& rng, int min_b, int max_b,
     const Mat& m = s.mats[hi.mat];
     Bsdf f(m, hi.ng, hi.ns);
     T = T * mk(1.f, 1.f, 1.f); /* void medium: SampleScattering throughput */
+    /* emission: on camera rays with MIS (pt.cpp:185-190), on every hit
+     * without (pt.cpp:282-286); AreaLight::Radiance (area_light.cpp:30-34) */
+    const int li = s.tri_light.empty() ? -1 : s.tri_light[h.prim];
+    if (li >= 0 && (bounce == 0 || !use_mis)) {
+      const AreaL& A = s.areas[s.lights[li].area];
+      const V3 le = dot(hi.ng, hi.wr) > 0 ? A.rad : mk(0, 0, 0);
+      L = L + T * le;
+    }
     if (use_mis) {
       V3 direct = mk(0, 0, 0);
       for (const Light& lt : s.lights) direct = direct + T * mis_light(s, lt, hi, f, rng);
@@ -1344,7 +1505,9 @@ void* orc_scene_create(const float* tris, const float* corner_n,
                        int64_t n_tris, const float* materials,
                        int32_t n_materials, const float* lights,
                        int32_t n_lights, const float* world,
-                       int64_t search_radius, int radix_compat, int tri_test) {
+                       int64_t search_radius, int radix_compat, int tri_test,
+                       const float* emit_rad, const int32_t* emit_info,
+                       int32_t n_emit) {
   if (n_tris < 1) return nullptr;
   auto* o = new OrcScene();
   auto t0 = std::chrono::steady_clock::now();
@@ -1363,9 +1526,17 @@ void* orc_scene_create(const float* tris, const float* corner_n,
   s.tri_flags = tri_flags;
   for (int i = 0; i < n_materials; ++i)
     s.mats.push_back(load_mat(materials + 16 * i));
+  /* the emissive primitives' area lights come first (default_scene.cpp) */
+  if (n_emit > 0) s.tri_light.assign(n_tris, -1);
+  for (int e = 0; e < n_emit; ++e) {
+    s.areas.push_back(make_area(tris, emit_rad + 3 * e, emit_info + 4 * e));
+    s.lights.emplace_back((int)e, s.areas.back().rad);
+    for (int t = 0; t < emit_info[4 * e + 1]; ++t)
+      s.tri_light[emit_info[4 * e] + t] = e;
+  }
   for (int i = 0; i < n_lights; ++i) {
     s.lights.emplace_back(lights + 12 * i);
-    if (s.lights.back().type == ORC_LIGHT_ENV) s.env = i;
+    if (s.lights.back().type == ORC_LIGHT_ENV) s.env = (int)s.lights.size() - 1;
   }
   Box wb = world_box(world);
   s.radius = length(wb.hi - box_center(wb));
@@ -1443,11 +1614,12 @@ int orc_render(const float* tris, const float* corner_n,
                const float* lights, int32_t n_lights, const float* world,
                const float* camera, const double* params, uint64_t seed,
                int64_t pixel_begin, int64_t pixel_end, float* out_li,
-               double* out_film, int threads) {
+               double* out_film, int threads, const float* emit_rad,
+               const int32_t* emit_info, int32_t n_emit) {
   void* h = orc_scene_create(tris, corner_n, tri_mat, tri_flags, n_tris,
                              materials, n_materials, lights, n_lights, world,
                              (int64_t)params[6], params[7] != 0,
-                             (int)params[5]);
+                             (int)params[5], emit_rad, emit_info, n_emit);
   if (!h) return -2;
   int rc = orc_scene_render(h, camera, params, seed, pixel_begin, pixel_end,
                             out_li, out_film, threads);

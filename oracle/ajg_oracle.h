@@ -29,6 +29,11 @@
  *   camera      [36]     raster2camera[16], camera2world[16] (column-major,
  *                        as ajisai/math matrices), lens_radius, focal_distance,
  *                        width, height
+ *   emit_rad    [k][3]   emissive primitives (area lights, in primitive
+ *   emit_info   [k][4]   order): radiance; int32 first triangle, triangle
+ *                        count, ORC_GEOM_* kind, two_sided.  The scene's
+ *                        light list is the area lights, then `lights`
+ *                        (default_scene.cpp:31-48).
  */
 #pragma once
 #include <stdint.h>
@@ -43,7 +48,8 @@ enum {
   ORC_TRI_HAS_NORMALS = 4  /* MeshGeo interpolated normals (mesh.cpp:183-204) */
 };
 enum { ORC_MAT_DIFFUSE = 0, ORC_MAT_DISNEY = 1 };
-enum { ORC_LIGHT_DIRECTIONAL = 0, ORC_LIGHT_ENV = 1 };
+enum { ORC_LIGHT_DIRECTIONAL = 0, ORC_LIGHT_ENV = 1, ORC_LIGHT_AREA = 2 };
+enum { ORC_GEOM_QUAD = 0, ORC_GEOM_CUBE = 1, ORC_GEOM_MESH = 2 };
 enum { ORC_TEST_MT = 0, ORC_TEST_WATERTIGHT = 1 };
 
 /* PLOCAggregate::Build restated (ploc_aggregate.cpp:252-327).  Writes
@@ -100,7 +106,8 @@ int orc_render(const float* tris, const float* corner_n,
                const float* lights, int32_t n_lights, const float* world,
                const float* camera, const double* params, uint64_t seed,
                int64_t pixel_begin, int64_t pixel_end, float* out_li,
-               double* out_film, int threads);
+               double* out_film, int threads, const float* emit_rad,
+               const int32_t* emit_info, int32_t n_emit);
 
 /* The same split in two: build once (PLOC tree), render many times.  The
  * arrays passed to orc_scene_create must outlive the handle. */
@@ -109,7 +116,9 @@ void* orc_scene_create(const float* tris, const float* corner_n,
                        int64_t n_tris, const float* materials,
                        int32_t n_materials, const float* lights,
                        int32_t n_lights, const float* world,
-                       int64_t search_radius, int radix_compat, int tri_test);
+                       int64_t search_radius, int radix_compat, int tri_test,
+                       const float* emit_rad, const int32_t* emit_info,
+                       int32_t n_emit);
 int orc_scene_render(void* scene, const float* camera, const double* params,
                      uint64_t seed, int64_t pixel_begin, int64_t pixel_end,
                      float* out_li, double* out_film, int threads);

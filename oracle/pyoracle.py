@@ -46,11 +46,13 @@ def lib():
         L.orc_render.argtypes = [_f32p, _f32p, _i32p, _i32p, C.c_int64,
                                  _f32p, C.c_int32, _f32p, C.c_int32, _f32p,
                                  _f32p, _f64p, C.c_uint64, C.c_int64,
-                                 C.c_int64, C.c_void_p, C.c_void_p, C.c_int]
+                                 C.c_int64, C.c_void_p, C.c_void_p, C.c_int,
+                                 _f32p, _i32p, C.c_int32]
         L.orc_scene_create.restype = C.c_void_p
         L.orc_scene_create.argtypes = [_f32p, _f32p, _i32p, _i32p, C.c_int64, _f32p,
                                        C.c_int32, _f32p, C.c_int32, _f32p,
-                                       C.c_int64, C.c_int, C.c_int]
+                                       C.c_int64, C.c_int, C.c_int, _f32p, _i32p,
+                                       C.c_int32]
         L.orc_scene_render.argtypes = [C.c_void_p, _f32p, _f64p, C.c_uint64,
                                        C.c_int64, C.c_int64, C.c_void_p,
                                        C.c_void_p, C.c_int]
@@ -61,18 +63,35 @@ def lib():
     return _lib
 
 
+def _emitters(flat):
+    """(radiance [k][3] float32, info [k][4] int32) of the flat scene's
+    emissive primitives."""
+    er = getattr(flat, "emit_rad", None)
+    ei = getattr(flat, "emit_info", None)
+    if er is None or len(er) == 0:
+        return np.zeros((1, 3), np.float32)[:0], np.zeros((1, 4), np.int32)[:0]
+    return _c(er, np.float32).reshape(-1, 3), _c(ei, np.int32).reshape(-1, 4)
+
+
+def _emitter_args(flat):
+    er, ei = _emitters(flat)
+    return er, ei, er.shape[0]
+
+
 class OracleScene:
     """Oracle scene built once (PLOC on the CPU) and rendered many times."""
 
     def __init__(self, flat, search_radius=14, radix_compat=False, tri_test=0):
+        er, ei = _emitters(flat)
         self._keep = [_c(flat.tris, np.float32), _c(flat.corner_n, np.float32),
                       _c(flat.tri_mat, np.int32), _c(flat.tri_flags, np.int32),
                       _c(flat.materials, np.float32), _c(flat.lights, np.float32),
-                      _c(flat.world, np.float32)]
+                      _c(flat.world, np.float32), er, ei]
         k = self._keep
         self.h = lib().orc_scene_create(k[0], k[1], k[2], k[3], flat.n_tris, k[4],
                                         k[4].shape[0], k[5], k[5].shape[0], k[6],
-                                        search_radius, int(radix_compat), tri_test)
+                                        search_radius, int(radix_compat), tri_test,
+                                        er, ei, er.shape[0])
         if not self.h:
             raise RuntimeError("orc_scene_create failed")
         self.build_seconds = lib().orc_scene_build_seconds(self.h)
@@ -194,7 +213,8 @@ def render(flat, params, seed=0, pixel_range=None, per_sample=True,
                           flat.lights.shape[0], _c(flat.world, np.float32), cam,
                           p, seed, b, e,
                           li.ctypes.data if li is not None else None,
-                          film.ctypes.data, threads or threads_default())
+                          film.ctypes.data, threads or threads_default(),
+                          *_emitter_args(flat))
     assert rc == 0
     return li, film
 
@@ -214,7 +234,7 @@ def ref():
         L.ref_scene_create.argtypes = [_i32p, _f32p, C.c_int32, _f32p, _f32p,
                                        _u32p, _f32p, C.c_int32, _f32p,
                                        C.c_int32, C.c_void_p, C.c_int32,
-                                       C.c_int32, C.c_int64]
+                                       C.c_int32, C.c_int64, _f32p]
         L.ref_scene_destroy.argtypes = [C.c_void_p]
         L.ref_scene_num_tris.argtypes = [C.c_void_p]
         L.ref_scene_num_tris.restype = C.c_int64
@@ -269,6 +289,12 @@ class RefScene:
             prims.append(rec)
             pf.append(f)
         self.mat_of_prim = np.array([p.material for p in scene.primitives], np.int32)
+        def emis(p):
+            e = getattr(p, "emission", None)
+            return np.broadcast_to(np.asarray(0.0 if e is None else e, np.float32), 3)
+        self.emission = np.array([emis(p) for p in scene.primitives],
+                                 np.float32).reshape(-1, 3)
+        self.flat_emitters = (fl.emit_rad, fl.emit_info)
         self._keep = dict(
             prims=np.stack(prims), pf=np.stack(pf),
             pos=np.concatenate(pos) if pos else np.zeros((1, 3), np.float32),
@@ -285,7 +311,8 @@ class RefScene:
             _c(k["nrm"], np.float32), _c(k["idx"], np.uint32), k["mats"],
             len(scene.materials), k["lights"], len(scene.lights),
             self.cam_in.ctypes.data if cam is not None else None,
-            cam.width if cam else 0, cam.height if cam else 0, search_radius)
+            cam.width if cam else 0, cam.height if cam else 0, search_radius,
+            self.emission)
         self.n = L.ref_scene_num_tris(self.h)
         self.n_lights = len(scene.lights)
         self.scene = scene
@@ -317,7 +344,9 @@ class RefScene:
         mats = self._keep["mats"]
         return FlatScene(tris, cn, tm, tf, world, mats.copy(),
                          lights[:self.n_lights].copy(),
-                         cam if self.cam_in is not None else None)
+                         cam if self.cam_in is not None else None,
+                         emit_rad=self.flat_emitters[0].copy(),
+                         emit_info=self.flat_emitters[1].copy())
 
     def ploc(self):
         n = self.n

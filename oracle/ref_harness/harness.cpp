@@ -102,6 +102,14 @@ class HarnessMesh : public Geometry {
       aabb_.min() = Min(aabb_.min(), v);
       aabb_.max() = Max(aabb_.max(), v);
     }
+    /* MeshGeo's surface area (mesh.cpp:62-68) */
+    surface_area_ = 0;
+    for (size_t idx = 0; idx < idx_.size(); idx += 3) {
+      int i = idx_[idx], j = idx_[idx + 1], k = idx_[idx + 2];
+      auto e0 = p_[j] - p_[i];
+      auto e1 = p_[k] - p_[i];
+      surface_area_ += 0.5 * cross(e0, e1).length();
+    }
   }
   bool Intersect(const Ray&, GeometryIntersection*) const noexcept override {
     return false;
@@ -136,18 +144,34 @@ class HarnessMesh : public Geometry {
     r.index_size = idx_.size() / 3;
     return r;
   }
-  Intersection Sample(float* pdf, const Vector3f&) const noexcept override {
-    *pdf = 0.f;
-    return Intersection{};
+  /* MeshGeo::Sample / Pdf (mesh.cpp:251-297), restated: the triangle index
+   * addresses the index buffer without the factor 3 */
+  Intersection Sample(float* pdf, const Vector3f& sam) const noexcept override {
+    Vector3f sam_new = sam;
+    if (sam_new.x() + sam_new.y() > 1.f) {
+      sam_new.x() = 1.f - sam_new.x();
+      sam_new.y() = 1.f - sam_new.y();
+    }
+    Intersection inct;
+    auto triangle_count = idx_.size() / 3;
+    int idx = std::min(int(sam.z() * triangle_count), (int)triangle_count - 1);
+    int i = idx_[idx], j = idx_[idx + 1], k = idx_[idx + 2];
+    inct.pos = (1 - sam_new.x() - sam_new.y()) * p_[i] + sam_new.x() * p_[j] +
+               sam_new.y() * p_[k];
+    inct.geometry_normal = cross(p_[j] - p_[i], p_[k] - p_[i]).normalized();
+    inct.shading_normal = inct.geometry_normal;
+    *pdf = 1.f / surface_area_;
+    return inct;
   }
   Intersection Sample(const Vector3f&, float* pdf,
-                      const Vector3f&) const noexcept override {
-    *pdf = 0.f;
-    return Intersection{};
+                      const Vector3f& sam) const noexcept override {
+    return Sample(pdf, sam);
   }
-  float Pdf(const Vector3f&) const noexcept override { return 0.f; }
-  float Pdf(const Vector3f&, const Vector3f&) const noexcept override {
-    return 0.f;
+  float Pdf(const Vector3f&) const noexcept override {
+    return 1.f / surface_area_;
+  }
+  float Pdf(const Vector3f&, const Vector3f& s) const noexcept override {
+    return Pdf(s);
   }
   const std::vector<Vector3f>& normals() const { return n_; }
   const std::vector<uint32_t>& indices() const { return idx_; }
@@ -156,6 +180,7 @@ class HarnessMesh : public Geometry {
   std::vector<Vector3f> p_, n_;
   std::vector<uint32_t> idx_;
   Bounds3f aabb_;
+  float surface_area_ = 0.f;
 };
 
 /* Counter sampler: the stand-in for RandomSampler keyed by
@@ -218,13 +243,14 @@ extern "C" {
  *   (the first 15 are read, as factory/creator/helper.h:86-91 does).
  * lights [nl][12]: type, rgb, direction (toward the light), angle (rad),
  *   scaler, rot (deg).
- * cam [12]: position, look_at, up, fov (deg), lens_radius, focal_distance. */
+ * cam [12]: position, look_at, up, fov (deg), lens_radius, focal_distance.
+ * emission [np][3]: per primitive radiance (0: not a light). */
 void* ref_scene_create(const int32_t* prims, const float* prim_f, int32_t np,
                        const float* mesh_pos, const float* mesh_nrm,
                        const uint32_t* mesh_idx, const float* mats,
                        int32_t nm, const float* lights, int32_t nl,
                        const float* cam, int32_t width, int32_t height,
-                       int64_t search_radius) {
+                       int64_t search_radius, const float* emission) {
   auto* s = new HScene();
   for (int i = 0; i < nm; ++i) s->mats.push_back(make_material(mats + 16 * i));
   MediumInterface med{};
@@ -262,8 +288,10 @@ void* ref_scene_create(const int32_t* prims, const float* prim_f, int32_t np,
       g = m;
     }
     if (p[1]) g = CreateTwoSided(g);
-    s->prims.push_back(CreateGeometric(g, s->mats[p[2]], med, Spectrum{},
-                                       false, -1));
+    const Spectrum e = emission ? Spectrum{emission[3 * i], emission[3 * i + 1],
+                                           emission[3 * i + 2]}
+                                : Spectrum{};
+    s->prims.push_back(CreateGeometric(g, s->mats[p[2]], med, e, false, -1));
     s->kind.push_back(p[0]);
     s->two_sided.push_back(p[1]);
     s->meshes.push_back(hm);

@@ -164,6 +164,11 @@ def gen_render():
          dict(spp=4, min_bounces=5, max_bounces=16, cont_prob=0.9, use_mis=1)),
         ("render_cornell_nomis.npz", S.cornell_box(16, 16),
          dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=0)),
+        # every emitter kind: one-sided and two-sided quads, a mesh, a cube
+        ("render_area.npz", S.cornell_area(24, 24),
+         dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=1)),
+        ("render_area_nomis.npz", S.cornell_area(16, 16),
+         dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=0)),
     ]
     for name, sc, params in cases:
         rs = O.RefScene(sc, search_radius=14)
@@ -172,6 +177,7 @@ def gen_render():
         save(name, tris=fl.tris, corner_n=fl.corner_n, tri_mat=fl.tri_mat,
              tri_flags=fl.tri_flags, world=fl.world, materials=fl.materials,
              lights=fl.lights, camera=fl.camera, seed=np.uint64(7),
+             emit_rad=fl.emit_rad, emit_info=fl.emit_info,
              params=np.array([params["spp"], params["min_bounces"],
                               params["max_bounces"], params["cont_prob"],
                               params["use_mis"]], np.float64),
