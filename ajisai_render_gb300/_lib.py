@@ -52,6 +52,12 @@ class Light(C.Structure):
                 ("pad", C.c_float * 2)]
 
 
+class Emitter(C.Structure):
+    _fields_ = [("radiance", C.c_float * 3), ("first_triangle", C.c_uint32),
+                ("num_triangles", C.c_uint32), ("geometry", C.c_uint32),
+                ("two_sided", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class SceneOpts(C.Structure):
     _fields_ = [("search_radius", C.c_uint32), ("tri_test", C.c_uint32),
                 ("radix_compat", C.c_uint32), ("bvh_width", C.c_uint32)]
@@ -131,6 +137,14 @@ SIGNATURES = {
                                C.POINTER(Material), C.c_uint32, C.POINTER(Light),
                                C.c_uint32, C.POINTER(SceneOpts), C.POINTER(_P)],
                               C.c_int),
+    "ajg_scene_create_ex": ([_P, C.POINTER(MeshDesc), C.c_uint32, C.POINTER(Material),
+                             C.c_uint32, C.POINTER(Light), C.c_uint32,
+                             C.POINTER(Emitter), C.c_uint32, C.POINTER(SceneOpts),
+                             C.POINTER(_P)], C.c_int),
+    "ajg_scene_create_flat_ex": ([_P, _P, _P, _P, _P, C.c_uint64, _P,
+                                  C.POINTER(Material), C.c_uint32, C.POINTER(Light),
+                                  C.c_uint32, C.POINTER(Emitter), C.c_uint32,
+                                  C.POINTER(SceneOpts), C.POINTER(_P)], C.c_int),
     "ajg_scene_release": ([_P], C.c_int),
     "ajg_scene_get_info": ([_P, C.POINTER(SceneInfo)], C.c_int),
     "ajg_scene_download_bvh": ([_P, _P, _P, _P], C.c_int),

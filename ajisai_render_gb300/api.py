@@ -184,6 +184,21 @@ def _lights(arr):
     return recs
 
 
+def _emitters(flat):
+    """ajg_emitter records of the flat scene's emissive primitives (radiance,
+    and first triangle, count, geometry, two-sided)."""
+    rad = np.asarray(getattr(flat, "emit_rad", np.zeros((0, 3))), F32).reshape(-1, 3)
+    info = np.asarray(getattr(flat, "emit_info", np.zeros((0, 4))), np.int64).reshape(-1, 4)
+    recs = (_lib.Emitter * max(1, rad.shape[0]))()
+    for i in range(rad.shape[0]):
+        recs[i].radiance[:] = [float(x) for x in rad[i]]
+        recs[i].first_triangle = int(info[i, 0])
+        recs[i].num_triangles = int(info[i, 1])
+        recs[i].geometry = int(info[i, 2])
+        recs[i].two_sided = int(info[i, 3])
+    return recs, rad.shape[0]
+
+
 class GpuScene:
     """A scene resident on the GPU: triangles, materials, lights and the PLOC
     tree built by the GPU (PLOCAggregate::Build + DefaultScene)."""
@@ -202,11 +217,12 @@ class GpuScene:
         tm = np.ascontiguousarray(flat.tri_mat, np.int32)
         tf = np.ascontiguousarray(flat.tri_flags, np.int32)
         world = np.ascontiguousarray(flat.world, F32)
+        emitters, n_emit = _emitters(flat)
         h = C.c_void_p()
-        ctx.check(ctx.lib.ajg_scene_create_flat(
+        ctx.check(ctx.lib.ajg_scene_create_flat_ex(
             ctx.h, _ptr(tris), _ptr(cn), _ptr(tm), _ptr(tf), tris.shape[0],
             _ptr(world), mats, flat.materials.shape[0], lights,
-            flat.lights.shape[0], C.byref(opts), C.byref(h)))
+            flat.lights.shape[0], emitters, n_emit, C.byref(opts), C.byref(h)))
         self.h = h
         ctx._scenes.add(self)
 

@@ -275,6 +275,73 @@ int ajg_set_profiling(ajg_ctx* ctx, int enable) {
   return AJG_OK;
 }
 
+namespace {
+
+// An emitter's AreaLight as the device reads it: the light record and the
+// corner points of its sampler (quad: a, b, c, d; mesh: its corners in
+// index order; cube: each triangle's corners in the order the cube's index
+// tuples declare them, the reverse of its MeshView's).  Areas and pdfs are
+// computed in float as the geometries compute them (quad.cpp:52-60,
+// mesh.cpp:62-68 with the sum in double, cube.cpp:145-191 from its first
+// triangle, two_sided.cpp:104-112).
+void area_light_record(const float* tris, const ajg_emitter& e,
+                       uint32_t pts_first, float rec[12],
+                       std::vector<float>& pts) {
+  auto corner = [&](uint64_t t, int k) {
+    const float* v = tris + 9 * ((uint64_t)e.first_triangle + t) + 3 * k;
+    return mk3(v[0], v[1], v[2]);
+  };
+  auto push = [&](F3 v) { pts.insert(pts.end(), {v.x, v.y, v.z}); };
+  auto len = [](F3 v) { return std::sqrt(dot3(v, v)); };
+  float inv_area = 0.f, share = 0.f, pdf = 0.f;
+  if (e.geometry == AJG_GEOM_QUAD) {
+    const F3 a = corner(0, 0), b = corner(0, 1), c = corner(0, 2),
+             d = corner(1, 2);
+    for (F3 v : {a, b, c, d}) push(v);
+    const float abc = len(cross3(b - a, c - a)) * 0.5f;
+    const float acd = len(cross3(c - a, d - a)) * 0.5f;
+    const float area = abc + acd;
+    share = abc / area;
+    inv_area = 1.f / area;
+    pdf = 1.f / area;
+  } else if (e.geometry == AJG_GEOM_MESH) {
+    float area = 0.f;
+    for (uint32_t t = 0; t < e.num_triangles; ++t) {
+      const F3 i = corner(t, 0), j = corner(t, 1), k = corner(t, 2);
+      push(i);
+      push(j);
+      push(k);
+      area = (float)((double)area + 0.5 * (double)len(cross3(j - i, k - i)));
+    }
+    inv_area = 1.f / area;
+    pdf = 1.f / area;
+  } else {
+    for (uint32_t t = 0; t < 12; ++t)
+      for (int k = 2; k >= 0; --k) push(corner(t, k));
+    const F3 pa = corner(0, 2), pb = corner(0, 1), pc = corner(0, 0);
+    pdf = 1.f / (12.f * len(cross3(pb - pa, pc - pa)) * 0.5f);
+  }
+  if (e.two_sided) pdf = pdf * 0.5f;
+  std::memset(rec, 0, 12 * sizeof(float));
+  rec[0] = (float)kLightArea;
+  rec[1] = e.radiance[0];
+  rec[2] = e.radiance[1];
+  rec[3] = e.radiance[2];
+  rec[4] = (float)e.geometry;
+  rec[5] = e.two_sided ? 1.f : 0.f;
+  std::memcpy(&rec[6], &e.num_triangles, 4);
+  rec[7] = inv_area;
+  rec[8] = share;
+  rec[9] = pdf;
+  std::memcpy(&rec[10], &pts_first, 4);
+}
+
+bool black_emission(const ajg_emitter& e) {
+  return e.radiance[0] == 0.f && e.radiance[1] == 0.f && e.radiance[2] == 0.f;
+}
+
+}  // namespace
+
 int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
                           const float* corner_normals,
                           const int32_t* tri_material,
@@ -283,14 +350,61 @@ int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
                           uint32_t num_materials, const ajg_light* lights,
                           uint32_t num_lights, const ajg_scene_opts* opts,
                           ajg_scene** out) {
+  return ajg_scene_create_flat_ex(ctx, tris, corner_normals, tri_material,
+                                  tri_flags, n, world, materials, num_materials,
+                                  lights, num_lights, nullptr, 0, opts, out);
+}
+
+int ajg_scene_create_flat_ex(ajg_ctx* ctx, const float* tris,
+                             const float* corner_normals,
+                             const int32_t* tri_material,
+                             const int32_t* tri_flags, uint64_t n,
+                             const float* world, const ajg_material* materials,
+                             uint32_t num_materials, const ajg_light* lights,
+                             uint32_t num_lights, const ajg_emitter* emitters,
+                             uint32_t num_emitters, const ajg_scene_opts* opts,
+                             ajg_scene** out) {
   if (!ctx || !out) return fail(ctx, AJG_ERR_INVALID, "NULL argument");
   *out = nullptr;
   if (!tris || !tri_material || !tri_flags || !world || n == 0)
     return fail(ctx, AJG_ERR_INVALID, "empty scene or NULL arrays");
   if (!materials || num_materials == 0)
     return fail(ctx, AJG_ERR_INVALID, "a scene needs at least one material");
-  if (num_lights > 15 || (num_lights && !lights))
-    return fail(ctx, AJG_ERR_UNSUPPORTED, "at most 15 lights");
+  if ((num_lights && !lights) || (num_emitters && !emitters))
+    return fail(ctx, AJG_ERR_INVALID, "NULL light or emitter array");
+  // emitters: each a disjoint triangle range of the shape its sampler needs
+  std::vector<int32_t> tri_emit;
+  uint32_t num_area = 0;
+  for (uint32_t i = 0; i < num_emitters; ++i) {
+    const ajg_emitter& e = emitters[i];
+    if (e.geometry > AJG_GEOM_MESH)
+      return fail(ctx, AJG_ERR_INVALID, "unknown emitter geometry");
+    const uint32_t need = e.geometry == AJG_GEOM_QUAD   ? 2u
+                          : e.geometry == AJG_GEOM_CUBE ? 12u
+                                                        : 0u;
+    if ((need && e.num_triangles != need) || e.num_triangles == 0)
+      return fail(ctx, AJG_ERR_INVALID,
+                  "emitter triangle count does not fit its geometry (quad 2, "
+                  "cube 12, mesh >= 1)");
+    if ((uint64_t)e.first_triangle + e.num_triangles > n)
+      return fail(ctx, AJG_ERR_INVALID, "emitter triangles out of range");
+    if (e.two_sided > 1) return fail(ctx, AJG_ERR_INVALID, "two_sided is 0 or 1");
+    if (black_emission(e)) continue;
+    if (tri_emit.empty()) tri_emit.assign(n, -1);
+    for (uint32_t t = 0; t < e.num_triangles; ++t) {
+      const uint64_t g = (uint64_t)e.first_triangle + t;
+      if (tri_emit[g] >= 0)
+        return fail(ctx, AJG_ERR_INVALID, "emitters share a triangle");
+      if (((tri_flags[g] & AJG_MESH_TWO_SIDED) != 0) != (e.two_sided != 0))
+        return fail(ctx, AJG_ERR_INVALID,
+                    "emitter two_sided differs from its triangles' flags");
+      tri_emit[g] = (int32_t)num_area;
+    }
+    ++num_area;
+  }
+  if (num_lights + num_area > 15)
+    return fail(ctx, AJG_ERR_UNSUPPORTED,
+                "at most 15 lights (emitters included)");
   ajg_scene_opts o{14, AJG_TRI_MOLLER_TRUMBORE, 0, 0};
   if (opts) o = *opts;
   if (o.tri_test > AJG_TRI_WATERTIGHT)
@@ -318,16 +432,24 @@ int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
   cudaSetDevice(ctx->device);
   auto* s = new ajg_scene();
   s->ctx = ctx;
-  // lights: records as given, env records get the two mass flags of the
-  // 1x1 Distribution2D (utility/distribution.h:40-60, 135-144)
-  s->host_lights.resize(12 * (size_t)num_lights);
+  // lights: the emitters' area lights first (default_scene.cpp:33-48), then
+  // the records as given; env records get the two mass flags of the 1x1
+  // Distribution2D (utility/distribution.h:40-60, 135-144)
+  const uint32_t nl_all = num_area + num_lights;
+  s->host_lights.resize(12 * (size_t)nl_all);
+  std::vector<float> emit_pts;
+  for (uint32_t i = 0, a = 0; i < num_emitters; ++i) {
+    if (black_emission(emitters[i])) continue;
+    area_light_record(tris, emitters[i], (uint32_t)(emit_pts.size() / 3),
+                      &s->host_lights[12 * (size_t)a++], emit_pts);
+  }
   int env = -1;
   for (uint32_t l = 0; l < num_lights; ++l) {
-    float* r = &s->host_lights[12 * l];
+    float* r = &s->host_lights[12 * (size_t)(num_area + l)];
     std::memcpy(r, &lights[l], sizeof(ajg_light));
     r[0] = (float)lights[l].type;
     if (lights[l].type == AJG_LIGHT_ENV) {
-      env = (int)l;
+      env = (int)(num_area + l);
       const float w = host_lum(lights[l].rgb) * std::sin(kPi * (0 + 0.5f) / 1.f);
       const float func_int = 0.f + w * (1.f / 1.f);
       r[10] = func_int > 0.f ? 1.f : 0.f;
@@ -355,22 +477,34 @@ int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
   float* d_light = (float*)keep(std::max<size_t>(1, s->host_lights.size()) *
                                 sizeof(float));
   float4* d_lum = (float4*)keep(num_materials * sizeof(float4));
-  if (!d_mat || !d_light || !d_lum) {
+  int32_t* d_tri_emit =
+      num_area ? (int32_t*)keep(n * sizeof(int32_t)) : nullptr;
+  float* d_pts = num_area ? (float*)keep(emit_pts.size() * sizeof(float)) : nullptr;
+  if (!d_mat || !d_light || !d_lum || (num_area && (!d_tri_emit || !d_pts))) {
     ajg_scene_release(s);
     return fail(ctx, AJG_ERR_OOM, "device allocation failed (scene tables)");
   }
   cudaMemcpy(d_mat, s->host_materials.data(),
              s->host_materials.size() * sizeof(float), cudaMemcpyHostToDevice);
-  if (num_lights)
+  if (nl_all)
     cudaMemcpy(d_light, s->host_lights.data(),
                s->host_lights.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (num_area) {
+    cudaMemcpy(d_tri_emit, tri_emit.data(), n * sizeof(int32_t),
+               cudaMemcpyHostToDevice);
+    cudaMemcpy(d_pts, emit_pts.data(), emit_pts.size() * sizeof(float),
+               cudaMemcpyHostToDevice);
+  }
+  s->d.tri_emit = d_tri_emit;
+  s->d.emit_pts = d_pts;
+  s->d.num_area = num_area;
   cudaMemcpy(d_lum, lum.data(), num_materials * sizeof(float4),
              cudaMemcpyHostToDevice);
   s->d.materials = d_mat;
   s->d.lights = d_light;
   s->d.mat_lum = d_lum;
   s->d.num_materials = num_materials;
-  s->d.num_lights = num_lights;
+  s->d.num_lights = nl_all;
   s->d.env = env;
   int rc = build_scene(ctx, s, tris, corner_normals, tri_material, tri_flags,
                        n, world, o);
@@ -390,6 +524,16 @@ int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
                      uint32_t num_materials, const ajg_light* lights,
                      uint32_t num_lights, const ajg_scene_opts* opts,
                      ajg_scene** out) {
+  return ajg_scene_create_ex(ctx, meshes, num_meshes, materials, num_materials,
+                             lights, num_lights, nullptr, 0, opts, out);
+}
+
+int ajg_scene_create_ex(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
+                        uint32_t num_meshes, const ajg_material* materials,
+                        uint32_t num_materials, const ajg_light* lights,
+                        uint32_t num_lights, const ajg_emitter* emitters,
+                        uint32_t num_emitters, const ajg_scene_opts* opts,
+                        ajg_scene** out) {
   if (!ctx || !out || (!meshes && num_meshes))
     return fail(ctx, AJG_ERR_INVALID, "NULL argument");
   uint64_t n = 0;
@@ -447,9 +591,10 @@ int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
     }
   }
   const float world[6] = {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
-  return ajg_scene_create_flat(ctx, tris.data(), any_normals ? cn.data() : nullptr,
-                               mat.data(), flags.data(), n, world, materials,
-                               num_materials, lights, num_lights, opts, out);
+  return ajg_scene_create_flat_ex(
+      ctx, tris.data(), any_normals ? cn.data() : nullptr, mat.data(),
+      flags.data(), n, world, materials, num_materials, lights, num_lights,
+      emitters, num_emitters, opts, out);
 }
 
 int ajg_scene_release(ajg_scene* s) {

@@ -275,6 +275,91 @@ __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
   flush_counters(ctr, nr, nn, nt);
 }
 
+// Closest hits of the MIS BSDF rays of scenes with emitters (the queue at
+// the top of the shadow queue's storage, see emit_closest); t and the
+// primitive go to two arrays the material lists' storage lends.
+template <int TEST, bool MJ, int W>
+__global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
+    k_bsdf_trace(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
+                 const float4* __restrict__ sq_d,
+                 const uint16_t* __restrict__ sq_scene,
+                 const uint32_t* __restrict__ count, uint32_t* fetch_next,
+                 uint32_t cap, uint32_t n_max, float* __restrict__ t_hit,
+                 int32_t* __restrict__ prim_hit, TraceCounters* ctr,
+                 uint32_t* err) {
+  // at most one entry per path (n_max = paths of the arena)
+  const uint32_t n = min(*count, n_max);
+  uint32_t nn = 0, nt = 0, nr = 0;
+  auto fetch = [&](uint32_t k, TraceScene& ts) {
+    const uint32_t i = cap - 1 - k;
+    const float4 o = sq_o[i], d = sq_d[i];
+    if constexpr (MJ) retarget(ts, t, sq_scene[i]);
+    return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
+  };
+  auto finish = [&](uint32_t k, const Hit& h, bool) {
+    t_hit[k] = h.t;
+    prim_hit[k] = h.prim;
+  };
+  trace_persistent<TEST, false, W>(trace_scene(s), n, fetch_next, fetch,
+                                   finish, nr, nn, nt, err);
+  flush_counters(ctr, nr, nn, nt);
+}
+
+// The MIS BSDF term from its closest hit (helper.h:223-264): an escaped ray
+// sees the environment, one that hits the lit side of an emitter its
+// radiance, weighted against AreaLight::Pdf; anything else adds nothing.
+template <bool MJ>
+__global__ void __launch_bounds__(kShadeThreads)
+    k_bsdf_emit(WaveArgs a, MJTables t, WaveBufs w, uint32_t NT, uint32_t cap,
+                uint32_t n_max, const float* __restrict__ t_hit,
+                const int32_t* __restrict__ prim_hit) {
+  const uint32_t n = min(w.counts[8], n_max);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += gridDim.x * blockDim.x) {
+    const uint32_t i = cap - 1 - k;
+    const float4 o4 = w.sq_o[i], d4 = w.sq_d[i];
+    const uint32_t slot = __float_as_uint(d4.w);
+    const uint32_t p = slot / NT;
+    const uint32_t jid = MJ ? w.pjob[p] : 0u;
+    const JobParams& J = Src<MJ>::job(a, t, jid);
+    const DeviceScene& s = Src<MJ>::scene(a, t, jid);
+    const F3 o = xyz(o4), d = xyz(d4);
+    const float pdf = o4.w;
+    const float4 fs = w.term_f[slot];
+    const F3 bf = xyz(fs);
+    const float cosv = fs.w;
+    const int prim = prim_hit[k];
+    F3 fo = mk3(0.f, 0.f, 0.f);
+    bool vis = false;
+    if (prim < 0) {
+      const F3 rad = mk3(J.env_rgb.x, J.env_rgb.y, J.env_rgb.z);
+      if (s.env >= 0 && !black3(rad)) {
+        const F3 fv = rad * bf * cosv;
+        const float lp = env_pdf(J.env_mass != 0, d);
+        fo = mk3(0, 0, 0) + fv / pdf * power_heuristic(pdf, lp);
+        vis = true;
+      }
+    } else {
+      const int li = __ldg(s.tri_emit + prim);
+      if (li >= 0) {
+        F3 pos, ng;
+        emitter_hit(s, o, d, t_hit[k], prim, pos, ng);
+        const float* L = s.lights + 12 * li;
+        const F3 le =
+            dot3(ng, -d) > 0 ? mk3(L[1], L[2], L[3]) : mk3(0.f, 0.f, 0.f);
+        if (!black3(le)) {
+          const F3 fv = le * bf * cosv;
+          const float lp = area_pdf(L[9], o, pos, ng);
+          fo = fv / pdf * power_heuristic(pdf, lp);
+          vis = true;
+        }
+      }
+    }
+    w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
+    w.term_vis[slot] = vis ? 1 : 0;
+  }
+}
+
 template <bool MJ>
 __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
@@ -289,6 +374,27 @@ __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
   w.sq_o[k] = make_float4(o.x, o.y, o.z, tmax);
   w.sq_d[k] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
   if constexpr (MJ) w.sq_scene[k] = (uint16_t)sid;
+}
+
+// The closest-hit queue of MIS BSDF rays in scenes with emitters: entry k
+// sits at cap - 1 - k of the shadow queue's storage.  A path appends at most
+// NT entries to the two queues together (its lights' shadow rays and one
+// BSDF ray) and cap = P * NT, so the queues cannot meet.
+template <bool MJ>
+__device__ __forceinline__ void emit_closest(const WaveBufs& w, F3 o, F3 d,
+                                             float pdf, uint32_t slot,
+                                             uint32_t sid, bool pred,
+                                             uint32_t cap, uint32_t* err) {
+  const uint32_t k = warp_append(&w.counts[8], pred);
+  if (!pred) return;
+  if (k >= cap) {
+    raise_device_error(err, kDevQueueOverflow);
+    return;
+  }
+  const uint32_t i = cap - 1 - k;
+  w.sq_o[i] = make_float4(o.x, o.y, o.z, pdf);
+  w.sq_d[i] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
+  if constexpr (MJ) w.sq_scene[i] = (uint16_t)sid;
 }
 
 // Escaped paths: the environment counts only for camera rays
@@ -350,8 +456,10 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
     BsdfT<MAT> f;
     F3 T = mk3(0, 0, 0);
     uint64_t key = 0;
+    int emitter = -1;
     if (hit) {
       const ajg_hit h = w.hits[k];
+      if (s.tri_emit) emitter = __ldg(s.tri_emit + h.prim);
       const F3 ro = xyz(w.ro[cur][k]), rd = xyz(w.rd[cur][k]);
       if constexpr (MJ) {
         key = w.pkey[p];
@@ -367,6 +475,19 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
       f.ns = hi.ns;
       f.lum = __ldg(&s.mat_lum[hi.mat].x);
       w.thr_shade[p] = make_float4(T.x, T.y, T.z, 0.f);
+      // an emitter seen by a camera ray, or by any ray without MIS
+      // (pt.cpp:185-190, 282-286; AreaLight::Radiance, area_light.cpp:30-34)
+      if (emitter >= 0 && (b == 0 || !J.use_mis)) {
+        const float* L = s.lights + 12 * emitter;
+        const F3 le = dot3(hi.ng, hi.wr) > 0 ? mk3(L[1], L[2], L[3])
+                                               : mk3(0.f, 0.f, 0.f);
+        const F3 c = T * le;
+        float4 R = w.rad[p];
+        R.x += c.x;
+        R.y += c.y;
+        R.z += c.z;
+        w.rad[p] = R;
+      }
     }
     int dim = dim_base(J, b) + (b > J.min_b ? 1 : 0);
     // lanes of a multi-job warp differ in lights and MIS: loop over the
@@ -387,12 +508,29 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
         bool emit = false;
         F3 fo = mk3(0, 0, 0), so = mk3(0, 0, 0), sd = mk3(0, 0, 1);
         float tmax = 0.f;
+        int draws = 2;
         if (on) {
           F3 lpos, lrad;
           float lpdf;
           const int type = (int)L[0];
           bool ok = true;
-          if (type == AJG_LIGHT_DIRECTIONAL) {
+          if (type == kLightArea) {
+            // AreaLight::Sample (area_light.cpp:36-57): three draws
+            draws = 3;
+            const AreaSample g =
+                area_sample(L, s.emit_pts, key_float(key, dim),
+                            key_float(key, dim + 1), key_float(key, dim + 2));
+            lrad = mk3(L[1], L[2], L[3]);
+            lpos = g.pos;
+            lpdf = 0.f;
+            if (dot3(g.ng, hi.pos - g.pos) <= 0) {
+              ok = false;
+            } else {
+              const F3 i2r = hi.pos - g.pos;
+              const float dist2 = dot3(i2r, i2r);
+              lpdf = g.pdf * dist2 / fabsf(dot3(g.ng, i2r));
+            }
+          } else if (type == AJG_LIGHT_DIRECTIONAL) {
             const float u0 = key_float(key, dim), u1 = key_float(key, dim + 1);
             const F3 dir = normalize3(mk3(L[4], L[5], L[6]));
             const F3 r2l = Frame(dir).to_world(uniform_cone(u0, u1, L[7]));
@@ -431,9 +569,11 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
               float bp;
               f.eval_pdf(wl, hi.wr, bf, bp);
               if (!black3(bf)) {
-                const F3 nn = normalize3(hi.ns);
+                // MISSampleAreaLight takes the shading normal as it is, the
+                // others normalise it (helper.h:64, 91, 120)
+                const F3 nn = type == kLightArea ? hi.ns : normalize3(hi.ns);
                 F3 fv;
-                if (type == AJG_LIGHT_DIRECTIONAL)
+                if (type != AJG_LIGHT_ENV)
                   fv = mk3(1.f, 1.f, 1.f) * lrad * bf * fabsf(dot3(wl, nn));
                 else
                   fv = lrad * bf * fabsf(dot3(wl, nn));
@@ -450,34 +590,52 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
         }
         emit_shadow<MJ>(w, so, sd, tmax, p * NT + l, sid, emit, shadow_cap,
                         err);
-        if (on) dim += 2;
+        if (on) dim += draws;
       }
       {
+        // MISSampleBsdf (helper.h:209-265).  Without emitters only the
+        // environment can answer, and an any-hit escape test decides; with
+        // emitters the closest hit decides, so the ray goes to the closest
+        // queue with the BSDF value and |cos| parked in its term and the pdf
+        // in the ray (k_bsdf_emit completes the term).
         const bool on = MJ ? mis : hit;
-        bool emit = false;
+        bool emit = false, closest = false;
         F3 fo = mk3(0, 0, 0), so = mk3(0, 0, 0), sd = mk3(0, 0, 1);
+        float w_o = __int_as_float(0x7f800000);
+        float cosv = 0.f;
         if (on) {
           const F3 sam = mk3(key_float(key, dim), key_float(key, dim + 1),
                              key_float(key, dim + 2));
           BsdfSample bs = f.sample(hi.wr, sam);
-          if (!(black3(bs.f) || bs.pdf == 0.f) && s.env >= 0) {
-            bs.dir = normalize3(bs.dir);
-            make_ray(eps_offset(hi, bs.dir), bs.dir, so, sd);
-            const F3 rad = mk3(J.env_rgb.x, J.env_rgb.y, J.env_rgb.z);
-            if (!black3(rad)) {
-              const F3 fv = rad * bs.f * fabsf(dot3(hi.ns, sd));
-              const float lp = env_pdf(J.env_mass != 0, sd);
-              fo = mk3(0, 0, 0) + fv / bs.pdf * power_heuristic(bs.pdf, lp);
-              emit = true;
+          if (!(black3(bs.f) || bs.pdf == 0.f)) {
+            if (s.tri_emit) {
+              bs.dir = normalize3(bs.dir);
+              make_ray(eps_offset(hi, bs.dir), bs.dir, so, sd);
+              fo = bs.f;
+              cosv = fabsf(dot3(hi.ns, sd));
+              w_o = bs.pdf;
+              closest = true;
+            } else if (s.env >= 0) {
+              bs.dir = normalize3(bs.dir);
+              make_ray(eps_offset(hi, bs.dir), bs.dir, so, sd);
+              const F3 rad = mk3(J.env_rgb.x, J.env_rgb.y, J.env_rgb.z);
+              if (!black3(rad)) {
+                const F3 fv = rad * bs.f * fabsf(dot3(hi.ns, sd));
+                const float lp = env_pdf(J.env_mass != 0, sd);
+                fo = mk3(0, 0, 0) + fv / bs.pdf * power_heuristic(bs.pdf, lp);
+                emit = true;
+              }
             }
           }
           const uint32_t slot = p * NT + (NT - 1);
-          w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
+          w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, cosv);
           w.term_vis[slot] = 0;
           dim += 3;
         }
         emit_shadow<MJ>(w, so, sd, __int_as_float(0x7f800000),
                         p * NT + (NT - 1), sid, emit, shadow_cap, err);
+        emit_closest<MJ>(w, so, sd, w_o, p * NT + (NT - 1), sid, closest,
+                         shadow_cap, err);
       }
     }
 
@@ -731,7 +889,7 @@ uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   add(slots * 16); add(slots * 16);  // shadow queue
   if (mj) add(slots * 2);      // sq_scene
   add(P * 4 * 3);              // material lists
-  add(32);                     // counts
+  add(64);                     // counts
   return b;
 }
 
@@ -758,7 +916,7 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj) {
   w.sq_d = carve<float4>(cur, P * nt);
   if (mj) w.sq_scene = carve<uint16_t>(cur, P * nt);
   w.lists = carve<uint32_t>(cur, P * 3);
-  w.counts = carve<uint32_t>(cur, 8);
+  w.counts = carve<uint32_t>(cur, 16);
   return w;
 }
 
@@ -802,7 +960,9 @@ JobParams make_job_params(const ajg_scene* sc, const ajg_camera& cam,
   j.cont = prm.cont_prob;
   j.use_mis = prm.use_mis ? 1 : 0;
   j.nl = (int)s.num_lights;
-  j.nd = j.use_mis ? (2 * j.nl + 6) : 3;
+  // draws per bounce: 2 per directional or env light, 3 per area light,
+  // 3 for the MIS BSDF sample and 3 for the continuation
+  j.nd = j.use_mis ? (2 * j.nl + (int)s.num_area + 6) : 3;
   j.env_rgb = make_float4(0, 0, 0, 0);
   j.env_mass = 0;
   if (s.env >= 0) {
@@ -862,6 +1022,18 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
           &ctx->d_counters[0], ctx->d_error);
     });
   };
+  auto bsdf_closest = [&]() {
+    dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
+      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+      const int g = resident_grid((const void*)k_bsdf_trace<TT, false, WW>,
+                                  kTraceThreads);
+      k_bsdf_trace<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
+          s, t, w.sq_o, w.sq_d, nullptr, &w.counts[8], &w.counts[9],
+          shadow_cap, (uint32_t)P, reinterpret_cast<float*>(w.lists),
+          reinterpret_cast<int32_t*>(w.lists + P), &ctx->d_counters[0],
+          ctx->d_error);
+    });
+  };
   auto shadow = [&]() {
     dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
@@ -880,7 +1052,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       a.S = (uint32_t)Sw;
       a.s0 = (uint32_t)s0;
       a.n_paths = (uint32_t)(n_pix * Sw);
-      cudaMemsetAsync(w.counts, 0, 32, st);
+      cudaMemsetAsync(w.counts, 0, 64, st);
       KernelTimer{ctx, st, -1};
       k_raygen<false><<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads,
                         0, st>>>(a, t, w);
@@ -888,7 +1060,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       for (int b = 0; b < a.j.max_b; ++b) {
         // next queue, shadow queue, fetch counters and material lists
         cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
-        cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
+        cudaMemsetAsync(&w.counts[2], 0, 8 * sizeof(uint32_t), st);
         {
           KernelTimer tm(ctx, st, kc);
           extend(q);
@@ -921,6 +1093,17 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
             KernelTimer tm(ctx, st, ka);
             shadow();
           }
+          if (s.tri_emit) {
+            {
+              KernelTimer tm(ctx, st, kc);
+              bsdf_closest();
+            }
+            KernelTimer{ctx, st, -1};
+            k_bsdf_emit<false><<<gs, kShadeThreads, 0, st>>>(
+                a, t, w, (uint32_t)nt, shadow_cap, (uint32_t)P,
+                reinterpret_cast<const float*>(w.lists),
+                reinterpret_cast<const int32_t*>(w.lists + P));
+          }
           KernelTimer{ctx, st, -1};
           k_accumulate<false><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
                                                             (uint32_t)nt);
@@ -952,22 +1135,23 @@ void prepare_mj_kernels() {
         constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
         resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
         resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
+        resident_grid((const void*)k_bsdf_trace<TT, true, WW>, kTraceThreads);
       });
 }
 
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
-                     int NT, int bounces, int tri_test, int width,
+                     int NT, int bounces, int tri_test, int width, bool emit,
                      TraceCounters* ctr, uint32_t* err, cudaStream_t st) {
   const DeviceScene s{};
   WaveArgs a{};
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
-  cudaMemsetAsync(w.counts, 0, 32, st);
+  cudaMemsetAsync(w.counts, 0, 64, st);
   k_raygen<true><<<gs, kShadeThreads, 0, st>>>(a, t, w);
   int q = 0;
   for (int b = 0; b < bounces; ++b) {
     cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
-    cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
+    cudaMemsetAsync(&w.counts[2], 0, 8 * sizeof(uint32_t), st);
     dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
       const int g =
@@ -994,6 +1178,21 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
           s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[2], &w.counts[3],
           w.term_vis, ctr + 1, err);
     });
+    if (emit) {
+      dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
+        constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
+        const int g = resident_grid((const void*)k_bsdf_trace<TT, true, WW>,
+                                    kTraceThreads);
+        k_bsdf_trace<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
+            s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[8], &w.counts[9],
+            shadow_cap, (uint32_t)P, reinterpret_cast<float*>(w.lists),
+            reinterpret_cast<int32_t*>(w.lists + P), ctr, err);
+      });
+      k_bsdf_emit<true><<<gs, kShadeThreads, 0, st>>>(
+          a, t, w, (uint32_t)NT, shadow_cap, (uint32_t)P,
+          reinterpret_cast<const float*>(w.lists),
+          reinterpret_cast<const int32_t*>(w.lists + P));
+    }
     k_accumulate<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
                                                      (uint32_t)NT);
     q ^= 1;

@@ -41,7 +41,23 @@ struct DeviceScene {
   int32_t tri_test = 0;
   int32_t width = 2;     // layout of `bvh`: 2 (binary PLOC tree), 4, 8, or
                          // 4 / 8 | kBvhCompressed
+  // area lights (emissive primitives): the first num_area light records
+  // (kLightArea), the corner points their samplers read, and per triangle
+  // (indexed like `shade`) the light it emits as, or -1; all null / 0 in a
+  // scene without emitters
+  const int32_t* tri_emit = nullptr;
+  const float* emit_pts = nullptr;  // [k][3]
+  uint32_t num_area = 0;
+  uint32_t pad_ = 0;
 };
+
+// Light record types ([12] floats, type in [0]): the two of the ABI, and the
+// area light of an emissive primitive:
+//   [1..3] radiance, [4] geometry (AJG_GEOM_*), [5] two-sided,
+//   [6] triangles (uint bits), [7] 1 / area, [8] the quad's (a,b,c) share of
+//   its area, [9] Geometry::Pdf (the same for every point of the surface),
+//   [10] first corner in emit_pts (uint bits)
+constexpr int kLightArea = 2;
 
 // Per-job constants of the integrator, shared by the single-job and the
 // multi-job waves.  The film of a job covers the window (x0, y0, win_w,
@@ -252,12 +268,15 @@ uint64_t wave_bytes(uint64_t P, int nt, bool mj);
 WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj);
 // Enqueues one multi-job wave on `st` (capturable: fixed arguments, queue
 // lengths and table contents read on the device): raygen, `bounces` bounce
-// iterations, film update.  NT = light terms per path of the arena.
+// iterations, film update.  NT = light terms per path of the arena; `emit`:
+// a scene of the wave has emitters (the closest-hit MIS BSDF pass runs).
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
-                     int NT, int bounces, int tri_test, int width,
+                     int NT, int bounces, int tri_test, int width, bool emit,
                      TraceCounters* ctr, uint32_t* err, cudaStream_t st);
 // Kernels of a multi-job wave launched per wave (for launch counts).
-inline int mj_wave_kernels(int bounces) { return 2 + 7 * bounces; }
+inline int mj_wave_kernels(int bounces, bool emit) {
+  return 2 + (emit ? 9 : 7) * bounces;
+}
 // Looks up the persistent grids of the multi-job kernels (call before a
 // stream capture).
 void prepare_mj_kernels();

@@ -33,6 +33,7 @@ static_assert(sizeof(ajg_job_status) == 56, "ajg_job_status layout");
 static_assert(sizeof(ajg_serve_opts) == 16, "ajg_serve_opts layout");
 static_assert(sizeof(ajg_serve_stats) == 80, "ajg_serve_stats layout");
 static_assert(sizeof(ajg_scene_info) == 48, "ajg_scene_info layout");
+static_assert(sizeof(ajg_emitter) == 32, "ajg_emitter layout");
 
 namespace ajg {
 namespace {
@@ -149,7 +150,7 @@ struct Server {
   std::vector<char*> h_tables;  // pinned, one per in-flight slot + 1
   size_t table_bytes = 0;
   uint64_t wave_no = 0;
-  std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, int, int, bool>, cudaGraphExec_t> graphs;
   std::deque<InFlight> inflight;
   std::vector<uint32_t*> err_words;  // pinned, recycled
   uint32_t* d_err = nullptr;
@@ -164,7 +165,7 @@ struct Server {
   void retire_oldest();
   void end_job_locked(Job* j, uint32_t state, int err);
   int ensure_arena(int nt, uint64_t target_paths);
-  cudaGraphExec_t graph_for(int bounces, int tri_test, int width);
+  cudaGraphExec_t graph_for(int bounces, int tri_test, int width, bool emit);
 };
 
 namespace {
@@ -200,8 +201,9 @@ int Server::ensure_arena(int nt, uint64_t target) {
   return AJG_OK;
 }
 
-cudaGraphExec_t Server::graph_for(int bounces, int tri_test, int width) {
-  const auto key = std::make_tuple(bounces, tri_test, width);
+cudaGraphExec_t Server::graph_for(int bounces, int tri_test, int width,
+                                  bool emit) {
+  const auto key = std::make_tuple(bounces, tri_test, width, emit);
   auto it = graphs.find(key);
   if (it != graphs.end()) return it->second;
   prepare_mj_kernels();
@@ -210,7 +212,8 @@ cudaGraphExec_t Server::graph_for(int bounces, int tri_test, int width) {
   if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) !=
       cudaSuccess)
     return nullptr;
-  enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, d_ctr, d_err, st);
+  enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, emit, d_ctr, d_err,
+                  st);
   if (cudaStreamEndCapture(st, &g) != cudaSuccess || !g) return nullptr;
   if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
   cudaGraphDestroy(g);
@@ -504,12 +507,16 @@ bool Server::plan_and_launch() {
   cudaMemcpyAsync(d_tables, h, table_bytes, cudaMemcpyHostToDevice, st);
 
   InFlight f{};
-  cudaGraphExec_t g = graph_for(bounces, tri_test, width);
+  // the closest-hit MIS BSDF pass runs when a scene of the wave has emitters
+  bool emit = false;
+  for (const Plan& p : plan) emit |= p.job->scene->d.tri_emit != nullptr;
+  cudaGraphExec_t g = graph_for(bounces, tri_test, width, emit);
   if (g) {
     cudaGraphLaunch(g, st);
   } else {  // capture unavailable: the same launches on the stream
     cudaGetLastError();
-    enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, d_ctr, d_err, st);
+    enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, emit, d_ctr, d_err,
+                    st);
   }
   // results this wave completes
   for (const Plan& p : plan) {
@@ -556,7 +563,7 @@ bool Server::plan_and_launch() {
     std::lock_guard<std::mutex> lk(mu);
     ++stats.waves;
     stats.paths += path_off;
-    stats.kernel_launches += mj_wave_kernels(bounces) + f.reports.size();
+    stats.kernel_launches += mj_wave_kernels(bounces, emit) + f.reports.size();
   }
   inflight.push_back(std::move(f));
   ++wave_no;

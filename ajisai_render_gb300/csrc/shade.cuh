@@ -726,6 +726,105 @@ __device__ __forceinline__ float env_pdf(bool env_has_mass, F3 ref2light) {
   return p2 / (2.f * kPi * kPi * st);
 }
 
+// ------------------------------------------------------------ area lights --
+struct AreaSample {
+  F3 pos, ng;
+  float pdf;  // per unit area
+};
+
+// Geometry::Sample(ref, pdf, sam) of an emitter's surface from its light
+// record `L` (kLightArea layout) and corner points `pts`:
+//   TwoSided: sam.x < 0.5 picks the back face, x rescaled to [0,1), pdf
+//     halved, the normal flipped there (two_sided.cpp:86-103);
+//   the triangle point: (u, v) reflected when u + v > 1, p = (1-u-v) a +
+//     u b + v c, n = normalize(cross(b - a, c - a));
+//   quad: (a,b,c) when sam.z is below its area share, else (a,c,d); pdf
+//     1 / area (quad.cpp:128-150);
+//   mesh: idx = min(int(sam.z * triangles), triangles - 1) and the corners
+//     idx, idx+1, idx+2 of the index buffer -- without the factor 3, so the
+//     windows that straddle two triangles (and repeat a vertex: a NaN
+//     normal) are sampled as the reference samples them; pdf 1 / area
+//     (mesh.cpp:251-275);
+//   cube: triangle min(int(sam.z * 12), 11), pdf 1 / (12 * its area)
+//     (cube.cpp:145-170).
+__device__ __forceinline__ AreaSample area_sample(const float* L,
+                                                  const float* pts, float x,
+                                                  float y, float z) {
+  const int kind = (int)L[4];
+  const bool two = L[5] != 0.f;
+  const uint32_t ntri = __float_as_uint(L[6]);
+  const float* P = pts + 3 * (uint64_t)__float_as_uint(L[10]);
+  F3 sam = mk3(x, y, z);
+  bool back = false;
+  if (two) {
+    back = sam.x < 0.5f;
+    if (back)
+      sam.x = 2 * x;
+    else
+      sam.x = 2 * (x - 0.5f);
+  }
+  F3 sn = sam;
+  if (sn.x + sn.y > 1.f) {
+    sn.x = 1.f - sn.x;
+    sn.y = 1.f - sn.y;
+  }
+  F3 a, b, c;
+  AreaSample g;
+  if (kind == AJG_GEOM_QUAD) {
+    a = ld3(P);
+    if (sam.z < L[8]) {
+      b = ld3(P + 3);
+      c = ld3(P + 6);
+    } else {
+      b = ld3(P + 6);
+      c = ld3(P + 9);
+    }
+    g.pdf = L[7];
+  } else if (kind == AJG_GEOM_MESH) {
+    const int idx = min((int)(sam.z * (float)ntri), (int)ntri - 1);
+    a = ld3(P + 3 * idx);
+    b = ld3(P + 3 * idx + 3);
+    c = ld3(P + 3 * idx + 6);
+    g.pdf = L[7];
+  } else {
+    const int idx = min((int)(sam.z * (float)12), 11);
+    a = ld3(P + 9 * idx);
+    b = ld3(P + 9 * idx + 3);
+    c = ld3(P + 9 * idx + 6);
+    g.pdf = 1.f / (12.f * len3(cross3(b - a, c - a)) * 0.5f);
+  }
+  g.pos = (1 - sn.x - sn.y) * a + sn.x * b + sn.y * c;
+  g.ng = normalize3(cross3(b - a, c - a));
+  if (two) {
+    g.pdf = g.pdf * 0.5f;
+    if (back) g.ng = g.ng * -1.f;
+  }
+  return g;
+}
+
+// AreaLight::Pdf (area_light.cpp:68-79); `pdf_area` = Geometry::Pdf.
+__device__ __forceinline__ float area_pdf(float pdf_area, F3 ref, F3 pos,
+                                          F3 normal) {
+  if (dot3(ref - pos, normal) <= 0.f) return 0.f;
+  const F3 l2r = ref - pos;
+  const float dist2 = dot3(l2r, l2r);
+  const float abscos = fabsf(dot3(l2r, normal));
+  return pdf_area * (dist2 / abscos);
+}
+
+// The part of PostIntersect an emitter hit needs: the position and the
+// geometric normal, flipped toward the ray on two-sided primitives.
+__device__ __forceinline__ void emitter_hit(const DeviceScene& s, F3 o, F3 d,
+                                            float t, int prim, F3& pos,
+                                            F3& ng) {
+  const float4 sh = __ldg(s.shade + prim);
+  pos = o + t * d;
+  ng = mk3(sh.x, sh.y, sh.z);
+  if (((__float_as_uint(sh.w) >> 24) & AJG_MESH_TWO_SIDED) &&
+      dot3(ng, -d) < 0)
+    ng = ng * -1.f;
+}
+
 // ----------------------------------------------------------------- camera --
 __device__ __forceinline__ void mat_vec(const float* M, const float v[4],
                                         float out[4]) {

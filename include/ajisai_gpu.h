@@ -111,6 +111,25 @@ typedef struct ajg_light {
   float pad[2];
 } ajg_light; /* 48 bytes */
 
+/* An emissive primitive (GeometricPrimitive with a non-black `emission`,
+ * core/primitive/geometric.cpp:33-45): its AreaLight samples the
+ * primitive's geometry (core/light/area_light.cpp:36-79).  The triangles
+ * [first_triangle, first_triangle + num_triangles) of the scene's order are
+ * the primitive's, as its MeshView lays them out: a quad's two (a,b,c),
+ * (a,c,d); a cube's twelve as the cube mesh gives them; a mesh's in index
+ * order.  Area lights precede the scene's other lights, in emitter order
+ * (default_scene.cpp:41-48). */
+enum { AJG_GEOM_QUAD = 0, AJG_GEOM_CUBE = 1, AJG_GEOM_MESH = 2 };
+typedef struct ajg_emitter {
+  float radiance[3];       /* emission; a black one adds no light */
+  uint32_t first_triangle;
+  uint32_t num_triangles;  /* quad 2, cube 12, mesh >= 1 */
+  uint32_t geometry;       /* AJG_GEOM_*: the sampler of its surface */
+  uint32_t two_sided;      /* TwoSided wrapper (two_sided.cpp:65-114); its
+                              triangles carry AJG_MESH_TWO_SIDED alike */
+  uint32_t reserved;       /* 0 */
+} ajg_emitter; /* 32 bytes */
+
 typedef struct ajg_scene_opts {
   uint32_t search_radius; /* PLOC neighbour radius (reference default 14) */
   uint32_t tri_test;      /* AJG_TRI_*; Moller-Trumbore matches the reference */
@@ -224,6 +243,22 @@ AJG_API int ajg_scene_create_flat(ajg_ctx* ctx, const float* tris,
                                   uint32_t num_materials,
                                   const ajg_light* lights, uint32_t num_lights,
                                   const ajg_scene_opts* opts, ajg_scene** out);
+/* The same with emissive primitives (area lights).  At most 15 lights in
+ * all: the non-black emitters plus `lights`. */
+AJG_API int ajg_scene_create_ex(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
+                                uint32_t num_meshes,
+                                const ajg_material* materials,
+                                uint32_t num_materials,
+                                const ajg_light* lights, uint32_t num_lights,
+                                const ajg_emitter* emitters,
+                                uint32_t num_emitters,
+                                const ajg_scene_opts* opts, ajg_scene** out);
+AJG_API int ajg_scene_create_flat_ex(
+    ajg_ctx* ctx, const float* tris, const float* corner_normals,
+    const int32_t* tri_material, const int32_t* tri_flags, uint64_t n,
+    const float* world, const ajg_material* materials, uint32_t num_materials,
+    const ajg_light* lights, uint32_t num_lights, const ajg_emitter* emitters,
+    uint32_t num_emitters, const ajg_scene_opts* opts, ajg_scene** out);
 AJG_API int ajg_scene_release(ajg_scene* scene);
 AJG_API int ajg_scene_get_info(ajg_scene* scene, ajg_scene_info* out);
 /* The built tree in the reference's layout (ploc_aggregate.cpp:146-152):

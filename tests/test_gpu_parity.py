@@ -268,7 +268,8 @@ def test_camera_rays_match_reference(ctx, golden):
 # ---------------------------------------------------------------- render --
 def flat_of(g):
     return S.FlatScene(g["tris"], g["corner_n"], g["tri_mat"], g["tri_flags"],
-                       g["world"], g["materials"], g["lights"], g["camera"])
+                       g["world"], g["materials"], g["lights"], g["camera"],
+                       g["emit_rad"], g["emit_info"])
 
 
 def params_of(g):
@@ -279,30 +280,38 @@ def params_of(g):
 
 
 @pytest.mark.parametrize("case", ["render_cornell.npz", "render_ico.npz",
-                                  "render_cornell_nomis.npz"])
+                                  "render_cornell_nomis.npz", "render_area.npz",
+                                  "render_area_nomis.npz"])
 def test_render_per_sample_matches_reference(ctx, golden, case):
     """Shared counter sampler: each sample's radiance equals the reference's
     within float32 tolerance, apart from rare paths that a last-ulp
-    difference of CUDA's transcendentals sends another way."""
+    difference of CUDA's transcendentals sends another way.  The area-light
+    scenes hold an emissive mesh whose sampler windows straddle triangles:
+    the reference's NaN samples there are NaN here too."""
     g = golden(case)
     flat = flat_of(g)
     sc = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, 0, True))
     r = api.PTRenderer(params_of(g), seed=int(g["seed"]))
     li = r.RenderSamples(sc, flat.camera)
     ref = g["li"]
-    close = np.isclose(li, ref, rtol=1e-4, atol=1e-6).all(axis=-1)
+    close = np.isclose(li, ref, rtol=1e-4, atol=1e-6, equal_nan=True).all(axis=-1)
     assert close.mean() > 0.99, close.mean()
-    # per-pixel means agree within 3 sigma of the sample spread
-    H, W = g["film"].shape[:2]
+    # per-pixel means agree within 3 sigma of the sample spread (pixels
+    # without a non-finite sample)
     spp = ref.shape[1]
-    m_gpu, m_ref = li.mean(1), ref.mean(1)
-    sigma = np.maximum(ref.std(1), 1e-3) / np.sqrt(spp)
+    fin = np.isfinite(ref).all(axis=(1, 2)) & np.isfinite(li).all(axis=(1, 2))
+    assert fin.mean() > 0.8
+    m_gpu, m_ref = li[fin].mean(1), ref[fin].mean(1)
+    sigma = np.maximum(ref[fin].std(1), 1e-3) / np.sqrt(spp)
     within = (np.abs(m_gpu - m_ref) <= 3 * sigma + 1e-5).all(axis=-1)
     assert within.mean() > 0.99
     # the film from Render() is the footprint sum of the same samples
     film = r.Render(sc, flat.camera)
-    np.testing.assert_allclose(film.rgbw[..., :3], g["film"][..., :3],
-                               rtol=1e-3, atol=1e-3 * spp)
+    fg, fr = film.rgbw[..., :3], g["film"][..., :3]
+    ok_g, ok_r = np.isfinite(fg).all(-1), np.isfinite(fr).all(-1)
+    assert (ok_g == ok_r).mean() > 0.97
+    np.testing.assert_allclose(fg[ok_g & ok_r], fr[ok_g & ok_r], rtol=1e-3,
+                               atol=1e-3 * spp)
     assert np.array_equal(film.rgbw[..., 3], g["film"][..., 3])
 
 
@@ -370,3 +379,106 @@ def test_trace_counters(ctx):
     sc.Intersect(rays)
     st = ctx.stats()
     assert st["closest_rays"] == 1000 and st["closest_nodes"] >= 1000
+
+
+# ------------------------------------------------------------ area lights --
+def _area_no_mesh(w, h):
+    """cornell_area without its emissive mesh (whose straddling sampler
+    windows make NaN samples): every sample finite."""
+    spec = S.cornell_area(w, h)
+    spec.primitives[9].emission = None
+    return spec
+
+
+@pytest.mark.parametrize("use_mis", [True, False])
+def test_area_lights_match_oracle_per_sample(ctx, use_mis):
+    """Quad (one- and two-sided), mesh and cube emitters at a size the
+    reference fixtures do not reach, against the oracle sample by sample."""
+    flat = S.flatten(S.cornell_area(40, 32))
+    sc = api.GpuScene(ctx, flat)
+    args = api.PTRendererArgs(spp=8, min_bounces=3, max_bounces=8,
+                              use_mis=use_mis)
+    li = api.PTRenderer(args, seed=11).RenderSamples(sc, flat.camera)
+    ref, _ = O.render(flat, dict(spp=8, min_bounces=3, max_bounces=8,
+                                 use_mis=int(use_mis)), seed=11)
+    ref = ref.reshape(li.shape)
+    close = np.isclose(li, ref, rtol=1e-4, atol=1e-6, equal_nan=True).all(axis=-1)
+    assert close.mean() > 0.99, close.mean()
+    if use_mis:  # the mesh emitter's NaN samples are there, as in the reference
+        assert np.isnan(ref).any()
+    # the emitters light the box: more light than the same box without them
+    dark = S.flatten(S.cornell_area(40, 32))
+    dark.emit_rad = dark.emit_rad[:0]
+    dark.emit_info = dark.emit_info[:0]
+    li_dark = api.PTRenderer(args, seed=11).RenderSamples(api.GpuScene(ctx, dark),
+                                                          dark.camera)
+    assert np.nanmean(li) > 2 * np.nanmean(li_dark)
+
+
+@pytest.mark.parametrize("width", LAYOUTS[1:])
+def test_area_lights_tree_independent(ctx, width):
+    """The closest-hit MIS BSDF pass over a wide tree gives the binary tree's
+    samples bit for bit."""
+    flat = S.flatten(_area_no_mesh(32, 24))
+    r = api.PTRenderer(api.PTRendererArgs(spp=8, min_bounces=2, max_bounces=8), seed=4)
+    a = r.RenderSamples(api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, bvh_width=2)),
+                        flat.camera)
+    b = r.RenderSamples(api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, bvh_width=width)),
+                        flat.camera)
+    assert np.isfinite(a).all()
+    assert same_bits(a, b)
+
+
+def test_area_lights_wave_split_and_film(ctx):
+    """Small waves give the same samples; the film equals the oracle's."""
+    flat = S.flatten(_area_no_mesh(24, 20))
+    args = api.PTRendererArgs(spp=8, min_bounces=3, max_bounces=8)
+    small = api.Context(0, wave_paths=1000)
+    a = api.PTRenderer(args, seed=2).RenderSamples(api.GpuScene(ctx, flat), flat.camera)
+    b = api.PTRenderer(args, seed=2).RenderSamples(api.GpuScene(small, flat), flat.camera)
+    small.close()
+    assert same_bits(a, b)
+    film = api.PTRenderer(args, seed=2).Render(api.GpuScene(ctx, flat), flat.camera).rgbw
+    _, film_o = O.render(flat, dict(spp=8, min_bounces=3, max_bounces=8), seed=2)
+    assert np.array_equal(film[..., 3], film_o[..., 3].astype(np.float32))
+    np.testing.assert_allclose(film[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
+
+
+def test_invalid_emitters_are_rejected(ctx):
+    from ajisai_render_gb300._lib import AjgError
+    base = S.flatten(S.cornell_area(8, 8))
+
+    def bad(mutate, code=1):
+        fl = S.flatten(S.cornell_area(8, 8))
+        fl.emit_info = fl.emit_info.copy()
+        fl.emit_rad = fl.emit_rad.copy()
+        mutate(fl)
+        with pytest.raises(AjgError) as e:
+            api.GpuScene(ctx, fl)
+        assert e.value.code == code
+
+    def quad_count(fl):
+        fl.emit_info[0, 1] = 3
+    def out_of_range(fl):
+        fl.emit_info[2, 0] = base.n_tris - 10
+    def overlap(fl):
+        fl.emit_info[1, 0] = fl.emit_info[0, 0]
+    def sidedness(fl):
+        fl.emit_info[0, 3] = 1
+    def geometry(fl):
+        fl.emit_info[0, 2] = 7
+    def too_many(fl):
+        k = 14
+        fl.emit_info = np.repeat(fl.emit_info[2:3], k, 0)
+        fl.emit_info[:, 0] = base.emit_info[2, 0] + np.arange(k)
+        fl.emit_info[:, 1] = 1
+        fl.emit_rad = np.ones((k, 3), np.float32)
+    for m in (quad_count, out_of_range, overlap, sidedness, geometry):
+        bad(m)
+    bad(too_many, code=4)
+    # a black emitter adds no light and is accepted
+    fl = S.flatten(S.cornell_area(8, 8))
+    fl.emit_rad = fl.emit_rad.copy()
+    fl.emit_rad[:] = 0
+    sc = api.GpuScene(ctx, fl)
+    sc.release()

@@ -33,6 +33,7 @@ def scenes(ctx):
     if len(clutter.primitives) < 3:  # make sure one scene is clutter
         clutter = S.mixed_scene(4, 3000, 64, 64)
     env_only = with_lights(S.icosphere_scene(2, 11, 64, 64), [S.EnvLight(0.7)])
+    area = S.cornell_area(64, 64)
     three = with_lights(S.cornell_box(64, 64),
                         [S.DirectionalLight((0.3, 1.0, 0.2), 3.0),
                          S.DirectionalLight((-0.5, 1.0, 0.1), 1.5, 5.0),
@@ -53,6 +54,11 @@ def scenes(ctx):
                    ico.camera),
         "box_c4": (api.GpuScene(ctx, box, api.CreatePLOCAggregate(14, bvh_width=0x104)),
                    box.camera),
+        # emitters: waves that mix them with emitter-free scenes run the
+        # closest-hit MIS BSDF pass for the paths of these only
+        "area": (api.GpuScene(ctx, area), area.camera),
+        "area_c8": (api.GpuScene(ctx, area, api.CreatePLOCAggregate(14, bvh_width=0x108)),
+                    area.camera),
     }
     return out
 
@@ -83,6 +89,9 @@ def job_list(scenes):
         ("clutter_w4", 40, 24, renderer(6, seed=8, mis=False)),
         ("ico_c8", 32, 32, renderer(9, seed=11)),
         ("box_c4", 24, 32, renderer(7, seed=12)),
+        ("area", 48, 40, renderer(9, seed=13)),
+        ("area", 24, 24, renderer(6, mis=False, seed=14)),
+        ("area_c8", 32, 24, renderer(5, seed=15, drop=True)),
     ]
 
 
