@@ -182,8 +182,9 @@ class HostSceneView(C.Structure):
                 ("num_materials", C.c_uint32), ("num_lights", C.c_uint32),
                 ("materials", C.c_void_p), ("lights", C.c_void_p),
                 ("opts", SceneOpts), ("camera", Camera), ("params", RenderParams),
-                ("num_outputs", C.c_uint32), ("reserved", C.c_uint32),
-                ("outputs", C.POINTER(C.c_char_p))]
+                ("num_outputs", C.c_uint32), ("num_emitters", C.c_uint32),
+                ("outputs", C.POINTER(C.c_char_p)),
+                ("emitters", C.POINTER(Emitter))]
 
 
 HOST_LIB_PATH = HERE / "_build" / "libajisai_host.so"

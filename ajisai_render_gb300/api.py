@@ -464,12 +464,19 @@ def load_scene_file(path) -> SceneFile:
         cam[16:32] = np.array(v.camera.camera2world, F32)
         cam[32], cam[33] = v.camera.lens_radius, v.camera.focal_distance
         cam[34], cam[35] = v.camera.width, v.camera.height
+        ne = v.num_emitters
+        emit_rad = np.array([list(v.emitters[i].radiance) for i in range(ne)],
+                            F32).reshape(-1, 3)
+        emit_info = np.array([[v.emitters[i].first_triangle, v.emitters[i].num_triangles,
+                               v.emitters[i].geometry, v.emitters[i].two_sided]
+                              for i in range(ne)], np.int32).reshape(-1, 4)
         flat = FlatScene(
             tris=arr(v.tris, n * 9, F32, (n, 9)),
             corner_n=arr(v.corner_normals, n * 9, F32, (n, 9)),
             tri_mat=arr(v.tri_material, n, np.int32, (n,)),
             tri_flags=arr(v.tri_flags, n, np.int32, (n,)),
-            world=np.array(v.world, F32), materials=mats, lights=lights, camera=cam)
+            world=np.array(v.world, F32), materials=mats, lights=lights, camera=cam,
+            emit_rad=emit_rad, emit_info=emit_info)
         p = v.params
         args = PTRendererArgs(spp=p.spp, min_bounces=p.min_bounces,
                               max_bounces=p.max_bounces, cont_prob=p.cont_prob,

@@ -89,11 +89,11 @@ int main(int argc, char** argv) {
   if (check(ajg_create_context(&cfg, &ctx), nullptr, "context")) return 1;
   ajg_scene* scene = nullptr;
   const auto t0 = std::chrono::steady_clock::now();
-  int rc = ajg_scene_create_flat(
+  int rc = ajg_scene_create_flat_ex(
       ctx, f.tris.data(), f.corner_normals.data(), f.tri_material.data(),
       f.tri_flags.data(), f.tri_material.size(), f.world, f.materials.data(),
       (uint32_t)f.materials.size(), f.lights.data(), (uint32_t)f.lights.size(),
-      &f.opts, &scene);
+      f.emitters.data(), (uint32_t)f.emitters.size(), &f.opts, &scene);
   if (check(rc, ctx, "scene")) {
     ajg_destroy_context(ctx);
     return 1;

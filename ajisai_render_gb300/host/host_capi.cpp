@@ -62,6 +62,8 @@ int ajh_scene_view_get(const ajh_scene* s, ajh_scene_view* v) {
   v->params = f.params;
   v->num_outputs = (uint32_t)s->out_ptrs.size();
   v->outputs = s->out_ptrs.data();
+  v->num_emitters = (uint32_t)f.emitters.size();
+  v->emitters = f.emitters.data();
   return 0;
 }
 

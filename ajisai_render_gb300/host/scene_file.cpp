@@ -148,6 +148,7 @@ struct Geo {
   std::vector<V3> tri;     // 3 per triangle
   std::vector<V3> corner;  // 3 per triangle (meshes)
   int flags = 0;
+  uint32_t kind = AJG_GEOM_MESH;  // how an AreaLight samples it
   Bounds bounds;
 };
 
@@ -240,6 +241,7 @@ Geo load_geometry(const std::string& file, const Node& n,
     const V3 c = transform_point(xf, corner("c", {1.f, 1.f, 0.f}));
     const V3 d = transform_point(xf, corner("d", {-1.f, 1.f, 0.f}));
     g.tri = {a, b, c, a, c, d};
+    g.kind = AJG_GEOM_QUAD;
     g.bounds = bounds_of(g.tri);
   } else if (type == "cube") {  // cube.cpp:35-76
     const M4 xf = get_transform(file, n["transform"]);
@@ -256,6 +258,7 @@ Geo load_geometry(const std::string& file, const Node& n,
       g.tri.insert(g.tri.end(), {pos[i + 2], pos[i + 3], pos[i]});
     }
     g.flags = AJG_MESH_NG_REVERSED;
+    g.kind = AJG_GEOM_CUBE;
     g.bounds = bounds_of(g.tri);
   } else if (type == "twosided") {  // two_sided.cpp
     g = load_geometry(file, n["internal"], scene_dir);
@@ -462,16 +465,26 @@ SceneFile LoadSceneFile(const std::string& path) {
     const std::string ptype = p["type"].AsString("");
     if (ptype != "geometry")
       fail(path, p, "unknown primitive type '" + ptype + "'");
-    if (p["emission"].IsDefined()) {
-      const V3 e = vec3(path, p["emission"]);
-      if (e.x != 0.f || e.y != 0.f || e.z != 0.f)
-        fail(path, p, "emissive primitives (area lights) are not on this "
-                      "path");
-    }
     for (const char* med : {"med_in", "med_out"})
       if (p[med].IsDefined() && p[med]["type"].AsString("void") != "void")
         fail(path, p, "participating media are not on this path");
     const Geo g = load_geometry(path, p["geometry"], dir);
+    // `emission` makes the primitive an area light (primitive_creators.cpp:
+    // 65-72, geometric.cpp:41-44); a black one makes none
+    if (p["emission"].IsDefined()) {
+      const V3 e = vec3(path, p["emission"]);
+      if (e.x != 0.f || e.y != 0.f || e.z != 0.f) {
+        ajg_emitter em{};
+        em.radiance[0] = e.x;
+        em.radiance[1] = e.y;
+        em.radiance[2] = e.z;
+        em.first_triangle = (uint32_t)out.tri_material.size();
+        em.num_triangles = (uint32_t)(g.tri.size() / 3);
+        em.geometry = g.kind;
+        em.two_sided = (g.flags & AJG_MESH_TWO_SIDED) ? 1u : 0u;
+        out.emitters.push_back(em);
+      }
+    }
     const ajg_material m = load_material(path, p["material"]);
     const int32_t mat = (int32_t)out.materials.size();
     out.materials.push_back(m);

@@ -23,7 +23,7 @@
 namespace ajh {
 
 struct SceneFile {
-  // ajg_scene_create_flat's arrays: triangles in MeshView order per
+  // ajg_scene_create_flat_ex's arrays: triangles in MeshView order per
   // primitive, YAML order (ploc_aggregate.cpp:252-285)
   std::vector<float> tris;            // [n][9]
   std::vector<float> corner_normals;  // [n][9], meshes only
@@ -32,6 +32,7 @@ struct SceneFile {
   float world[6];                     // Join of the primitives' bounds
   std::vector<ajg_material> materials;  // one per primitive
   std::vector<ajg_light> lights;        // YAML order
+  std::vector<ajg_emitter> emitters;    // emissive primitives, YAML order
   ajg_scene_opts opts;
   ajg_camera camera;
   ajg_render_params params;

@@ -2,7 +2,7 @@
  * ajisai_host: the host side of the drop-in around libajisai_gpu -- Ajisai
  * YAML scene files (the reference's factory, app/main.cpp:84-112 and
  * factory/creator/*.cpp, for the nodes the PT/PLOC path renders) read into
- * the flat description ajg_scene_create_flat takes, and the film written as
+ * the flat description ajg_scene_create_flat_ex takes, and the film written as
  * PFM (float) or PNG (8-bit, as the reference's ImageWriter).  Plain C ABI;
  * no CUDA.  Errors: status 1 with a message in `err`.
  */
@@ -38,8 +38,9 @@ typedef struct ajh_scene_view {
   ajg_camera camera;
   ajg_render_params params;
   uint32_t num_outputs;  /* save_to_img files: filename + "." + ext */
-  uint32_t reserved;
+  uint32_t num_emitters; /* emissive primitives (area lights) */
   const char* const* outputs;
+  const ajg_emitter* emitters;
 } ajh_scene_view;
 
 AJH_API int ajh_load_scene(const char* path, ajh_scene** out, char* err,

@@ -1,8 +1,9 @@
 """Writes the scene-file fixtures in the reference's YAML format
 (factory/creator/*.cpp keys): the Cornell-style box of
 ajisai_render_gb300.scenes.cornell_box, block style, and the same scene in
-flow style.  The cube matrices are the float32 values scenes.py uses,
-printed so that they read back bit for bit.
+flow style; scenes.cornell_area with its emitters (and ball.obj, its
+emissive mesh).  The cube matrices and mesh vertices are the float32 values
+scenes.py uses, printed so that they read back bit for bit.
 
     python tests/golden/gen_scene_files.py
 """
@@ -76,8 +77,62 @@ def cornell_yaml(flow: bool) -> str:
     return "\n".join(lines) + "\n"
 
 
+def _texel(v) -> str:
+    return "{type: constant, texel: %s}" % (vec(v) if np.ndim(v) else f32(v))
+
+
+def _material_yaml(m) -> str:
+    if m.type == S.MAT_DIFFUSE:
+        return "{type: diffuse, albedo: %s}" % _texel(m.base_color)
+    keys = ("subsurface", "metallic", "specular", "specular_tint", "roughness",
+            "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss")
+    return "{type: disney, base_color: %s, %s}" % (
+        _texel(m.base_color),
+        ", ".join(f"{k}: {_texel(getattr(m, k))}" for k in keys))
+
+
+def area_files() -> tuple[str, str]:
+    """scenes.cornell_area as a scene file: its emissive quads, cube and
+    icosphere mesh (ball.obj) carry `emission`."""
+    sc = S.cornell_area(256, 256)
+    obj = ["# emissive icosphere of scenes.cornell_area"]
+    lines = ["# scenes.cornell_area: the box lit by a one-sided ceiling quad, a",
+             "# two-sided quad, an emissive icosphere mesh and an emissive cube.",
+             "scene:", "  type: default", "  primitives:"]
+    for p in sc.primitives:
+        if isinstance(p, S.Quad):
+            geo = (f"{{type: quad, a: {vec(p.a)}, b: {vec(p.b)}, c: {vec(p.c)}, "
+                   f"d: {vec(p.d)}}}")
+        elif isinstance(p, S.Cube):
+            geo = (f"{{type: cube, transform: {{type: matrix, matrix: "
+                   f"{vec(p.transform)}}}}}")
+        else:
+            for v in p.positions:
+                obj.append("v " + " ".join(f32(x) for x in v))
+            for t in p.indices:
+                obj.append("f " + " ".join(str(int(i) + 1) for i in t))
+            geo = "{type: mesh, filename: ball.obj}"
+        if p.two_sided:
+            geo = f"{{type: twosided, internal: {geo}}}"
+        lines += ["    - type: geometry", f"      geometry: {geo}",
+                  f"      material: {_material_yaml(sc.materials[p.material])}"]
+        if p.emission is not None:
+            lines.append(f"      emission: {vec(p.emission)}")
+    lines += ["  lights:",
+              "    - {type: directional, direction: [0.3, 1.0, 0.2], emission: [1, 1, 1]}",
+              "    - {type: envmap, texture: {type: constant, texel: 0.05}}",
+              "  aggregate: {type: ploc, search_radius: 14}",
+              "camera: {type: thin_lens, resolution: [256, 256], position: [0, 0, 1.9],",
+              "         look_at: [0, 0, 0], up: [0, 1, 0], fov: 40}",
+              "renderer: {type: pt, spp: 64, min_bounces: 3, max_bounces: 8}"]
+    return "\n".join(lines) + "\n", "\n".join(obj) + "\n"
+
+
 if __name__ == "__main__":
     OUT.mkdir(exist_ok=True)
     (OUT / "cornell_box.yaml").write_text(cornell_yaml(False))
     (OUT / "cornell_box_flow.yaml").write_text(cornell_yaml(True))
+    yml, obj = area_files()
+    (OUT / "cornell_area.yaml").write_text(yml)
+    (OUT / "ball.obj").write_text(obj)
     print("wrote", OUT)
