@@ -30,6 +30,11 @@ TRI_HAS_NORMALS = 4  # MeshGeo: interpolated per-vertex shading normals
 
 MAT_DIFFUSE = 0
 MAT_DISNEY = 1
+MAT_MIRROR = 2
+MAT_GLASS = 3
+MAT_METAL = 4
+MAT_PLASTIC = 5
+MAT_NULL = 6
 LIGHT_DIRECTIONAL = 0
 LIGHT_ENV = 1
 
@@ -50,15 +55,21 @@ class Material:
     sheen_tint: float = 0.0
     clearcoat: float = 0.0
     clearcoat_gloss: float = 0.0
+    # the ten parameter floats of the non-Disney types (None: the Disney
+    # fields above)
+    params: Optional[Sequence[float]] = None
 
     def pack(self) -> np.ndarray:
         r = np.zeros(16, F32)
         r[0] = self.type
         r[1:4] = self.base_color
-        r[4:14] = [self.subsurface, self.metallic, self.specular,
-                   self.specular_tint, self.roughness, self.anisotropic,
-                   self.sheen, self.sheen_tint, self.clearcoat,
-                   self.clearcoat_gloss]
+        if self.params is not None:
+            r[4:4 + len(self.params)] = self.params
+        else:
+            r[4:14] = [self.subsurface, self.metallic, self.specular,
+                       self.specular_tint, self.roughness, self.anisotropic,
+                       self.sheen, self.sheen_tint, self.clearcoat,
+                       self.clearcoat_gloss]
         return r
 
 
@@ -74,6 +85,39 @@ def Disney(base_color, subsurface=0.0, metallic=0.0, specular=0.5,
     return Material(MAT_DISNEY, tuple(base_color), subsurface, metallic,
                     specular, specular_tint, roughness, anisotropic, sheen,
                     sheen_tint, clearcoat, clearcoat_gloss)
+
+
+def Mirror(kr) -> Material:
+    """CreateMirror (core/material/mirror.cpp:100-102)."""
+    return Material(MAT_MIRROR, tuple(np.broadcast_to(kr, 3)), params=())
+
+
+def Glass(ior, color_reflection=1.0, color_refraction=1.0) -> Material:
+    """CreateGlass (core/material/glass.cpp:160-165) with the YAML creator's
+    defaults (material_creators.cpp:133-152): the refraction colour is
+    stored as given; shading takes its square root."""
+    return Material(MAT_GLASS, tuple(np.broadcast_to(color_reflection, 3)),
+                    params=(*np.broadcast_to(color_refraction, 3), ior))
+
+
+def Metal(color, k, eta, uroughness=0.1, vroughness=0.1) -> Material:
+    """CreateMetal (core/material/metal.cpp:75-80): a GGX reflection with a
+    coloured conductor Fresnel of (eta, k)."""
+    return Material(MAT_METAL, tuple(np.broadcast_to(color, 3)),
+                    params=(*np.broadcast_to(k, 3), *np.broadcast_to(eta, 3),
+                            uroughness, vroughness))
+
+
+def Plastic(albedo, ior=1.5, thickness=1.0, sigma_a=0.0) -> Material:
+    """CreatePlastic (core/material/plastic.cpp:62-65) with the YAML
+    creator's defaults (material_creators.cpp:44-52)."""
+    return Material(MAT_PLASTIC, tuple(np.broadcast_to(albedo, 3)),
+                    params=(ior, thickness, sigma_a))
+
+
+def Null() -> Material:
+    """CreateNull (core/material/null.cpp:74): rays pass straight through."""
+    return Material(MAT_NULL, (0.0, 0.0, 0.0), params=())
 
 
 # ------------------------------------------------------------------ lights --
@@ -449,6 +493,43 @@ def cornell_area(width: int = 256, height: int = 256) -> Scene:
              white, False, emission=(2.0, 4.0, 2.0)),
     ]
     lights = [DirectionalLight((0.3, 1.0, 0.2), 1.0), EnvLight(0.05)]
+    cam = Camera((0.0, 0.0, 1.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0,
+                 width, height)
+    return Scene(prims, mats, lights, cam)
+
+
+def material_box(width: int = 256, height: int = 256) -> Scene:
+    """The box of ``cornell_box`` with the other materials: a plastic floor
+    (ior 1.5, thickness 1, sigma_a 0.3), a mirror tall box, a rough gold-like
+    metal short box, a glass ball of 320 smooth-shaded triangles (ior 1.5)
+    on it, and a ceiling light quad of radiance (6,6,6) with the null
+    material (rays pass through it); a directional light of radiance 1 and
+    a constant environment of 0.1."""
+    white, red, green, plastic, mirror, metal, glass, null = range(8)
+    mats = [Diffuse((0.73, 0.73, 0.73)), Diffuse((0.65, 0.05, 0.05)),
+            Diffuse((0.12, 0.45, 0.15)),
+            Plastic((0.6, 0.55, 0.5), 1.5, 1.0, 0.3),
+            Mirror((0.9, 0.9, 0.9)),
+            Metal((1.0, 0.95, 0.9), (3.98, 2.38, 1.60), (0.14, 0.37, 1.44), 0.25, 0.15),
+            Glass(1.5, (1.0, 1.0, 1.0), (0.9, 0.95, 1.0)),
+            Null()]
+    h = 0.5
+    v, f = icosphere(2)
+    ball = (v * 0.12 + np.array([0.17, -0.2 + 0.12, 0.12])).astype(F32)
+    prims = [
+        Quad((-h, -h, h), (h, -h, h), (h, -h, -h), (-h, -h, -h), plastic, True),  # floor
+        Quad((-h, h, -h), (h, h, -h), (h, h, h), (-h, h, h), white, True),        # ceiling
+        Quad((-h, -h, -h), (h, -h, -h), (h, h, -h), (-h, h, -h), white, True),    # back
+        Quad((-h, -h, h), (-h, -h, -h), (-h, h, -h), (-h, h, h), red, True),      # left
+        Quad((h, -h, -h), (h, -h, h), (h, h, h), (h, h, -h), green, True),        # right
+        Cube(_rot_y_matrix_rowmajor((0.3, 0.6, 0.3), 15.0, (-0.17, -0.2, -0.12)), mirror, False),
+        Cube(_rot_y_matrix_rowmajor((0.3, 0.3, 0.3), -18.0, (0.17, -0.35, 0.12)), metal, False),
+        Mesh(ball, f.astype(np.int32), v.astype(F32), glass, False),
+        Quad((-0.12, h - 1e-3, -0.12), (0.12, h - 1e-3, -0.12),
+             (0.12, h - 1e-3, 0.12), (-0.12, h - 1e-3, 0.12), null, False,
+             emission=(6.0, 6.0, 6.0)),
+    ]
+    lights = [DirectionalLight((0.3, 1.0, 0.2), 1.0), EnvLight(0.1)]
     cam = Camera((0.0, 0.0, 1.9), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 40.0,
                  width, height)
     return Scene(prims, mats, lights, cam)

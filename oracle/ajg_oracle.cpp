@@ -605,14 +605,89 @@ inline float correct_shading_normal(V3 ng, V3 ns, V3 wi) {
   return denom == 0 ? 1.f : std::fabs(dot(ns, wi) / denom);
 }
 
+/* ------------------------------------------------------------ Fresnel --- */
+/* Fresnel::dielectricReflectance (bsdf/helper.h:35-56) */
+inline float dielectric_reflectance(float eta, float cos_i) {
+  if (cos_i < 0.0f) {
+    eta = 1.0f / eta;
+    cos_i = -cos_i;
+  }
+  const float sin_t2 = eta * eta * (1.0f - cos_i * cos_i);
+  if (sin_t2 > 1.0f) return 1.0f;
+  const float cos_t = std::sqrt(fmax_ref(1.0f - sin_t2, 0.0f));
+  const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+  const float rp = (eta * cos_t - cos_i) / (eta * cos_t + cos_i);
+  return (rs * rs + rp * rp) * 0.5f;
+}
+
+/* DielectricFresnel::Eval (material/fresnel.h:95-118), one channel */
+inline float dielectric_fresnel(float eta_in, float eta_out, float cos_i) {
+  if (cos_i < 0) {
+    std::swap(eta_in, eta_out);
+    cos_i = -cos_i;
+  }
+  const float sin_i = std::sqrt(fmax_ref(0.f, 1 - cos_i * cos_i));
+  const float sin_t = eta_out / eta_in * sin_i;
+  if (sin_t >= 1.f) return 1.f;
+  const float cos_t = std::sqrt(fmax_ref(0.f, 1 - sin_t * sin_t));
+  const float para = ((eta_in * cos_i) - (eta_out * cos_t)) /
+                     ((eta_in * cos_i) + (eta_out * cos_t));
+  const float perp = ((eta_out * cos_i) - (eta_in * cos_t)) /
+                     ((eta_out * cos_i) + (eta_in * cos_t));
+  return 0.5f * (para * para + perp * perp);
+}
+
+/* ConductorFresnel::Eval (material/fresnel.h:40-58), eta_out = 1:
+ * eta2 = eta * eta, etak2 = k * k */
+inline V3 conductor_fresnel(V3 eta2, V3 etak2, float cos_i) {
+  if (cos_i <= 0.f) return mk(0, 0, 0);
+  const float cos2 = cos_i * cos_i;
+  const float sin2 = fmax_ref(0.f, 1 - cos2);
+  V3 out;
+  float* o = &out.x;
+  const float* e2 = &eta2.x;
+  const float* k2 = &etak2.x;
+  for (int c = 0; c < 3; ++c) {
+    const float t0 = e2[c] - k2[c] - sin2;
+    const float a2b2 = std::sqrt(t0 * t0 + 4.f * e2[c] * k2[c]);
+    const float t1 = a2b2 + cos2;
+    const float a = std::sqrt(0.5f * (a2b2 + t0));
+    const float t2 = 2.f * cos_i * a;
+    const float rs = (t1 - t2) / (t1 + t2);
+    const float t3 = cos2 * a2b2 + sin2 * sin2;
+    const float t4 = t2 * sin2;
+    const float rp = rs * (t3 - t4) / (t3 + t4);
+    o[c] = 0.5f * (rp + rs);
+  }
+  return out;
+}
+
+}  // namespace
+
+/* Fresnel::computeDiffuseFresnel (bsdf/helper.h:58-73) */
+float orc_diffuse_fresnel(float ior, int n) {
+  double acc = 0.0;
+  float fb = dielectric_reflectance(ior, 0.0f);
+  for (int i = 1; i <= n; ++i) {
+    const float cos2 = float(i) / n;
+    const float fa = dielectric_reflectance(ior, std::min(std::sqrt(cos2), 1.0f));
+    acc += double(fa + fb) * (0.5 / n);
+    fb = fa;
+  }
+  return float(acc);
+}
+
+namespace {
+
 /* --------------------------------------------------------------- BSDF --- */
 struct Sample {
   V3 dir, f;
   float pdf;
   bool valid;
+  bool delta = false; /* BSDFSampleResult::is_delta */
 };
 inline Sample invalid_sample() {
-  return Sample{mk(0, 0, 0), mk(0, 0, 0), 0.f, false};
+  return Sample{mk(0, 0, 0), mk(0, 0, 0), 0.f, false, false};
 }
 
 struct Mat {
@@ -620,7 +695,10 @@ struct Mat {
   V3 base;
   float subsurface, metallic, specular, specular_tint, roughness, anisotropic,
       sheen, sheen_tint, clearcoat, clearcoat_gloss;
-  float lum; /* base.Luminance() */
+  float p[10]; /* the same ten floats, read by the other material types */
+  float lum;   /* base.Luminance() */
+  /* plastic: PlasticBsdf's constructor terms (plastic_bsdf.cpp:32-45) */
+  float plastic_avg_t = 0.f, plastic_diffuse_fresnel = 0.f;
 };
 Mat load_mat(const float* m) {
   Mat x;
@@ -636,7 +714,17 @@ Mat load_mat(const float* m) {
   x.sheen_tint = m[11];
   x.clearcoat = m[12];
   x.clearcoat_gloss = m[13];
+  for (int i = 0; i < 10; ++i) x.p[i] = m[4 + i];
   x.lum = luminance(x.base);
+  if (x.type == ORC_MAT_PLASTIC) {
+    const float ior = x.p[0], thickness = x.p[1], sigma_a = x.p[2];
+    const float sc = thickness * sigma_a;
+    const float avg = (sc + sc + sc) / 3.f;
+    x.plastic_avg_t = std::exp(-2.0f * avg);
+    /* a process-wide std::call_once in the reference: the first PlasticBsdf
+     * constructed fixes it for every plastic; here each material's own */
+    x.plastic_diffuse_fresnel = orc_diffuse_fresnel(ior, 1000000);
+  }
   return x;
 }
 
@@ -953,20 +1041,344 @@ struct Disney {
   }
 };
 
+/* The base BSDF's black-fringe fallbacks (bsdf.cpp:30-63) for a BSDF of
+ * albedo `alb` (Metal's AggregateBSDF: 1; PlasticBsdf: its albedo). */
+struct Fringe {
+  V3 ng, ns, alb;
+  Frame gf;
+  Fringe(V3 ng_, V3 ns_, V3 a) : ng(ng_), ns(ns_), alb(a), gf(ng_) {}
+  bool causes(V3 w) const { return (dot(ng, w) > 0) != (dot(ns, w) > 0); }
+  Sample sample(V3 wo, V3 sam) const {
+    if (dot(ng, wo) <= 0.f) return invalid_sample();
+    float pdf;
+    V3 lwi = cosine_hemisphere(sam.x, sam.y, &pdf);
+    if (pdf < FLT_EPSILON) return invalid_sample();
+    V3 wi = normalized(gf.to_world(lwi));
+    float factor = correct_shading_normal(ng, ns, wi);
+    return Sample{wi, alb / kPi * factor, pdf, true, false};
+  }
+  V3 eval(V3 wi, V3 wo) const {
+    if ((dot(ng, wi) <= 0.f) || (dot(ng, wo) <= 0.f)) return mk(0, 0, 0);
+    return alb / kPi;
+  }
+  float pdf(V3 wi, V3 wo) const {
+    if ((dot(ng, wi) > 0.f) != (dot(ng, wo) > 0.f)) return 0.f;
+    V3 local = normalized(gf.to_local(wi));
+    return local.z * kInvPi;
+  }
+};
+
+/* MirrorBSDF (mirror.cpp:32-66): a delta reflection about the shading
+ * normal, kr / |cos|, pdf 1; eval and pdf are 0. */
+struct MirrorB {
+  V3 ng, ns, kr;
+  Frame sf;
+  MirrorB(V3 ng_, V3 ns_, V3 kr_) : ng(ng_), ns(ns_), kr(kr_), sf(ns_) {}
+  Sample sample(V3 wo) const {
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (lwo.z <= 0.f) return invalid_sample();
+    const V3 lwi = mk(-lwo.x, -lwo.y, lwo.z);
+    const V3 wi = sf.to_world(lwi);
+    const float factor = correct_shading_normal(ng, ns, wi);
+    return Sample{wi, kr * factor / std::fabs(lwi.z), 1.f, true, true};
+  }
+};
+
+/* GlassBSDF (glass.cpp:31-116) with Glass::Shade's colours (glass.cpp:
+ * 128-150): reflection with probability Fr, else refraction, both delta. */
+struct GlassB {
+  V3 ng, ns, refl, refr;
+  float ior;
+  Frame sf;
+  GlassB(V3 ng_, V3 ns_, const Mat& m)
+      : ng(ng_), ns(ns_), refl(m.base), ior(m.p[3]), sf(ns_) {
+    refr = mk(std::sqrt(m.p[0]), std::sqrt(m.p[1]), std::sqrt(m.p[2]));
+  }
+  Sample sample(V3 wo, V3 sam) const {
+    const V3 lwo = normalized(sf.to_local(wo));
+    const V3 normal = lwo.z > 0 ? mk(0.f, 0.f, 1.f) : mk(0.f, 0.f, -1.f);
+    /* DielectricFresnel(eta_in = ior, eta_out = 1) */
+    const float fr = dielectric_fresnel(ior, 1.f, lwo.z);
+    if (sam.x < fr) {
+      const V3 lwi = mk(-lwo.x, -lwo.y, lwo.z);
+      const V3 wi = sf.to_world(lwi);
+      const V3 f = refl * mk(fr, fr, fr) / std::fabs(lwi.z);
+      const float factor = correct_shading_normal(ng, ns, wi);
+      return Sample{wi, f * factor, fr, true, true};
+    }
+    const float eta_i = lwo.z > 0 ? 1.f : ior;
+    const float eta_t = lwo.z > 0 ? ior : 1.f;
+    const float eta = eta_i / eta_t;
+    const float cos_i = std::fabs(lwo.z);
+    const float sin2_i = fmax_ref(0.f, 1.f - cos_i * cos_i);
+    const float sin2_t = eta * eta * sin2_i;
+    if (sin2_t > 1.f) return invalid_sample();
+    const float cos_t = std::sqrt(1 - sin2_t);
+    const V3 w = (eta * cos_i - cos_t) * normal - eta * lwo;
+    const V3 lwi = normalized(w);
+    const V3 dir = sf.to_world(lwi);
+    const V3 f = eta * eta * refr * (1.f - fr) / std::fabs(lwi.z);
+    const float pdf = 1.f - fr;
+    const float factor = correct_shading_normal(ng, ns, dir);
+    return Sample{dir, f * factor, pdf, true, true};
+  }
+};
+
+/* TrowbridgeReitzDistribution and EvalPdf of the GGX reflection component
+ * (microfacet_reflection_component.cpp:26-135) */
+inline float sqr(float x) { return x * x; }
+inline float ggx_phi(V3 w) {
+  if (w.x <= 0.f && w.y <= 0.f) return 0.f;
+  const float r = std::atan2(w.y, w.x);
+  return r < 0.f ? (r + 2 * kPi) : r;
+}
+inline float ggx_tan_theta(V3 w) {
+  const float t = 1 - w.z * w.z;
+  if (t <= 0) return 0;
+  return std::sqrt(t) / w.z;
+}
+inline float ggx_d(float sin_phi_h, float cos_phi_h, float sin_theta_h,
+                   float cos_theta_h, float ax, float ay) {
+  const float A = sqr(cos_phi_h / ax) + sqr(sin_phi_h / ay);
+  const float RD = sqr(sin_theta_h) * A + sqr(cos_theta_h);
+  return 1.f / (kPi * ax * ay * sqr(RD));
+}
+inline float ggx_g(float cos_phi, float sin_phi, float ax, float ay,
+                   float tan_theta) {
+  const float t = sqr(ax * cos_phi) + sqr(ay * sin_phi);
+  const float sq = 1 + t * sqr(tan_theta);
+  const float lambda = -0.5f + 0.5f * std::sqrt(sq);
+  return 1 / (1 + lambda);
+}
+inline V3 ggx_sample_wh(V3 ve, float ax, float ay, float sx, float sy) {
+  const V3 vh = normalized(mk(ax * ve.x, ay * ve.y, ve.z));
+  const float lensq = vh.x * vh.x + vh.y * vh.y;
+  const V3 t1 = lensq > FLT_EPSILON ? mk(-vh.y, vh.x, 0) / std::sqrt(lensq)
+                                    : mk(1, 0, 0);
+  const V3 t2 = cross(vh, t1);
+  const float r = std::sqrt(sx);
+  const float phi = 2 * kPi * sy;
+  const float t_1 = r * std::cos(phi);
+  const float t_2s = r * std::sin(phi);
+  const float s = 0.5f * (1 + vh.z);
+  const float t_2 = (1 - s) * std::sqrt(1 - t_1 * t_1) + s * t_2s;
+  const V3 nh = t_1 * t1 + t_2 * t2 +
+                std::sqrt(fmax_ref(0.f, 1.f - t_1 * t_1 - t_2 * t_2)) * vh;
+  return normalized(mk(ax * nh.x, ay * nh.y, fmax_ref(0.f, nh.z)));
+}
+/* EvalPdf<eval, pdf>: f (colored conductor Fresnel) and pdf */
+inline void ggx_eval_pdf(V3 lwi, V3 lwo, V3 color, V3 eta2, V3 etak2,
+                         float ax, float ay, V3* f, float* pdf) {
+  if (lwi.z <= 0 || lwo.z <= 0) {
+    if (f) *f = mk(0, 0, 0);
+    if (pdf) *pdf = 0.f;
+    return;
+  }
+  const float cos_i = lwi.z, cos_o = lwo.z;
+  const V3 lwh = normalized(lwi + lwo);
+  const float cos_d = dot(lwi, lwh);
+  const float phi_h = ggx_phi(lwh);
+  const float sin_phi_h = std::sin(phi_h), cos_phi_h = std::cos(phi_h);
+  const float cos_h = lwh.z;
+  const float sin_h = std::sqrt(fmax_ref(0.f, 1 - cos_h * cos_h));
+  const float D = ggx_d(sin_phi_h, cos_phi_h, sin_h, cos_h, ax, ay);
+  const float phi_i = ggx_phi(lwi), phi_o = ggx_phi(lwo);
+  const float sin_phi_i = std::sin(phi_i), cos_phi_i = std::cos(phi_i);
+  const float sin_phi_o = std::sin(phi_o), cos_phi_o = std::cos(phi_o);
+  const float tan_i = ggx_tan_theta(lwi), tan_o = ggx_tan_theta(lwo);
+  const float Go = ggx_g(cos_phi_o, sin_phi_o, ax, ay, tan_o);
+  if (f) {
+    const float Gi = ggx_g(cos_phi_i, sin_phi_i, ax, ay, tan_i);
+    const float G = Gi * Go;
+    const V3 F = color * conductor_fresnel(eta2, etak2, cos_d);
+    *f = F * D * G / std::fabs(4 * cos_i * cos_o);
+  }
+  if (pdf) *pdf = Go * D / (4 * lwo.z);
+}
+
+/* Metal::Shade (metal.cpp:42-66): an AggregateBSDF of albedo 1 holding one
+ * GGX reflection component of weight 1 with a ColoredConductorFresnel
+ * (aggregate_bsdf.cpp:43-131). */
+struct MetalB {
+  V3 ng, ns, color, eta2, etak2;
+  float ax, ay;
+  Frame sf;
+  Fringe fr;
+  MetalB(V3 ng_, V3 ns_, const Mat& m)
+      : ng(ng_), ns(ns_), color(m.base), ax(m.p[6]), ay(m.p[7]), sf(ns_),
+        fr(ng_, ns_, mk(1.f, 1.f, 1.f)) {
+    const V3 k = mk(m.p[0], m.p[1], m.p[2]);
+    const V3 eta = mk(m.p[3], m.p[4], m.p[5]);
+    eta2 = (eta / mk(1.f, 1.f, 1.f)) * (eta / mk(1.f, 1.f, 1.f));
+    etak2 = (k / mk(1.f, 1.f, 1.f)) * (k / mk(1.f, 1.f, 1.f));
+  }
+  Sample sample(V3 wo, V3 sam) const {
+    if (fr.causes(wo)) return fr.sample(wo, sam);
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (lwo.z <= 0.f) return invalid_sample();
+    /* GGXMicrofacetReflectionComponent::Sample (:137-154) */
+    if (lwo.z <= 0) return invalid_sample();
+    const V3 lwh = normalized(ggx_sample_wh(lwo, ax, ay, sam.y, sam.z));
+    if (lwh.z <= 0) return invalid_sample();
+    V3 lwi = normalized(2 * dot(lwo, lwh) * lwh - lwo);
+    if (lwi.z <= 0) return invalid_sample();
+    V3 f;
+    float pdf;
+    ggx_eval_pdf(lwi, lwo, color, eta2, etak2, ax, ay, &f, &pdf);
+    if (pdf == 0) return invalid_sample();
+    lwi = normalized(lwi);
+    pdf *= 1.f;
+    const V3 wi = sf.to_world(lwi);
+    const float factor = correct_shading_normal(ng, ns, wi);
+    return Sample{wi, f * factor, pdf, true, false};
+  }
+  V3 eval(V3 wi, V3 wo) const {
+    if (fr.causes(wo)) return fr.eval(wi, wo);
+    const V3 lwi = normalized(sf.to_local(wi));
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (lwi.z <= 0.f || lwo.z <= 0.f) return mk(0, 0, 0);
+    V3 f;
+    ggx_eval_pdf(lwi, lwo, color, eta2, etak2, ax, ay, &f, nullptr);
+    return mk(0, 0, 0) + f;
+  }
+  float pdf(V3 wi, V3 wo) const {
+    if (fr.causes(wo)) return fr.pdf(wi, wo);
+    const V3 lwi = normalized(sf.to_local(wi));
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (lwi.z <= 0.f || lwo.z <= 0.f) return 0.f;
+    float p;
+    ggx_eval_pdf(lwi, lwo, color, eta2, etak2, ax, ay, nullptr, &p);
+    float wsum = 0.f, acc = 0.f;
+    wsum += 1.f;
+    acc += 1.f * p;
+    return wsum > 0 ? acc / wsum : 0;
+  }
+};
+
+/* checkReflectionConstraint (bsdf/helper.h:26-31) */
+inline bool reflection_constraint(V3 wi, V3 wo) {
+  return std::fabs(wi.z * wo.z - wi.x * wo.x - wi.y * wo.y - 1.0f) < 1e-3f;
+}
+
+/* PlasticBsdf (plastic_bsdf.cpp:29-185): a delta coat reflection with
+ * probability Fi / (Fi + T (1 - Fi)), else the cosine-sampled substrate.
+ * No shading-normal correction; Eval does not reject wi below the
+ * surface. */
+struct PlasticB {
+  V3 ng, ns, albedo;
+  float ior, avg_t, dfres;
+  V3 scaled;
+  Frame sf;
+  Fringe fr;
+  PlasticB(V3 ng_, V3 ns_, const Mat& m)
+      : ng(ng_), ns(ns_), albedo(m.base), ior(m.p[0]), avg_t(m.plastic_avg_t),
+        dfres(m.plastic_diffuse_fresnel), sf(ns_), fr(ng_, ns_, m.base) {
+    const float sc = m.p[1] * m.p[2];
+    scaled = mk(sc, sc, sc);
+  }
+  V3 substrate(float Fi, float Fo, float eta) const {
+    return ((1.0f - Fi) * (1.0f - Fo) * eta * eta) *
+           (albedo / (mk(1.0f, 1.0f, 1.0f) - albedo * dfres));
+  }
+  V3 absorb(V3 lwi, V3 lwo) const {
+    const V3 e = scaled * (-1.0f / lwi.z - 1.0f / lwo.z);
+    return mk(std::exp(e.x), std::exp(e.y), std::exp(e.z));
+  }
+  Sample sample(V3 wo, V3 sam) const {
+    if (fr.causes(wo)) return fr.sample(wo, sam);
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (lwo.z <= 0.f) return invalid_sample();
+    const float eta = 1.f / ior;
+    const float Fi = dielectric_reflectance(eta, lwo.z);
+    const float substrate_weight = avg_t * (1.0f - Fi);
+    const float specular_weight = Fi;
+    const float sp = specular_weight / (specular_weight + substrate_weight);
+    V3 lwi, f;
+    float pdf;
+    bool delta;
+    if (sam.x < sp) {
+      lwi = mk(-lwo.x, -lwo.y, lwo.z);
+      pdf = sp;
+      const float v = Fi / sp;
+      f = mk(v, v, v);
+      delta = true;
+    } else {
+      lwi = cosine_hemisphere(sam.y, sam.z, &pdf);
+      const float Fo = dielectric_reflectance(eta, lwi.z);
+      f = substrate(Fi, Fo, eta);
+      if (maxc(scaled) > 0.0f) f = f * absorb(lwi, lwo);
+      pdf *= (1.0f - sp);
+      f = f / (1.0f - sp);
+      delta = false;
+    }
+    const V3 wi = sf.to_world(lwi);
+    return Sample{normalized(wi), f, pdf, true, delta};
+  }
+  V3 eval(V3 wi, V3 wo) const {
+    if (fr.causes(wo)) return fr.eval(wi, wo);
+    const V3 lwi = normalized(sf.to_local(wi));
+    const V3 lwo = normalized(sf.to_local(wo));
+    const float eta = 1.0f / ior;
+    const float Fi = dielectric_reflectance(eta, lwo.z);
+    const float Fo = dielectric_reflectance(eta, lwi.z);
+    if (reflection_constraint(lwo, lwi)) return mk(Fi, Fi, Fi);
+    V3 brdf = ((1.0f - Fi) * (1.0f - Fo) * eta * eta * lwi.z * (1.f / kPi)) *
+              (albedo / (mk(1.0f, 1.0f, 1.0f) - albedo * dfres));
+    if (maxc(scaled) > 0.0f) brdf = brdf * absorb(lwi, lwo);
+    return brdf;
+  }
+  float pdf(V3 wi, V3 wo) const {
+    if (fr.causes(wo)) return fr.pdf(wi, wo);
+    const V3 lwi = normalized(sf.to_local(wi));
+    const V3 lwo = normalized(sf.to_local(wo));
+    if (lwi.z <= 0.0f || lwo.z <= 0.0f) return 0.0f;
+    const float Fi = dielectric_reflectance(1.0f / ior, lwo.z);
+    const float substrate_weight = avg_t * (1.0f - Fi);
+    const float specular_weight = Fi;
+    const float sp = specular_weight / (specular_weight + substrate_weight);
+    if (reflection_constraint(lwo, lwi)) return sp;
+    return lwi.z * kInvPi * (1.0f - sp);
+  }
+};
+
 struct Bsdf {
   int type;
   Lambert lam;
   Disney dis;
-  Bsdf(const Mat& m, V3 ng, V3 ns)
-      : type(m.type), lam(ng, ns, m.base), dis(m, ns) {}
+  V3 ng, ns;
+  const Mat& m;
+  Bsdf(const Mat& m_, V3 ng_, V3 ns_)
+      : type(m_.type), lam(ng_, ns_, m_.base), dis(m_, ns_), ng(ng_), ns(ns_),
+        m(m_) {}
   Sample sample(V3 wo, V3 s) const {
-    return type == ORC_MAT_DIFFUSE ? lam.sample(wo, s) : dis.sample(wo, s);
+    switch (type) {
+      case ORC_MAT_DIFFUSE: return lam.sample(wo, s);
+      case ORC_MAT_DISNEY: return dis.sample(wo, s);
+      case ORC_MAT_MIRROR: return MirrorB(ng, ns, m.base).sample(wo);
+      case ORC_MAT_GLASS: return GlassB(ng, ns, m).sample(wo, s);
+      case ORC_MAT_METAL: return MetalB(ng, ns, m).sample(wo, s);
+      case ORC_MAT_PLASTIC: return PlasticB(ng, ns, m).sample(wo, s);
+      default: /* NullBsdf (null.cpp:31-52): straight through */
+        return Sample{-wo, mk(1.f, 1.f, 1.f), 1.f, true, true};
+    }
   }
   V3 eval(V3 wi, V3 wo) const {
-    return type == ORC_MAT_DIFFUSE ? lam.eval(wi, wo) : dis.eval(wi, wo);
+    switch (type) {
+      case ORC_MAT_DIFFUSE: return lam.eval(wi, wo);
+      case ORC_MAT_DISNEY: return dis.eval(wi, wo);
+      case ORC_MAT_METAL: return MetalB(ng, ns, m).eval(wi, wo);
+      case ORC_MAT_PLASTIC: return PlasticB(ng, ns, m).eval(wi, wo);
+      default: return mk(0, 0, 0);
+    }
   }
   float pdf(V3 wi, V3 wo) const {
-    return type == ORC_MAT_DIFFUSE ? lam.pdf(wi, wo) : dis.pdf(wi, wo);
+    switch (type) {
+      case ORC_MAT_DIFFUSE: return lam.pdf(wi, wo);
+      case ORC_MAT_DISNEY: return dis.pdf(wi, wo);
+      case ORC_MAT_METAL: return MetalB(ng, ns, m).pdf(wi, wo);
+      case ORC_MAT_PLASTIC: return PlasticB(ng, ns, m).pdf(wi, wo);
+      default: return 0.f;
+    }
   }
 };
 
@@ -1290,6 +1702,7 @@ V3 mis_bsdf(const Scene& s, const HitInfo& h, const Bsdf& f, Rng& rng) {
     const V3 le = dot(lh.ng, lh.wr) > 0 ? A.rad : mk(0, 0, 0);
     if (is_black(le)) return mk(0, 0, 0);
     const V3 fv = le * bs.f * std::fabs(dot(h.ns, r.d));
+    if (bs.delta) return fv / bs.pdf;
     const float lp = area_pdf(A, r.o, lh.pos, lh.ng);
     return fv / bs.pdf * power_heuristic(bs.pdf, lp);
   }
@@ -1298,9 +1711,13 @@ V3 mis_bsdf(const Scene& s, const HitInfo& h, const Bsdf& f, Rng& rng) {
   V3 rad = L.scaler * L.rgb;
   if (is_black(rad)) return mk(0, 0, 0);
   V3 fv = rad * bs.f * std::fabs(dot(h.ns, r.d));
-  float lp = env_pdf(L, r.d);
   V3 out = mk(0, 0, 0);
-  out = out + fv / bs.pdf * power_heuristic(bs.pdf, lp);
+  if (bs.delta) {
+    out = out + fv / bs.pdf;
+  } else {
+    float lp = env_pdf(L, r.d);
+    out = out + fv / bs.pdf * power_heuristic(bs.pdf, lp);
+  }
   return out;
 }
 
@@ -1474,7 +1891,7 @@ void orc_bsdf(const float* material, const float* ng, const float* ns,
     out[0] = s.f.x; out[1] = s.f.y; out[2] = s.f.z;
     out[3] = s.pdf;
     out[4] = s.dir.x; out[5] = s.dir.y; out[6] = s.dir.z;
-    out[7] = s.valid ? 1.f : 0.f;
+    out[7] = (s.valid ? 1.f : 0.f) + (s.valid && s.delta ? 2.f : 0.f);
   }
 }
 

@@ -47,10 +47,27 @@ enum {
   ORC_TRI_NG_REVERSED = 2, /* Cube's tuple-order normal (cube.cpp:96-108) */
   ORC_TRI_HAS_NORMALS = 4  /* MeshGeo interpolated normals (mesh.cpp:183-204) */
 };
-enum { ORC_MAT_DIFFUSE = 0, ORC_MAT_DISNEY = 1 };
+/* Material records ([16] floats: type, base colour, ten parameters, two
+ * reserved).  Mirror: base = kr.  Glass: base = color_reflection, p0..2 =
+ * color_refraction (before its square root), p3 = ior.  Metal: base =
+ * color, p0..2 = k, p3..5 = eta, p6/p7 = u/v roughness.  Plastic: base =
+ * albedo, p0 = ior, p1 = thickness, p2 = sigma_a.  Null: nothing. */
+enum {
+  ORC_MAT_DIFFUSE = 0,
+  ORC_MAT_DISNEY = 1,
+  ORC_MAT_MIRROR = 2,
+  ORC_MAT_GLASS = 3,
+  ORC_MAT_METAL = 4,
+  ORC_MAT_PLASTIC = 5,
+  ORC_MAT_NULL = 6
+};
 enum { ORC_LIGHT_DIRECTIONAL = 0, ORC_LIGHT_ENV = 1, ORC_LIGHT_AREA = 2 };
 enum { ORC_GEOM_QUAD = 0, ORC_GEOM_CUBE = 1, ORC_GEOM_MESH = 2 };
 enum { ORC_TEST_MT = 0, ORC_TEST_WATERTIGHT = 1 };
+
+/* Fresnel::computeDiffuseFresnel(ior, n) (bsdf/helper.h:58-73): the
+ * hemispherical integral PlasticBsdf divides the albedo by. */
+float orc_diffuse_fresnel(float ior, int n);
 
 /* PLOCAggregate::Build restated (ploc_aggregate.cpp:252-327).  Writes
  * 2n-1 nodes: bounds [6] (lo, hi), count_first [2] (primitive_count,

@@ -58,6 +58,14 @@ REF_TUS = [
     "ajisai/core/renderer/pt.cpp",
     "ajisai/core/material/disney.cpp",
     "ajisai/core/material/diffuse.cpp",
+    "ajisai/core/material/mirror.cpp",
+    "ajisai/core/material/glass.cpp",
+    "ajisai/core/material/metal.cpp",
+    "ajisai/core/material/plastic.cpp",
+    "ajisai/core/material/null.cpp",
+    "ajisai/core/material/fresnel.cpp",
+    "ajisai/core/bsdf/microfacet_reflection_component.cpp",
+    "ajisai/core/bsdf/plastic_bsdf.cpp",
     "ajisai/core/bsdf/aggregate_bsdf.cpp",
     "ajisai/core/bsdf/bsdf.cpp",
     "ajisai/core/bsdf/diffuse_component.cpp",
@@ -98,8 +106,10 @@ def build_ref(force: bool = False) -> Path | None:
     objdir.mkdir(exist_ok=True)
     # Release flags as the reference builds by default (exec.py:8: CMake
     # Release = -O3 -DNDEBUG); baseline x86-64 has no FMA to contract into.
+    # glass.cpp names std::optional without including <optional> (its own
+    # build gets it through another header): force-include it.
     flags = ["-O3", "-DNDEBUG", "-std=c++20", "-fPIC", "-ffp-contract=off", "-pthread",
-             "-w", "-DAJISAI_BUILD_STATIC",
+             "-w", "-DAJISAI_BUILD_STATIC", "-include", "optional",
              "-I", str(shim), "-I", str(REFERENCE_ROOT)]
     procs, objs = [], []
     for s in srcs:

@@ -211,7 +211,17 @@ Rc<Texture2D> constant3(const float* v) {
 }
 
 Rc<Material> make_material(const float* m) {
-  if ((int)m[0] == 0) return CreateDiffuse(constant3(m + 1));
+  switch ((int)m[0]) {
+    case 0: return CreateDiffuse(constant3(m + 1));
+    case 2: return CreateMirror(constant3(m + 1));
+    case 3: return CreateGlass(constant3(m + 1), constant3(m + 4), constant(m[7]));
+    case 4:
+      return CreateMetal(constant3(m + 1), constant3(m + 4), constant3(m + 7),
+                         m[10], m[11]);
+    case 5: return CreatePlastic(constant3(m + 1), m[4], m[5], m[6]);
+    case 6: return CreateNull();
+    default: break;
+  }
   return CreateDisney(constant3(m + 1), constant(m[4]), constant(m[5]),
                       constant(m[6]), constant(m[7]), constant(m[8]),
                       constant(m[9]), constant(m[10]), constant(m[11]),
@@ -453,7 +463,7 @@ void ref_scene_trace(void* h, const float* rays, int64_t n, int any_hit,
 }
 
 /* One BSDF query through Material::Shade + BSDF::*All.  op 0: eval and
- * pdf; op 1: sample.  out[8]: f rgb, pdf, wi xyz, valid. */
+ * pdf; op 1: sample.  out[8]: f rgb, pdf, wi xyz, valid (1) + delta (2). */
 void ref_bsdf(const float* mat, const float* ng, const float* ns,
               const float* wo, const float* wi, const float* sam, int op,
               float* out) {
@@ -487,7 +497,7 @@ void ref_bsdf(const float* mat, const float* ng, const float* ns,
     out[7] = (r.f.IsBlack() && r.pdf == 0.f && r.dir.max() <= 0.f &&
               r.dir.min() >= 0.f)
                  ? 0.f
-                 : 1.f;
+                 : (r.is_delta ? 3.f : 1.f);
   }
 }
 

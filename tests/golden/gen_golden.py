@@ -12,6 +12,7 @@ functions, and stores what the reference computes:
   ploc_*.npz     PLOCAggregate's tree (nodes_, primitive_indices_)
   trace_*.npz    Scene::Intersect / Occlude hits of seeded ray sets
   bsdf.npz       Material::Shade + BSDF::SampleAll/EvalAll/PdfAll values
+  bsdf_more.npz  the same for mirror, glass, metal, plastic and null
   render_*.npz   per-sample radiance of PathTracing::TraceMIS driven by the
                  counter sampler, and the merged film
   camera.npz     ThinLensCamera::GenerateRay rays
@@ -156,6 +157,61 @@ def gen_bsdf():
          op=np.array(ops, np.int32), out=np.stack(outs))
 
 
+def material_queries(rng, n):
+    """Seeded queries over mirror, glass, metal, plastic and null materials:
+    (material, ng, ns, wo, wi, sam) tuples.  Every plastic has ior 1.5: the
+    reference fixes its diffuse-Fresnel term once per process, from the
+    first plastic it shades."""
+    def unit(v):
+        return v / np.linalg.norm(v)
+
+    kinds = ("mirror", "glass", "metal", "plastic", "null")
+    out = []
+    for i in range(n):
+        kind = kinds[i % len(kinds)]
+        if kind == "mirror":
+            m = S.Mirror(rng.uniform(0, 1, 3)).pack()
+        elif kind == "glass":
+            m = S.Glass(float(rng.uniform(1.1, 2.5)), rng.uniform(0, 1, 3),
+                        rng.uniform(0, 1, 3)).pack()
+        elif kind == "metal":
+            m = S.Metal(rng.uniform(0, 1, 3), rng.uniform(0, 5, 3),
+                        rng.uniform(0.1, 3, 3), float(rng.uniform(0.05, 1)),
+                        float(rng.uniform(0.05, 1))).pack()
+        elif kind == "plastic":
+            m = S.Plastic(rng.uniform(0, 1, 3), 1.5, float(rng.uniform(0, 2)),
+                          float(rng.uniform(0, 1)) if i % 2 else 0.0).pack()
+        else:
+            m = S.Null().pack()
+        ng = unit(rng.normal(size=3)).astype(np.float32)
+        ns = unit(ng + 0.35 * rng.normal(size=3)).astype(np.float32)
+        if i % 7 == 0:
+            ns = (ns * 1.07).astype(np.float32)   # unnormalised (MeshGeo)
+        wo = unit(rng.normal(size=3)).astype(np.float32)
+        if i % 4:
+            wo = (np.sign(wo @ ng) * wo).astype(np.float32)
+        wi = unit(rng.normal(size=3)).astype(np.float32)
+        if i % 9 == 0:   # exactly the mirror direction about ns
+            nn = unit(ns.astype(np.float64))
+            wi = (2 * (wo @ nn) * nn - wo).astype(np.float32)
+        sam = rng.uniform(0, 1, 3).astype(np.float32)
+        out.append((m, ng, ns, wo, wi, sam))
+    return out
+
+
+def gen_bsdf_more():
+    rng = np.random.default_rng(17)
+    mats, ngs, nss, wos, wis, sams, ops, outs = [], [], [], [], [], [], [], []
+    for m, ng, ns, wo, wi, sam in material_queries(rng, 2000):
+        for op in (0, 1):
+            mats.append(m); ngs.append(ng); nss.append(ns); wos.append(wo)
+            wis.append(wi); sams.append(sam); ops.append(op)
+            outs.append(O.ref_bsdf(m, ng, ns, wo, wi, sam, op))
+    save("bsdf_more.npz", material=np.stack(mats), ng=np.stack(ngs), ns=np.stack(nss),
+         wo=np.stack(wos), wi=np.stack(wis), sam=np.stack(sams),
+         op=np.array(ops, np.int32), out=np.stack(outs))
+
+
 def gen_render():
     cases = [
         ("render_cornell.npz", S.cornell_box(32, 32),
@@ -168,6 +224,11 @@ def gen_render():
         ("render_area.npz", S.cornell_area(24, 24),
          dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=1)),
         ("render_area_nomis.npz", S.cornell_area(16, 16),
+         dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=0)),
+        # plastic, mirror, metal, glass and a null-material emitter
+        ("render_materials.npz", S.material_box(24, 24),
+         dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=1)),
+        ("render_materials_nomis.npz", S.material_box(16, 16),
          dict(spp=4, min_bounces=3, max_bounces=8, cont_prob=0.9, use_mis=0)),
     ]
     for name, sc, params in cases:
@@ -209,5 +270,6 @@ if __name__ == "__main__":
     gen_ploc()
     gen_trace()
     gen_bsdf()
+    gen_bsdf_more()
     gen_render()
     gen_camera()

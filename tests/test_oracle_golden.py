@@ -74,8 +74,11 @@ def test_brute_force_agrees_where_reference_tree_is_complete(golden):
     assert np.all(~kept[p[differ & (p >= 0)]])
 
 
-def test_bsdf_matches_reference(golden):
-    g = golden("bsdf.npz")
+@pytest.mark.parametrize("case", ["bsdf.npz", "bsdf_more.npz"])
+def test_bsdf_matches_reference(golden, case):
+    """Lambertian and Disney (bsdf.npz); mirror, glass, metal, plastic and
+    null (bsdf_more.npz; the sample's flag is valid + 2 * delta)."""
+    g = golden(case)
     n = g["op"].shape[0]
     out = np.stack([O.bsdf(g["material"][i], g["ng"][i], g["ns"][i], g["wo"][i],
                            g["wi"][i], g["sam"][i], g["op"][i]) for i in range(n)])
@@ -97,7 +100,8 @@ def same_bits_or_nan(a, b):
 
 @pytest.mark.parametrize("case", ["render_cornell.npz", "render_ico.npz",
                                   "render_cornell_nomis.npz", "render_area.npz",
-                                  "render_area_nomis.npz"])
+                                  "render_area_nomis.npz", "render_materials.npz",
+                                  "render_materials_nomis.npz"])
 def test_render_matches_reference_per_sample(golden, case):
     from ajisai_render_gb300.scenes import FlatScene
     g = golden(case)
