@@ -5,6 +5,8 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -74,6 +76,63 @@ struct StreamJoin {
   }
 };
 
+// Fresnel::computeDiffuseFresnel(ior, 1000000) (bsdf/helper.h:36-73), the
+// term PlasticBsdf divides its albedo by; a million steps, so cached per
+// ior.  (The reference computes it once per process, for the first
+// PlasticBsdf it constructs; here each material uses its own ior.)
+float host_dielectric_reflectance(float eta, float cos_i) {
+  if (cos_i < 0.0f) {
+    eta = 1.0f / eta;
+    cos_i = -cos_i;
+  }
+  const float sin_t2 = eta * eta * (1.0f - cos_i * cos_i);
+  if (sin_t2 > 1.0f) return 1.0f;
+  const float cos_t = std::sqrt(ref_max(1.0f - sin_t2, 0.0f));
+  const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+  const float rp = (eta * cos_t - cos_i) / (eta * cos_t + cos_i);
+  return (rs * rs + rp * rp) * 0.5f;
+}
+float diffuse_fresnel(float ior) {
+  static std::mutex mu;
+  static std::map<uint32_t, float> cache;
+  uint32_t key;
+  std::memcpy(&key, &ior, 4);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  const int n = 1000000;
+  double acc = 0.0;
+  float fb = host_dielectric_reflectance(ior, 0.0f);
+  for (int i = 1; i <= n; ++i) {
+    const float cos2 = float(i) / n;
+    const float fa =
+        host_dielectric_reflectance(ior, std::min(std::sqrt(cos2), 1.0f));
+    acc += double(fa + fb) * (0.5 / n);
+    fb = fa;
+  }
+  const float v = float(acc);
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = v;
+  return v;
+}
+
+// The device record of a material: the ABI record with the type as a float
+// and, for plastic, the constructor's terms (plastic_bsdf.cpp:32-45) in the
+// two reserved floats.
+void material_record(const ajg_material& in, float r[16]) {
+  std::memcpy(r, &in, sizeof(ajg_material));
+  r[0] = (float)in.type;
+  r[14] = r[15] = 0.f;
+  if (in.type == AJG_MAT_PLASTIC) {
+    const float ior = in.params[0], sc = in.params[1] * in.params[2];
+    const float avg = (sc + sc + sc) / 3.f;
+    r[14] = std::exp(-2.0f * avg);
+    r[15] = diffuse_fresnel(ior);
+  }
+}
+
 float host_lum(const float* rgb) {  // spectrum.h:80-82 in double
   return (float)(0.2126 * (double)rgb[0] + 0.7152 * (double)rgb[1] +
                  0.0722 * (double)rgb[2]);
@@ -120,7 +179,7 @@ __global__ void k_bsdf_query(const ajg_material* __restrict__ mats,
       o[6] = s.dir.z;
       const bool invalid = black3(s.f) && s.pdf == 0.f && maxc3(s.dir) <= 0.f &&
                            ref_min(ref_min(s.dir.x, s.dir.y), s.dir.z) >= 0.f;
-      o[7] = invalid ? 0.f : 1.f;
+      o[7] = invalid ? 0.f : (s.delta ? 3.f : 1.f);  // valid + 2 * delta
     }
   }
 }
@@ -418,7 +477,7 @@ int ajg_scene_create_flat_ex(ajg_ctx* ctx, const float* tris,
       return fail(ctx, AJG_ERR_INVALID, "unknown triangle flag");
   }
   for (uint32_t m = 0; m < num_materials; ++m)
-    if (materials[m].type > AJG_MAT_DISNEY)
+    if (materials[m].type > AJG_MAT_NULL)
       return fail(ctx, AJG_ERR_UNSUPPORTED, "unknown material type");
   for (uint32_t l = 0; l < num_lights; ++l)
     if (lights[l].type > AJG_LIGHT_ENV)
@@ -460,11 +519,11 @@ int ajg_scene_create_flat_ex(ajg_ctx* ctx, const float* tris,
   }
   s->host_materials.resize(16 * (size_t)num_materials);
   std::vector<float4> lum(num_materials);
+  uint32_t mat_mask = 0;
   for (uint32_t m = 0; m < num_materials; ++m) {
-    float* r = &s->host_materials[16 * m];
-    std::memcpy(r, &materials[m], sizeof(ajg_material));
-    r[0] = (float)materials[m].type;
+    material_record(materials[m], &s->host_materials[16 * m]);
     lum[m] = make_float4(host_lum(materials[m].base_color), 0, 0, 0);
+    mat_mask |= 1u << materials[m].type;
   }
   auto keep = [&](size_t bytes) -> void* {
     void* p = nullptr;
@@ -504,6 +563,7 @@ int ajg_scene_create_flat_ex(ajg_ctx* ctx, const float* tris,
   s->d.lights = d_light;
   s->d.mat_lum = d_lum;
   s->d.num_materials = num_materials;
+  s->d.mat_mask = mat_mask;
   s->d.num_lights = nl_all;
   s->d.env = env;
   int rc = build_scene(ctx, s, tris, corner_normals, tri_material, tri_flags,
@@ -745,7 +805,17 @@ int ajg_bsdf_query(ajg_ctx* ctx, const ajg_material* materials,
   CK(dv.alloc(15 * n, st), "bsdf_query");
   CK(dout.alloc(8 * n, st), "bsdf_query");
   CK(dop.alloc(n, st), "bsdf_query");
-  cudaMemcpyAsync(dm.p, materials, n * sizeof(ajg_material), cudaMemcpyHostToDevice, st);
+  // the device records: plastic's precomputed terms in the reserved floats
+  std::vector<ajg_material> recs(materials, materials + n);
+  for (uint64_t i = 0; i < n; ++i) {
+    if (recs[i].type > AJG_MAT_NULL)
+      return fail(ctx, AJG_ERR_UNSUPPORTED, "unknown material type");
+    float r[16];
+    material_record(recs[i], r);
+    recs[i].pad[0] = r[14];
+    recs[i].pad[1] = r[15];
+  }
+  cudaMemcpyAsync(dm.p, recs.data(), n * sizeof(ajg_material), cudaMemcpyHostToDevice, st);
   const float* srcs[5] = {ng, ns, wo, wi, sam};
   for (int k = 0; k < 5; ++k)
     cudaMemcpyAsync(dv.p + 3 * n * k, srcs[k], 3 * n * sizeof(float),

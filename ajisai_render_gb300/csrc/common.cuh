@@ -38,6 +38,9 @@ __host__ __device__ __forceinline__ F3 operator*(F3 a, float s) {
 __host__ __device__ __forceinline__ F3 operator*(float s, F3 a) {
   return mk3(a.x * s, a.y * s, a.z * s);
 }
+__host__ __device__ __forceinline__ F3 operator/(F3 a, F3 b) {
+  return mk3(a.x / b.x, a.y / b.y, a.z / b.z);
+}
 __host__ __device__ __forceinline__ F3 operator/(F3 a, float s) {
   return mk3(a.x / s, a.y / s, a.z / s);
 }

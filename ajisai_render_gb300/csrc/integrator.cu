@@ -211,9 +211,10 @@ __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
   flush_counters(ctr, nr, nn, nt);
 }
 
-// Files every queue slot under its hit's material type (or as a miss), so
-// that shading runs in material-specialised kernels; warps stay converged,
-// so each list append is one atomic per warp.
+// Files every queue slot under its hit's shading class (a miss, Lambertian,
+// Disney, or one of the other material types), so that shading runs in
+// class-specialised kernels; warps stay converged, so each list append is
+// one atomic per warp.
 template <bool MJ>
 __global__ void k_classify(DeviceScene s, MJTables t,
                            const float4* __restrict__ ro,
@@ -242,11 +243,12 @@ __global__ void k_classify(DeviceScene s, MJTables t,
         }
         const uint32_t mat =
             __float_as_uint(__ldg(&shade[prim].w)) & 0xffffffu;
-        cls = 1 + ((int)__ldg(materials + 16 * mat) == AJG_MAT_DISNEY);
+        const int type = (int)__ldg(materials + 16 * mat);
+        cls = type == AJG_MAT_DIFFUSE ? 1 : (type == AJG_MAT_DISNEY ? 2 : 3);
       }
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < 4; ++c) {
       const uint32_t j = warp_append(&list_counts[c], cls == c);
       if (cls == c) lists[(uint64_t)c * list_cap + j] = k;
     }
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(kShadeThreads)
     k_bsdf_emit(WaveArgs a, MJTables t, WaveBufs w, uint32_t NT, uint32_t cap,
                 uint32_t n_max, const float* __restrict__ t_hit,
                 const int32_t* __restrict__ prim_hit) {
-  const uint32_t n = min(w.counts[8], n_max);
+  const uint32_t n = min(w.counts[9], n_max);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += gridDim.x * blockDim.x) {
     const uint32_t i = cap - 1 - k;
@@ -324,7 +326,8 @@ __global__ void __launch_bounds__(kShadeThreads)
     const JobParams& J = Src<MJ>::job(a, t, jid);
     const DeviceScene& s = Src<MJ>::scene(a, t, jid);
     const F3 o = xyz(o4), d = xyz(d4);
-    const float pdf = o4.w;
+    const bool delta = signbit(o4.w);  // see k_shade
+    const float pdf = fabsf(o4.w);
     const float4 fs = w.term_f[slot];
     const F3 bf = xyz(fs);
     const float cosv = fs.w;
@@ -335,8 +338,12 @@ __global__ void __launch_bounds__(kShadeThreads)
       const F3 rad = mk3(J.env_rgb.x, J.env_rgb.y, J.env_rgb.z);
       if (s.env >= 0 && !black3(rad)) {
         const F3 fv = rad * bf * cosv;
-        const float lp = env_pdf(J.env_mass != 0, d);
-        fo = mk3(0, 0, 0) + fv / pdf * power_heuristic(pdf, lp);
+        if (delta) {
+          fo = mk3(0, 0, 0) + fv / pdf;
+        } else {
+          const float lp = env_pdf(J.env_mass != 0, d);
+          fo = mk3(0, 0, 0) + fv / pdf * power_heuristic(pdf, lp);
+        }
         vis = true;
       }
     } else {
@@ -349,8 +356,12 @@ __global__ void __launch_bounds__(kShadeThreads)
             dot3(ng, -d) > 0 ? mk3(L[1], L[2], L[3]) : mk3(0.f, 0.f, 0.f);
         if (!black3(le)) {
           const F3 fv = le * bf * cosv;
-          const float lp = area_pdf(L[9], o, pos, ng);
-          fo = fv / pdf * power_heuristic(pdf, lp);
+          if (delta) {
+            fo = fv / pdf;
+          } else {
+            const float lp = area_pdf(L[9], o, pos, ng);
+            fo = fv / pdf * power_heuristic(pdf, lp);
+          }
           vis = true;
         }
       }
@@ -385,7 +396,7 @@ __device__ __forceinline__ void emit_closest(const WaveBufs& w, F3 o, F3 d,
                                              float pdf, uint32_t slot,
                                              uint32_t sid, bool pred,
                                              uint32_t cap, uint32_t* err) {
-  const uint32_t k = warp_append(&w.counts[8], pred);
+  const uint32_t k = warp_append(&w.counts[9], pred);
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -613,7 +624,7 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
               make_ray(eps_offset(hi, bs.dir), bs.dir, so, sd);
               fo = bs.f;
               cosv = fabsf(dot3(hi.ns, sd));
-              w_o = bs.pdf;
+              w_o = bs.delta ? -bs.pdf : bs.pdf;  // a delta sample: negated
               closest = true;
             } else if (s.env >= 0) {
               bs.dir = normalize3(bs.dir);
@@ -621,8 +632,14 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
               const F3 rad = mk3(J.env_rgb.x, J.env_rgb.y, J.env_rgb.z);
               if (!black3(rad)) {
                 const F3 fv = rad * bs.f * fabsf(dot3(hi.ns, sd));
-                const float lp = env_pdf(J.env_mass != 0, sd);
-                fo = mk3(0, 0, 0) + fv / bs.pdf * power_heuristic(bs.pdf, lp);
+                // a delta sample is not weighted (helper.h:236-241)
+                if (bs.delta) {
+                  fo = mk3(0, 0, 0) + fv / bs.pdf;
+                } else {
+                  const float lp = env_pdf(J.env_mass != 0, sd);
+                  fo = mk3(0, 0, 0) +
+                       fv / bs.pdf * power_heuristic(bs.pdf, lp);
+                }
                 emit = true;
               }
             }
@@ -888,7 +905,7 @@ uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   add(slots);                  // term_vis
   add(slots * 16); add(slots * 16);  // shadow queue
   if (mj) add(slots * 2);      // sq_scene
-  add(P * 4 * 3);              // material lists
+  add(P * 4 * 4);              // shading-class lists
   add(64);                     // counts
   return b;
 }
@@ -915,7 +932,7 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj) {
   w.sq_o = carve<float4>(cur, P * nt);
   w.sq_d = carve<float4>(cur, P * nt);
   if (mj) w.sq_scene = carve<uint16_t>(cur, P * nt);
-  w.lists = carve<uint32_t>(cur, P * 3);
+  w.lists = carve<uint32_t>(cur, P * 4);
   w.counts = carve<uint32_t>(cur, 16);
   return w;
 }
@@ -1018,7 +1035,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       const int g = resident_grid((const void*)k_extend<TT, false, WW>,
                                   kTraceThreads);
       k_extend<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits,
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], w.hits,
           &ctx->d_counters[0], ctx->d_error);
     });
   };
@@ -1028,7 +1045,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       const int g = resident_grid((const void*)k_bsdf_trace<TT, false, WW>,
                                   kTraceThreads);
       k_bsdf_trace<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.sq_o, w.sq_d, nullptr, &w.counts[8], &w.counts[9],
+          s, t, w.sq_o, w.sq_d, nullptr, &w.counts[9], &w.counts[10],
           shadow_cap, (uint32_t)P, reinterpret_cast<float*>(w.lists),
           reinterpret_cast<int32_t*>(w.lists + P), &ctx->d_counters[0],
           ctx->d_error);
@@ -1060,7 +1077,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       for (int b = 0; b < a.j.max_b; ++b) {
         // next queue, shadow queue, fetch counters and material lists
         cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
-        cudaMemsetAsync(&w.counts[2], 0, 8 * sizeof(uint32_t), st);
+        cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
         {
           KernelTimer tm(ctx, st, kc);
           extend(q);
@@ -1086,6 +1103,12 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
           KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DISNEY, false><<<gs, kShadeThreads, 0, st>>>(
               a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)nt,
+              shadow_cap, ctx->d_error);
+        }
+        if (s.mat_mask >> AJG_MAT_MIRROR) {
+          KernelTimer tm(ctx, st, ks);
+          k_shade<kMatOther, false><<<gs, kShadeThreads, 0, st>>>(
+              a, t, w, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
         if (a.j.use_mis) {
@@ -1151,13 +1174,13 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
   int q = 0;
   for (int b = 0; b < bounces; ++b) {
     cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
-    cudaMemsetAsync(&w.counts[2], 0, 8 * sizeof(uint32_t), st);
+    cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
     dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
       const int g =
           resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
       k_extend<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[7], w.hits, ctr,
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], w.hits, ctr,
           err);
     });
     k_classify<true><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q], w.hits,
@@ -1169,6 +1192,9 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
         err);
     k_shade<AJG_MAT_DISNEY, true><<<gs, kShadeThreads, 0, st>>>(
         a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
+        shadow_cap, err);
+    k_shade<kMatOther, true><<<gs, kShadeThreads, 0, st>>>(
+        a, t, w, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)NT,
         shadow_cap, err);
     dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
@@ -1184,7 +1210,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
         const int g = resident_grid((const void*)k_bsdf_trace<TT, true, WW>,
                                     kTraceThreads);
         k_bsdf_trace<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-            s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[8], &w.counts[9],
+            s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[9], &w.counts[10],
             shadow_cap, (uint32_t)P, reinterpret_cast<float*>(w.lists),
             reinterpret_cast<int32_t*>(w.lists + P), ctr, err);
       });

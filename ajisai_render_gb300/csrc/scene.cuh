@@ -48,7 +48,7 @@ struct DeviceScene {
   const int32_t* tri_emit = nullptr;
   const float* emit_pts = nullptr;  // [k][3]
   uint32_t num_area = 0;
-  uint32_t pad_ = 0;
+  uint32_t mat_mask = 0;  // bit t: a material of type t is present
 };
 
 // Light record types ([12] floats, type in [0]): the two of the ABI, and the
@@ -125,10 +125,11 @@ struct WaveBufs {
   float4* sq_o;  // shadow queue: o.xyz, t_max
   float4* sq_d;  // d.xyz, slot bits
   uint16_t* sq_scene;  // multi-job waves: scene index per shadow ray
-  uint32_t* lists;   // [3][P]: queue slots of misses, Lambertian and
-                     // Disney hits
+  uint32_t* lists;   // [4][P]: queue slots of misses, Lambertian, Disney
+                     // and other hits
   uint32_t* counts;  // [0],[1] path queues, [2] shadow queue, [3] shadow
-                     // fetch, [4..6] lists, [7] extend fetch
+                     // fetch, [4..7] lists, [8] extend fetch, [9] closest
+                     // MIS BSDF queue, [10] its fetch
 };
 
 // Tables of a multi-job wave in device memory.
@@ -275,7 +276,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                      TraceCounters* ctr, uint32_t* err, cudaStream_t st);
 // Kernels of a multi-job wave launched per wave (for launch counts).
 inline int mj_wave_kernels(int bounces, bool emit) {
-  return 2 + (emit ? 9 : 7) * bounces;
+  return 2 + (emit ? 10 : 8) * bounces;
 }
 // Looks up the persistent grids of the multi-job kernels (call before a
 // stream capture).

@@ -99,12 +99,14 @@ __device__ __forceinline__ float correct_shading_normal(F3 ng, F3 ns, F3 wi) {
 struct BsdfSample {
   F3 dir, f;
   float pdf;
+  bool delta = false;  // BSDFSampleResult::is_delta
 };
 __device__ __forceinline__ BsdfSample invalid_sample() {
   BsdfSample s;
   s.dir = mk3(0, 0, 0);
   s.f = mk3(0, 0, 0);
   s.pdf = 0.f;
+  s.delta = false;
   return s;
 }
 
@@ -613,6 +615,411 @@ static __device__ __noinline__ float lambert_pdf(F3 ng, F3 ns, F3 alb, F3 wi, F3
   return Lambert(ng, ns, alb).pdf(wi, wo);
 }
 
+// ------------------------------------- mirror, glass, metal, plastic, null --
+// Material records ([16] floats after the type): base colour in [1..3], the
+// type's parameters in [4..13] (glass: refraction colour, ior; metal: k,
+// eta, u/v roughness; plastic: ior, thickness, sigma_a), and for plastic
+// the constructor's terms the host computes once (plastic_bsdf.cpp:32-45):
+// [14] the average transmittance exp(-2 thickness sigma_a), [15] the
+// diffuse Fresnel integral.
+constexpr int kMatOther = 7;  // shading class of the types >= AJG_MAT_MIRROR
+
+// Fresnel::dielectricReflectance (bsdf/helper.h:35-56)
+__device__ __forceinline__ float dielectric_reflectance(float eta,
+                                                        float cos_i) {
+  if (cos_i < 0.0f) {
+    eta = 1.0f / eta;
+    cos_i = -cos_i;
+  }
+  const float sin_t2 = eta * eta * (1.0f - cos_i * cos_i);
+  if (sin_t2 > 1.0f) return 1.0f;
+  const float cos_t = sqrtf(ref_max(1.0f - sin_t2, 0.0f));
+  const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+  const float rp = (eta * cos_t - cos_i) / (eta * cos_t + cos_i);
+  return (rs * rs + rp * rp) * 0.5f;
+}
+
+// DielectricFresnel::Eval (material/fresnel.h:95-118), one channel
+__device__ __forceinline__ float dielectric_fresnel(float eta_in,
+                                                    float eta_out,
+                                                    float cos_i) {
+  if (cos_i < 0) {
+    const float t = eta_in;
+    eta_in = eta_out;
+    eta_out = t;
+    cos_i = -cos_i;
+  }
+  const float sin_i = sqrtf(ref_max(0.f, 1 - cos_i * cos_i));
+  const float sin_t = eta_out / eta_in * sin_i;
+  if (sin_t >= 1.f) return 1.f;
+  const float cos_t = sqrtf(ref_max(0.f, 1 - sin_t * sin_t));
+  const float para = ((eta_in * cos_i) - (eta_out * cos_t)) /
+                     ((eta_in * cos_i) + (eta_out * cos_t));
+  const float perp = ((eta_out * cos_i) - (eta_in * cos_t)) /
+                     ((eta_out * cos_i) + (eta_in * cos_t));
+  return 0.5f * (para * para + perp * perp);
+}
+
+// ConductorFresnel::Eval (material/fresnel.h:40-58) with eta_out = 1, one
+// channel: e2 = eta^2, k2 = k^2
+__device__ __forceinline__ float conductor_fresnel1(float e2, float k2,
+                                                    float cos_i) {
+  const float cos2 = cos_i * cos_i;
+  const float sin2 = ref_max(0.f, 1 - cos2);
+  const float t0 = e2 - k2 - sin2;
+  const float a2b2 = sqrtf(t0 * t0 + 4.f * e2 * k2);
+  const float t1 = a2b2 + cos2;
+  const float a = sqrtf(0.5f * (a2b2 + t0));
+  const float t2 = 2.f * cos_i * a;
+  const float rs = (t1 - t2) / (t1 + t2);
+  const float t3 = cos2 * a2b2 + sin2 * sin2;
+  const float t4 = t2 * sin2;
+  const float rp = rs * (t3 - t4) / (t3 + t4);
+  return 0.5f * (rp + rs);
+}
+
+// The base BSDF's black-fringe fallbacks (bsdf.cpp:30-63) for a BSDF of
+// albedo `alb` (Metal's AggregateBSDF: 1; PlasticBsdf: its albedo).
+struct Fringe {
+  F3 ng, ns, alb;
+  __device__ __forceinline__ bool causes(F3 w) const {
+    return (dot3(ng, w) > 0) != (dot3(ns, w) > 0);
+  }
+  __device__ __forceinline__ BsdfSample sample(F3 wo, F3 sam) const {
+    if (dot3(ng, wo) <= 0.f) return invalid_sample();
+    float pdf;
+    const F3 lwi = cosine_hemisphere(sam.x, sam.y, &pdf);
+    if (pdf < FLT_EPSILON) return invalid_sample();
+    const F3 wi = normalize3(Frame(ng).to_world(lwi));
+    const float factor = correct_shading_normal(ng, ns, wi);
+    BsdfSample s;
+    s.dir = wi;
+    s.f = alb / kPi * factor;
+    s.pdf = pdf;
+    return s;
+  }
+  __device__ __forceinline__ F3 eval(F3 wi, F3 wo) const {
+    if ((dot3(ng, wi) <= 0.f) || (dot3(ng, wo) <= 0.f)) return mk3(0, 0, 0);
+    return alb / kPi;
+  }
+  __device__ __forceinline__ float pdf(F3 wi, F3 wo) const {
+    if ((dot3(ng, wi) > 0.f) != (dot3(ng, wo) > 0.f)) return 0.f;
+    const F3 local = normalize3(Frame(ng).to_local(wi));
+    return local.z * kInvPi;
+  }
+};
+
+// MirrorBSDF (mirror.cpp:32-66): delta reflection about the shading normal.
+__device__ __forceinline__ BsdfSample mirror_sample(const float* m, F3 ng,
+                                                    F3 ns, F3 wo) {
+  const Frame sf(ns);
+  const F3 lwo = normalize3(sf.to_local(wo));
+  if (lwo.z <= 0.f) return invalid_sample();
+  const F3 lwi = mk3(-lwo.x, -lwo.y, lwo.z);
+  const F3 wi = sf.to_world(lwi);
+  const float factor = correct_shading_normal(ng, ns, wi);
+  BsdfSample s;
+  s.dir = wi;
+  s.f = mk3(m[1], m[2], m[3]) * factor / fabsf(lwi.z);
+  s.pdf = 1.f;
+  s.delta = true;
+  return s;
+}
+
+// GlassBSDF (glass.cpp:31-116) with Glass::Shade's colours (glass.cpp:
+// 128-150: the refraction colour's square root): reflect with probability
+// Fr, else refract; both delta.
+__device__ __forceinline__ BsdfSample glass_sample(const float* m, F3 ng,
+                                                   F3 ns, F3 wo, F3 sam) {
+  const Frame sf(ns);
+  const float ior = m[7];
+  const F3 lwo = normalize3(sf.to_local(wo));
+  const F3 normal = lwo.z > 0 ? mk3(0.f, 0.f, 1.f) : mk3(0.f, 0.f, -1.f);
+  const float fr = dielectric_fresnel(ior, 1.f, lwo.z);
+  BsdfSample s;
+  s.delta = true;
+  if (sam.x < fr) {
+    const F3 lwi = mk3(-lwo.x, -lwo.y, lwo.z);
+    const F3 wi = sf.to_world(lwi);
+    const F3 f = mk3(m[1], m[2], m[3]) * mk3(fr, fr, fr) / fabsf(lwi.z);
+    s.dir = wi;
+    s.f = f * correct_shading_normal(ng, ns, wi);
+    s.pdf = fr;
+    return s;
+  }
+  const float eta_i = lwo.z > 0 ? 1.f : ior;
+  const float eta_t = lwo.z > 0 ? ior : 1.f;
+  const float eta = eta_i / eta_t;
+  const float cos_i = fabsf(lwo.z);
+  const float sin2_i = ref_max(0.f, 1.f - cos_i * cos_i);
+  const float sin2_t = eta * eta * sin2_i;
+  if (sin2_t > 1.f) return invalid_sample();
+  const float cos_t = sqrtf(1 - sin2_t);
+  const F3 lwi = normalize3((eta * cos_i - cos_t) * normal - eta * lwo);
+  const F3 dir = sf.to_world(lwi);
+  const F3 refr = mk3(sqrtf(m[4]), sqrtf(m[5]), sqrtf(m[6]));
+  const F3 f = eta * eta * refr * (1.f - fr) / fabsf(lwi.z);
+  s.dir = dir;
+  s.f = f * correct_shading_normal(ng, ns, dir);
+  s.pdf = 1.f - fr;
+  return s;
+}
+
+// TrowbridgeReitzDistribution and EvalPdf of the GGX reflection component
+// (microfacet_reflection_component.cpp:26-135)
+__device__ __forceinline__ float sqrf(float x) { return x * x; }
+__device__ __forceinline__ float ggx_phi(F3 w) {
+  if (w.x <= 0.f && w.y <= 0.f) return 0.f;
+  const float r = atan2f(w.y, w.x);
+  return r < 0.f ? (r + 2 * kPi) : r;
+}
+__device__ __forceinline__ float ggx_tan_theta(F3 w) {
+  const float t = 1 - w.z * w.z;
+  if (t <= 0) return 0;
+  return sqrtf(t) / w.z;
+}
+__device__ __forceinline__ float ggx_g(float cos_phi, float sin_phi, float ax,
+                                       float ay, float tan_theta) {
+  const float t = sqrf(ax * cos_phi) + sqrf(ay * sin_phi);
+  const float sq = 1 + t * sqrf(tan_theta);
+  const float lambda = -0.5f + 0.5f * sqrtf(sq);
+  return 1 / (1 + lambda);
+}
+// f (coloured conductor Fresnel) when `f` is given, and the pdf
+__device__ __forceinline__ void ggx_eval_pdf(const float* m, F3 lwi, F3 lwo,
+                                             F3* f, float* pdf) {
+  if (lwi.z <= 0 || lwo.z <= 0) {
+    if (f) *f = mk3(0, 0, 0);
+    if (pdf) *pdf = 0.f;
+    return;
+  }
+  const float ax = m[10], ay = m[11];
+  const float cos_i = lwi.z, cos_o = lwo.z;
+  const F3 lwh = normalize3(lwi + lwo);
+  const float cos_d = dot3(lwi, lwh);
+  const float phi_h = ggx_phi(lwh);
+  const float sin_phi_h = sinf(phi_h), cos_phi_h = cosf(phi_h);
+  const float cos_h = lwh.z;
+  const float sin_h = sqrtf(ref_max(0.f, 1 - cos_h * cos_h));
+  const float A = sqrf(cos_phi_h / ax) + sqrf(sin_phi_h / ay);
+  const float RD = sqrf(sin_h) * A + sqrf(cos_h);
+  const float D = 1.f / (kPi * ax * ay * sqrf(RD));
+  const float phi_o = ggx_phi(lwo);
+  const float Go = ggx_g(cosf(phi_o), sinf(phi_o), ax, ay, ggx_tan_theta(lwo));
+  if (f) {
+    const float phi_i = ggx_phi(lwi);
+    const float Gi =
+        ggx_g(cosf(phi_i), sinf(phi_i), ax, ay, ggx_tan_theta(lwi));
+    const float G = Gi * Go;
+    F3 F = mk3(0.f, 0.f, 0.f);
+    if (cos_d > 0.f)
+      F = mk3(conductor_fresnel1((m[7] / 1.f) * (m[7] / 1.f),
+                                 (m[4] / 1.f) * (m[4] / 1.f), cos_d),
+              conductor_fresnel1((m[8] / 1.f) * (m[8] / 1.f),
+                                 (m[5] / 1.f) * (m[5] / 1.f), cos_d),
+              conductor_fresnel1((m[9] / 1.f) * (m[9] / 1.f),
+                                 (m[6] / 1.f) * (m[6] / 1.f), cos_d));
+    F = mk3(m[1], m[2], m[3]) * F;
+    *f = F * D * G / fabsf(4 * cos_i * cos_o);
+  }
+  if (pdf) *pdf = Go * D / (4 * lwo.z);
+}
+
+// Metal::Shade (metal.cpp:42-66): an AggregateBSDF of albedo 1 with one
+// GGX reflection component of weight 1 (aggregate_bsdf.cpp:43-131,
+// microfacet_reflection_component.cpp:137-183).
+__device__ __forceinline__ BsdfSample metal_sample(const float* m, F3 ng,
+                                                   F3 ns, F3 wo, F3 sam) {
+  const Fringe fr{ng, ns, mk3(1.f, 1.f, 1.f)};
+  if (fr.causes(wo)) return fr.sample(wo, sam);
+  const Frame sf(ns);
+  const F3 lwo = normalize3(sf.to_local(wo));
+  if (lwo.z <= 0.f) return invalid_sample();
+  const float ax = m[10], ay = m[11];
+  // TrowbridgeReitzDistribution::SampleWh
+  const F3 vh = normalize3(mk3(ax * lwo.x, ay * lwo.y, lwo.z));
+  const float lensq = vh.x * vh.x + vh.y * vh.y;
+  const F3 t1 = lensq > FLT_EPSILON ? mk3(-vh.y, vh.x, 0) / sqrtf(lensq)
+                                    : mk3(1, 0, 0);
+  const F3 t2 = cross3(vh, t1);
+  const float r = sqrtf(sam.y);
+  const float phi = 2 * kPi * sam.z;
+  const float t_1 = r * cosf(phi);
+  const float t_2s = r * sinf(phi);
+  const float sv = 0.5f * (1 + vh.z);
+  const float t_2 = (1 - sv) * sqrtf(1 - t_1 * t_1) + sv * t_2s;
+  const F3 nh = t_1 * t1 + t_2 * t2 +
+                sqrtf(ref_max(0.f, 1.f - t_1 * t_1 - t_2 * t_2)) * vh;
+  const F3 ne = normalize3(mk3(ax * nh.x, ay * nh.y, ref_max(0.f, nh.z)));
+  const F3 lwh = normalize3(ne);
+  if (lwh.z <= 0) return invalid_sample();
+  F3 lwi = normalize3(2 * dot3(lwo, lwh) * lwh - lwo);
+  if (lwi.z <= 0) return invalid_sample();
+  F3 f;
+  float pdf;
+  ggx_eval_pdf(m, lwi, lwo, &f, &pdf);
+  if (pdf == 0) return invalid_sample();
+  lwi = normalize3(lwi);
+  pdf *= 1.f;
+  const F3 wi = sf.to_world(lwi);
+  BsdfSample s;
+  s.dir = wi;
+  s.f = f * correct_shading_normal(ng, ns, wi);
+  s.pdf = pdf;
+  return s;
+}
+__device__ __forceinline__ void metal_eval_pdf(const float* m, F3 ng, F3 ns,
+                                               F3 wi, F3 wo, F3& f,
+                                               float& pdf) {
+  const Fringe fr{ng, ns, mk3(1.f, 1.f, 1.f)};
+  if (fr.causes(wo)) {
+    f = fr.eval(wi, wo);
+    pdf = fr.pdf(wi, wo);
+    return;
+  }
+  const Frame sf(ns);
+  const F3 lwi = normalize3(sf.to_local(wi));
+  const F3 lwo = normalize3(sf.to_local(wo));
+  if (lwi.z <= 0.f || lwo.z <= 0.f) {
+    f = mk3(0, 0, 0);
+    pdf = 0.f;
+    return;
+  }
+  F3 g;
+  float p;
+  ggx_eval_pdf(m, lwi, lwo, &g, &p);
+  f = mk3(0, 0, 0) + g;
+  float wsum = 0.f, acc = 0.f;
+  wsum += 1.f;
+  acc += 1.f * p;
+  pdf = wsum > 0 ? acc / wsum : 0;
+}
+
+// checkReflectionConstraint (bsdf/helper.h:26-31)
+__device__ __forceinline__ bool reflection_constraint(F3 wi, F3 wo) {
+  return fabsf(wi.z * wo.z - wi.x * wo.x - wi.y * wo.y - 1.0f) < 1e-3f;
+}
+
+// PlasticBsdf (plastic_bsdf.cpp:47-185): a delta coat reflection with
+// probability Fi / (Fi + T (1 - Fi)), else the cosine-sampled substrate; no
+// shading-normal correction, and Eval does not reject wi below the surface.
+struct PlasticB {
+  F3 ng, ns, albedo, scaled;
+  float ior, avg_t, dfres;
+  __device__ __forceinline__ PlasticB(const float* m, F3 ng_, F3 ns_)
+      : ng(ng_), ns(ns_), albedo(mk3(m[1], m[2], m[3])), ior(m[4]),
+        avg_t(m[14]), dfres(m[15]) {
+    const float sc = m[5] * m[6];
+    scaled = mk3(sc, sc, sc);
+  }
+  // Sample's substrate f (k = (1 - Fi)(1 - Fo) eta^2), and Eval's, which
+  // also carries lwi.z / pi inside the scalar
+  __device__ __forceinline__ F3 substrate_albedo() const {
+    return albedo / (mk3(1.0f, 1.0f, 1.0f) - albedo * dfres);
+  }
+  __device__ __forceinline__ F3 absorb(F3 lwi, F3 lwo) const {
+    const F3 e = scaled * (-1.0f / lwi.z - 1.0f / lwo.z);
+    return mk3(expf(e.x), expf(e.y), expf(e.z));
+  }
+  __device__ __forceinline__ float spec_prob(float Fi) const {
+    const float substrate_weight = avg_t * (1.0f - Fi);
+    const float specular_weight = Fi;
+    return specular_weight / (specular_weight + substrate_weight);
+  }
+  __device__ BsdfSample sample(F3 wo, F3 sam) const {
+    const Fringe fr{ng, ns, albedo};
+    if (fr.causes(wo)) return fr.sample(wo, sam);
+    const Frame sf(ns);
+    const F3 lwo = normalize3(sf.to_local(wo));
+    if (lwo.z <= 0.f) return invalid_sample();
+    const float eta = 1.f / ior;
+    const float Fi = dielectric_reflectance(eta, lwo.z);
+    const float sp = spec_prob(Fi);
+    BsdfSample s;
+    F3 lwi;
+    if (sam.x < sp) {
+      lwi = mk3(-lwo.x, -lwo.y, lwo.z);
+      s.pdf = sp;
+      const float v = Fi / sp;
+      s.f = mk3(v, v, v);
+      s.delta = true;
+    } else {
+      float pdf;
+      lwi = cosine_hemisphere(sam.y, sam.z, &pdf);
+      const float Fo = dielectric_reflectance(eta, lwi.z);
+      F3 f = ((1.0f - Fi) * (1.0f - Fo) * eta * eta) * substrate_albedo();
+      if (maxc3(scaled) > 0.0f) f = f * absorb(lwi, lwo);
+      pdf *= (1.0f - sp);
+      s.f = f / (1.0f - sp);
+      s.pdf = pdf;
+      s.delta = false;
+    }
+    s.dir = normalize3(sf.to_world(lwi));
+    return s;
+  }
+  __device__ void eval_pdf(F3 wi, F3 wo, F3& f, float& pdf) const {
+    const Fringe fr{ng, ns, albedo};
+    if (fr.causes(wo)) {
+      f = fr.eval(wi, wo);
+      pdf = fr.pdf(wi, wo);
+      return;
+    }
+    const Frame sf(ns);
+    const F3 lwi = normalize3(sf.to_local(wi));
+    const F3 lwo = normalize3(sf.to_local(wo));
+    const float eta = 1.0f / ior;
+    const float Fi = dielectric_reflectance(eta, lwo.z);
+    const float Fo = dielectric_reflectance(eta, lwi.z);
+    const bool coat = reflection_constraint(lwo, lwi);
+    if (coat) {
+      f = mk3(Fi, Fi, Fi);
+    } else {
+      f = ((1.0f - Fi) * (1.0f - Fo) * eta * eta * lwi.z * (1.f / kPi)) *
+          substrate_albedo();
+      if (maxc3(scaled) > 0.0f) f = f * absorb(lwi, lwo);
+    }
+    if (lwi.z <= 0.0f || lwo.z <= 0.0f) {
+      pdf = 0.f;
+      return;
+    }
+    const float sp = spec_prob(dielectric_reflectance(1.0f / ior, lwo.z));
+    pdf = coat ? sp : lwi.z * kInvPi * (1.0f - sp);
+  }
+};
+
+// The types >= AJG_MAT_MIRROR (type passed separately: the record's first
+// word is a float in the scene tables and a uint32 in ajg_bsdf_query's).
+static __device__ __noinline__ BsdfSample other_sample(int type,
+                                                       const float* m, F3 ng,
+                                                       F3 ns, F3 wo, F3 sam) {
+  switch (type) {
+    case AJG_MAT_MIRROR: return mirror_sample(m, ng, ns, wo);
+    case AJG_MAT_GLASS: return glass_sample(m, ng, ns, wo, sam);
+    case AJG_MAT_METAL: return metal_sample(m, ng, ns, wo, sam);
+    case AJG_MAT_PLASTIC: return PlasticB(m, ng, ns).sample(wo, sam);
+    default: {  // NullBsdf (null.cpp:31-52): straight through
+      BsdfSample s;
+      s.dir = -wo;
+      s.f = mk3(1.f, 1.f, 1.f);
+      s.pdf = 1.f;
+      s.delta = true;
+      return s;
+    }
+  }
+}
+static __device__ __noinline__ void other_eval_pdf(int type, const float* m,
+                                                   F3 ng, F3 ns, F3 wi, F3 wo,
+                                                   F3& f, float& pdf) {
+  if (type == AJG_MAT_METAL) {
+    metal_eval_pdf(m, ng, ns, wi, wo, f, pdf);
+  } else if (type == AJG_MAT_PLASTIC) {
+    PlasticB(m, ng, ns).eval_pdf(wi, wo, f, pdf);
+  } else {  // mirror, glass, null: Eval 0, Pdf 0
+    f = mk3(0, 0, 0);
+    pdf = 0.f;
+  }
+}
+
 // The BSDF at a hit: material record (in global memory) and the two normals.
 struct Bsdf {
   int type;
@@ -624,15 +1031,24 @@ struct Bsdf {
   }
   __device__ __forceinline__ BsdfSample sample(F3 wo, F3 s) const {
     if (type == AJG_MAT_DIFFUSE) return lambert_sample(ng, ns, albedo(), wo, s);
-    return disney_sample(m, lum, ns, wo, s);
+    if (type == AJG_MAT_DISNEY) return disney_sample(m, lum, ns, wo, s);
+    return other_sample(type, m, ng, ns, wo, s);
   }
   __device__ __forceinline__ F3 eval(F3 wi, F3 wo) const {
     if (type == AJG_MAT_DIFFUSE) return lambert_eval(ng, ns, albedo(), wi, wo);
-    return disney_eval(m, lum, ns, wi, wo);
+    if (type == AJG_MAT_DISNEY) return disney_eval(m, lum, ns, wi, wo);
+    F3 f;
+    float p;
+    other_eval_pdf(type, m, ng, ns, wi, wo, f, p);
+    return f;
   }
   __device__ __forceinline__ float pdf(F3 wi, F3 wo) const {
     if (type == AJG_MAT_DIFFUSE) return lambert_pdf(ng, ns, albedo(), wi, wo);
-    return disney_pdf(m, lum, ns, wi, wo);
+    if (type == AJG_MAT_DISNEY) return disney_pdf(m, lum, ns, wi, wo);
+    F3 f;
+    float p;
+    other_eval_pdf(type, m, ng, ns, wi, wo, f, p);
+    return p;
   }
 };
 
@@ -648,6 +1064,7 @@ struct BsdfT {
   }
   __device__ __forceinline__ BsdfSample sample(F3 wo, F3 s) const {
     if (MAT == AJG_MAT_DIFFUSE) return Lambert(ng, ns, albedo()).sample(wo, s);
+    if (MAT == kMatOther) return other_sample((int)m[0], m, ng, ns, wo, s);
     return disney_sample(m, lum, ns, wo, s);
   }
   __device__ __forceinline__ void eval_pdf(F3 wi, F3 wo, F3& f,
@@ -656,6 +1073,10 @@ struct BsdfT {
       const Lambert l(ng, ns, albedo());
       f = l.eval(wi, wo);
       pdf = black3(f) ? 0.f : l.pdf(wi, wo);
+      return;
+    }
+    if (MAT == kMatOther) {
+      other_eval_pdf((int)m[0], m, ng, ns, wi, wo, f, pdf);
       return;
     }
     disney_eval_pdf(m, lum, ns, wi, wo, f, pdf, false);

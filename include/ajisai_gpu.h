@@ -61,7 +61,15 @@ enum {
   AJG_MESH_NG_REVERSED = 2, /* Cube: normal from (c,b,a) (core/geometry/cube.cpp:96-108) */
   AJG_MESH_HAS_NORMALS = 4  /* MeshGeo shading normals (core/geometry/mesh.cpp:183-204) */
 };
-enum { AJG_MAT_DIFFUSE = 0, AJG_MAT_DISNEY = 1 };
+enum {
+  AJG_MAT_DIFFUSE = 0, /* Diffuse (diffuse.cpp) */
+  AJG_MAT_DISNEY = 1,  /* Disney (disney.cpp) */
+  AJG_MAT_MIRROR = 2,  /* Mirror (mirror.cpp) */
+  AJG_MAT_GLASS = 3,   /* Glass (glass.cpp) */
+  AJG_MAT_METAL = 4,   /* Metal (metal.cpp) */
+  AJG_MAT_PLASTIC = 5, /* Plastic (plastic.cpp, bsdf/plastic_bsdf.cpp) */
+  AJG_MAT_NULL = 6     /* Null (null.cpp): rays pass straight through */
+};
 enum { AJG_LIGHT_DIRECTIONAL = 0, AJG_LIGHT_ENV = 1 };
 enum { AJG_TRI_MOLLER_TRUMBORE = 0, AJG_TRI_WATERTIGHT = 1 };
 #define AJG_BVH_COMPRESSED 0x100 /* ajg_scene_opts.bvh_width flag */
@@ -92,11 +100,25 @@ typedef struct ajg_mesh_desc {
 } ajg_mesh_desc;
 
 /* Constant-texture material (Diffuse: base_color is the albedo). */
+/* Constant-texture material.  base_color: the diffuse albedo, Disney's
+ * base colour, the mirror's kr, the glass's color_reflection, the metal's
+ * color, the plastic's albedo.  The ten floats after it are Disney's named
+ * parameters, or as `params`:
+ *   glass:   color_refraction[3] (as given; shading takes its square root,
+ *            glass.cpp:131-138), ior
+ *   metal:   k[3], eta[3], uroughness, vroughness
+ *   plastic: ior, thickness, sigma_a
+ * pad: 0 (the library keeps plastic's precomputed terms there). */
 typedef struct ajg_material {
   uint32_t type; /* AJG_MAT_* */
   float base_color[3];
-  float subsurface, metallic, specular, specular_tint, roughness,
-      anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss;
+  union {
+    struct {
+      float subsurface, metallic, specular, specular_tint, roughness,
+          anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss;
+    };
+    float params[10];
+  };
   float pad[2];
 } ajg_material; /* 64 bytes, the [16]-float record of the flat layout */
 
@@ -282,7 +304,8 @@ AJG_API int ajg_trace_any_device(ajg_scene* scene, const ajg_ray* d_rays,
 
 /* ---- shading and camera queries (golden-vector entry points) ---------- */
 /* n queries; op[i] 0: eval+pdf of (wi, wo), 1: sample(wo, sam).
- * ng, ns, wo, wi, sam: [n][3]; out [n][8]: f rgb, pdf, wi xyz, valid. */
+ * ng, ns, wo, wi, sam: [n][3]; out [n][8]: f rgb, pdf, wi xyz, and the
+ * sample's flag: valid (1) + delta (2). */
 AJG_API int ajg_bsdf_query(ajg_ctx* ctx, const ajg_material* materials,
                            const float* ng, const float* ns, const float* wo,
                            const float* wi, const float* sam,

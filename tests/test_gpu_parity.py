@@ -256,6 +256,40 @@ def test_bsdf_sample_matches_reference(ctx, golden):
     assert close.mean() > 0.98
 
 
+def test_more_materials_match_reference(ctx, golden):
+    """Mirror, glass, metal, plastic and null (bsdf_more.npz): EvalAll /
+    PdfAll within 1e-5 relative (mirror, glass and null: exactly 0); the
+    sample's validity and delta flag, direction (within 2e-5), f and pdf
+    (within 1e-5) -- apart from the few queries where a last-ulp difference
+    of CUDA's atan2/sin/cos/exp (GGX, cosine sampling, absorption) moves a
+    branch."""
+    g = golden("bsdf_more.npz")
+    typ = g["material"][:, 0].astype(int)
+    e = g["op"] == 0
+    out = ctx.bsdf_query(g["material"][e], g["ng"][e], g["ns"][e], g["wo"][e],
+                         g["wi"][e], g["sam"][e], g["op"][e])
+    ref = g["out"][e]
+    zero = np.isin(typ[e], (S.MAT_MIRROR, S.MAT_GLASS, S.MAT_NULL))
+    assert np.all(out[zero, :4] == 0) and np.all(ref[zero, :4] == 0)
+    close = np.isclose(out[:, :4], ref[:, :4], rtol=1e-5, atol=1e-30).all(1)
+    assert close.mean() > 0.995, close.mean()
+    np.testing.assert_allclose(out[:, :4], ref[:, :4], rtol=1e-3, atol=1e-6)
+    s = g["op"] == 1
+    out = ctx.bsdf_query(g["material"][s], g["ng"][s], g["ns"][s], g["wo"][s],
+                         g["wi"][s], g["sam"][s], g["op"][s])
+    ref = g["out"][s]
+    assert (out[:, 7] == ref[:, 7]).mean() > 0.995
+    assert np.any(ref[:, 7] == 3) and np.any(ref[:, 7] == 1)  # delta and not
+    same = (out[:, 7] == ref[:, 7]) & (ref[:, 7] > 0)
+    dclose = np.isclose(out[same, 4:7], ref[same, 4:7], rtol=0, atol=2e-5).all(1)
+    assert dclose.mean() > 0.99
+    fclose = np.isclose(out[same, :4], ref[same, :4], rtol=1e-5, atol=1e-30).all(1)
+    assert fclose.mean() > 0.98, fclose.mean()
+    # no transcendental on the way: mirror, glass and null samples are exact
+    exact = same & np.isin(typ[s], (S.MAT_MIRROR, S.MAT_GLASS, S.MAT_NULL))
+    assert np.array_equal(out[exact].view(np.uint32), ref[exact].view(np.uint32))
+
+
 # ---------------------------------------------------------------- camera --
 def test_camera_rays_match_reference(ctx, golden):
     g = golden("camera.npz")
@@ -281,7 +315,8 @@ def params_of(g):
 
 @pytest.mark.parametrize("case", ["render_cornell.npz", "render_ico.npz",
                                   "render_cornell_nomis.npz", "render_area.npz",
-                                  "render_area_nomis.npz"])
+                                  "render_area_nomis.npz", "render_materials.npz",
+                                  "render_materials_nomis.npz"])
 def test_render_per_sample_matches_reference(ctx, golden, case):
     """Shared counter sampler: each sample's radiance equals the reference's
     within float32 tolerance, apart from rare paths that a last-ulp
@@ -482,3 +517,23 @@ def test_invalid_emitters_are_rejected(ctx):
     fl.emit_rad[:] = 0
     sc = api.GpuScene(ctx, fl)
     sc.release()
+
+
+# -------------------------------------------------------- more materials --
+@pytest.mark.parametrize("use_mis", [True, False])
+def test_materials_match_oracle_per_sample(ctx, use_mis):
+    """Plastic, mirror, metal, glass and a null-material emitter at 40x32x8
+    against the oracle; tree layouts and wave sizes give the same samples."""
+    flat = S.flatten(S.material_box(40, 32))
+    args = api.PTRendererArgs(spp=8, min_bounces=3, max_bounces=8, use_mis=use_mis)
+    li = api.PTRenderer(args, seed=21).RenderSamples(api.GpuScene(ctx, flat), flat.camera)
+    ref, _ = O.render(flat, dict(spp=8, min_bounces=3, max_bounces=8,
+                                 use_mis=int(use_mis)), seed=21)
+    ref = ref.reshape(li.shape)
+    close = np.isclose(li, ref, rtol=1e-4, atol=1e-6, equal_nan=True).all(axis=-1)
+    assert close.mean() > 0.98, close.mean()
+    for width in (2, 0x108):
+        b = api.PTRenderer(args, seed=21).RenderSamples(
+            api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, bvh_width=width)),
+            flat.camera)
+        assert same_bits(li, b)

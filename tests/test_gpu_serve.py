@@ -34,6 +34,7 @@ def scenes(ctx):
         clutter = S.mixed_scene(4, 3000, 64, 64)
     env_only = with_lights(S.icosphere_scene(2, 11, 64, 64), [S.EnvLight(0.7)])
     area = S.cornell_area(64, 64)
+    mats = S.material_box(64, 64)
     three = with_lights(S.cornell_box(64, 64),
                         [S.DirectionalLight((0.3, 1.0, 0.2), 3.0),
                          S.DirectionalLight((-0.5, 1.0, 0.1), 1.5, 5.0),
@@ -59,6 +60,8 @@ def scenes(ctx):
         "area": (api.GpuScene(ctx, area), area.camera),
         "area_c8": (api.GpuScene(ctx, area, api.CreatePLOCAggregate(14, bvh_width=0x108)),
                     area.camera),
+        # mirror, glass, metal, plastic and a null-material emitter
+        "mats": (api.GpuScene(ctx, mats), mats.camera),
     }
     return out
 
@@ -92,6 +95,8 @@ def job_list(scenes):
         ("area", 48, 40, renderer(9, seed=13)),
         ("area", 24, 24, renderer(6, mis=False, seed=14)),
         ("area_c8", 32, 24, renderer(5, seed=15, drop=True)),
+        ("mats", 40, 40, renderer(8, seed=16)),
+        ("mats", 24, 32, renderer(6, mis=False, seed=17)),
     ]
 
 
