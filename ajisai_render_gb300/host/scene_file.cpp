@@ -278,10 +278,18 @@ Geo load_geometry(const std::string& file, const Node& n,
 ajg_material load_material(const std::string& file, const Node& n) {
   ajg_material m;
   std::memset(&m, 0, sizeof(m));
-  if (!n.IsDefined())
-    fail(file, n, "primitive without a material (the null material is not "
-                  "rendered by this path)");
+  // no material node: CreateNull (primitive_creators.cpp:54-59)
+  if (!n.IsDefined()) {
+    m.type = AJG_MAT_NULL;
+    return m;
+  }
   const std::string type = n["type"].AsString("");
+  auto color = [&](const char* key, float* out) {
+    const V3 c = constant_texel(file, n[key], type + "." + key);
+    out[0] = c.x;
+    out[1] = c.y;
+    out[2] = c.z;
+  };
   if (type == "diffuse") {  // material_creators.cpp:28-39
     const V3 a = constant_texel(file, n["albedo"], "diffuse.albedo");
     m.type = AJG_MAT_DIFFUSE;
@@ -308,9 +316,37 @@ ajg_material load_material(const std::string& file, const Node& n) {
     m.sheen_tint = real("sheen_tint");
     m.clearcoat = real("clearcoat");
     m.clearcoat_gloss = real("clearcoat_gloss");
+  } else if (type == "mirror") {  // material_creators.cpp:70-79
+    m.type = AJG_MAT_MIRROR;
+    color("kr", m.base_color);
+  } else if (type == "glass") {  // material_creators.cpp:128-152
+    m.type = AJG_MAT_GLASS;
+    // absent colours are constant 1 textures
+    if (n["color_reflection"].IsDefined())
+      color("color_reflection", m.base_color);
+    else
+      m.base_color[0] = m.base_color[1] = m.base_color[2] = 1.f;
+    if (n["color_refraction"].IsDefined())
+      color("color_refraction", m.params);
+    else
+      m.params[0] = m.params[1] = m.params[2] = 1.f;
+    // the ior texture is read with SampleReal: its first component
+    m.params[3] = constant_texel(file, n["ior"], "glass.ior").x;
+  } else if (type == "metal") {  // material_creators.cpp:54-68
+    m.type = AJG_MAT_METAL;
+    color("color", m.base_color);
+    color("k", m.params);
+    color("eta", m.params + 3);
+    m.params[6] = n["uroughness"].AsFloat(0.1f);
+    m.params[7] = n["vroughness"].AsFloat(0.1f);
+  } else if (type == "plastic") {  // material_creators.cpp:40-52
+    m.type = AJG_MAT_PLASTIC;
+    color("albedo", m.base_color);
+    m.params[0] = n["ior"].AsFloat(1.5f);
+    m.params[1] = n["thickness"].AsFloat(1.f);
+    m.params[2] = n["sigma_a"].AsFloat(0.f);
   } else {
-    fail(file, n, "material '" + type + "' is not on this path (diffuse and "
-                  "disney are)");
+    fail(file, n, "unknown material type '" + type + "'");
   }
   return m;
 }

@@ -84,6 +84,19 @@ def _texel(v) -> str:
 def _material_yaml(m) -> str:
     if m.type == S.MAT_DIFFUSE:
         return "{type: diffuse, albedo: %s}" % _texel(m.base_color)
+    p = list(m.params) if m.params is not None else []
+    if m.type == S.MAT_MIRROR:
+        return "{type: mirror, kr: %s}" % _texel(m.base_color)
+    if m.type == S.MAT_GLASS:
+        return ("{type: glass, color_reflection: %s, color_refraction: %s, ior: %s}"
+                % (_texel(m.base_color), _texel(p[0:3]), _texel(p[3])))
+    if m.type == S.MAT_METAL:
+        return ("{type: metal, color: %s, k: %s, eta: %s, uroughness: %s, vroughness: %s}"
+                % (_texel(m.base_color), _texel(p[0:3]), _texel(p[3:6]), f32(p[6]),
+                   f32(p[7])))
+    if m.type == S.MAT_PLASTIC:
+        return ("{type: plastic, albedo: %s, ior: %s, thickness: %s, sigma_a: %s}"
+                % (_texel(m.base_color), f32(p[0]), f32(p[1]), f32(p[2])))
     keys = ("subsurface", "metallic", "specular", "specular_tint", "roughness",
             "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss")
     return "{type: disney, base_color: %s, %s}" % (
@@ -91,14 +104,11 @@ def _material_yaml(m) -> str:
         ", ".join(f"{k}: {_texel(getattr(m, k))}" for k in keys))
 
 
-def area_files() -> tuple[str, str]:
-    """scenes.cornell_area as a scene file: its emissive quads, cube and
-    icosphere mesh (ball.obj) carry `emission`."""
-    sc = S.cornell_area(256, 256)
-    obj = ["# emissive icosphere of scenes.cornell_area"]
-    lines = ["# scenes.cornell_area: the box lit by a one-sided ceiling quad, a",
-             "# two-sided quad, an emissive icosphere mesh and an emissive cube.",
-             "scene:", "  type: default", "  primitives:"]
+def scene_files(sc, header, obj_name, lights, env) -> tuple[str, str]:
+    """A scene of quads, cubes and one mesh (written to `obj_name`, with its
+    normals when it has them) as a scene file."""
+    obj = ["# " + header[0]]
+    lines = ["# " + h for h in header] + ["scene:", "  type: default", "  primitives:"]
     for p in sc.primitives:
         if isinstance(p, S.Quad):
             geo = (f"{{type: quad, a: {vec(p.a)}, b: {vec(p.b)}, c: {vec(p.c)}, "
@@ -109,18 +119,26 @@ def area_files() -> tuple[str, str]:
         else:
             for v in p.positions:
                 obj.append("v " + " ".join(f32(x) for x in v))
-            for t in p.indices:
-                obj.append("f " + " ".join(str(int(i) + 1) for i in t))
-            geo = "{type: mesh, filename: ball.obj}"
+            if p.normals is not None:
+                for v in p.normals:
+                    obj.append("vn " + " ".join(f32(x) for x in v))
+                for t in p.indices:
+                    obj.append("f " + " ".join(f"{int(i) + 1}//{int(i) + 1}" for i in t))
+            else:
+                for t in p.indices:
+                    obj.append("f " + " ".join(str(int(i) + 1) for i in t))
+            geo = f"{{type: mesh, filename: {obj_name}}}"
         if p.two_sided:
             geo = f"{{type: twosided, internal: {geo}}}"
-        lines += ["    - type: geometry", f"      geometry: {geo}",
-                  f"      material: {_material_yaml(sc.materials[p.material])}"]
+        lines += ["    - type: geometry", f"      geometry: {geo}"]
+        mat = sc.materials[p.material]
+        if mat.type != S.MAT_NULL:  # the null material is the absent node
+            lines.append(f"      material: {_material_yaml(mat)}")
         if p.emission is not None:
             lines.append(f"      emission: {vec(p.emission)}")
     lines += ["  lights:",
-              "    - {type: directional, direction: [0.3, 1.0, 0.2], emission: [1, 1, 1]}",
-              "    - {type: envmap, texture: {type: constant, texel: 0.05}}",
+              f"    - {{type: directional, direction: [0.3, 1.0, 0.2], emission: {lights}}}",
+              f"    - {{type: envmap, texture: {{type: constant, texel: {env}}}}}",
               "  aggregate: {type: ploc, search_radius: 14}",
               "camera: {type: thin_lens, resolution: [256, 256], position: [0, 0, 1.9],",
               "         look_at: [0, 0, 0], up: [0, 1, 0], fov: 40}",
@@ -132,7 +150,16 @@ if __name__ == "__main__":
     OUT.mkdir(exist_ok=True)
     (OUT / "cornell_box.yaml").write_text(cornell_yaml(False))
     (OUT / "cornell_box_flow.yaml").write_text(cornell_yaml(True))
-    yml, obj = area_files()
+    yml, obj = scene_files(S.cornell_area(256, 256),
+                           ["scenes.cornell_area: the box lit by a one-sided ceiling quad, a",
+                            "two-sided quad, an emissive icosphere mesh and an emissive cube."],
+                           "ball.obj", "[1, 1, 1]", "0.05")
     (OUT / "cornell_area.yaml").write_text(yml)
     (OUT / "ball.obj").write_text(obj)
+    yml, obj = scene_files(S.material_box(256, 256),
+                           ["scenes.material_box: plastic, mirror, metal, glass and a",
+                            "null-material emitter."],
+                           "glass_ball.obj", "[1, 1, 1]", "0.1")
+    (OUT / "material_box.yaml").write_text(yml)
+    (OUT / "glass_ball.obj").write_text(obj)
     print("wrote", OUT)

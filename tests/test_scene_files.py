@@ -67,6 +67,23 @@ def test_area_scene_file_reads_its_emitters():
     assert same_bits(f.camera, ref.camera)
 
 
+def test_material_scene_file_reads_every_material():
+    """mirror, glass, metal and plastic nodes and a primitive without a
+    material (the null material) read to scenes.material_box's records; the
+    glass ball's OBJ carries its normals."""
+    f = api.load_scene_file(GOLDEN / "material_box.yaml")
+    ref = S.flatten(S.material_box(256, 256))
+    assert same_bits(f.flat.tris, ref.tris)
+    assert np.array_equal(f.flat.tri_flags, ref.tri_flags)
+    # the loader normalises the file's normals (the Python mesh keeps them)
+    m = ref.tri_flags & S.TRI_HAS_NORMALS > 0
+    np.testing.assert_allclose(f.flat.corner_n[m], ref.corner_n[m], rtol=0, atol=3e-7)
+    assert same_bits(f.flat.materials[f.flat.tri_mat], ref.materials[ref.tri_mat])
+    assert np.array_equal(f.flat.emit_info, ref.emit_info)
+    assert same_bits(f.flat.emit_rad, ref.emit_rad)
+    assert same_bits(f.flat.lights, ref.lights)
+
+
 def write_obj(path, pos, idx, nrm=None, quads=False):
     with open(path, "w") as fh:
         fh.write("# test mesh\no mesh\n")
@@ -174,10 +191,11 @@ def test_polygons_are_split_into_fans(tmp_path):
 @pytest.mark.parametrize("snippet,message", [
     ("{type: geometry, geometry: {type: sphere, radius: 1, center: [0, 0, 0]},"
      " material: {type: diffuse, albedo: {type: constant, texel: 0.5}}}", "sphere"),
-    ("{type: geometry, geometry: {type: quad}, material: {type: glass}}", "glass"),
+    ("{type: geometry, geometry: {type: quad}, material: {type: velvet}}", "velvet"),
     ("{type: geometry, geometry: {type: quad},"
      " material: {type: diffuse, albedo: {type: image, filename: a.png}}}", "constant"),
-    ("{type: geometry, geometry: {type: quad}, emission: [1, 1, 1]}", "null material"),
+    ("{type: geometry, geometry: {type: quad}, material: {type: diffuse},"
+     " med_in: {type: homogeneous}}", "media"),
 ])
 def test_unsupported_nodes_are_refused_with_the_reason(tmp_path, snippet, message):
     (tmp_path / "s.yaml").write_text(f"""scene:
@@ -257,7 +275,8 @@ def test_film_pfm_writers_agree(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cornell_box.yaml", "cornell_area.yaml"])
+@pytest.mark.parametrize("name", ["cornell_box.yaml", "cornell_area.yaml",
+                                  "material_box.yaml"])
 def test_command_line_renders_the_scene_file(tmp_path, name):
     """ajisai_gpu -s scene.yaml: the film equals the Python API's render of
     the same file (with and without emitters)."""
@@ -266,7 +285,8 @@ def test_command_line_renders_the_scene_file(tmp_path, name):
     build.build_host()
     src = (GOLDEN / name).read_text().replace("spp: 64", "spp: 8") \
         .replace("resolution: [256, 256]", "resolution: [64, 48]")
-    (tmp_path / "ball.obj").write_text((GOLDEN / "ball.obj").read_text())
+    for obj in ("ball.obj", "glass_ball.obj"):
+        (tmp_path / obj).write_text((GOLDEN / obj).read_text())
     (tmp_path / "c.yaml").write_text(src.replace("filename: cornell.png",
                                                  f"filename: {tmp_path / 'out.png'}"))
     r = subprocess.run([str(build.CLI), "-s", str(tmp_path / "c.yaml"), "--out",
