@@ -1566,6 +1566,7 @@ struct Scene {
   std::vector<int> tri_light; /* light index of an emissive triangle, or -1 */
   int env = -1;
   float radius; /* (aabb.max - aabb.center).length() */
+  Box world;     /* the primitives' joined bounds */
   int mode;
 };
 
@@ -1766,6 +1767,260 @@ V3 trace_path(const Scene& s, Ray ray, Rng& rng, int min_b, int max_b,
   return L;
 }
 
+/* ---------------------------------------------------------------- SPPM --- */
+/* HasDiffuseComponent (sppm.cpp:77's visible-point rule): Lambert and
+ * plastic yes, Disney when metallic < 1 (disney.cpp:79), mirror, glass and
+ * null no.  Metal's AggregateBSDF::HasDiffuseComponent (aggregate_bsdf.cpp:
+ * 37-41) runs off its end when no component is diffuse -- the reference's
+ * Release build faults there; the loop's own verdict, no, is taken. */
+bool has_diffuse(const Mat& m) {
+  switch (m.type) {
+    case ORC_MAT_DIFFUSE: return true;
+    case ORC_MAT_DISNEY: return m.metallic < 1.f;
+    case ORC_MAT_PLASTIC: return true;
+    default: return false;
+  }
+}
+
+struct VisPoint {
+  bool valid = false;
+  V3 pos, wr, thr, ng, ns;
+  int mat = -1;
+};
+
+/* TracerVP (sppm.cpp:35-101) */
+VisPoint tracer_vp(const Scene& s, Ray ray, Rng& rng, int fmd, V3& direct) {
+  V3 T = mk(1.f, 1.f, 1.f);
+  for (int depth = 0; depth < fmd; ++depth) {
+    Hit h = trace_closest(s.acc, ray, s.mode, true);
+    if (h.prim < 0) {
+      if (depth == 0 && s.env >= 0) {
+        const Light& E = s.lights[s.env];
+        direct = direct + T * (E.scaler * E.rgb);
+      }
+      return VisPoint{};
+    }
+    HitInfo hi = complete_hit(s, ray, h);
+    const Mat& m = s.mats[hi.mat];
+    Bsdf f(m, hi.ng, hi.ns);
+    if (depth == 0) {
+      const int li = s.tri_light.empty() ? -1 : s.tri_light[h.prim];
+      if (li >= 0) {
+        const AreaL& A = s.areas[s.lights[li].area];
+        const V3 le = dot(hi.ng, hi.wr) > 0 ? A.rad : mk(0, 0, 0);
+        direct = direct + T * le;
+      }
+    }
+    V3 sum = mk(0, 0, 0);
+    for (const Light& lt : s.lights) sum = sum + T * mis_light(s, lt, hi, f, rng);
+    sum = sum + T * mis_bsdf(s, hi, f, rng);
+    direct = direct + 1.f / 1 * sum;
+    if (has_diffuse(m) || depth == fmd - 1) {
+      if (!(std::isfinite(T.x) && std::isfinite(T.y) && std::isfinite(T.z)))
+        return VisPoint{};
+      VisPoint vp;
+      vp.valid = true;
+      vp.pos = hi.pos;
+      vp.thr = T;
+      vp.wr = hi.wr;
+      vp.ng = hi.ng;
+      vp.ns = hi.ns;
+      vp.mat = (int)hi.mat;
+      return vp;
+    }
+    float a = rng.next(), b = rng.next(), c = rng.next();
+    Sample bs = f.sample(hi.wr, mk(a, b, c));
+    if (is_black(bs.f) || bs.pdf < 0.f) return VisPoint{};
+    T = T * (bs.f * std::fabs(dot(hi.ng, bs.dir)) / bs.pdf);
+    ray = make_ray(eps_offset(hi, bs.dir), bs.dir);
+  }
+  return VisPoint{};
+}
+
+/* sppm::Pixel (photon_mapping.h:54-67) */
+struct SppmPixel {
+  VisPoint vp;
+  float radius = 0.1f;
+  float phi[3] = {0.f, 0.f, 0.f};
+  int M = 0;
+  float N = 0;
+  V3 tau = mk(0, 0, 0);
+  V3 direct = mk(0, 0, 0);
+};
+
+/* VisiblePointSearcher (photon_mapping.h:69-148): 40960 hash entries of
+ * pixel lists; a visible point joins the cells [lo, hi) of its radius box
+ * (the last cell on each axis is left out). */
+struct VpGrid {
+  Box bound;
+  float side;
+  std::vector<std::vector<int>> entries;
+  VpGrid(Box b, float s_) : bound(b), side(s_), entries(40960) {}
+  void cell(V3 pos, int c[3]) const {
+    const V3 hd = pos - bound.lo;
+    c[0] = static_cast<int>(fmax_ref(hd.x, 0.f) / side);
+    c[1] = static_cast<int>(fmax_ref(hd.y, 0.f) / side);
+    c[2] = static_cast<int>(fmax_ref(hd.z, 0.f) / side);
+  }
+  static size_t hash_combine(size_t a, size_t b) {
+    return a ^ (b + 0x9e3779b97f4a7c15ull + (a << 6) + (a >> 2));
+  }
+  size_t entry(int x, int y, int z) const {
+    const size_t low3 = ((x & 1) << 0) | ((y & 1) << 1) | ((z & 2) << 0);
+    size_t h = (size_t)x; /* std::hash<int> */
+    h = hash_combine(h, (size_t)y);
+    h = hash_combine(h, (size_t)z);
+    return ((h << 3) % entries.size()) | low3;
+  }
+  void add_vp(int pix, V3 pos, float r) {
+    int lo[3], hi[3];
+    cell(pos - mk(r, r, r), lo);
+    cell(pos + mk(r, r, r), hi);
+    for (int z = lo[2]; z < hi[2]; ++z)
+      for (int y = lo[1]; y < hi[1]; ++y)
+        for (int x = lo[0]; x < hi[0]; ++x) entries[entry(x, y, z)].push_back(pix);
+  }
+};
+
+/* AddPhoton (photon_mapping.h:101-120) */
+void add_photon(const Scene& s, VpGrid& g, std::vector<SppmPixel>& px, V3 pos,
+                V3 phi, V3 wr) {
+  int c[3];
+  g.cell(pos, c);
+  const std::vector<int>& list = g.entries[g.entry(c[0], c[1], c[2])];
+  for (auto it = list.rbegin(); it != list.rend(); ++it) {
+    SppmPixel& p = px[*it];
+    const V3 d = p.vp.pos - pos;
+    if (dot(d, d) > p.radius * p.radius) continue;
+    const Bsdf f(s.mats[p.vp.mat], p.vp.ng, p.vp.ns);
+    const V3 dp = phi * f.eval(wr, p.vp.wr);
+    if (!(std::isfinite(dp.x) && std::isfinite(dp.y) && std::isfinite(dp.z)))
+      continue;
+    p.phi[0] += dp.x;
+    p.phi[1] += dp.y;
+    p.phi[2] += dp.z;
+    ++p.M;
+  }
+}
+
+struct Emit {
+  V3 pos, dir, normal, radiance;
+  float pdf_pos = 0.f, pdf_dir = 0.f;
+};
+
+/* Light::SampleEmit: directional_light.cpp:60-79, env_light.cpp:105-150,
+ * area_light.cpp:59-70 */
+Emit sample_emit(const Scene& s, const Light& L, Rng& rng) {
+  Emit e;
+  const V3 center = box_center(s.world);
+  if (L.type == ORC_LIGHT_AREA) {
+    const float x = rng.next(), y = rng.next(), z = rng.next();
+    const GeomSample g = area_sample(s.areas[L.area], x, y, z);
+    const float u0 = rng.next(), u1 = rng.next();
+    float pdf_dir;
+    const V3 lwi = cosine_hemisphere(u0, u1, &pdf_dir);
+    e.pos = g.pos;
+    e.dir = Frame(g.ng).to_world(lwi);
+    e.normal = g.ng;
+    e.radiance = s.areas[L.area].rad;
+    e.pdf_pos = g.pdf;
+    e.pdf_dir = pdf_dir;
+  } else if (L.type == ORC_LIGHT_DIRECTIONAL) {
+    const float u0 = rng.next(), u1 = rng.next();
+    const V3 r2l = L.frame.to_world(uniform_cone(u0, u1, L.cosmax));
+    const float pdf_dir = uniform_cone_pdf(L.cosmax);
+    const float radius = s.radius;
+    const float d0 = rng.next(), d1 = rng.next();
+    float dx, dy;
+    concentric(d0, d1, &dx, &dy);
+    const Frame dc(r2l);
+    e.pos = center + (dx * dc.dx + dy * dc.dy + r2l) * radius;
+    e.dir = -r2l;
+    e.normal = normalized(-r2l);
+    e.radiance = L.rgb;
+    e.pdf_pos = 1.f / (kPi * radius * radius);
+    e.pdf_dir = pdf_dir;
+  } else {
+    float v = rng.next(), u = rng.next(); /* g++: right to left */
+    if (!L.env_ok) return Emit{};
+    float pdf = 1.f;
+    constexpr float inv_2_pi = 1.f / (2.f * kPi);
+    constexpr float two_pi = 2.f * kPi;
+    u -= L.rot / 180 * kPi * inv_2_pi;
+    if (u > 1.f) u -= 1.f;
+    if (u < 0.f) u += 1.f;
+    const float phi = u * two_pi;
+    const float theta = v * kPi;
+    const float st = std::sin(theta);
+    pdf = st != 0.f ? pdf / (2.f * kPi * kPi * st) : 0.f;
+    V3 dir = mk(-std::sin(theta) * std::cos(phi), std::cos(theta),
+                -std::sin(theta) * std::sin(phi));
+    dir = -dir;
+    const float radius = s.radius;
+    const float d0 = rng.next(), d1 = rng.next();
+    float dx, dy;
+    concentric(d0, d1, &dx, &dy);
+    const Frame dc(-dir);
+    e.pos = center + (dx * dc.dx + dy * dc.dy - dir) * radius;
+    e.dir = dir;
+    e.normal = normalized(dir);
+    e.radiance = L.rgb; /* the texel, without the scaler */
+    e.pdf_pos = 1.f / (kPi * radius * radius);
+    e.pdf_dir = pdf;
+  }
+  return e;
+}
+
+/* TracerPhoton (sppm.cpp:103-143); DefaultScene::SampleLight's uniform
+ * Distribution (default_scene.cpp:48-53, 77-86) */
+void tracer_photon(const Scene& s, const std::vector<float>& cdf, float lpdf,
+                   int min_d, int max_d, float cont, VpGrid& g,
+                   std::vector<SppmPixel>& px, Rng& rng) {
+  const int n = (int)s.lights.size();
+  if (n == 0) return;
+  const float u = rng.next();
+  int j = 0;
+  while (j < (int)cdf.size() && !(u <= cdf[j])) ++j; /* upper_bound, <= */
+  const int idx = std::min(std::max(j - 1, 0), n - 1);
+  const Emit e = sample_emit(s, s.lights[idx], rng);
+  if (is_black(e.radiance) || e.pdf_dir == 0.f || e.pdf_pos == 0.f) return;
+  V3 coef = e.radiance * std::fabs(dot(e.normal, e.dir)) /
+            (lpdf * e.pdf_pos * e.pdf_dir);
+  Ray ray = make_ray(e.pos, e.dir);
+  for (int depth = 1; depth <= max_d; ++depth) {
+    if (depth > min_d) {
+      if (rng.next() > cont) return;
+      coef = coef / cont;
+    }
+    Hit h = trace_closest(s.acc, ray, s.mode, true);
+    if (h.prim < 0) return;
+    HitInfo hi = complete_hit(s, ray, h);
+    if (depth > 1) add_photon(s, g, px, hi.pos, coef, hi.wr);
+    Bsdf f(s.mats[hi.mat], hi.ng, hi.ns);
+    float a = rng.next(), b = rng.next(), c = rng.next();
+    Sample bs = f.sample(hi.wr, mk(a, b, c));
+    if (is_black(bs.f) || bs.pdf < 0.f) return;
+    coef = coef * (bs.f / bs.pdf * std::fabs(dot(hi.ng, bs.dir)));
+    ray = make_ray(eps_offset(hi, bs.dir), bs.dir);
+  }
+}
+
+/* UpdatePixel (sppm.cpp:145-169) */
+void update_pixel(float alpha, SppmPixel& p) {
+  if (p.M > 0) {
+    const float new_N = p.N + alpha * p.M;
+    const float new_R = p.radius * std::sqrt(new_N / (p.N + p.M));
+    const V3 phi = mk(p.phi[0], p.phi[1], p.phi[2]);
+    p.tau = (p.tau + p.vp.thr * phi) * (new_R * new_R) / (p.radius * p.radius);
+    p.N = new_N;
+    p.radius = new_R;
+    p.M = 0;
+    p.phi[0] = p.phi[1] = p.phi[2] = 0.f;
+  }
+  p.vp.thr = mk(0, 0, 0);
+  p.vp.valid = false;
+}
+
 /* ThinLensCamera::GenerateRay (thin_lens.cpp:62-83) */
 inline void mat_vec(const float* M, const float v[4], float out[4]) {
   for (int row = 0; row < 4; ++row) {
@@ -1956,6 +2211,7 @@ void* orc_scene_create(const float* tris, const float* corner_n,
     if (s.lights.back().type == ORC_LIGHT_ENV) s.env = (int)s.lights.size() - 1;
   }
   Box wb = world_box(world);
+  s.world = wb;
   s.radius = length(wb.hi - box_center(wb));
   s.mode = tri_test;
   return o;
@@ -2021,6 +2277,103 @@ int orc_scene_render(void* h, const float* camera, const double* params,
           o[3] += spp;
         }
     }
+  }
+  return 0;
+}
+
+/* SPPMRenderer::Render (sppm.cpp:180-296) with the counter sampler: the
+ * camera pass reseeds every pixel each iteration (the same visible points
+ * every iteration, as in the reference), photon i of iteration k draws from
+ * path_key(photon_seed(seed), i, k).  Serial.  params[8]: iterations,
+ * photons per iteration, forward_max_depth, photon_min_depth,
+ * photon_max_depth, photon_cont_prob, init_radius (< 0: the world
+ * diagonal / 1000), update_alpha.  out_rad [H][W][3]; out_film [H][W][4]
+ * the footprint sums (weight 1 per pixel). */
+int orc_scene_sppm(void* h, const float* camera, const double* params,
+                   uint64_t seed, float* out_rad, double* out_film) {
+  const Scene& s = static_cast<OrcScene*>(h)->s;
+  const int iters = (int)params[0], photons = (int)params[1];
+  const int fmd = (int)params[2], pmin = (int)params[3], pmax = (int)params[4];
+  const float cont = (float)params[5], alpha = (float)params[7];
+  const int W = (int)camera[34], H = (int)camera[35];
+  Box world = s.world;
+  float init_radius = (float)params[6];
+  if (init_radius < 0) init_radius = length(world.hi - world.lo) / 1000.f;
+  world.lo = world.lo - mk(init_radius, init_radius, init_radius);
+  world.hi = world.hi + mk(init_radius, init_radius, init_radius);
+  std::vector<SppmPixel> px((size_t)W * H);
+  for (auto& p : px) p.radius = init_radius;
+  /* the scene's light selector */
+  const int nl = (int)s.lights.size();
+  std::vector<float> table(nl, 1.f), cdf(nl + 1, 0.f);
+  float lpdf = 0.f;
+  if (nl) {
+    float sum = 0.f;
+    for (float t : table) sum += t;
+    const float ratio = 1.f / sum;
+    for (float& t : table) t *= ratio;
+    const float inv = 1.f / float(nl);
+    for (int i = 1; i <= nl; ++i) cdf[i] = cdf[i - 1] + table[i - 1] * inv;
+    const float fi = cdf[nl];
+    if (fi > 0.f)
+      for (float& c : cdf) c /= fi;
+    else
+      for (int i = 0; i <= nl; ++i) cdf[i] = float(i) / float(nl);
+    lpdf = table[0];
+  }
+  const uint64_t pseed = ajg_photon_seed(seed);
+  float max_radius = init_radius;
+  for (int it = 0; it < iters; ++it) {
+    VpGrid g(world, 1.05f * max_radius);
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const int p = y * W + x;
+        Rng rng{path_key(seed, (uint32_t)p, 0)};
+        const float u = x + rng.next();
+        const float v = y + rng.next();
+        const float l0 = rng.next(), l1 = rng.next();
+        Ray ray = camera_ray(camera, u, v, l0, l1);
+        px[p].vp = tracer_vp(s, ray, rng, fmd, px[p].direct);
+        if (px[p].vp.valid) g.add_vp(p, px[p].vp.pos, px[p].radius);
+      }
+    for (int i = 0; i < photons; ++i) {
+      Rng rng{path_key(pseed, (uint32_t)i, (uint32_t)it)};
+      tracer_photon(s, cdf, lpdf, pmin, pmax, cont, g, px, rng);
+    }
+    max_radius = 0.f;
+    for (auto& p : px)
+      if (p.vp.valid) max_radius = fmax_ref(max_radius, p.radius);
+    if (max_radius == 0.f) max_radius = init_radius;
+    for (auto& p : px)
+      if (p.vp.valid) update_pixel(alpha, p);
+  }
+  /* ComputePixelRadiance (sppm.cpp:171-180) */
+  const uint64_t photon_n = uint64_t(iters) * uint64_t(photons);
+  std::vector<V3> rad(px.size());
+  for (size_t i = 0; i < px.size(); ++i) {
+    const V3 d = px[i].direct / float(iters);
+    const float dem = photon_n * kPi * px[i].radius * px[i].radius;
+    rad[i] = d + px[i].tau / dem;
+    if (out_rad) {
+      out_rad[3 * i] = rad[i].x;
+      out_rad[3 * i + 1] = rad[i].y;
+      out_rad[3 * i + 2] = rad[i].z;
+    }
+  }
+  if (out_film) {
+    for (int64_t i = 0; i < 4 * (int64_t)W * H; ++i) out_film[i] = 0.0;
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x)
+        for (int dy = -1; dy <= 0; ++dy)
+          for (int dx = -1; dx <= 0; ++dx) {
+            const int tx = std::max(0, x + dx), ty = std::max(0, y + dy);
+            double* o = out_film + 4 * ((int64_t)ty * W + tx);
+            const V3& r = rad[(size_t)y * W + x];
+            o[0] += r.x;
+            o[1] += r.y;
+            o[2] += r.z;
+            o[3] += 1.0;
+          }
   }
   return 0;
 }

@@ -65,6 +65,14 @@ enum { ORC_LIGHT_DIRECTIONAL = 0, ORC_LIGHT_ENV = 1, ORC_LIGHT_AREA = 2 };
 enum { ORC_GEOM_QUAD = 0, ORC_GEOM_CUBE = 1, ORC_GEOM_MESH = 2 };
 enum { ORC_TEST_MT = 0, ORC_TEST_WATERTIGHT = 1 };
 
+/* SPPMRenderer::Render restated (sppm.cpp:180-296) over a scene of
+ * orc_scene_create; see ajg_oracle.cpp for the sampler streams.
+ * params[8]: iterations, photons per iteration, forward_max_depth,
+ * photon_min_depth, photon_max_depth, photon_cont_prob, init_radius,
+ * update_alpha.  out_rad [H][W][3] (may be NULL), out_film [H][W][4]. */
+int orc_scene_sppm(void* scene, const float* camera, const double* params,
+                   uint64_t seed, float* out_rad, double* out_film);
+
 /* Fresnel::computeDiffuseFresnel(ior, n) (bsdf/helper.h:58-73): the
  * hemispherical integral PlasticBsdf divides the albedo by. */
 float orc_diffuse_fresnel(float ior, int n);

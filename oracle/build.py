@@ -56,6 +56,7 @@ def build_oracle(force: bool = False) -> Path:
 REF_TUS = [
     "ajisai/core/aggregate/ploc_aggregate.cpp",
     "ajisai/core/renderer/pt.cpp",
+    "ajisai/core/renderer/sppm.cpp",
     "ajisai/core/material/disney.cpp",
     "ajisai/core/material/diffuse.cpp",
     "ajisai/core/material/mirror.cpp",

@@ -31,3 +31,9 @@ static inline float ajg_key_float(uint64_t key, uint32_t dim) {
   memcpy(&f, &b, 4);
   return f - 1.0f;
 }
+
+/* SPPM photon streams: photon i of iteration k draws from
+ * ajg_path_key(ajg_photon_seed(seed), i, k). */
+static inline uint64_t ajg_photon_seed(uint64_t seed) {
+  return ajg_mix64(seed ^ 0x50484F544F4E5321ull);
+}

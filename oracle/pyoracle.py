@@ -56,6 +56,9 @@ def lib():
         L.orc_scene_render.argtypes = [C.c_void_p, _f32p, _f64p, C.c_uint64,
                                        C.c_int64, C.c_int64, C.c_void_p,
                                        C.c_void_p, C.c_int]
+        L.orc_scene_sppm.argtypes = [C.c_void_p, _f32p, _f64p, C.c_uint64,
+                                     C.c_void_p, C.c_void_p]
+        L.orc_scene_sppm.restype = C.c_int
         L.orc_scene_build_seconds.argtypes = [C.c_void_p]
         L.orc_scene_build_seconds.restype = C.c_double
         L.orc_scene_destroy.argtypes = [C.c_void_p]
@@ -95,6 +98,18 @@ class OracleScene:
         if not self.h:
             raise RuntimeError("orc_scene_create failed")
         self.build_seconds = lib().orc_scene_build_seconds(self.h)
+
+    def sppm(self, camera, params, seed=0):
+        """SPPMRenderer::Render restated: (radiance [H, W, 3], film
+        [H, W, 4] float64)."""
+        cam = _c(camera, np.float32)
+        W, H = int(cam[34]), int(cam[35])
+        rad = np.zeros((H, W, 3), np.float32)
+        film = np.zeros((H, W, 4), np.float64)
+        rc = lib().orc_scene_sppm(self.h, cam, sppm_param_array(params), seed,
+                                  rad.ctypes.data, film.ctypes.data)
+        assert rc == 0
+        return rad, film
 
     def render(self, camera, params, seed=0, pixel_range=None, per_sample=False,
                threads=None):
@@ -248,6 +263,10 @@ def ref():
                                        _f32p]
         L.ref_scene_render.restype = C.c_int
         L.ref_camera_rays.argtypes = [C.c_void_p, _f32p, C.c_int64, _f32p]
+        L.ref_has_diffuse.argtypes = [_f32p]
+        L.ref_has_diffuse.restype = C.c_int
+        L.ref_sppm_render.argtypes = [C.c_void_p, _f64p, C.c_uint64, _f32p, _f32p]
+        L.ref_sppm_render.restype = C.c_int
         _ref = L
     return _ref
 
@@ -378,6 +397,18 @@ class RefScene:
         assert rc == 0
         return li, film
 
+    def sppm(self, params, seed=0):
+        """SPPMRenderer::Render over the reference's own SPPM functions (see
+        ref_sppm_render): (radiance [H, W, 3], film [H, W, 4])."""
+        cam = self.scene.camera
+        W, H = cam.width, cam.height
+        p = sppm_param_array(params)
+        rad = np.zeros((H, W, 3), np.float32)
+        film = np.zeros((H, W, 4), np.float32)
+        rc = ref().ref_sppm_render(self.h, p, seed, rad, film)
+        assert rc == 0
+        return rad, film
+
     def camera_rays(self, raster):
         raster = _c(raster, np.float32).reshape(-1, 4)
         out = np.zeros((raster.shape[0], 6), np.float32)
@@ -390,3 +421,22 @@ def ref_bsdf(material, ng, ns, wo, wi, sam, op):
     ref().ref_bsdf(*(_c(x, np.float32) for x in (material, ng, ns, wo, wi, sam)),
                    int(op), out)
     return out
+
+
+SPPM_DEFAULTS = dict(iterations=100, photons_per_iteration=100000,
+                     forward_max_depth=8, photon_min_depth=5, photon_max_depth=10,
+                     photon_cont_prob=0.9, init_radius=0.1, update_alpha=2.0 / 3)
+
+
+def sppm_param_array(params):
+    """SPPMRendererArgs (core/renderer/renderer.h:82-96) as [8] float64, the
+    YAML creator's defaults (renderer_creators.cpp:57-76) filling gaps."""
+    q = dict(SPPM_DEFAULTS, **params)
+    return np.array([q["iterations"], q["photons_per_iteration"],
+                     q["forward_max_depth"], q["photon_min_depth"],
+                     q["photon_max_depth"], q["photon_cont_prob"],
+                     q["init_radius"], q["update_alpha"]], np.float64)
+
+
+def ref_has_diffuse(material):
+    return bool(ref().ref_has_diffuse(_c(material, np.float32)))

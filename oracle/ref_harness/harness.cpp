@@ -58,6 +58,7 @@
 #include <ajisai/core/material/material.h>
 #include <ajisai/core/medium/medium.h>
 #include <ajisai/core/primitive/primitive.h>
+#include <ajisai/core/renderer/photon_mapping.h>
 #include <ajisai/core/ray.h>
 #include <ajisai/core/renderer/renderer.h>
 #include <ajisai/core/sampler/sampler.h>
@@ -243,6 +244,19 @@ struct HScene {
 };
 
 }  // namespace
+
+// sppm.cpp's free functions (external linkage in the reference)
+namespace aj {
+sppm::VisiblePoint TracerVP(int forward_max_depth, const Scene* scene,
+                            const Ray& r, Sampler* sampler,
+                            Spectrum& direct_illum, MemoryArena& arena);
+void TracerPhoton(int min_depth, int max_depth, float cont_prob,
+                  sppm::VisiblePointSearcher& vp_searcher, const Scene* scene,
+                  Sampler* sampler, MemoryArena& arena);
+void UpdatePixel(float alpha, sppm::Pixel& pixel);
+Spectrum ComputePixelRadiance(int iter_count, uint64_t photon_N,
+                              const sppm::Pixel& pixel);
+}  // namespace aj
 
 extern "C" {
 
@@ -562,6 +576,109 @@ void ref_camera_rays(void* h, const float* raster, int64_t n, float* rays) {
       rays[6 * i + 3 + k] = r.d[k];
     }
   }
+}
+
+/* Material::Shade then BSDF::HasDiffuseComponent (SPPM's visible-point
+ * rule, sppm.cpp:77). */
+int ref_has_diffuse(const float* mat) {
+  auto m = make_material(mat);
+  MemoryArena arena;
+  PrimitiveIntersection inct{};
+  inct.geometry_normal = Vector3f{0.f, 0.f, 1.f};
+  inct.shading_normal = Vector3f{0.f, 0.f, 1.f};
+  auto sp = m->Shade(inct, arena);
+  return sp.bsdf->HasDiffuseComponent() ? 1 : 0;
+}
+
+/* SPPMRenderer::Render (sppm.cpp:180-296) driven serially over the
+ * reference's own TracerVP, TracerPhoton, VisiblePointSearcher, UpdatePixel
+ * and ComputePixelRadiance, with the counter sampler: the camera pass
+ * reseeds every pixel each iteration (SetSeed(x + y * W), as the reference
+ * does, so every iteration sees the same visible points), and photon i of
+ * iteration k draws from its own stream (ajg_path_key(ajg_photon_seed(seed),
+ * i, k)) -- the reference hands every photon the render's one shared
+ * sampler from all pool threads (sppm.cpp:275-279).
+ * params[8]: iterations, photons per iteration, forward_max_depth,
+ * photon_min_depth, photon_max_depth, photon_cont_prob, init_radius,
+ * update_alpha.  out_rad [H][W][3]: ComputePixelRadiance; out_film
+ * [H][W][4]: the one full-image tile merged as ref_scene_render does. */
+int ref_sppm_render(void* h, const double* params, uint64_t seed,
+                    float* out_rad, float* out_film) {
+  auto* s = static_cast<HScene*>(h);
+  if (!s->camera) return -1;
+  const int iters = (int)params[0], photons = (int)params[1];
+  const int fmd = (int)params[2], pmin = (int)params[3], pmax = (int)params[4];
+  const float cont = (float)params[5], alpha = (float)params[7];
+  const int W = s->width, H = s->height;
+  const Scene* scene = s->scene.get();
+  auto world = scene->WorldBound();
+  float init_radius = (float)params[6];
+  if (init_radius < 0)
+    init_radius = (world.max() - world.min()).length() / 1000.f;
+  world.min() -= Vector3f{init_radius};
+  world.max() += Vector3f{init_radius};
+  std::vector<sppm::Pixel> px((size_t)W * H);
+  for (auto& p : px) p.radius = init_radius;
+  float max_radius = init_radius;
+  MemoryArena arena;
+  for (int it = 0; it < iters; ++it) {
+    const float side = 1.05f * max_radius;
+    sppm::VisiblePointSearcher vps(world, side, 40960);
+    arena.Release();
+    for (int ty = 0; ty < (H + 63) / 64; ++ty)
+      for (int tx = 0; tx < (W + 63) / 64; ++tx)
+        for (int y = 64 * ty; y < std::min(H, 64 * ty + 64); ++y)
+          for (int x = 64 * tx; x < std::min(W, 64 * tx + 64); ++x) {
+            CounterSampler cs;
+            cs.seed = seed;
+            cs.SetSeed(x + y * W);
+            const float u = x + cs.Next1D();
+            const float v = y + cs.Next1D();
+            auto ray = s->camera->GenerateRay(Vector2f{u, v}, cs.Next2D());
+            sppm::Pixel& p = px[(size_t)y * W + x];
+            p.vp = TracerVP(fmd, scene, ray, &cs, p.direct_illum, arena);
+            if (p.vp.IsValid()) vps.AddVp(p, arena);
+          }
+    for (int i = 0; i < photons; ++i) {
+      CounterSampler ps;
+      ps.seed = ajg_photon_seed(seed);
+      ps.pixel = (uint32_t)i;
+      ps.Begin((uint32_t)it);
+      TracerPhoton(pmin, pmax, cont, vps, scene, &ps, arena);
+    }
+    max_radius = 0.f;
+    for (auto& p : px)
+      if (p.vp.IsValid()) max_radius = std::max(max_radius, p.radius);
+    if (max_radius == 0.f) max_radius = init_radius;
+    for (auto& p : px)
+      if (p.vp.IsValid()) UpdatePixel(alpha, p);
+  }
+  const uint64_t photon_count = uint64_t(iters) * uint64_t(photons);
+  auto film = s->camera->CreateFilm();
+  auto tile = film->GetTile(Bounds2i{Vector2i{0, 0}, Vector2i{W, H}});
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const Spectrum r = ComputePixelRadiance(iters, photon_count,
+                                              px[(size_t)y * W + x]);
+      float* o = out_rad + 3 * ((int64_t)y * W + x);
+      o[0] = r[0];
+      o[1] = r[1];
+      o[2] = r[2];
+      tile.AddSample(Vector2i{x, y}, r, 1.f);
+    }
+  for (int64_t i = 0; i < 4 * (int64_t)W * H; ++i) out_film[i] = 0.f;
+  const auto lo = tile.bounds.min(), hi = tile.bounds.max();
+  for (int y = lo.y(); y < hi.y(); ++y)
+    for (int x = lo.x(); x < hi.x(); ++x) {
+      auto pix = tile(Vector2i{x, y});
+      int cx = std::clamp(x, 0, W - 1), cy = std::clamp(y, 0, H - 1);
+      float* o = out_film + 4 * ((int64_t)cy * W + cx);
+      o[0] += pix.radiance[0];
+      o[1] += pix.radiance[1];
+      o[2] += pix.radiance[2];
+      o[3] += pix.weight;
+    }
+  return 0;
 }
 
 }  // extern "C"

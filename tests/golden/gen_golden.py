@@ -16,6 +16,7 @@ functions, and stores what the reference computes:
   render_*.npz   per-sample radiance of PathTracing::TraceMIS driven by the
                  counter sampler, and the merged film
   camera.npz     ThinLensCamera::GenerateRay rays
+  sppm_*.npz     SPPMRenderer's radiance and film (ref_sppm_render)
 
 Every input is seeded; the fixtures are small enough to commit.
 """
@@ -245,6 +246,40 @@ def gen_render():
              li=li, film=film)
 
 
+SPPM_PARAMS = dict(iterations=4, photons_per_iteration=20000, forward_max_depth=6,
+                   photon_min_depth=3, photon_max_depth=8, photon_cont_prob=0.9,
+                   init_radius=0.03, update_alpha=2.0 / 3)
+
+
+def sppm_scenes():
+    """The SPPM fixtures' scenes: the Cornell box; the emitter box without its
+    emissive mesh (whose straddling sampler windows make NaN samples); the
+    material box with a Disney box in place of the metal one (the
+    reference's SPPM faults on metal: AggregateBSDF::HasDiffuseComponent
+    runs off its end, aggregate_bsdf.cpp:37-41)."""
+    area = S.cornell_area(64, 64)
+    area.primitives[9].emission = None
+    mats = S.material_box(64, 64)
+    mats.materials[5] = S.Disney((0.9, 0.7, 0.4), metallic=0.6, roughness=0.3)
+    return [("sppm_cornell.npz", S.cornell_box(64, 64)), ("sppm_area.npz", area),
+            ("sppm_materials.npz", mats)]
+
+
+def gen_sppm():
+    """SPPMRenderer's result (per-pixel radiance and film) from the
+    reference's own TracerVP / TracerPhoton / VisiblePointSearcher /
+    UpdatePixel / ComputePixelRadiance, driven by ref_sppm_render."""
+    for name, sc in sppm_scenes():
+        rs = O.RefScene(sc, search_radius=14)
+        fl = rs.dump()
+        rad, film = rs.sppm(SPPM_PARAMS, seed=5)
+        save(name, tris=fl.tris, corner_n=fl.corner_n, tri_mat=fl.tri_mat,
+             tri_flags=fl.tri_flags, world=fl.world, materials=fl.materials,
+             lights=fl.lights, camera=fl.camera, seed=np.uint64(5),
+             emit_rad=fl.emit_rad, emit_info=fl.emit_info,
+             params=O.sppm_param_array(SPPM_PARAMS), rad=rad, film=film)
+
+
 def gen_camera():
     rng = np.random.default_rng(14)
     out = {}
@@ -272,4 +307,5 @@ if __name__ == "__main__":
     gen_bsdf()
     gen_bsdf_more()
     gen_render()
+    gen_sppm()
     gen_camera()
