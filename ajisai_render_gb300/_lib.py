@@ -58,6 +58,14 @@ class Emitter(C.Structure):
                 ("two_sided", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class SppmParams(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("photons_per_iteration", C.c_uint32),
+                ("forward_max_depth", C.c_int32), ("photon_min_depth", C.c_int32),
+                ("photon_max_depth", C.c_int32), ("photon_cont_prob", C.c_float),
+                ("init_radius", C.c_float), ("update_alpha", C.c_float),
+                ("seed", C.c_uint64)]
+
+
 class SceneOpts(C.Structure):
     _fields_ = [("search_radius", C.c_uint32), ("tri_test", C.c_uint32),
                 ("radix_compat", C.c_uint32), ("bvh_width", C.c_uint32)]
@@ -155,6 +163,8 @@ SIGNATURES = {
     "ajg_bsdf_query": ([_P, _P, _P, _P, _P, _P, _P, _P, C.c_uint64, _P], C.c_int),
     "ajg_camera_rays": ([_P, C.POINTER(Camera), _P, C.c_uint64, _P], C.c_int),
     "ajg_render": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P], C.c_int),
+    "ajg_render_sppm": ([_P, C.POINTER(Camera), C.POINTER(SppmParams), _P, _P],
+                        C.c_int),
     "ajg_render_device": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P, _P],
                           C.c_int),
     "ajg_render_static": ([_P, C.POINTER(Camera), C.POINTER(RenderParams), _P, _P],

@@ -353,6 +353,64 @@ class PTRenderer:
         return out
 
 
+@dataclass
+class SPPMRendererArgs:
+    """SPPMRendererArgs (core/renderer/renderer.h:82-96) with the defaults of
+    the YAML creator (factory/creator/renderer_creators.cpp:57-76)."""
+    forward_max_depth: int = 8
+    init_radius: float = 0.1
+    iteration_count: int = 100
+    photons_per_iteration: int = 100000
+    photon_min_depth: int = 5
+    photon_max_depth: int = 10
+    photon_cont_prob: float = 0.9
+    update_alpha: float = 2.0 / 3
+
+
+class SPPMRenderer:
+    """SPPMRenderer::Render (core/renderer/sppm.cpp:180-296), on the GPU."""
+
+    def __init__(self, args: SPPMRendererArgs, seed: int = 0):
+        self.args = args
+        self.seed = seed
+
+    def params(self) -> _lib.SppmParams:
+        a = self.args
+        return _lib.SppmParams(a.iteration_count, a.photons_per_iteration,
+                               a.forward_max_depth, a.photon_min_depth,
+                               a.photon_max_depth, a.photon_cont_prob,
+                               a.init_radius, a.update_alpha, self.seed)
+
+    def _run(self, scene: GpuScene, camera, film, radiance):
+        cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+        cam = camera_struct(cam36)
+        p = self.params()
+        scene.ctx.check(scene.ctx.lib.ajg_render_sppm(
+            scene.h, C.byref(cam), C.byref(p),
+            _ptr(film.rgbw) if film is not None else None,
+            _ptr(radiance) if radiance is not None else None))
+        return cam
+
+    def Render(self, scene: GpuScene, camera, film: Film | None = None) -> Film:
+        cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+        cam = camera_struct(cam36)
+        film = film or Film(cam.width, cam.height)
+        self._run(scene, cam36, film, None)
+        return film
+
+    def RenderRadiance(self, scene: GpuScene, camera) -> np.ndarray:
+        """ComputePixelRadiance per pixel [h, w, 3] (parity checks)."""
+        cam36 = camera if isinstance(camera, np.ndarray) else camera.pack()
+        cam = camera_struct(cam36)
+        out = np.zeros((cam.height, cam.width, 3), F32)
+        self._run(scene, cam36, None, out)
+        return out
+
+
+def CreateSPPMRenderer(args: SPPMRendererArgs, seed: int = 0) -> SPPMRenderer:
+    return SPPMRenderer(args, seed)
+
+
 def CreatePTRenderer(args: PTRendererArgs, seed: int = 0) -> PTRenderer:
     return PTRenderer(args, seed)
 

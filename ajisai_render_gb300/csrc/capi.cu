@@ -867,6 +867,37 @@ int ajg_render(ajg_scene* s, const ajg_camera* cam,
   return check_device(ctx);
 }
 
+int ajg_render_sppm(ajg_scene* s, const ajg_camera* cam,
+                    const ajg_sppm_params* params, float* out_rgbw,
+                    float* out_radiance) {
+  if (!s || !cam || !params) return AJG_ERR_INVALID;
+  ajg_ctx* ctx = s->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const uint64_t npix = (uint64_t)cam->width * cam->height;
+  DevBuf<float4> d;
+  DevBuf<float> r;
+  if (out_rgbw) CK(d.alloc(npix, st), "render_sppm: alloc");
+  if (out_radiance) CK(r.alloc(3 * npix, st), "render_sppm: alloc");
+  int rc = sppm_render(s, *cam, *params, out_rgbw ? d.p : nullptr,
+                       out_radiance ? r.p : nullptr, st);
+  if (rc) {
+    cudaStreamSynchronize(st);
+    return rc;
+  }
+  if (out_rgbw)
+    CK(cudaMemcpyAsync(out_rgbw, d.p, npix * sizeof(float4),
+                       cudaMemcpyDeviceToHost, st),
+       "render_sppm: copy out");
+  if (out_radiance)
+    CK(cudaMemcpyAsync(out_radiance, r.p, 3 * npix * sizeof(float),
+                       cudaMemcpyDeviceToHost, st),
+       "render_sppm: copy out");
+  CK(cudaStreamSynchronize(st), "render_sppm");
+  return check_device(ctx);
+}
+
 int ajg_render_device(ajg_scene* s, const ajg_camera* cam,
                       const ajg_render_params* params, float* d_out_rgbw,
                       void* stream) {

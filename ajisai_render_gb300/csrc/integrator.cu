@@ -53,6 +53,7 @@ struct WaveArgs {
   ajg_camera cam;
   JobParams j;
   uint32_t pix0, S, s0, n_paths;
+  VisPointD* vp;  // SPPM camera pass: the visible points (else null)
 };
 
 // Where a kernel finds the job and the scene of a path: the kernel
@@ -656,9 +657,34 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
       }
     }
 
+    // SPPM's camera pass ends a path at its first diffuse surface or its
+    // last bounce with a visible point (sppm.cpp:77-92)
+    bool vp_here = false;
+    if constexpr (!MJ) {
+      if (a.vp && hit) {
+        bool diffuse;
+        if (MAT == AJG_MAT_DIFFUSE)
+          diffuse = true;
+        else if (MAT == AJG_MAT_DISNEY)
+          diffuse = f.m[5] < 1.f;  // DisneyBSDF: metallic < 1
+        else
+          diffuse = (int)f.m[0] == AJG_MAT_PLASTIC;
+        vp_here = diffuse || b == J.max_b - 1;
+        if (vp_here && isfinite(T.x) && isfinite(T.y) && isfinite(T.z)) {
+          VisPointD v;
+          v.pos = make_float4(hi.pos.x, hi.pos.y, hi.pos.z,
+                              __uint_as_float(hi.mat));
+          v.wr = make_float4(hi.wr.x, hi.wr.y, hi.wr.z, 0.f);
+          v.thr = make_float4(T.x, T.y, T.z, 0.f);
+          v.ng = make_float4(hi.ng.x, hi.ng.y, hi.ng.z, 0.f);
+          v.ns = make_float4(hi.ns.x, hi.ns.y, hi.ns.z, 0.f);
+          a.vp[a.pix0 + p / a.S] = v;
+        }
+      }
+    }
     bool alive = false;
     F3 nro = mk3(0, 0, 0), nrd = mk3(0, 0, 1);
-    if (hit && b + 1 < J.max_b) {
+    if (hit && !vp_here && b + 1 < J.max_b) {
       const F3 sam = mk3(key_float(key, dim), key_float(key, dim + 1),
                          key_float(key, dim + 2));
       const BsdfSample bs = f.sample(hi.wr, sam);
@@ -857,6 +883,14 @@ int fail(ajg_ctx* ctx, int code, const std::string& m) {
   return code;
 }
 
+// SPPM's camera pass: each pixel's direct light (one path per pixel).
+__global__ void k_copy_direct(WaveArgs a, const float4* __restrict__ rad,
+                              float4* __restrict__ direct) {
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n_paths;
+       p += gridDim.x * blockDim.x)
+    direct[a.pix0 + p] = rad[p];
+}
+
 template <class T>
 T* carve(char*& cur, uint64_t count) {
   T* p = reinterpret_cast<T*>(cur);
@@ -864,8 +898,8 @@ T* carve(char*& cur, uint64_t count) {
   return p;
 }
 
-// Blocks of `fn` (launched with `threads` threads) that are resident on the
-// device at once: the grid of a persistent kernel.
+}  // namespace
+
 int resident_grid(const void* fn, int threads) {
   static std::mutex mu;
   static std::map<std::pair<const void*, int>, int> cache;
@@ -885,8 +919,6 @@ int resident_grid(const void* fn, int threads) {
   cache[key] = g;
   return g;
 }
-
-}  // namespace
 
 uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   const uint64_t slots = P * nt;
@@ -1005,7 +1037,8 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
                       const ajg_render_params& prm, const WaveBufs& w,
                       uint64_t P, float4* fsum, float4* fcomp, double* fsum64,
                       float4* d_out, uint64_t li_begin, uint64_t li_end,
-                      float* d_li, cudaStream_t st, bool timers) {
+                      float* d_li, cudaStream_t st, bool timers,
+                      VisPointD* vp = nullptr, float4* d_direct = nullptr) {
   ajg_ctx* ctx = sc->ctx;
   const DeviceScene& s = sc->d;
   const int nt = (int)s.num_lights + 1;
@@ -1020,6 +1053,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   a.s = s;
   a.cam = cam;
   a.j = make_job_params(sc, cam, prm);
+  a.vp = vp;
 
   const uint64_t pb = d_li ? li_begin : 0;
   const uint64_t pe = d_li ? li_end : npix_all;
@@ -1141,6 +1175,11 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       if (d_li)
         k_copy_li<<<grid_for(a.n_paths, 256, gs), 256, 0, st>>>(
             a, w.rad, li_begin, prm.spp, d_li);
+      if (d_direct) {
+        KernelTimer{ctx, st, -1};
+        k_copy_direct<<<grid_for(a.n_paths, 256, gs), 256, 0, st>>>(
+            a, w.rad, d_direct);
+      }
     }
   }
   if (want_film) {
@@ -1308,6 +1347,34 @@ int render_in_scratch(ajg_scene* sc, const ajg_camera& cam,
   const WaveBufs w = carve_wave(scratch + film_bytes, P, nt, false);
   run_waves(sc, cam, prm, w, P, fsum, fcomp, fsum64, d_out, 0, 0, nullptr, st,
             false);
+  return AJG_OK;
+}
+
+int sppm_camera_pass(ajg_scene* sc, const ajg_camera& cam, int fmd,
+                     uint64_t seed, VisPointD* vp, float4* direct,
+                     cudaStream_t st) {
+  ajg_ctx* ctx = sc->ctx;
+  // TracerVP is TraceMIS without roulette that stops at a visible point:
+  // min = max bounces = fmd, sample 0 of each pixel (SetSeed(x + y W))
+  ajg_render_params prm{};
+  prm.spp = 1;
+  prm.min_bounces = fmd;
+  prm.max_bounces = fmd;
+  prm.cont_prob = 1.f;
+  prm.use_mis = 1;
+  prm.seed = seed;
+  int rc = check_render(ctx, sc->d, cam, prm);
+  if (rc) return rc;
+  const int nt = (int)sc->d.num_lights + 1;
+  const uint64_t P = ctx->wave_paths;
+  char* base = nullptr;
+  rc = ensure_arena(ctx, P, nt, &base);
+  if (rc) return rc;
+  const WaveBufs w = carve_wave(base, P, nt, false);
+  const uint64_t npix = (uint64_t)cam.width * cam.height;
+  cudaMemsetAsync(vp, 0xff, npix * sizeof(VisPointD), st);
+  run_waves(sc, cam, prm, w, P, nullptr, nullptr, nullptr, nullptr, 0, 0,
+            nullptr, st, false, vp, direct);
   return AJG_OK;
 }
 

@@ -914,6 +914,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
                                                 : CwLayout<4>::kFloat4)
                                : 32u * (uint32_t)wn);
   s->info.bvh_nodes = num_nodes;
+  for (int k = 0; k < 6; ++k) s->world[k] = world[k];
   // lights are fitted to the world bounds (default_scene.cpp:41-48)
   const F3 center = (whi + wlo) / 2.f;
   const F3 half = whi - center;

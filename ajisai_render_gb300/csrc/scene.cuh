@@ -78,6 +78,14 @@ struct JobParams {
   uint32_t x0, y0, win_w, win_h;
 };
 
+// SPPM's visible point (TracerVP's result, sppm.cpp:77-92): the hit, its
+// throughput and what EvalAll needs there; pos.w carries the material
+// index bits, 0xffffffff for a pixel without one.
+struct VisPointD {
+  float4 pos, wr, thr, ng, ns;
+};
+constexpr uint32_t kNoVisPoint = 0xffffffffu;
+
 // Device record of a job in a multi-job wave.
 struct JobRec {
   JobParams j;
@@ -234,6 +242,7 @@ struct ajg_scene {
   std::atomic<int> jobs{0};  // unfinished jobs of the request loop
   std::vector<float> host_lights;
   std::vector<float> host_materials;
+  float world[6] = {0, 0, 0, 0, 0, 0};  // the primitives' joined bounds
 };
 
 namespace ajg {
@@ -281,6 +290,20 @@ inline int mj_wave_kernels(int bounces, bool emit) {
 // Looks up the persistent grids of the multi-job kernels (call before a
 // stream capture).
 void prepare_mj_kernels();
+// Blocks of `fn` (launched with `threads` threads) resident on the device at
+// once: the grid of a persistent kernel.
+int resident_grid(const void* fn, int threads);
+// SPPM's camera pass (TracerVP, sppm.cpp:35-101) through the path-tracing
+// wave: one path per pixel (sample 0), no roulette, depth `fmd`; fills
+// vp[npix] (kNoVisPoint where none) and the direct light direct[npix].
+int sppm_camera_pass(ajg_scene* sc, const ajg_camera& cam, int fmd,
+                     uint64_t seed, VisPointD* vp, float4* direct,
+                     cudaStream_t st);
+// SPPMRenderer::Render on `st`: the footprint film (d_out, [h][w] float4, or
+// null) and ComputePixelRadiance per pixel (d_rad, [h][w][3], or null).
+int sppm_render(ajg_scene* sc, const ajg_camera& cam,
+                const ajg_sppm_params& p, float4* d_out, float* d_rad,
+                cudaStream_t st);
 // Resolves a window-sized film into (sum rgb, sum w) per target pixel.
 void enqueue_resolve(const float4* fsum, const float4* fcomp,
                      const double* fsum64, uint32_t w, uint32_t h,

@@ -34,6 +34,7 @@ static_assert(sizeof(ajg_serve_opts) == 16, "ajg_serve_opts layout");
 static_assert(sizeof(ajg_serve_stats) == 80, "ajg_serve_stats layout");
 static_assert(sizeof(ajg_scene_info) == 48, "ajg_scene_info layout");
 static_assert(sizeof(ajg_emitter) == 32, "ajg_emitter layout");
+static_assert(sizeof(ajg_sppm_params) == 40, "ajg_sppm_params layout");
 
 namespace ajg {
 namespace {

@@ -18,6 +18,7 @@
  *   ajg_render*          Renderer::Render          core/renderer/renderer.h:53-59
  *                        (TiledIntegrator::Render  core/renderer/pt.cpp:40-73 with
  *                         PathTracing::TraceMIS/Trace pt.cpp:98-311)
+ *   ajg_render_sppm      SPPMRenderer::Render      core/renderer/sppm.cpp:180-296
  *   ajg_submit/poll/...  (no counterpart: the request loop that keeps scenes
  *                         resident and batches jobs on one GPU)
  *
@@ -322,6 +323,30 @@ AJG_API int ajg_camera_rays(ajg_ctx* ctx, const ajg_camera* cam,
  * (film.cpp:27-63, film.h:119-129, image.h:38-42).  image = rgb / w. */
 AJG_API int ajg_render(ajg_scene* scene, const ajg_camera* cam,
                        const ajg_render_params* params, float* out_rgbw);
+/* ---- stochastic progressive photon mapping (SPPMRenderer) ------------ */
+/* SPPMRendererArgs (core/renderer/renderer.h:82-96) and the sampler seed. */
+typedef struct ajg_sppm_params {
+  uint32_t iterations;            /* iteration_count (100) */
+  uint32_t photons_per_iteration; /* 100000 */
+  int32_t forward_max_depth;      /* camera pass depth (8) */
+  int32_t photon_min_depth;       /* roulette after this depth (5) */
+  int32_t photon_max_depth;       /* 10 */
+  float photon_cont_prob;         /* 0.9 */
+  float init_radius;              /* 0.1; < 0: the world diagonal / 1000 */
+  float update_alpha;             /* 2/3 */
+  uint64_t seed;
+} ajg_sppm_params; /* 40 bytes */
+
+/* SPPMRenderer::Render (sppm.cpp:180-296), blocking.  out_rgbw as
+ * ajg_render's (each pixel's radiance is one sample of weight 1);
+ * out_radiance [h][w][3] ComputePixelRadiance per pixel; either may be
+ * NULL.  The camera pass draws sample 0 of each pixel's counter stream every
+ * iteration (the reference reseeds each pixel every iteration); photon i of
+ * iteration k draws from its own stream. */
+AJG_API int ajg_render_sppm(ajg_scene* scene, const ajg_camera* cam,
+                            const ajg_sppm_params* params, float* out_rgbw,
+                            float* out_radiance);
+
 /* Same into device memory (float [h][w][4]), asynchronous on `stream`. */
 AJG_API int ajg_render_device(ajg_scene* scene, const ajg_camera* cam,
                               const ajg_render_params* params,

@@ -51,6 +51,7 @@ def test_struct_layouts_match_header(lib):
     assert C.sizeof(_lib.MeshDesc) == 40
     assert C.sizeof(_lib.RenderParams) == 32
     assert C.sizeof(_lib.Emitter) == 32
+    assert C.sizeof(_lib.SppmParams) == 40
 
 
 def test_null_arguments_are_rejected_without_a_gpu(lib):

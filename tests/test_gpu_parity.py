@@ -537,3 +537,61 @@ def test_materials_match_oracle_per_sample(ctx, use_mis):
             api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, bvh_width=width)),
             flat.camera)
         assert same_bits(li, b)
+
+
+# ------------------------------------------------------------------ SPPM --
+def sppm_args(p):
+    return api.SPPMRendererArgs(forward_max_depth=int(p[2]), init_radius=float(p[6]),
+                                iteration_count=int(p[0]),
+                                photons_per_iteration=int(p[1]),
+                                photon_min_depth=int(p[3]), photon_max_depth=int(p[4]),
+                                photon_cont_prob=float(p[5]), update_alpha=float(p[7]))
+
+
+def sppm_close(rad, ref):
+    """Per pixel within 1e-3 on >= 97% of pixels (a photon whose path a
+    last-ulp difference of a transcendental turns elsewhere moves the few
+    pixels it lands in; deposits are summed atomically), image means within
+    0.5%."""
+    close = np.isclose(rad, ref, rtol=1e-3, atol=1e-5).all(-1)
+    assert close.mean() > 0.97, close.mean()
+    np.testing.assert_allclose(rad.mean((0, 1)), ref.mean((0, 1)), rtol=5e-3)
+
+
+@pytest.mark.parametrize("case", ["sppm_cornell.npz", "sppm_area.npz",
+                                  "sppm_materials.npz"])
+def test_sppm_matches_reference(ctx, golden, case):
+    g = golden(case)
+    flat = flat_of(g)
+    sc = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, 0, True))
+    r = api.SPPMRenderer(sppm_args(g["params"]), seed=int(g["seed"]))
+    rad = r.RenderRadiance(sc, flat.camera)
+    assert np.isfinite(rad).all()
+    sppm_close(rad, g["rad"])
+    film = r.Render(sc, flat.camera)
+    assert np.array_equal(film.rgbw[..., 3], g["film"][..., 3])
+    np.testing.assert_allclose(film.rgbw[..., :3].mean((0, 1)),
+                               g["film"][..., :3].mean((0, 1)), rtol=5e-3)
+
+
+def test_sppm_matches_oracle_and_is_stable(ctx):
+    """More photons and iterations and other depths against the oracle;
+    every tree layout gives the same radiance up to the order of the atomic
+    sums."""
+    spec = S.cornell_area(64, 64)
+    spec.primitives[9].emission = None
+    flat = S.flatten(spec)
+    args = api.SPPMRendererArgs(forward_max_depth=5, init_radius=0.025,
+                                iteration_count=6, photons_per_iteration=50000,
+                                photon_min_depth=2, photon_max_depth=7)
+    r = api.SPPMRenderer(args, seed=9)
+    rad = r.RenderRadiance(api.GpuScene(ctx, flat), flat.camera)
+    osc = O.OracleScene(flat, search_radius=14)
+    ref, _ = osc.sppm(flat.camera, dict(iterations=6, photons_per_iteration=50000,
+                                        forward_max_depth=5, photon_min_depth=2,
+                                        photon_max_depth=7, init_radius=0.025), seed=9)
+    sppm_close(rad, ref)
+    for width in (2, 0x108):
+        b = r.RenderRadiance(api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, bvh_width=width)),
+                             flat.camera)
+        np.testing.assert_allclose(b, rad, rtol=1e-4, atol=1e-6)
