@@ -194,7 +194,9 @@ class HostSceneView(C.Structure):
                 ("opts", SceneOpts), ("camera", Camera), ("params", RenderParams),
                 ("num_outputs", C.c_uint32), ("num_emitters", C.c_uint32),
                 ("outputs", C.POINTER(C.c_char_p)),
-                ("emitters", C.POINTER(Emitter))]
+                ("emitters", C.POINTER(Emitter)),
+                ("renderer", C.c_uint32), ("reserved", C.c_uint32),
+                ("sppm", SppmParams)]
 
 
 HOST_LIB_PATH = HERE / "_build" / "libajisai_host.so"

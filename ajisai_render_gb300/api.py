@@ -485,7 +485,7 @@ class SceneFile:
     save_to_img post processors name."""
     flat: FlatScene
     camera: np.ndarray
-    args: PTRendererArgs
+    args: "PTRendererArgs | SPPMRendererArgs"
     seed: int
     aggregate: AggregateOptions
     outputs: list
@@ -536,9 +536,17 @@ def load_scene_file(path) -> SceneFile:
             world=np.array(v.world, F32), materials=mats, lights=lights, camera=cam,
             emit_rad=emit_rad, emit_info=emit_info)
         p = v.params
-        args = PTRendererArgs(spp=p.spp, min_bounces=p.min_bounces,
-                              max_bounces=p.max_bounces, cont_prob=p.cont_prob,
-                              use_mis=bool(p.use_mis))
+        if v.renderer == 1:  # sppm
+            q = v.sppm
+            args = SPPMRendererArgs(q.forward_max_depth, q.init_radius, q.iterations,
+                                    q.photons_per_iteration, q.photon_min_depth,
+                                    q.photon_max_depth, q.photon_cont_prob,
+                                    q.update_alpha)
+            p.seed = q.seed
+        else:
+            args = PTRendererArgs(spp=p.spp, min_bounces=p.min_bounces,
+                                  max_bounces=p.max_bounces, cont_prob=p.cont_prob,
+                                  use_mis=bool(p.use_mis))
         agg = AggregateOptions(v.opts.search_radius, v.opts.tri_test,
                                bool(v.opts.radix_compat), v.opts.bvh_width)
         outs = [v.outputs[i].decode() for i in range(v.num_outputs)]

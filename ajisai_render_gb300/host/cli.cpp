@@ -1,6 +1,6 @@
 // ajisai_gpu: the reference's command line (app/main.cpp: `-s scene.yaml`)
 // over the GPU path: read the scene file, build the scene (PLOC on the
-// GPU), render with the file's renderer settings, run its save_to_img
+// GPU), render with the file's renderer (pt or sppm), run its save_to_img
 // post processors.
 //
 //   ajisai_gpu -s scene.yaml [--device N] [--out image.pfm] [--spp N]
@@ -82,7 +82,7 @@ int main(int argc, char** argv) {
   }
   for (const std::string& n : f.notes) std::fprintf(stderr, "note: %s\n", n.c_str());
   if (spp > 0) f.params.spp = (uint32_t)spp;
-  if (seed >= 0) f.params.seed = (uint64_t)seed;
+  if (seed >= 0) f.params.seed = f.sppm.seed = (uint64_t)seed;
 
   ajg_config cfg{device, 0, 0};
   ajg_ctx* ctx = nullptr;
@@ -100,18 +100,29 @@ int main(int argc, char** argv) {
   }
   const auto t1 = std::chrono::steady_clock::now();
   std::vector<float> rgbw(4ull * f.camera.width * f.camera.height);
-  rc = ajg_render(scene, &f.camera, &f.params, rgbw.data());
+  rc = f.is_sppm ? ajg_render_sppm(scene, &f.camera, &f.sppm, rgbw.data(), nullptr)
+                 : ajg_render(scene, &f.camera, &f.params, rgbw.data());
   const auto t2 = std::chrono::steady_clock::now();
   int status = check(rc, ctx, "render") ? 1 : 0;
   if (!status) {
     const double build_s = std::chrono::duration<double>(t1 - t0).count();
     const double render_s = std::chrono::duration<double>(t2 - t1).count();
-    const double samples =
-        (double)f.camera.width * f.camera.height * f.params.spp;
-    std::printf("%zu triangles, %ux%u, %u spp: scene %.3f s, render %.3f s "
-                "(%.1f Msamples/s)\n",
-                f.tri_material.size(), f.camera.width, f.camera.height,
-                f.params.spp, build_s, render_s, samples / render_s / 1e6);
+    if (f.is_sppm) {
+      const double photons =
+          (double)f.sppm.iterations * f.sppm.photons_per_iteration;
+      std::printf("%zu triangles, %ux%u, sppm %u x %u photons: scene %.3f s, "
+                  "render %.3f s (%.1f Mphotons/s)\n",
+                  f.tri_material.size(), f.camera.width, f.camera.height,
+                  f.sppm.iterations, f.sppm.photons_per_iteration, build_s,
+                  render_s, photons / render_s / 1e6);
+    } else {
+      const double samples =
+          (double)f.camera.width * f.camera.height * f.params.spp;
+      std::printf("%zu triangles, %ux%u, %u spp: scene %.3f s, render %.3f s "
+                  "(%.1f Msamples/s)\n",
+                  f.tri_material.size(), f.camera.width, f.camera.height,
+                  f.params.spp, build_s, render_s, samples / render_s / 1e6);
+    }
     std::vector<std::string> files = f.outputs;
     for (std::string& o : files)
       if (o.size() > 4 && o.compare(o.size() - 4, 4, ".jpg") == 0)

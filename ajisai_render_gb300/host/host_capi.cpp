@@ -64,6 +64,8 @@ int ajh_scene_view_get(const ajh_scene* s, ajh_scene_view* v) {
   v->outputs = s->out_ptrs.data();
   v->num_emitters = (uint32_t)f.emitters.size();
   v->emitters = f.emitters.data();
+  v->renderer = f.is_sppm ? AJH_RENDERER_SPPM : AJH_RENDERER_PT;
+  v->sppm = f.sppm;
   return 0;
 }
 

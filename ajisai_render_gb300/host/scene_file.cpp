@@ -488,6 +488,7 @@ SceneFile LoadSceneFile(const std::string& path) {
   std::memset(out.world, 0, sizeof(out.world));
   std::memset(&out.opts, 0, sizeof(out.opts));
   std::memset(&out.params, 0, sizeof(out.params));
+  std::memset(&out.sppm, 0, sizeof(out.sppm));
 
   // ---- scene
   const Node& scene = root["scene"];
@@ -588,10 +589,24 @@ SceneFile LoadSceneFile(const std::string& path) {
   const Node& rn = root["renderer"];
   if (!rn.IsDefined()) fail(path, root, "no 'renderer' node");
   out.renderer = rn["type"].AsString("");
-  if (out.renderer != "pt" && out.renderer != "pt_gpu")
-    fail(path, rn, "renderer '" + out.renderer + "' is not on this path (pt "
-                   "and pt_gpu are)");
-  out.params.spp = (uint32_t)rn["spp"].AsInt();
+  if (out.renderer == "sppm" || out.renderer == "sppm_gpu") {
+    // SPPMCreatorImpl (renderer_creators.cpp:55-76)
+    ajg_sppm_params& q = out.sppm;
+    q.forward_max_depth = (int32_t)rn["forward_max_depth"].AsInt(8);
+    q.init_radius = rn["init_radius"].AsFloat(0.1f);
+    q.iterations = (uint32_t)rn["iteration_count"].AsInt(100);
+    q.photons_per_iteration = (uint32_t)rn["photons_per_iteration"].AsInt(100000);
+    q.photon_min_depth = (int32_t)rn["photon_min_depth"].AsInt(5);
+    q.photon_max_depth = (int32_t)rn["photon_max_depth"].AsInt(10);
+    q.photon_cont_prob = rn["photon_cont_prob"].AsFloat(0.9f);
+    q.update_alpha = rn["update_alpha"].AsFloat(2.f / 3);
+    q.seed = (uint64_t)rn["seed"].AsInt(0);
+    out.is_sppm = true;
+  } else if (out.renderer != "pt" && out.renderer != "pt_gpu") {
+    fail(path, rn, "renderer '" + out.renderer + "' is not on this path (pt, "
+                   "pt_gpu, sppm and sppm_gpu are)");
+  }
+  out.params.spp = out.is_sppm ? 1u : (uint32_t)rn["spp"].AsInt();
   out.params.min_bounces = (int32_t)rn["min_bounces"].AsInt(5);
   out.params.max_bounces = (int32_t)rn["max_bounces"].AsInt(10);
   out.params.cont_prob = rn["cont_prob"].AsFloat(0.9f);

@@ -36,6 +36,8 @@ struct SceneFile {
   ajg_scene_opts opts;
   ajg_camera camera;
   ajg_render_params params;
+  ajg_sppm_params sppm;  // the sppm renderer's node
+  bool is_sppm = false;
   std::string renderer;
   std::vector<std::string> outputs;  // files save_to_img would write
   std::vector<std::string> notes;    // fallbacks taken

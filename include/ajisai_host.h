@@ -41,7 +41,12 @@ typedef struct ajh_scene_view {
   uint32_t num_emitters; /* emissive primitives (area lights) */
   const char* const* outputs;
   const ajg_emitter* emitters;
+  uint32_t renderer; /* AJH_RENDERER_* */
+  uint32_t reserved;
+  ajg_sppm_params sppm; /* AJH_RENDERER_SPPM: the renderer node */
 } ajh_scene_view;
+
+enum { AJH_RENDERER_PT = 0, AJH_RENDERER_SPPM = 1 };
 
 AJH_API int ajh_load_scene(const char* path, ajh_scene** out, char* err,
                            size_t err_len);

@@ -304,3 +304,53 @@ def test_command_line_renders_the_scene_file(tmp_path, name):
     finally:
         ctx.close()
     assert (tmp_path / "c.pfm").read_bytes() == (tmp_path / "py.pfm").read_bytes()
+
+
+def test_sppm_renderer_node(tmp_path):
+    """renderer: {type: sppm, ...} reads SPPMCreatorImpl's keys and defaults."""
+    src = (GOLDEN / "cornell_box.yaml").read_text()
+    i = src.index("renderer:")
+    j = src.index("post_processors:")
+    (tmp_path / "s.yaml").write_text(
+        src[:i] + "renderer: {type: sppm, iteration_count: 12, init_radius: 0.02,"
+        " photon_max_depth: 7}\n" + src[j:])
+    f = api.load_scene_file(tmp_path / "s.yaml")
+    assert isinstance(f.args, api.SPPMRendererArgs)
+    assert (f.args.iteration_count, f.args.photon_max_depth) == (12, 7)
+    assert f.args.init_radius == np.float32(0.02)
+    assert (f.args.forward_max_depth, f.args.photons_per_iteration,
+            f.args.photon_min_depth) == (8, 100000, 5)
+    assert f.args.update_alpha == np.float32(2.0 / 3)
+
+
+@pytest.mark.gpu
+def test_command_line_renders_sppm(tmp_path):
+    """ajisai_gpu with an sppm renderer node: the image agrees with the
+    Python API's SPPM render of the same file (deposits are summed
+    atomically, so to float tolerance)."""
+    from ajisai_render_gb300 import build
+    build.build()
+    build.build_host()
+    src = (GOLDEN / "cornell_box.yaml").read_text() \
+        .replace("resolution: [256, 256]", "resolution: [64, 64]")
+    i, j = src.index("renderer:"), src.index("post_processors:")
+    src = (src[:i] + "renderer: {type: sppm, iteration_count: 3,"
+           " photons_per_iteration: 20000, init_radius: 0.03, forward_max_depth: 6}\n"
+           + src[j:])
+    (tmp_path / "c.yaml").write_text(src.replace("filename: cornell.png",
+                                                 f"filename: {tmp_path / 'out.png'}"))
+    r = subprocess.run([str(build.CLI), "-s", str(tmp_path / "c.yaml"), "--out",
+                        str(tmp_path / "c.pfm"), "--seed", "4"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Mphotons/s" in r.stdout
+    f = api.load_scene_file(tmp_path / "c.yaml")
+    ctx = api.Context(0)
+    try:
+        sc = api.GpuScene(ctx, f.flat, f.aggregate)
+        film = api.SPPMRenderer(f.args, seed=4).Render(sc, f.camera)
+    finally:
+        ctx.close()
+    data = (tmp_path / "c.pfm").read_bytes()
+    cli = np.frombuffer(data[data.index(b"-1.0\n") + 5:], "<f4").reshape(64, 64, 3)[::-1]
+    np.testing.assert_allclose(cli, film.image(), rtol=1e-3, atol=1e-5)
