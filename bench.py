@@ -76,6 +76,9 @@ def parse():
                     help="paths in flight per wave (0: library default)")
     ap.add_argument("--batch-wave-paths", type=int, default=0,
                     help="paths per wave of the batched/served context (0: default)")
+    ap.add_argument("--no-sppm", action="store_true")
+    ap.add_argument("--sppm-iters", type=int, default=32)
+    ap.add_argument("--sppm-photons", type=int, default=4_000_000)
     ap.add_argument("--large", action="store_true",
                     help="also run the large-scene workload (26.2 M triangles, "
                          "1920x1080, 1024 spp, depth 32, FP64 crop reference)")
@@ -359,9 +362,11 @@ def run_ours(args):
     img = out.float().cpu().numpy()
     nonfinite = int((~np.isfinite(img)).any(-1).sum())
 
-    batched = served = large = None
+    batched = served = large = sppm = None
     if rank == 0 and world == 1 and args.large:
         large = run_large(args, local)
+    if rank == 0 and world == 1 and not args.no_sppm:
+        sppm = run_sppm(args, local)
     if rank == 0 and world == 1 and not args.no_batch:
         bctx = api.Context(local, wave_paths=args.batch_wave_paths,
                            hbm_budget_bytes=150 << 30)
@@ -393,7 +398,7 @@ def run_ours(args):
                 for kind in ("closest", "any")},
             "step_ms": step_ms, "nonfinite_pixels": nonfinite,
             "batched": batched, "served": served, "large": large,
-            "impl": "ours"}))
+            "sppm": sppm, "impl": "ours"}))
     scene.release()
     ctx.close()
     if dist:
@@ -612,6 +617,65 @@ def run_large(args, local):
                 "scene_generation_s": gen_s}
     finally:
         ctx.close()
+
+
+SPPM_RES = 512
+
+
+def run_sppm(args, local):
+    """SPPM on the single-job scene: the photon throughput of ajg_render_sppm
+    (camera pass, grid builds, photon wavefronts, updates, the film copy)
+    over a render of --sppm-iters x --sppm-photons, and the oracle's SPPM
+    timed on a bounded sample of the same scene (one iteration)."""
+    from ajisai_render_gb300 import api
+    from oracle import pyoracle as O
+    flat = workload_scene(SPPM_RES)
+    ctx = api.Context(local)
+    try:
+        scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
+        sargs = api.SPPMRendererArgs(forward_max_depth=8, init_radius=0.01,
+                                     iteration_count=args.sppm_iters,
+                                     photons_per_iteration=args.sppm_photons,
+                                     photon_min_depth=5, photon_max_depth=10)
+        warm = api.SPPMRendererArgs(forward_max_depth=8, init_radius=0.01,
+                                    iteration_count=1, photons_per_iteration=100000)
+        api.SPPMRenderer(warm, seed=1).Render(scene, flat.camera)
+        t = time.perf_counter()
+        film = api.SPPMRenderer(sargs, seed=2).Render(scene, flat.camera)
+        dt = time.perf_counter() - t
+        photons = args.sppm_iters * args.sppm_photons
+        img = film.image()
+    finally:
+        ctx.close()
+    out = {"workload": f"SPPM on the single-job scene (1,310,722 triangles), "
+                       f"{SPPM_RES}x{SPPM_RES}, {args.sppm_iters} iterations x "
+                       f"{args.sppm_photons:,} photons, photon depth 10 (roulette "
+                       "after 5), camera depth 8, initial radius 0.01",
+           "mphotons_s": photons / dt / 1e6, "render_s": dt,
+           "nonfinite_pixels": int((~np.isfinite(img)).any(-1).sum()),
+           "mean_radiance": float(np.nanmean(img))}
+    if args.no_cpu:
+        return out
+    # the CPU baseline: the oracle's serial SPPM, one iteration of a photon
+    # count sized to the time budget, on a smaller film of the same scene
+    small = workload_scene(64)
+    sc = O.OracleScene(small, RADIUS)
+    params = dict(iterations=1, photons_per_iteration=20000, forward_max_depth=8,
+                  init_radius=0.01, photon_min_depth=5, photon_max_depth=10)
+    t = time.perf_counter()
+    sc.sppm(small.camera, params, seed=1)
+    per = time.perf_counter() - t
+    n = int(min(50_000_000, max(20000, 20000 * args.cpu_seconds / max(per, 1e-6))))
+    params["photons_per_iteration"] = n
+    t = time.perf_counter()
+    sc.sppm(small.camera, params, seed=1)
+    cdt = time.perf_counter() - t
+    sc.close()
+    out["cpu_baseline"] = {"value": n / cdt / 1e6, "unit": "Mphotons/s", "cores": 1,
+                           "kind": "port",
+                           "sample": f"oracle SPPM (serial), 64x64 film of the same scene, "
+                                     f"1 iteration x {n:,} photons, {cdt:.2f} s"}
+    return out
 
 
 def i_seed(k, res, spp):
