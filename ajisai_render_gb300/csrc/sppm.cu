@@ -76,6 +76,8 @@ struct Grid {
   uint32_t* offsets;  // [kEntries + 1]
   uint32_t* cursor;   // [kEntries]
   uint32_t* items;    // pixel indices, entry by entry
+  float4* spheres;    // per item: the visible point and radius^2, so the
+                      // distance test of a deposit reads one 16-byte record
   uint32_t cap;
   const float* maxr;  // this iteration's max radius (the cell side / 1.05)
 };
@@ -177,7 +179,10 @@ __global__ void k_grid_fill(SppmArgs a, SppmPixels px, Grid g,
             raise_device_error(err, kDevQueueOverflow);
             continue;
           }
+          const float4 p4 = px.vp[i].pos;
+          const float r = px.radius[i];
           g.items[slot] = i;
+          g.spheres[slot] = make_float4(p4.x, p4.y, p4.z, r * r);
         }
   }
 }
@@ -368,11 +373,11 @@ __device__ void add_photon(const SppmArgs& a, const SppmPixels& px,
   const uint32_t e = to_entry(c[0], c[1], c[2]);
   const uint32_t end = min(g.offsets[e + 1], g.cap);
   for (uint32_t j = g.offsets[e]; j < end; ++j) {
+    const float4 sp = __ldg(&g.spheres[j]);
+    const F3 d = xyz(sp) - pos;
+    if (dot3(d, d) > sp.w) continue;
     const uint32_t i = g.items[j];
     const VisPointD v = px.vp[i];
-    const F3 d = xyz(v.pos) - pos;
-    const float r = px.radius[i];
-    if (dot3(d, d) > r * r) continue;
     const Bsdf f = bsdf_at(a.s, __float_as_uint(v.pos.w), xyz(v.ng), xyz(v.ns));
     const F3 dp = phi * f.eval(wr, xyz(v.wr));
     if (!(isfinite(dp.x) && isfinite(dp.y) && isfinite(dp.z))) continue;
@@ -573,6 +578,7 @@ int sppm_render(ajg_scene* sc, const ajg_camera& cam, const ajg_sppm_params& p,
   Dev<float4> direct, phi, tau, film;
   Dev<float> radius, N, maxr;
   Dev<uint32_t> M, counts, offsets, cursor, items, bits;
+  Dev<float4> spheres;
   const uint32_t cap = (uint32_t)std::min<uint64_t>(8 * npix, 0xffffffffull);
   cudaError_t e = cudaSuccess;
   auto A = [&](cudaError_t r) {
@@ -591,6 +597,7 @@ int sppm_render(ajg_scene* sc, const ajg_camera& cam, const ajg_sppm_params& p,
   A(offsets.alloc(kEntries + 1, st));
   A(cursor.alloc(kEntries, st));
   A(items.alloc(cap, st));
+  A(spheres.alloc(cap, st));
   A(bits.alloc(1, st));
   // the photon queue, in chunks of at most the context's wave size
   const uint64_t chunk = std::max<uint64_t>(
@@ -618,7 +625,7 @@ int sppm_render(ajg_scene* sc, const ajg_camera& cam, const ajg_sppm_params& p,
   k_fill_f<<<grid_for(npix, 256, gs), 256, 0, st>>>(radius.p, npix, init_radius);
   k_fill_f<<<1, 32, 0, st>>>(maxr.p, 1, init_radius);
   const SppmPixels px{vp.p, direct.p, radius.p, N.p, M.p, phi.p, tau.p};
-  const Grid g{counts.p, offsets.p, cursor.p, items.p, cap, maxr.p};
+  const Grid g{counts.p, offsets.p, cursor.p, items.p, spheres.p, cap, maxr.p};
   PhotonQ q{};
   q.ro[0] = qro.p;
   q.ro[1] = qro.p + chunk;

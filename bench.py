@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--batch-wave-paths", type=int, default=0,
                     help="paths per wave of the batched/served context (0: default)")
     ap.add_argument("--no-sppm", action="store_true")
+    ap.add_argument("--only-sppm", action="store_true",
+                    help="run the SPPM section alone (one JSON line)")
     ap.add_argument("--sppm-iters", type=int, default=32)
     ap.add_argument("--sppm-photons", type=int, default=4_000_000)
     ap.add_argument("--large", action="store_true",
@@ -630,7 +632,7 @@ def run_sppm(args, local):
     from ajisai_render_gb300 import api
     from oracle import pyoracle as O
     flat = workload_scene(SPPM_RES)
-    ctx = api.Context(local)
+    ctx = api.Context(local, wave_paths=args.wave_paths)
     try:
         scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS))
         sargs = api.SPPMRendererArgs(forward_max_depth=8, init_radius=0.01,
@@ -686,6 +688,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_sppm:
+        # the SPPM section alone (profiling runs)
+        print(json.dumps({"sppm": run_sppm(args, int(os.environ.get("LOCAL_RANK", "0")))}))
     else:
         run_ours(args)
 
