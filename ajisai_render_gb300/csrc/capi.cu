@@ -3,6 +3,7 @@
 // context's stream under the context mutex, and turns CUDA or device-guard
 // failures into a status code plus a message for ajg_last_error().
 #include <cfloat>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -251,7 +252,15 @@ int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
   if (cfg && cfg->wave_paths) ctx->wave_paths = cfg->wave_paths;
   if (ctx->wave_paths < 1024) ctx->wave_paths = 1024;
   if (cfg) ctx->hbm_budget = cfg->hbm_budget_bytes;
+  if (const char* ov = std::getenv("AJG_TRACE_OVERLAP"))
+    ctx->overlap = std::strcmp(ov, "0") != 0;
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) !=
+          cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->trace_stream, cudaStreamNonBlocking) !=
+          cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_queue, cudaEventDisableTiming) !=
+          cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_hits, cudaEventDisableTiming) !=
           cudaSuccess ||
       cudaMalloc(&ctx->d_error, sizeof(uint32_t)) != cudaSuccess ||
       cudaMalloc(&ctx->d_fetch, sizeof(uint32_t)) != cudaSuccess ||
@@ -278,6 +287,10 @@ int ajg_destroy_context(ajg_ctx* ctx) {
   cudaFree(ctx->d_error);
   cudaFree(ctx->d_fetch);
   cudaFree(ctx->d_counters);
+  cudaStreamSynchronize(ctx->trace_stream);
+  cudaEventDestroy(ctx->ev_queue);
+  cudaEventDestroy(ctx->ev_hits);
+  cudaStreamDestroy(ctx->trace_stream);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return AJG_OK;

@@ -933,6 +933,7 @@ uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   add(P * 16); add(P * 16);    // ro
   add(P * 16); add(P * 16);    // rd
   add(P * sizeof(ajg_hit));
+  if (!mj) add(P * sizeof(ajg_hit));  // hits2
   add(slots * 16);             // term_f
   add(slots);                  // term_vis
   add(slots * 16); add(slots * 16);  // shadow queue
@@ -959,6 +960,7 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj) {
   w.rd[0] = carve<float4>(cur, P);
   w.rd[1] = carve<float4>(cur, P);
   w.hits = carve<ajg_hit>(cur, P);
+  if (!mj) w.hits2 = carve<ajg_hit>(cur, P);
   w.term_f = carve<float4>(cur, P * nt);
   w.term_vis = carve<uint8_t>(cur, P * nt);
   w.sq_o = carve<float4>(cur, P * nt);
@@ -984,6 +986,17 @@ static int ensure_arena(ajg_ctx* ctx, uint64_t P, int nt, char** base) {
   }
   *base = static_cast<char*>(ctx->arena[0].ptr);
   return AJG_OK;
+}
+
+// Paths per wave of a single-job render: the context's wave size, but no
+// more than the render needs (its paths, in whole KiB) and no more than
+// kArenaBytes of wave state for its light count.
+constexpr uint64_t kArenaBytes = 48ull << 30;
+static uint64_t job_wave_paths(const ajg_ctx* ctx, uint64_t needed, int nt) {
+  const uint64_t per_path = (wave_bytes(1u << 20, nt, false) >> 20) + 1;
+  uint64_t P = std::min<uint64_t>(ctx->wave_paths, (needed + 1023) / 1024 * 1024);
+  P = std::min<uint64_t>(P, kArenaBytes / per_path);
+  return std::max<uint64_t>(1024, P / 1024 * 1024);
 }
 
 int check_render(ajg_ctx* ctx, const DeviceScene& s, const ajg_camera& cam,
@@ -1063,15 +1076,30 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const uint32_t shadow_cap = (uint32_t)(P * nt);
   const int gs = kSMs * 8;
   // persistent traversal: resident blocks only
-  auto extend = [&](int q) {
+  auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
     dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
       const int g = resident_grid((const void*)k_extend<TT, false, WW>,
                                   kTraceThreads);
-      k_extend<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], w.hits,
+      k_extend<TT, false, WW><<<g, kTraceThreads, 0, es>>>(
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], hits,
           &ctx->d_counters[0], ctx->d_error);
     });
+  };
+  // Bounce b+1's closest hits run on the trace stream beside bounce b's
+  // shadow rays: the two persistent launches fill each other's drain.  The
+  // hits alternate between two buffers by bounce parity (k_accumulate of
+  // bounce b still reads its own); everything else bounce b+1 touches is
+  // written after k_accumulate of bounce b on the render stream.
+  const bool overlap = ctx->overlap && !ctx->profiling && w.hits2 != nullptr;
+  cudaStream_t ts = ctx->trace_stream;
+  auto extend_ahead = [&](int q, ajg_hit* hits) {
+    cudaEventRecord(ctx->ev_queue, st);
+    cudaStreamWaitEvent(ts, ctx->ev_queue, 0);
+    cudaMemsetAsync(&w.counts[8], 0, sizeof(uint32_t), ts);
+    KernelTimer tm(ctx, ts, kc);
+    extend(q, hits, ts);
+    cudaEventRecord(ctx->ev_hits, ts);
   };
   auto bsdf_closest = [&]() {
     dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
@@ -1108,43 +1136,54 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       k_raygen<false><<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads,
                         0, st>>>(a, t, w);
       int q = 0;
+      if (overlap && a.j.max_b > 0) extend_ahead(0, w.hits);
       for (int b = 0; b < a.j.max_b; ++b) {
+        WaveBufs wb = w;
+        if (overlap) {
+          wb.hits = (b & 1) ? w.hits2 : w.hits;
+          cudaStreamWaitEvent(st, ctx->ev_hits, 0);
+        }
         // next queue, shadow queue, fetch counters and material lists
         cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
-        cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
-        {
+        if (overlap) {
+          cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
+          cudaMemsetAsync(&w.counts[9], 0, 2 * sizeof(uint32_t), st);
+        } else {
+          cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
           KernelTimer tm(ctx, st, kc);
-          extend(q);
+          extend(q, w.hits, st);
         }
         {
           KernelTimer tm(ctx, st, -1);
           k_classify<false><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q],
-                                                w.hits, w.lists, &w.counts[4],
+                                                wb.hits, w.lists, &w.counts[4],
                                                 (uint32_t)P);
         }
         if ((b == 0 || !a.j.use_mis) && s.env >= 0) {
           KernelTimer tm(ctx, st, ks);
           k_shade_miss<false><<<gs, kShadeThreads, 0, st>>>(
-              a, t, w, b, q, w.lists, &w.counts[4]);
+              a, t, wb, b, q, w.lists, &w.counts[4]);
         }
         {
           KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DIFFUSE, false><<<gs, kShadeThreads, 0, st>>>(
-              a, t, w, b, q, w.lists + P, &w.counts[5], (uint32_t)nt,
+              a, t, wb, b, q, w.lists + P, &w.counts[5], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
         {
           KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DISNEY, false><<<gs, kShadeThreads, 0, st>>>(
-              a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)nt,
+              a, t, wb, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
         if (s.mat_mask >> AJG_MAT_MIRROR) {
           KernelTimer tm(ctx, st, ks);
           k_shade<kMatOther, false><<<gs, kShadeThreads, 0, st>>>(
-              a, t, w, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)nt,
+              a, t, wb, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
+        if (overlap && b + 1 < a.j.max_b)
+          extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2);
         if (a.j.use_mis) {
           {
             KernelTimer tm(ctx, st, ka);
@@ -1162,7 +1201,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
                 reinterpret_cast<const int32_t*>(w.lists + P));
           }
           KernelTimer{ctx, st, -1};
-          k_accumulate<false><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
+          k_accumulate<false><<<gs, kShadeThreads, 0, st>>>(a, t, wb, q,
                                                             (uint32_t)nt);
         }
         q ^= 1;
@@ -1282,8 +1321,9 @@ int render_impl(ajg_scene* sc, const ajg_camera& cam,
   int rc = check_render(ctx, s, cam, prm);
   if (rc) return rc;
   const int nt = (int)s.num_lights + 1;
-  const uint64_t P = ctx->wave_paths;
   const uint64_t npix_all = (uint64_t)cam.width * cam.height;
+  const uint64_t npix_job = d_li ? std::min(li_end, npix_all) - li_begin : npix_all;
+  const uint64_t P = job_wave_paths(ctx, npix_job * prm.spp, nt);
   char* base = nullptr;
   rc = ensure_arena(ctx, P, nt, &base);
   if (rc) return rc;
@@ -1366,12 +1406,12 @@ int sppm_camera_pass(ajg_scene* sc, const ajg_camera& cam, int fmd,
   int rc = check_render(ctx, sc->d, cam, prm);
   if (rc) return rc;
   const int nt = (int)sc->d.num_lights + 1;
-  const uint64_t P = ctx->wave_paths;
+  const uint64_t npix = (uint64_t)cam.width * cam.height;
+  const uint64_t P = job_wave_paths(ctx, npix, nt);
   char* base = nullptr;
   rc = ensure_arena(ctx, P, nt, &base);
   if (rc) return rc;
   const WaveBufs w = carve_wave(base, P, nt, false);
-  const uint64_t npix = (uint64_t)cam.width * cam.height;
   cudaMemsetAsync(vp, 0xff, npix * sizeof(VisPointD), st);
   run_waves(sc, cam, prm, w, P, nullptr, nullptr, nullptr, nullptr, 0, 0,
             nullptr, st, false, vp, direct);

@@ -126,6 +126,7 @@ struct WaveBufs {
   float4* ro[2];
   float4* rd[2];
   ajg_hit* hits;
+  ajg_hit* hits2;  // single-job waves: bounce parity 1's hits (overlap)
   // light terms: slot = path * NT + term (lights first, the MIS BSDF term
   // last at NT - 1)
   float4* term_f;
@@ -209,12 +210,20 @@ struct ajg_ctx {
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
   ajg::Server* server = nullptr;  // the request loop, started on first use
   std::mutex server_mu;
-  // paths in flight per wave: big enough that the persistent traversal
-  // launches are long against their drain (~10 GB of wave state)
-  uint32_t wave_paths = 1u << 25;
+  // paths in flight per single-job wave: big enough that the persistent
+  // traversal launches are long against their drain (a render takes no
+  // more than it needs, and at most 48 GB of wave state)
+  uint32_t wave_paths = 1u << 27;
   uint64_t hbm_budget = 0;
   uint64_t resident_bytes = 0;
   cudaStream_t stream = nullptr;
+  // single-job waves trace bounce b+1's closest hits on trace_stream while
+  // bounce b's shadow rays run on the render's stream (ev_queue: the next
+  // queue is written; ev_hits: its hits are); AJG_TRACE_OVERLAP=0 keeps one
+  // stream
+  cudaStream_t trace_stream = nullptr;
+  cudaEvent_t ev_queue = nullptr, ev_hits = nullptr;
+  bool overlap = true;
   std::mutex mu;
   std::string last_error;
   uint32_t* d_error = nullptr;            // device error flag

@@ -173,6 +173,12 @@ namespace {
 
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
+// The request loop's default wave (its arena counts against the HBM
+// admission budget): the context's wave size, at most 32 Mi paths.
+uint64_t serve_default_paths(const ajg_ctx* ctx) {
+  return std::min<uint64_t>(ctx->wave_paths, 1u << 25);
+}
+
 size_t tables_size() {
   return align256(sizeof(WaveHeader)) +
          align256(sizeof(DeviceScene) * kMaxWaveChunks) +
@@ -264,7 +270,7 @@ bool Server::admit_locked() {
     // the wave arena counts from the first admission on, allocated or not
     const uint64_t arena_need = std::max<uint64_t>(
         arena_bytes,
-        wave_bytes(want_P ? want_P : ctx->wave_paths,
+        wave_bytes(want_P ? want_P : serve_default_paths(ctx),
                    std::max(3, (int)j->jp.nl + 1), true));
     const uint64_t held =
         ctx->resident_bytes + arena_need + stats.active_bytes;
@@ -381,7 +387,7 @@ bool Server::plan_and_launch() {
   uint64_t target_P = 0;
   {
     std::lock_guard<std::mutex> lk(mu);
-    target_P = want_P ? want_P : ctx->wave_paths;
+    target_P = want_P ? want_P : serve_default_paths(ctx);
     for (Job* j : active) {
       if (j->cancel || j->s_cur >= j->prm.spp) continue;
       if (tri_test < 0) {

@@ -385,7 +385,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene, no dataset)",
             "config": {**config(args), "bvh_width": scene.info()["bvh_width"],
-                       "wave_paths": args.wave_paths or (1 << 22)},
+                       "wave_paths": args.wave_paths or (1 << 27),
+                       "trace_overlap": os.environ.get("AJG_TRACE_OVERLAP", "1") != "0"},
             "clocks": clk, "e2e": e2e, "roofline": roofline,
             "cpu_baseline": cpu, "gpu_launches": launches_timed,
             "ploc_build_ms": scene.info()["build_ms"],

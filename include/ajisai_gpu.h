@@ -80,8 +80,10 @@ typedef struct ajg_scene ajg_scene;
 
 typedef struct ajg_config {
   int32_t device;            /* CUDA device ordinal */
-  uint32_t wave_paths;       /* paths in flight per wave (0: default 32 Mi,
-                                ~10 GB of wave state) */
+  uint32_t wave_paths;       /* paths in flight per wave (0: default 128 Mi;
+                                a render takes no more than its own paths
+                                and at most 48 GB of wave state; the request
+                                loop's default is at most 32 Mi) */
   uint64_t hbm_budget_bytes; /* admission budget for resident scenes and
                                 films (0: no limit) */
 } ajg_config;
@@ -427,8 +429,9 @@ typedef struct ajg_serve_opts {
   uint32_t inflight_waves;  /* waves queued on the GPU ahead of the host
                                (0: 2) */
   uint32_t wave_paths;      /* paths per wave of the request loop (0: the
-                               context's); smaller waves deliver results
-                               sooner, bigger ones run faster */
+                               context's, at most 32 Mi); smaller waves
+                               deliver results sooner, bigger ones run
+                               faster */
 } ajg_serve_opts;
 
 typedef struct ajg_serve_stats {
