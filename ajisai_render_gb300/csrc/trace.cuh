@@ -190,10 +190,15 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 // nodes: the children's boxes as lo.x, hi.x, lo.y, hi.y, lo.z, hi.z groups
 // of four, then the child references); 4 or 8 | kBvhCompressed the
 // quantised wide nodes (scene.cuh).  In a wide node the leaf children whose
-// box passes are tested at once; for closest hits the nearest interior
-// child is visited next and the others are pushed farthest first.
+// box passes are gathered during the box tests and then tested in one loop
+// (one call site, so the lanes with an i-th leaf test it together); for
+// closest hits the nearest interior child is visited next and the others
+// are pushed farthest first.
 #ifndef AJG_REFILL
 #define AJG_REFILL 16
+#endif
+#ifndef AJG_LEAF_BATCH
+#define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
 constexpr int kRefill = AJG_REFILL;
 constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
@@ -307,6 +312,12 @@ __device__ __forceinline__ void trace_persistent(
       float tn[W];
       int ref[W];
       unsigned inner = 0;  // interior children whose box passed
+#if AJG_LEAF_BATCH
+      // leaf children whose box passed, tested after the box tests from
+      // one call site (all lanes with an i-th leaf test it together)
+      int leaf_slot[W];
+      int nleaf = 0;
+#endif
       if constexpr (!CMP) {
         constexpr int G = W / 4;  // float4 groups per plane
         const float4* nd = bvh + (uint64_t)node * (2 * W);
@@ -332,10 +343,14 @@ __device__ __forceinline__ void trace_persistent(
                            slab2(plx[j], phx[j], ply[j], phy[j], plz[j],
                                  phz[j], r, lim, t0);
             tn[c] = t0;
+#if AJG_LEAF_BATCH
+            if (h && ref[c] < 0) leaf_slot[nleaf++] = ~ref[c];
+#else
             if (h && ref[c] < 0 && !finished) {
               ++n_tris;
               finished = leaf_test<TEST, ANY>(tris, ~ref[c], r, w, hit);
             }
+#endif
             if (h && ref[c] >= 0) inner |= 1u << c;
           }
         }
@@ -384,13 +399,29 @@ __device__ __forceinline__ void trace_persistent(
           if ((imask >> c) & 1u) {
             ref[c] = (int)(cbase + __popc(imask & below));
             inner |= 1u << c;
-          } else if (!finished) {
-            ++n_tris;
-            finished = leaf_test<TEST, ANY>(
-                tris, (int)(tbase + __popc(lmask & below)), r, w, hit);
+          } else {
+#if AJG_LEAF_BATCH
+            leaf_slot[nleaf++] = (int)(tbase + __popc(lmask & below));
+#else
+            if (!finished) {
+              ++n_tris;
+              finished = leaf_test<TEST, ANY>(
+                  tris, (int)(tbase + __popc(lmask & below)), r, w, hit);
+            }
+#endif
           }
         }
       }
+#if AJG_LEAF_BATCH
+      for (int i = 0; i < nleaf && !finished; ++i) {
+        ++n_tris;
+        int slot = 0;
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          if (j == i) slot = leaf_slot[j];
+        finished = leaf_test<TEST, ANY>(tris, slot, r, w, hit);
+      }
+#endif
       if (!finished && inner && ANY) {
         // occlusion: any order will do -- visit the first, push the rest
         const int c0 = __ffs(inner) - 1;
