@@ -933,7 +933,7 @@ uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   add(P * 16); add(P * 16);    // ro
   add(P * 16); add(P * 16);    // rd
   add(P * sizeof(ajg_hit));
-  if (!mj) add(P * sizeof(ajg_hit));  // hits2
+  add(P * sizeof(ajg_hit));    // hits2
   add(slots * 16);             // term_f
   add(slots);                  // term_vis
   add(slots * 16); add(slots * 16);  // shadow queue
@@ -960,7 +960,7 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj) {
   w.rd[0] = carve<float4>(cur, P);
   w.rd[1] = carve<float4>(cur, P);
   w.hits = carve<ajg_hit>(cur, P);
-  if (!mj) w.hits2 = carve<ajg_hit>(cur, P);
+  w.hits2 = carve<ajg_hit>(cur, P);
   w.term_f = carve<float4>(cur, P * nt);
   w.term_vis = carve<uint8_t>(cur, P * nt);
   w.sq_o = carve<float4>(cur, P * nt);
@@ -1242,38 +1242,65 @@ void prepare_mj_kernels() {
 
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                      int NT, int bounces, int tri_test, int width, bool emit,
-                     TraceCounters* ctr, uint32_t* err, cudaStream_t st) {
+                     TraceCounters* ctr, uint32_t* err, cudaStream_t st,
+                     cudaStream_t ts, cudaEvent_t ev_queue,
+                     cudaEvent_t ev_hits) {
   const DeviceScene s{};
   WaveArgs a{};
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
-  cudaMemsetAsync(w.counts, 0, 64, st);
-  k_raygen<true><<<gs, kShadeThreads, 0, st>>>(a, t, w);
-  int q = 0;
-  for (int b = 0; b < bounces; ++b) {
-    cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
-    cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
+  auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
     dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
       const int g =
           resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
-      k_extend<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], w.hits, ctr,
-          err);
+      k_extend<TT, true, WW><<<g, kTraceThreads, 0, es>>>(
+          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], hits, ctr, err);
     });
-    k_classify<true><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q], w.hits,
+  };
+  // bounce b+1's closest hits on the trace stream beside bounce b's shadow
+  // rays, as in the single-job waves (run_waves)
+  const bool overlap = ts && ev_queue && ev_hits && w.hits2;
+  auto extend_ahead = [&](int q, ajg_hit* hits) {
+    cudaEventRecord(ev_queue, st);
+    cudaStreamWaitEvent(ts, ev_queue, 0);
+    cudaMemsetAsync(&w.counts[8], 0, sizeof(uint32_t), ts);
+    extend(q, hits, ts);
+    cudaEventRecord(ev_hits, ts);
+  };
+  cudaMemsetAsync(w.counts, 0, 64, st);
+  k_raygen<true><<<gs, kShadeThreads, 0, st>>>(a, t, w);
+  int q = 0;
+  if (overlap && bounces > 0) extend_ahead(0, w.hits);
+  for (int b = 0; b < bounces; ++b) {
+    WaveBufs wb = w;
+    if (overlap) {
+      wb.hits = (b & 1) ? w.hits2 : w.hits;
+      cudaStreamWaitEvent(st, ev_hits, 0);
+    }
+    cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
+    if (overlap) {
+      cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
+      cudaMemsetAsync(&w.counts[9], 0, 2 * sizeof(uint32_t), st);
+    } else {
+      cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
+      extend(q, w.hits, st);
+    }
+    k_classify<true><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q], wb.hits,
                                          w.lists, &w.counts[4], (uint32_t)P);
-    k_shade_miss<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, b, q, w.lists,
+    k_shade_miss<true><<<gs, kShadeThreads, 0, st>>>(a, t, wb, b, q, w.lists,
                                                      &w.counts[4]);
     k_shade<AJG_MAT_DIFFUSE, true><<<gs, kShadeThreads, 0, st>>>(
-        a, t, w, b, q, w.lists + P, &w.counts[5], (uint32_t)NT, shadow_cap,
+        a, t, wb, b, q, w.lists + P, &w.counts[5], (uint32_t)NT, shadow_cap,
         err);
     k_shade<AJG_MAT_DISNEY, true><<<gs, kShadeThreads, 0, st>>>(
-        a, t, w, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
+        a, t, wb, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
         shadow_cap, err);
     k_shade<kMatOther, true><<<gs, kShadeThreads, 0, st>>>(
-        a, t, w, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)NT,
+        a, t, wb, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)NT,
         shadow_cap, err);
+    if (overlap && b + 1 < bounces)
+      extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2);
     dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
       constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
       const int g =
@@ -1297,7 +1324,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
           reinterpret_cast<const float*>(w.lists),
           reinterpret_cast<const int32_t*>(w.lists + P));
     }
-    k_accumulate<true><<<gs, kShadeThreads, 0, st>>>(a, t, w, q,
+    k_accumulate<true><<<gs, kShadeThreads, 0, st>>>(a, t, wb, q,
                                                      (uint32_t)NT);
     q ^= 1;
   }

@@ -289,9 +289,13 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj);
 // lengths and table contents read on the device): raygen, `bounces` bounce
 // iterations, film update.  NT = light terms per path of the arena; `emit`:
 // a scene of the wave has emitters (the closest-hit MIS BSDF pass runs).
+// With a trace stream and two events, bounce b+1's closest hits run there
+// beside bounce b's shadow rays (null: one stream).
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                      int NT, int bounces, int tri_test, int width, bool emit,
-                     TraceCounters* ctr, uint32_t* err, cudaStream_t st);
+                     TraceCounters* ctr, uint32_t* err, cudaStream_t st,
+                     cudaStream_t ts = nullptr, cudaEvent_t ev_queue = nullptr,
+                     cudaEvent_t ev_hits = nullptr);
 // Kernels of a multi-job wave launched per wave (for launch counts).
 inline int mj_wave_kernels(int bounces, bool emit) {
   return 2 + (emit ? 10 : 8) * bounces;

@@ -142,6 +142,9 @@ struct Server {
 
   // request-loop thread only
   cudaStream_t st = nullptr;
+  // the trace stream of the waves' overlapped closest-hit launches
+  cudaStream_t ts = nullptr;
+  cudaEvent_t ev_queue = nullptr, ev_hits = nullptr;
   void* arena = nullptr;
   uint64_t arena_bytes = 0, P = 0;
   int NT = 0;
@@ -220,7 +223,7 @@ cudaGraphExec_t Server::graph_for(int bounces, int tri_test, int width,
       cudaSuccess)
     return nullptr;
   enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, emit, d_ctr, d_err,
-                  st);
+                  st, ctx->overlap ? ts : nullptr, ev_queue, ev_hits);
   if (cudaStreamEndCapture(st, &g) != cudaSuccess || !g) return nullptr;
   if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
   cudaGraphDestroy(g);
@@ -523,7 +526,7 @@ bool Server::plan_and_launch() {
   } else {  // capture unavailable: the same launches on the stream
     cudaGetLastError();
     enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, emit, d_ctr, d_err,
-                    st);
+                    st, ctx->overlap ? ts : nullptr, ev_queue, ev_hits);
   }
   // results this wave completes
   for (const Plan& p : plan) {
@@ -679,6 +682,12 @@ static int ensure_server(ajg_ctx* ctx, Server** out) {
     auto* s = new Server(ctx);
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) ==
                   cudaSuccess &&
+              cudaStreamCreateWithFlags(&s->ts, cudaStreamNonBlocking) ==
+                  cudaSuccess &&
+              cudaEventCreateWithFlags(&s->ev_queue, cudaEventDisableTiming) ==
+                  cudaSuccess &&
+              cudaEventCreateWithFlags(&s->ev_hits, cudaEventDisableTiming) ==
+                  cudaSuccess &&
               cudaMalloc(&s->d_err, sizeof(uint32_t)) == cudaSuccess &&
               cudaMalloc(&s->d_ctr, 2 * sizeof(TraceCounters)) == cudaSuccess;
     s->table_bytes = tables_size();
@@ -711,6 +720,9 @@ static int ensure_server(ajg_ctx* ctx, Server** out) {
       if (s->d_err) cudaFree(s->d_err);
       if (s->d_ctr) cudaFree(s->d_ctr);
       if (s->st) cudaStreamDestroy(s->st);
+      if (s->ts) cudaStreamDestroy(s->ts);
+      if (s->ev_queue) cudaEventDestroy(s->ev_queue);
+      if (s->ev_hits) cudaEventDestroy(s->ev_hits);
       delete s;
       return fail(ctx, AJG_ERR_OOM, "request loop: allocation failed");
     }
@@ -752,6 +764,10 @@ void server_shutdown(ajg_ctx* ctx) {
   cudaFree(s->d_tables);
   cudaFree(s->d_err);
   cudaFree(s->d_ctr);
+  cudaStreamSynchronize(s->ts);
+  cudaEventDestroy(s->ev_queue);
+  cudaEventDestroy(s->ev_hits);
+  cudaStreamDestroy(s->ts);
   cudaStreamDestroy(s->st);
   for (auto& kv : s->jobs) delete kv.second;
   delete s;
