@@ -234,6 +234,20 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
+# ----------------------------------------------------------------- ranks --
+def whole_job_rate(dist, world, units_per_rank, seconds, device=None):
+    """Throughput of the whole job under N replicas: every rank processed
+    `units_per_rank` in its own `seconds`; the job took the slowest rank's
+    time (a MAX all-reduce).  Returns (M units/s over all ranks, that
+    time)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        seconds = float(t.item())
+    return world * units_per_rank / seconds / 1e6, seconds
+
+
 # ------------------------------------------------------------- GPU side --
 def run_ours(args):
     import torch
@@ -298,11 +312,9 @@ def run_ours(args):
     prof_ms = pa.elapsed_time(pb)
     st = ctx.stats()
     ctx.set_profiling(False)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * samples_per_step * args.steps / (total_ms / 1e3) / 1e6
+    value, total_s = whole_job_rate(dist, world, samples_per_step * args.steps,
+                                    total_ms / 1e3, dev)
+    total_ms = total_s * 1e3
 
     # roofline of the dominant traversal kernel
     kinds = {"closest": ("closest_ms", "closest_launches", "closest_nodes", "closest_tris",
@@ -344,11 +356,9 @@ def run_ours(args):
             rend.Render(s2, flat.camera, film)
             s2.release()
         dt = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([dt], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-        e2e = {"value": world * samples_per_step * args.steps / dt / 1e6,
+        e2e_value, dt = whole_job_rate(dist, world, samples_per_step * args.steps,
+                                       dt, dev)
+        e2e = {"value": e2e_value,
                "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": dt / args.steps * 1e3}
 

@@ -1,0 +1,61 @@
+"""bench.py's multi-GPU contract on CPU with gloo, world size 2: every rank
+renders its own replica, the job's time is the slowest rank's (a MAX
+all-reduce) and the value counts all ranks' units; the reference arm runs
+on rank 0 alone."""
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank_main(rank, world, port, out_dir):
+    import torch.distributed as dist
+    sys.path.insert(0, str(ROOT))
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # rank r took r + 1 seconds for 3 M units
+    v, secs = bench.whole_job_rate(dist, world, 3_000_000, float(rank + 1))
+    (Path(out_dir) / f"r{rank}.txt").write_text(f"{v} {secs}")
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_whole_job_rate_takes_the_slowest_rank(tmp_path):
+    import torch.multiprocessing as mp
+    port = _free_port()
+    mp.spawn(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    for r in (0, 1):
+        v, secs = map(float, (tmp_path / f"r{r}.txt").read_text().split())
+        assert secs == 2.0              # the slower rank's time on both ranks
+        assert v == pytest.approx(2 * 3.0 / 2.0)  # all ranks' units / that time
+
+
+def test_single_rank_rate():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    v, secs = bench.whole_job_rate(None, 1, 5_000_000, 2.5)
+    assert (v, secs) == (2.0, 2.5)
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    """Under torchrun every rank but 0 exits 0 without work or output."""
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--gpus", "2", "--steps", "1", "--warmup", "1"],
+                       capture_output=True, text=True, env=env, timeout=120, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == ""
