@@ -40,7 +40,7 @@ namespace {
 constexpr int kShadeThreads = 128;
 constexpr int kTraceThreads = 128;
 #ifndef AJG_SHADE_MIN_BLOCKS
-#define AJG_SHADE_MIN_BLOCKS 8
+#define AJG_SHADE_MIN_BLOCKS 4  // up to 128 registers: no spills (8: 64)
 #endif
 #ifndef AJG_TRACE_MIN_BLOCKS
 #define AJG_TRACE_MIN_BLOCKS 1
