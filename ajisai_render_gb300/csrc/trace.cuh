@@ -197,6 +197,10 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 #ifndef AJG_REFILL
 #define AJG_REFILL 16
 #endif
+#ifndef AJG_SMEM_STACK
+#define AJG_SMEM_STACK 16  // stack entries per lane in shared memory (a power
+                           // of two; 0: the whole stack in local memory)
+#endif
 #ifndef AJG_LEAF_BATCH
 #define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
@@ -222,6 +226,46 @@ __device__ __forceinline__ void trace_persistent(
   uint32_t visits = 0;
   int stack_node[kStack];
   float stack_t[kStack];
+#if AJG_SMEM_STACK > 0
+  // The top kShort entries of each lane's stack live in shared memory (a
+  // ring: entry i in slot i % kShort, lane-interleaved); a push evicts the
+  // entry kShort below the top to the local array, a pop refills its slot.
+  constexpr int kShort = AJG_SMEM_STACK;
+  static_assert((kShort & (kShort - 1)) == 0, "a power of two");
+  __shared__ int2 s_ring[kShort * 128];
+  int2* const ring = s_ring + threadIdx.x;
+  auto push = [&](int nd, float t) {
+    const int slot = sp & (kShort - 1);
+    if (sp >= kShort) {
+      const int2 old = ring[slot * 128];
+      stack_node[sp - kShort] = old.x;
+      stack_t[sp - kShort] = __int_as_float(old.y);
+    }
+    ring[slot * 128] = make_int2(nd, __float_as_int(t));
+    ++sp;
+  };
+  auto pop = [&](int& nd, float& t) {
+    --sp;
+    const int slot = sp & (kShort - 1);
+    const int2 v = ring[slot * 128];
+    nd = v.x;
+    t = __int_as_float(v.y);
+    if (sp >= kShort)
+      ring[slot * 128] =
+          make_int2(stack_node[sp - kShort], __float_as_int(stack_t[sp - kShort]));
+  };
+#else
+  auto push = [&](int nd, float t) {
+    stack_node[sp] = nd;
+    stack_t[sp] = t;
+    ++sp;
+  };
+  auto pop = [&](int& nd, float& t) {
+    --sp;
+    nd = stack_node[sp];
+    t = stack_t[sp];
+  };
+#endif
   for (;;) {
     const unsigned idle = __ballot_sync(full, k == kIdle);
     const unsigned done = __ballot_sync(full, k == kDone);
@@ -294,9 +338,7 @@ __device__ __forceinline__ void trace_persistent(
             raise_device_error(err, kDevStackOverflow);
             finished = true;
           } else {
-            stack_node[sp] = first0 ? r1 : r0;
-            stack_t[sp] = first0 ? tn1 : tn0;
-            ++sp;
+            push(first0 ? r1 : r0, first0 ? tn1 : tn0);
             node = first0 ? r0 : r1;
             descend = true;
           }
@@ -442,9 +484,7 @@ __device__ __forceinline__ void trace_persistent(
               fr = ref[cc];
               ft = tn[cc];
             }
-          stack_node[sp] = fr;
-          stack_t[sp] = ft;
-          ++sp;
+          push(fr, ft);
         }
         if (!finished) {
           int nr = 0;
@@ -474,9 +514,7 @@ __device__ __forceinline__ void trace_persistent(
 #pragma unroll
           for (int c = 0; c < W; ++c)
             if (c == far_c) fr = ref[c];
-          stack_node[sp] = fr;
-          stack_t[sp] = far_t;
-          ++sp;
+          push(fr, far_t);
           inner &= ~(1u << far_c);
         }
         if (!finished) {
@@ -494,10 +532,12 @@ __device__ __forceinline__ void trace_persistent(
       // pop, skipping boxes a closer hit has since excluded
       finished = true;
       while (sp > 0) {
-        --sp;
+        int nd;
+        float st;
+        pop(nd, st);
         const float lim2 = ANY ? r.tmax : fminf(hit.t, r.tmax);
-        if (stack_t[sp] <= lim2) {
-          node = stack_node[sp];
+        if (st <= lim2) {
+          node = nd;
           finished = false;
           break;
         }
