@@ -42,9 +42,6 @@ constexpr int kTraceThreads = 128;
 #ifndef AJG_SHADE_MIN_BLOCKS
 #define AJG_SHADE_MIN_BLOCKS 4  // up to 128 registers: no spills (8: 64)
 #endif
-#ifndef AJG_TRACE_MIN_BLOCKS
-#define AJG_TRACE_MIN_BLOCKS 1
-#endif
 constexpr int kMaxLights = 15;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -187,7 +184,7 @@ __device__ __forceinline__ void retarget(TraceScene& ts, const MJTables& t,
 
 // Closest hits of the path queue.
 template <int TEST, bool MJ, int W>
-__global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
     k_extend(DeviceScene s, MJTables t, const float4* __restrict__ ro,
              const float4* __restrict__ rd, const uint32_t* __restrict__ count,
              uint32_t* fetch_next, ajg_hit* __restrict__ hits,
@@ -257,7 +254,7 @@ __global__ void k_classify(DeviceScene s, MJTables t,
 }
 
 template <int TEST, bool MJ, int W>
-__global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
     k_shadow(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
              const float4* __restrict__ sq_d,
              const uint16_t* __restrict__ sq_scene,
@@ -282,7 +279,7 @@ __global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
 // the top of the shadow queue's storage, see emit_closest); t and the
 // primitive go to two arrays the material lists' storage lends.
 template <int TEST, bool MJ, int W>
-__global__ void __launch_bounds__(kTraceThreads, AJG_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
     k_bsdf_trace(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
                  const float4* __restrict__ sq_d,
                  const uint16_t* __restrict__ sq_scene,

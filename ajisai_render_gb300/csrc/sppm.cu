@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 template <int TEST, int W>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, trace_min_blocks<W>())
     k_photon_extend(DeviceScene s, const float4* __restrict__ ro,
                     const float4* __restrict__ rd,
                     const uint32_t* __restrict__ count, uint32_t* fetch_next,

@@ -8,7 +8,7 @@ namespace {
 constexpr int kTraceThreads = 128;
 
 template <int TEST, int W>
-__global__ void __launch_bounds__(kTraceThreads)
+__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
     k_trace_closest(DeviceScene s, const ajg_ray* __restrict__ rays,
                     uint64_t n, uint32_t* next, ajg_hit* __restrict__ hits,
                     TraceCounters* ctr, uint32_t* err) {
@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kTraceThreads)
 }
 
 template <int TEST, int W>
-__global__ void __launch_bounds__(kTraceThreads)
+__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
     k_trace_any(DeviceScene s, const ajg_ray* __restrict__ rays, uint64_t n,
                 uint32_t* next, uint8_t* __restrict__ occ, TraceCounters* ctr,
                 uint32_t* err) {

@@ -197,6 +197,16 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 #ifndef AJG_REFILL
 #define AJG_REFILL 16
 #endif
+// Blocks of 128 threads per SM the traversal kernels over 2- and 4-wide
+// trees are compiled for: 8 caps them at 64 registers, which they fit without
+// spills.  The 8-wide ones would spill there and stay uncapped (1).
+#ifndef AJG_TRACE_MIN_BLOCKS
+#define AJG_TRACE_MIN_BLOCKS 8
+#endif
+template <int L>
+constexpr int trace_min_blocks() {
+  return (L & ~kBvhCompressed) == 8 ? 1 : AJG_TRACE_MIN_BLOCKS;
+}
 #ifndef AJG_SMEM_STACK
 #define AJG_SMEM_STACK 16  // stack entries per lane in shared memory (a power
                            // of two; 0: the whole stack in local memory)
