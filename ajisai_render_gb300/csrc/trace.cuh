@@ -122,6 +122,26 @@ __device__ __forceinline__ bool slab2(float lox, float hix, float loy,
   return tn <= tf && tn <= lim && tf >= r.tmin;
 }
 
+// Two consecutive float4 of a node (32-byte aligned: node arrays come from
+// cudaMalloc and their strides are multiples of 64 bytes).  With
+// AJG_WIDE_LOADS one 256-bit load per lane (sm_100 and later): one sector
+// and one load instruction instead of two.
+#ifndef AJG_WIDE_LOADS
+#define AJG_WIDE_LOADS 1
+#endif
+__device__ __forceinline__ void ldg_node(const float4* p, float4& a,
+                                         float4& b) {
+#if AJG_WIDE_LOADS
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y),
+        "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+#else
+  a = __ldg(p);
+  b = __ldg(p + 1);
+#endif
+}
+
 __device__ __forceinline__ RayQ make_query(F3 o, F3 d, float tmin,
                                            float tmax) {
   RayQ r;
@@ -318,10 +338,9 @@ __device__ __forceinline__ void trace_persistent(
     const float lim = ANY ? r.tmax : fminf(hit.t, r.tmax);
     bool descend = false;  // `node` holds the next node to visit
     if constexpr (W == 2) {
-      const float4 n0 = __ldg(bvh + 4 * node + 0);
-      const float4 n1 = __ldg(bvh + 4 * node + 1);
-      const float4 n2 = __ldg(bvh + 4 * node + 2);
-      const float4 n3 = __ldg(bvh + 4 * node + 3);
+      float4 n0, n1, n2, n3;
+      ldg_node(bvh + 4 * (uint64_t)node, n0, n1);
+      ldg_node(bvh + 4 * (uint64_t)node + 2, n2, n3);
       float tn0, tn1;
       bool h0 = slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
       bool h1 = slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
@@ -373,12 +392,15 @@ __device__ __forceinline__ void trace_persistent(
       if constexpr (!CMP) {
         constexpr int G = W / 4;  // float4 groups per plane
         const float4* nd = bvh + (uint64_t)node * (2 * W);
+        float4 q[8 * G];  // the node's 2W float4, the last G padding
+#pragma unroll
+        for (int i = 0; i < 7 * G; i += 2) ldg_node(nd + i, q[i], q[i + 1]);
 #pragma unroll
         for (int g = 0; g < G; ++g) {
-          const float4 lx = __ldg(nd + 0 * G + g), hx = __ldg(nd + 1 * G + g);
-          const float4 ly = __ldg(nd + 2 * G + g), hy = __ldg(nd + 3 * G + g);
-          const float4 lz = __ldg(nd + 4 * G + g), hz = __ldg(nd + 5 * G + g);
-          const float4 rf = __ldg(nd + 6 * G + g);
+          const float4 lx = q[0 * G + g], hx = q[1 * G + g];
+          const float4 ly = q[2 * G + g], hy = q[3 * G + g];
+          const float4 lz = q[4 * G + g], hz = q[5 * G + g];
+          const float4 rf = q[6 * G + g];
           const float* plx = &lx.x;
           const float* phx = &hx.x;
           const float* ply = &ly.x;
