@@ -163,14 +163,18 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_launch(kernel):
-    """DRAM bytes per launch of the kernel from the committed ncu summary."""
+def traffic_per_launch(kernel, workload):
+    """DRAM bytes per launch of the kernel from the committed ncu summary,
+    when it was captured on this workload (resolution, spp, wave size, tree
+    width); None otherwise."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
     k = d.get(kernel)
-    return float(k["dram_bytes_per_launch"]) if k else None
+    if not k or d.get("workload") != workload:
+        return None
+    return float(k["dram_bytes_per_launch"])
 
 
 # ------------------------------------------------------------- CPU side --
@@ -330,7 +334,10 @@ def run_ours(args):
     peak, peak_kind = peaks()
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak if achieved else None,
-                "traffic": traffic_per_launch(kname),
+                "traffic": traffic_per_launch(kname, {
+                    "res": args.res, "spp": args.spp,
+                    "wave_paths": args.wave_paths or (1 << 27),
+                    "bvh_width": scene.info()["bvh_width"]}),
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "avg_launch_ms": avg_ms, "launches": int(st[l_k]),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
