@@ -148,6 +148,45 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
   return pred ? base + __popc(ballot & ((1u << lane) - 1)) : 0xffffffffu;
 }
 
+// Stream compaction of a whole block into NC queues at once: each thread
+// passes the queue of its item (-1: none) and gets the item's slot in it.
+// One atomicAdd per queue and block replaces one per warp -- the queue
+// counters are single addresses shared by the whole grid, and same-address
+// atomics otherwise bound the short kernels that fill the queues.  Every
+// thread of the block must call it (block-uniform control flow); NW is the
+// number of warps of the block.
+template <int NC, int NW>
+__device__ __forceinline__ uint32_t block_append(uint32_t* counters,
+                                                 int cls) {
+  __shared__ uint32_t s_cnt[NC][NW];
+  __shared__ uint32_t s_base[NC][NW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t rank = 0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const unsigned b = __ballot_sync(0xffffffffu, cls == c);
+    if (lane == 0) s_cnt[c][warp] = (uint32_t)__popc(b);
+    if (cls == c) rank = (uint32_t)__popc(b & lt);
+  }
+  __syncthreads();
+  if (threadIdx.x < NC) {
+    const int c = threadIdx.x;
+    uint32_t tot = 0;
+#pragma unroll
+    for (int v = 0; v < NW; ++v) {
+      const uint32_t x = s_cnt[c][v];
+      s_base[c][v] = tot;
+      tot += x;
+    }
+    const uint32_t g = tot ? atomicAdd(&counters[c], tot) : 0u;
+#pragma unroll
+    for (int v = 0; v < NW; ++v) s_base[c][v] += g;
+  }
+  __syncthreads();
+  return cls >= 0 ? s_base[cls][warp] + rank : 0xffffffffu;
+}
+
 inline int grid_for(uint64_t n, int block, int max_blocks = kSMs * 32) {
   uint64_t g = (n + block - 1) / block;
   if (g < 1) g = 1;

@@ -38,6 +38,22 @@ namespace ajg {
 namespace {
 
 constexpr int kShadeThreads = 128;
+constexpr int kClassifyThreads = 256;
+#ifndef AJG_BLOCK_APPEND
+#define AJG_BLOCK_APPEND 1
+#endif
+
+// Queue appends of the shading kernels: single-job launches run
+// block-uniform loops and append a block at a time (block_append); the
+// multi-job ones, whose light loops are warp-uniform only, a warp at a time.
+template <bool MJ>
+__device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
+                                                 bool pred) {
+  if constexpr (!MJ && AJG_BLOCK_APPEND)
+    return block_append<1, kShadeThreads / 32>(counter, pred ? 0 : -1);
+  else
+    return warp_append(counter, pred);
+}
 constexpr int kTraceThreads = 128;
 #ifndef AJG_SHADE_MIN_BLOCKS
 #define AJG_SHADE_MIN_BLOCKS 4  // up to 128 registers: no spills (8: 64)
@@ -130,6 +146,10 @@ __global__ void __launch_bounds__(kShadeThreads)
     k_raygen(WaveArgs a, MJTables t, WaveBufs w) {
   __shared__ uint32_t s_off[MJ ? kMaxWaveChunks : 1];
   uint32_t n_paths = a.n_paths, n_chunks = 0;
+  const bool all_alive =
+      AJG_BLOCK_APPEND && !MJ && a.j.max_b > 0 && !(0 > a.j.min_b);
+  if (all_alive && blockIdx.x == 0 && threadIdx.x == 0)
+    atomicAdd(&w.counts[0], n_paths);
   if constexpr (MJ) {
     n_paths = t.hdr->n_paths;
     n_chunks = t.hdr->n_chunks;
@@ -165,7 +185,9 @@ __global__ void __launch_bounds__(kShadeThreads)
     }
     w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
     w.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const uint32_t k = warp_append(&w.counts[0], alive);
+    // a single job whose paths all start (no roulette before bounce 0) is
+    // queued in path order without atomics; the count is added once below
+    const uint32_t k = all_alive ? p : warp_append(&w.counts[0], alive);
     if (alive) {
       w.qpath[0][k] = p;
       w.ro[0][k] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(sid));
@@ -214,7 +236,8 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
 // class-specialised kernels; warps stay converged, so each list append is
 // one atomic per warp.
 template <bool MJ>
-__global__ void k_classify(DeviceScene s, MJTables t,
+__global__ void __launch_bounds__(kClassifyThreads)
+    k_classify(DeviceScene s, MJTables t,
                            const float4* __restrict__ ro,
                            const uint32_t* __restrict__ count,
                            const ajg_hit* __restrict__ hits,
@@ -223,10 +246,9 @@ __global__ void k_classify(DeviceScene s, MJTables t,
                            uint32_t list_cap) {
   const uint32_t n = *count;
   const uint32_t stride = gridDim.x * blockDim.x;
-  const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t wb = blockIdx.x * blockDim.x + (threadIdx.x - lane); wb < n;
-       wb += stride) {
-    const uint32_t k = wb + lane;
+  // block-uniform iterations: block_append synchronises the block
+  for (uint32_t bb = blockIdx.x * blockDim.x; bb < n; bb += stride) {
+    const uint32_t k = bb + threadIdx.x;
     int cls = -1;
     if (k < n) {
       const int prim = hits[k].prim;
@@ -245,11 +267,16 @@ __global__ void k_classify(DeviceScene s, MJTables t,
         cls = type == AJG_MAT_DIFFUSE ? 1 : (type == AJG_MAT_DISNEY ? 2 : 3);
       }
     }
+#if AJG_BLOCK_APPEND
+    const uint32_t j = block_append<4, kClassifyThreads / 32>(list_counts, cls);
+    if (cls >= 0) lists[(uint64_t)cls * list_cap + j] = k;
+#else
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const uint32_t j = warp_append(&list_counts[c], cls == c);
       if (cls == c) lists[(uint64_t)c * list_cap + j] = k;
     }
+#endif
   }
 }
 
@@ -374,7 +401,7 @@ __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
                                             uint32_t sid, bool pred,
                                             uint32_t cap, uint32_t* err) {
-  const uint32_t k = warp_append(&w.counts[2], pred);
+  const uint32_t k = shade_append<MJ>(&w.counts[2], pred);
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -394,7 +421,7 @@ __device__ __forceinline__ void emit_closest(const WaveBufs& w, F3 o, F3 d,
                                              float pdf, uint32_t slot,
                                              uint32_t sid, bool pred,
                                              uint32_t cap, uint32_t* err) {
-  const uint32_t k = warp_append(&w.counts[9], pred);
+  const uint32_t k = shade_append<MJ>(&w.counts[9], pred);
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -444,13 +471,15 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
             uint32_t shadow_cap, uint32_t* err) {
   const uint32_t n = *list_count;
   const int nxt = cur ^ 1;
-  // warp-uniform loop: every lane of a warp runs the same iterations, so the
-  // warp-wide queue appends see all lanes
+  // warp-uniform loop (block-uniform for a single job): every lane of a
+  // warp (thread of the block) runs the same iterations, so the queue
+  // appends see all of them
+  constexpr bool kBlockLoop = !MJ && AJG_BLOCK_APPEND;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t wb = blockIdx.x * blockDim.x + (threadIdx.x - lane); wb < n;
-       wb += stride) {
-    const uint32_t j = wb + lane;
+  const uint32_t first = kBlockLoop ? 0u : threadIdx.x - lane;
+  for (uint32_t wb = blockIdx.x * blockDim.x + first; wb < n; wb += stride) {
+    const uint32_t j = wb + (kBlockLoop ? threadIdx.x : lane);
     const bool hit = j < n;
     uint32_t p = 0, k = 0, jid = 0;
     if (hit) {
@@ -698,7 +727,7 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
       }
       w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
     }
-    const uint32_t kn = warp_append(&w.counts[nxt], alive);
+    const uint32_t kn = shade_append<MJ>(&w.counts[nxt], alive);
     if (alive) {
       w.qpath[nxt][kn] = p;
       w.ro[nxt][kn] = make_float4(nro.x, nro.y, nro.z, __uint_as_float(sid));
@@ -1152,7 +1181,7 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
         }
         {
           KernelTimer tm(ctx, st, -1);
-          k_classify<false><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q],
+          k_classify<false><<<gs, kClassifyThreads, 0, st>>>(s, t, w.ro[q], &w.counts[q],
                                                 wb.hits, w.lists, &w.counts[4],
                                                 (uint32_t)P);
         }
@@ -1283,7 +1312,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
       cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
       extend(q, w.hits, st);
     }
-    k_classify<true><<<gs, 256, 0, st>>>(s, t, w.ro[q], &w.counts[q], wb.hits,
+    k_classify<true><<<gs, kClassifyThreads, 0, st>>>(s, t, w.ro[q], &w.counts[q], wb.hits,
                                          w.lists, &w.counts[4], (uint32_t)P);
     k_shade_miss<true><<<gs, kShadeThreads, 0, st>>>(a, t, wb, b, q, w.lists,
                                                      &w.counts[4]);
