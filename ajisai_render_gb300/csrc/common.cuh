@@ -187,6 +187,20 @@ __device__ __forceinline__ uint32_t block_append(uint32_t* counters,
   return cls >= 0 ? s_base[cls][warp] + rank : 0xffffffffu;
 }
 
+// Maximum of v over the block (every thread must call it).
+template <int NW>
+__device__ __forceinline__ uint32_t block_max(uint32_t v) {
+  __shared__ uint32_t s_m[NW];
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = v;
+  __syncthreads();
+  uint32_t m = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) m = m > s_m[w] ? m : s_m[w];
+  __syncthreads();
+  return m;
+}
+
 inline int grid_for(uint64_t n, int block, int max_blocks = kSMs * 32) {
   uint64_t g = (n + block - 1) / block;
   if (g < 1) g = 1;

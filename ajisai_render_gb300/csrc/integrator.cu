@@ -43,13 +43,11 @@ constexpr int kClassifyThreads = 256;
 #define AJG_BLOCK_APPEND 1
 #endif
 
-// Queue appends of the shading kernels: single-job launches run
-// block-uniform loops and append a block at a time (block_append); the
-// multi-job ones, whose light loops are warp-uniform only, a warp at a time.
-template <bool MJ>
+// Queue appends of the shading kernels: a block at a time (block_append,
+// block-uniform loops), or with AJG_BLOCK_APPEND=0 a warp at a time.
 __device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
                                                  bool pred) {
-  if constexpr (!MJ && AJG_BLOCK_APPEND)
+  if constexpr (AJG_BLOCK_APPEND)
     return block_append<1, kShadeThreads / 32>(counter, pred ? 0 : -1);
   else
     return warp_append(counter, pred);
@@ -157,12 +155,16 @@ __global__ void __launch_bounds__(kShadeThreads)
       s_off[c] = t.chunks[c].path_off;
     __syncthreads();
   }
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_paths;
-       p += gridDim.x * blockDim.x) {
-    F3 ro, rd, T;
-    bool alive;
+  // block-uniform iterations (block_append synchronises the block)
+  for (uint32_t pb = blockIdx.x * blockDim.x; pb < n_paths;
+       pb += gridDim.x * blockDim.x) {
+    const uint32_t p = pb + threadIdx.x;
+    F3 ro = mk3(0, 0, 0), rd = mk3(0, 0, 1), T = mk3(1, 1, 1);
+    bool alive = false;
     uint32_t sid = 0;
-    if constexpr (MJ) {
+    if (p >= n_paths) {
+      // past the wave: only the queue append below
+    } else if constexpr (MJ) {
       const Chunk C = t.chunks[find_le(s_off, n_chunks, p)];
       const uint32_t q = p - C.path_off;
       const uint32_t i = C.pix0 + q / C.S;
@@ -183,11 +185,13 @@ __global__ void __launch_bounds__(kShadeThreads)
       const int x = (int)(pixel % a.cam.width), y = (int)(pixel / a.cam.width);
       raygen_path(a.cam, a.j, key, x, y, ro, rd, T, alive);
     }
-    w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
-    w.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p < n_paths) {
+      w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
+      w.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     // a single job whose paths all start (no roulette before bounce 0) is
-    // queued in path order without atomics; the count is added once below
-    const uint32_t k = all_alive ? p : warp_append(&w.counts[0], alive);
+    // queued in path order without atomics (the count is added once above)
+    const uint32_t k = all_alive ? p : shade_append(&w.counts[0], alive);
     if (alive) {
       w.qpath[0][k] = p;
       w.ro[0][k] = make_float4(ro.x, ro.y, ro.z, __uint_as_float(sid));
@@ -401,7 +405,7 @@ __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
                                             uint32_t sid, bool pred,
                                             uint32_t cap, uint32_t* err) {
-  const uint32_t k = shade_append<MJ>(&w.counts[2], pred);
+  const uint32_t k = shade_append(&w.counts[2], pred);
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -421,7 +425,7 @@ __device__ __forceinline__ void emit_closest(const WaveBufs& w, F3 o, F3 d,
                                              float pdf, uint32_t slot,
                                              uint32_t sid, bool pred,
                                              uint32_t cap, uint32_t* err) {
-  const uint32_t k = shade_append<MJ>(&w.counts[9], pred);
+  const uint32_t k = shade_append(&w.counts[9], pred);
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -474,7 +478,7 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
   // warp-uniform loop (block-uniform for a single job): every lane of a
   // warp (thread of the block) runs the same iterations, so the queue
   // appends see all of them
-  constexpr bool kBlockLoop = !MJ && AJG_BLOCK_APPEND;
+  constexpr bool kBlockLoop = AJG_BLOCK_APPEND;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t first = kBlockLoop ? 0u : threadIdx.x - lane;
@@ -528,13 +532,16 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
       }
     }
     int dim = dim_base(J, b) + (b > J.min_b ? 1 : 0);
-    // lanes of a multi-job warp differ in lights and MIS: loop over the
-    // warp's maximum with the lanes past their own count idle
+    // lanes of a multi-job block differ in lights and MIS: loop over the
+    // block's maximum with the lanes past their own count idle
     const int nl = (int)s.num_lights;
     const bool mis = hit && J.use_mis;
     int nl_loop = nl;
     bool any_mis = J.use_mis != 0;
-    if constexpr (MJ) {
+    if constexpr (MJ && kBlockLoop) {
+      nl_loop = (int)block_max<kShadeThreads / 32>(mis ? (unsigned)nl : 0u);
+      any_mis = __syncthreads_or(mis) != 0;
+    } else if constexpr (MJ) {
       nl_loop = (int)__reduce_max_sync(kFull, mis ? (unsigned)nl : 0u);
       any_mis = __any_sync(kFull, mis);
     }
@@ -727,7 +734,7 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
       }
       w.thr[p] = make_float4(T.x, T.y, T.z, 0.f);
     }
-    const uint32_t kn = shade_append<MJ>(&w.counts[nxt], alive);
+    const uint32_t kn = shade_append(&w.counts[nxt], alive);
     if (alive) {
       w.qpath[nxt][kn] = p;
       w.ro[nxt][kn] = make_float4(nro.x, nro.y, nro.z, __uint_as_float(sid));
