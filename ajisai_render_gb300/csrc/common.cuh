@@ -148,6 +148,11 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
   return pred ? base + __popc(ballot & ((1u << lane) - 1)) : 0xffffffffu;
 }
 
+// 0: queue appends a warp at a time (warp_append) in every kernel.
+#ifndef AJG_BLOCK_APPEND
+#define AJG_BLOCK_APPEND 1
+#endif
+
 // Stream compaction of a whole block into NC queues at once: each thread
 // passes the queue of its item (-1: none) and gets the item's slot in it.
 // One atomicAdd per queue and block replaces one per warp -- the queue

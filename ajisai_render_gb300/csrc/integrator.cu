@@ -39,10 +39,6 @@ namespace {
 
 constexpr int kShadeThreads = 128;
 constexpr int kClassifyThreads = 256;
-#ifndef AJG_BLOCK_APPEND
-#define AJG_BLOCK_APPEND 1
-#endif
-
 // Queue appends of the shading kernels: a block at a time (block_append,
 // block-uniform loops), or with AJG_BLOCK_APPEND=0 a warp at a time.
 __device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
