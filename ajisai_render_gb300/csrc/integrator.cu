@@ -37,7 +37,10 @@
 namespace ajg {
 namespace {
 
-constexpr int kShadeThreads = 128;
+#ifndef AJG_SHADE_THREADS
+#define AJG_SHADE_THREADS 256
+#endif
+constexpr int kShadeThreads = AJG_SHADE_THREADS;
 constexpr int kClassifyThreads = 256;
 // Queue appends of the shading kernels: a block at a time (block_append,
 // block-uniform loops), or with AJG_BLOCK_APPEND=0 a warp at a time.
@@ -50,7 +53,9 @@ __device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
 }
 constexpr int kTraceThreads = 128;
 #ifndef AJG_SHADE_MIN_BLOCKS
-#define AJG_SHADE_MIN_BLOCKS 4  // up to 128 registers: no spills (8: 64)
+// blocks per SM the shading kernels are compiled for: 512 threads, up to
+// 128 registers, no spills (1024 threads: 64)
+#define AJG_SHADE_MIN_BLOCKS (512 / AJG_SHADE_THREADS)
 #endif
 constexpr int kMaxLights = 15;
 constexpr unsigned kFull = 0xffffffffu;
