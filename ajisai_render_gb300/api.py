@@ -290,9 +290,17 @@ class Film:
     """The film of a render: rgbw [h, w, 4] = (sum of radiance, sum of
     weights) per pixel in the reference's box-footprint convention."""
 
-    def __init__(self, width: int, height: int):
+    def __init__(self, width: int, height: int, rgbw: np.ndarray | None = None):
+        """rgbw: an optional caller-owned float32 [height, width, 4] buffer
+        (e.g. pinned host memory, which the device-to-host copy of the
+        result reads faster); zeros are allocated otherwise."""
         self.width, self.height = width, height
-        self.rgbw = np.zeros((height, width, 4), F32)
+        if rgbw is None:
+            rgbw = np.zeros((height, width, 4), F32)
+        elif (rgbw.dtype != F32 or rgbw.shape != (height, width, 4)
+              or not rgbw.flags.c_contiguous):
+            raise ValueError("rgbw must be a contiguous float32 [height, width, 4] array")
+        self.rgbw = rgbw
 
     def image(self) -> np.ndarray:
         w = self.rgbw[..., 3:4]

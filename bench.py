@@ -33,6 +33,7 @@ slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -352,15 +353,26 @@ def run_ours(args):
                flat.tri_flags.nbytes + flat.world.nbytes + flat.materials.nbytes +
                flat.lights.nbytes)
         d2h = W * H * 16
-        film = api.Film(W, H)
+
+        # the step's inputs and its result live in pinned host memory (numpy
+        # views of pinned tensors, handed to the C ABI as plain pointers)
+        def pinned(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+        flat_h = dataclasses.replace(
+            flat, tris=pinned(flat.tris), corner_n=pinned(flat.corner_n),
+            tri_mat=pinned(flat.tri_mat), tri_flags=pinned(flat.tri_flags),
+            world=pinned(flat.world), materials=pinned(flat.materials),
+            lights=pinned(flat.lights))
+        film = api.Film(W, H, rgbw=pinned(np.zeros((H, W, 4), np.float32)))
         torch.cuda.synchronize(dev)
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            s2 = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(RADIUS,
-                                                                  bvh_width=args.bvh_width))
-            rend.Render(s2, flat.camera, film)
+            s2 = api.GpuScene(ctx, flat_h, api.CreatePLOCAggregate(RADIUS,
+                                                                    bvh_width=args.bvh_width))
+            rend.Render(s2, flat_h.camera, film)
             s2.release()
         dt = time.perf_counter() - t0
         e2e_value, dt = whole_job_rate(dist, world, samples_per_step * args.steps,
