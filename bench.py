@@ -480,7 +480,7 @@ def run_batched(ctx, args):
                                               max_bounces=BATCH_DEPTH), seed=7)
         descs.append((g, _cam(cam, j["res"], j["res"]), r))
     samples = sum(j["res"] ** 2 * j["spp"] for j in jobs)
-    ctx.configure_serving("fifo")
+    ctx.configure_serving("fifo", wave_paths=args.batch_wave_paths)
     # warm both paths (arenas, graphs) on a small job
     descs[0][2].Render(descs[0][0], _cam(descs[0][1], 16, 16))
     ctx.render_batch([(descs[0][0], _cam(descs[0][1], 16, 16), descs[0][2])])
@@ -551,7 +551,7 @@ def run_served(ctx, args, capacity_samples_s):
     mean_samples = np.mean([r * r * s for _, r, s, _ in plan])
     rate = args.serve_load * capacity_samples_s / mean_samples  # jobs per second
     gaps = rng.exponential(1.0 / rate, n)
-    ctx.configure_serving("fair")
+    ctx.configure_serving("fair", wave_paths=args.batch_wave_paths)
     submitted = []
     t0 = time.perf_counter()
     at = 0.0
