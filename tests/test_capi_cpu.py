@@ -98,3 +98,17 @@ def test_context_creation_reports_missing_device(lib):
     rc = lib.ajg_create_context(None, C.byref(h))
     assert rc == 2 and not h.value                            # AJG_ERR_CUDA
     assert lib.ajg_last_error(None)
+
+
+def test_film_takes_a_caller_owned_buffer():
+    from ajisai_render_gb300 import api
+    buf = np.zeros((3, 5, 4), np.float32)
+    f = api.Film(5, 3, rgbw=buf)
+    assert f.rgbw is buf
+    buf[1, 2] = (2.0, 4.0, 6.0, 2.0)
+    assert np.allclose(f.image()[1, 2], (1.0, 2.0, 3.0))
+    assert api.Film(5, 3).rgbw.shape == (3, 5, 4)
+    for bad in (np.zeros((5, 3, 4), np.float32), np.zeros((3, 5, 4), np.float64),
+                np.zeros((3, 5, 8), np.float32)[..., ::2]):
+        with pytest.raises(ValueError):
+            api.Film(5, 3, rgbw=bad)
