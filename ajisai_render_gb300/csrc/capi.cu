@@ -268,17 +268,6 @@ int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
     delete ctx;
     return fail(nullptr, AJG_ERR_CUDA, "context allocation failed");
   }
-  cudaMemPoolProps props = {};
-  props.allocType = cudaMemAllocationTypePinned;
-  props.location.type = cudaMemLocationTypeDevice;
-  props.location.id = dev;
-  uint64_t cached = 4ull << 30;  // freed scene memory kept for reuse
-  if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess ||
-      cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold,
-                              &cached) != cudaSuccess) {
-    delete ctx;
-    return fail(nullptr, AJG_ERR_CUDA, "memory pool creation failed");
-  }
   cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
   cudaMemset(ctx->d_counters, 0, 2 * sizeof(TraceCounters));
   *out = ctx;
@@ -299,7 +288,6 @@ int ajg_destroy_context(ajg_ctx* ctx) {
   cudaFree(ctx->d_fetch);
   cudaFree(ctx->d_counters);
   cudaStreamSynchronize(ctx->trace_stream);
-  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   cudaEventDestroy(ctx->ev_queue);
   cudaEventDestroy(ctx->ev_hits);
   cudaStreamDestroy(ctx->trace_stream);
@@ -552,7 +540,7 @@ int ajg_scene_create_flat_ex(ajg_ctx* ctx, const float* tris,
   }
   auto keep = [&](size_t bytes) -> void* {
     void* p = nullptr;
-    if (pool_alloc(ctx, &p, bytes, ctx->stream) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&p, bytes > 0 ? bytes : 16) != cudaSuccess) return nullptr;
     s->allocations.push_back(p);
     s->info.device_bytes += bytes;
     return p;
@@ -689,10 +677,8 @@ int ajg_scene_release(ajg_scene* s) {
     return fail(ctx, AJG_ERR_INVALID, "scene has unfinished jobs");
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  cudaStreamSynchronize(ctx->trace_stream);
   server_sync(ctx);
-  // nothing uses the scene any more: its memory goes back to the pool
-  for (void* p : s->allocations) cudaFreeAsync(p, ctx->stream);
+  for (void* p : s->allocations) cudaFree(p);
   if (ctx->resident_bytes >= s->info.device_bytes)
     ctx->resident_bytes -= s->info.device_bytes;
   delete s;

@@ -605,25 +605,20 @@ __global__ void k_lum(const float* __restrict__ mats, uint32_t m,
   }
 }
 
-// Build temporaries from the context's pool, ordered on the build stream
-// and handed back to it when the build ends.
 struct Arena {
-  ajg_ctx* ctx;
-  cudaStream_t st;
   std::vector<void*> ptrs;
   cudaError_t err = cudaSuccess;
-  Arena(ajg_ctx* c, cudaStream_t s) : ctx(c), st(s) {}
   template <class T>
   T* get(uint64_t count) {
     void* p = nullptr;
     if (err != cudaSuccess) return nullptr;
-    err = pool_alloc(ctx, &p, count * sizeof(T), st);
+    err = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
     if (err != cudaSuccess) return nullptr;
     ptrs.push_back(p);
     return static_cast<T*>(p);
   }
   ~Arena() {
-    for (void* p : ptrs) cudaFreeAsync(p, st);
+    for (void* p : ptrs) cudaFree(p);
   }
 };
 
@@ -655,7 +650,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   // persistent scene buffers
   auto keep = [&](size_t bytes) -> void* {
     void* p = nullptr;
-    if (pool_alloc(ctx, &p, bytes, st) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&p, bytes > 0 ? bytes : 16) != cudaSuccess) return nullptr;
     s->allocations.push_back(p);
     s->info.device_bytes += bytes;
     return p;
@@ -682,7 +677,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
       !ploc_nodes || !perm_keep)
     return set_err(ctx, AJG_ERR_OOM, "device allocation failed (scene)");
 
-  Arena tmp(ctx, st);
+  Arena tmp;
   float* d_tris = tmp.get<float>(n * 9);
   int32_t* d_mat = tmp.get<int32_t>(n);
   int32_t* d_flags = tmp.get<int32_t>(n);

@@ -222,9 +222,6 @@ struct ajg_ctx {
   // queue is written; ev_hits: its hits are); AJG_TRACE_OVERLAP=0 keeps one
   // stream
   cudaStream_t trace_stream = nullptr;
-  // scene buffers and build temporaries (stream-ordered, cached up to a
-  // release threshold: building another scene reuses the memory)
-  cudaMemPool_t pool = nullptr;
   cudaEvent_t ev_queue = nullptr, ev_hits = nullptr;
   bool overlap = true;
   std::mutex mu;
@@ -242,12 +239,6 @@ struct ajg_ctx {
   std::vector<ajg::Buffer> arena;
   uint64_t arena_paths = 0;
 };
-
-// An allocation from the context's pool, ordered on stream st.
-inline cudaError_t pool_alloc(ajg_ctx* ctx, void** p, size_t bytes,
-                              cudaStream_t st) {
-  return cudaMallocFromPoolAsync(p, bytes > 0 ? bytes : 16, ctx->pool, st);
-}
 
 struct ajg_scene {
   ajg_ctx* ctx = nullptr;

@@ -239,10 +239,6 @@ typedef struct ajg_stats {
 } ajg_stats;
 
 /* ---- context --------------------------------------------------------- */
-/* A context owns a stream, a wavefront arena grown on demand and a
- * stream-ordered memory pool for scene buffers and build temporaries; the
- * pool keeps up to 4 GiB of released scene memory cached for the next scene
- * and returns the rest to the device (all of it at ajg_destroy_context). */
 AJG_API int ajg_abi_version(void);
 AJG_API int ajg_create_context(const ajg_config* cfg, ajg_ctx** out);
 AJG_API int ajg_destroy_context(ajg_ctx* ctx);
