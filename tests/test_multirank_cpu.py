@@ -59,3 +59,16 @@ def test_reference_arm_runs_on_rank_zero_only():
                        capture_output=True, text=True, env=env, timeout=120, cwd=ROOT)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_committed_traffic_only_for_its_workload():
+    sys.path.insert(0, str(ROOT))
+    import json
+    import bench
+    d = json.loads((ROOT / "profiles" / "traffic.json").read_text())
+    w = d["workload"]
+    got = bench.traffic_per_launch("k_shadow", dict(w))
+    assert got == float(d["k_shadow"]["dram_bytes_per_launch"])
+    assert bench.traffic_per_launch("k_shadow", {**w, "res": w["res"] // 2}) is None
+    assert bench.traffic_per_launch("k_shadow", {**w, "wave_paths": 1 << 25}) is None
+    assert bench.traffic_per_launch("k_nothing", dict(w)) is None
