@@ -686,8 +686,11 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
         }
         emit_shadow<MJ>(w, so, sd, __int_as_float(0x7f800000),
                         p * NT + (NT - 1), sid, emit, shadow_cap, err);
-        emit_closest<MJ>(w, so, sd, w_o, p * NT + (NT - 1), sid, closest,
-                         shadow_cap, err);
+        // (a single job's scene without emitters never fills this queue:
+        // skip its block-wide append; the condition is uniform)
+        if (MJ || s.tri_emit)
+          emit_closest<MJ>(w, so, sd, w_o, p * NT + (NT - 1), sid, closest,
+                           shadow_cap, err);
       }
     }
 
