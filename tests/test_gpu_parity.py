@@ -595,3 +595,19 @@ def test_sppm_matches_oracle_and_is_stable(ctx):
         b = r.RenderRadiance(api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14, bvh_width=width)),
                              flat.camera)
         np.testing.assert_allclose(b, rad, rtol=1e-4, atol=1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("min_b", [-1, 0])
+def test_roulette_from_the_first_bounce_matches_oracle(ctx, min_b):
+    """min_bounces -1 rolls the roulette before bounce 0 (paths can end
+    before their camera ray is traced: ray generation then compacts its
+    queue); 0 rolls it from bounce 1 on.  Film weights are exact and the
+    radiance agrees with the oracle's film."""
+    flat = S.flatten(S.cornell_box(40, 32))
+    sc = api.GpuScene(ctx, flat)
+    args = api.PTRendererArgs(spp=16, min_bounces=min_b, max_bounces=8)
+    f = api.PTRenderer(args, seed=7).Render(sc, flat.camera).rgbw
+    _, film_o = O.render(flat, dict(spp=16, min_bounces=min_b, max_bounces=8), seed=7)
+    assert np.array_equal(f[..., 3], film_o[..., 3].astype(np.float32))
+    np.testing.assert_allclose(f[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
