@@ -431,6 +431,154 @@ __global__ void k_collapse(const PNode* __restrict__ nodes,
   }
 }
 
+// SAH-optimal collapse into 4-wide nodes (the dynamic program of Ylitie,
+// Karras, Laine, "Efficient incoherent ray traversal on GPUs through
+// compressed wide BVHs", HPG 2017, with one triangle per leaf): cost[n].i
+// (i = 1..4 slots) is the least sum of wide-node surface areas with which
+// the subtree of binary node n fills at most i children of a wide node --
+// one slot holding n itself (a leaf, or a wide node of its own: its area
+// plus its children's best use of 4 slots), or its two children sharing
+// the slots.  Leaves cost 0 in every slot count (a leaf's triangle test is
+// the same whatever the tree).  choice[n] packs the decisions: byte 0 the
+// left child's share of a wide node's 4 slots, byte i-1 (i = 2..4) for i
+// slots 0 (n itself) or (left share << 4 | slots used).  One launch per
+// block of nodes the PLOC loop finalised, in the order they were
+// finalised: children always come before their parents.
+#ifndef AJG_SAH_COLLAPSE
+#define AJG_SAH_COLLAPSE 1
+#endif
+__global__ void k_sah_dp(const PNode* __restrict__ nodes, uint32_t lo,
+                         uint32_t hi, float4* __restrict__ cost,
+                         uint32_t* __restrict__ choice) {
+  for (uint32_t n = lo + blockIdx.x * blockDim.x + threadIdx.x; n < hi;
+       n += gridDim.x * blockDim.x) {
+    const PNode x = nodes[n];
+    if (__float_as_int(x.b.w) != 0) {  // leaf
+      cost[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+      choice[n] = 0u;
+      continue;
+    }
+    const uint32_t f = (uint32_t)__float_as_int(x.a.w);
+    const float4 L = cost[f], R = cost[f + 1];
+    const float l[5] = {0.f, L.x, L.y, L.z, L.w};
+    const float r[5] = {0.f, R.x, R.y, R.z, R.w};
+    float dist[5];
+    uint32_t dk[5];
+#pragma unroll
+    for (int j = 2; j <= 4; ++j) {
+      dist[j] = __int_as_float(0x7f800000);
+      dk[j] = 1;
+#pragma unroll
+      for (int k = 1; k < j; ++k) {
+        const float v = l[k] + r[j - k];
+        if (v < dist[j]) {
+          dist[j] = v;
+          dk[j] = (uint32_t)k;
+        }
+      }
+    }
+    float c[5];
+    uint32_t kind[5] = {0u, 0u, 0u, 0u, 0u};
+    c[1] = area(xyz(x.a), xyz(x.b)) + dist[4];
+#pragma unroll
+    for (int i = 2; i <= 4; ++i) {
+      if (dist[i] < c[i - 1]) {
+        c[i] = dist[i];
+        kind[i] = (dk[i] << 4) | (uint32_t)i;
+      } else {
+        c[i] = c[i - 1];
+        kind[i] = kind[i - 1];
+      }
+    }
+    cost[n] = make_float4(c[1], c[2], c[3], c[4]);
+    choice[n] = dk[4] | (kind[2] << 8) | (kind[3] << 16) | (kind[4] << 24);
+  }
+}
+
+// k_collapse with the children of each wide node taken from the dynamic
+// program above instead of by expanding the largest-area child.
+__global__ void k_collapse_sah(const PNode* __restrict__ nodes,
+                               const uint32_t* __restrict__ choice,
+                               const uint2* __restrict__ fin, uint32_t n_in,
+                               uint2* __restrict__ fout,
+                               uint32_t* __restrict__ counters,
+                               float4* __restrict__ wide) {
+  constexpr int W = 4;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in;
+       i += gridDim.x * blockDim.x) {
+    const uint2 e = fin[i];  // (binary node, wide slot)
+    uint32_t ch[W];
+    int nc = 0;
+    const PNode root = nodes[e.x];
+    if (__float_as_int(root.b.w) != 0) {
+      ch[nc++] = e.x;  // a one-triangle tree
+    } else {
+      // (node, slots) still to resolve; each entry holds >= 1 of the 4 slots
+      uint32_t sn[W], sj[W];
+      int sp = 0;
+      const uint32_t f = (uint32_t)__float_as_int(root.a.w);
+      const uint32_t k = choice[e.x] & 0xffu;
+      sn[sp] = f + 1;
+      sj[sp++] = W - k;
+      sn[sp] = f;
+      sj[sp++] = k;
+      while (sp > 0) {
+        --sp;
+        const uint32_t c = sn[sp], j = sj[sp];
+        const uint32_t kd = j < 2 ? 0u : (choice[c] >> (8 * (j - 1))) & 0xffu;
+        if (kd == 0u || nc + sp + 2 > W) {  // (the second never holds)
+          ch[nc++] = c;
+        } else {
+          const uint32_t fc = (uint32_t)__float_as_int(nodes[c].a.w);
+          const uint32_t k2 = kd >> 4, used = kd & 15u;
+          sn[sp] = fc + 1;
+          sj[sp++] = used - k2;
+          sn[sp] = fc;
+          sj[sp++] = k2;
+        }
+      }
+    }
+    int ni = 0;
+    for (int c = 0; c < nc; ++c)
+      ni += __float_as_int(nodes[ch[c]].b.w) == 0 ? 1 : 0;
+    uint32_t base = 0, fo = 0;
+    if (ni) {
+      base = atomicAdd(&counters[1], (uint32_t)ni);
+      fo = atomicAdd(&counters[0], (uint32_t)ni);
+    }
+    float pl[6][W];
+    int rf[W];
+    int jn = 0;
+    for (int c = 0; c < W; ++c) {
+      if (c < nc) {
+        const PNode x = nodes[ch[c]];
+        pl[0][c] = x.a.x;
+        pl[1][c] = x.b.x;
+        pl[2][c] = x.a.y;
+        pl[3][c] = x.b.y;
+        pl[4][c] = x.a.z;
+        pl[5][c] = x.b.z;
+        if (__float_as_int(x.b.w) != 0) {
+          rf[c] = ~__float_as_int(x.a.w);
+        } else {
+          rf[c] = (int)(base + jn);
+          fout[fo + jn] = make_uint2(ch[c], base + jn);
+          ++jn;
+        }
+      } else {
+        for (int k = 0; k < 6; ++k) pl[k][c] = 0.f;
+        rf[c] = kWideEmpty;
+      }
+    }
+    float4* o = wide + (uint64_t)e.y * (2 * W);
+    for (int k = 0; k < 6; ++k)
+      o[k] = make_float4(pl[k][0], pl[k][1], pl[k][2], pl[k][3]);
+    o[6] = make_float4(__int_as_float(rf[0]), __int_as_float(rf[1]),
+                       __int_as_float(rf[2]), __int_as_float(rf[3]));
+    o[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
 // The same collapse into compressed nodes (layout in scene.cuh), moving the
 // leaf triangles of every node next to each other in `tris_new`.
 template <int W>
@@ -768,6 +916,9 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
   uint32_t merged_h = 0;
+  // the blocks of nodes each iteration finalises, in order (children
+  // before their parents), for the SAH collapse
+  std::vector<std::pair<uint64_t, uint64_t>> fin_blocks;
   while (end - begin > 1) {
     if (++iters > 100000)
       return set_err(ctx, AJG_ERR_DEVICE, "PLOC did not converge");
@@ -791,6 +942,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     const uint64_t children = merged * 2;
     const uint64_t children_begin = end - children;
     const uint64_t unmerged_begin = end - (children + unmerged);
+    fin_blocks.emplace_back(children_begin, end);
     k_cluster_scatter<<<grid_for(cnt, 256), 256, 0, st>>>(
         in, out, nbr, mi, (uint32_t)begin, (uint32_t)end,
         (uint32_t)unmerged_begin, (uint32_t)children_begin);
@@ -803,6 +955,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     end = children_begin;
   }
   const PNode* nodes = in;
+  fin_blocks.emplace_back(begin, end);  // the root
 
   // traversal layout
   cudaMemcpyAsync(ploc_nodes, nodes, m * sizeof(PNode),
@@ -833,6 +986,19 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     uint32_t* wc = tmp.get<uint32_t>(3);
     if (tmp.err != cudaSuccess)
       return set_err(ctx, AJG_ERR_OOM, "device allocation failed (wide BVH)");
+    const bool sah = AJG_SAH_COLLAPSE && wn == 4 && !compressed;
+    uint32_t* choice = nullptr;
+    if (sah) {
+      float4* cost = tmp.get<float4>(m);
+      choice = tmp.get<uint32_t>(m);
+      if (tmp.err != cudaSuccess)
+        return set_err(ctx, AJG_ERR_OOM, "device allocation failed (SAH collapse)");
+      for (const auto& b : fin_blocks) {
+        const uint32_t cnt = (uint32_t)(b.second - b.first);
+        k_sah_dp<<<grid_for(cnt, 256), 256, 0, st>>>(
+            nodes, (uint32_t)b.first, (uint32_t)b.second, cost, choice);
+      }
+    }
     const uint32_t init[3] = {0u, 1u, 0u};
     cudaMemcpyAsync(wc, init, sizeof(init), cudaMemcpyHostToDevice, st);
     const uint2 root = make_uint2(0u, 0u);
@@ -847,6 +1013,9 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
       else if (compressed)
         k_collapse_c<8><<<g, 128, 0, st>>>(nodes, slot_tris, fa, n_in, fb, wc,
                                            wtmp, tri_tmp);
+      else if (sah)
+        k_collapse_sah<<<g, 128, 0, st>>>(nodes, choice, fa, n_in, fb, wc,
+                                          wtmp);
       else if (wn == 4)
         k_collapse<4><<<g, 128, 0, st>>>(nodes, fa, n_in, fb, wc, wtmp);
       else
