@@ -27,7 +27,7 @@ from typing import Callable, Iterable
 import numpy as np
 
 LAYOUTS = (2, 4, 8, 4 | 0x100, 8 | 0x100)
-WAVES = (1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26, 1 << 27)
+WAVES = (1 << 22, 1 << 23, 1 << 24, 1 << 25, 1 << 26, 1 << 27, 1 << 28)
 DEFAULT_CACHE = Path(os.environ.get("AJG_TUNE_CACHE",
                                     Path.home() / ".cache" / "ajisai_gpu_tune.json"))
 

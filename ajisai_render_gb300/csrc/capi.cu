@@ -244,9 +244,9 @@ int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
     return fail(nullptr, AJG_ERR_INVALID, "device ordinal out of range");
   e = cudaSetDevice(dev);
   if (e != cudaSuccess) return fail(nullptr, AJG_ERR_CUDA, cudaGetErrorString(e));
-  // path x light-term slots (16 per path at most) stay 32-bit
-  if (cfg && cfg->wave_paths > (1u << 27))
-    return fail(nullptr, AJG_ERR_INVALID, "wave_paths above 2^27");
+  // each render also keeps paths x light terms below 2^31 (job_wave_paths)
+  if (cfg && cfg->wave_paths > (1u << 28))
+    return fail(nullptr, AJG_ERR_INVALID, "wave_paths above 2^28");
   auto* ctx = new ajg_ctx();
   ctx->device = dev;
   if (cfg && cfg->wave_paths) ctx->wave_paths = cfg->wave_paths;

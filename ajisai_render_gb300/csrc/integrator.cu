@@ -1028,11 +1028,14 @@ static int ensure_arena(ajg_ctx* ctx, uint64_t P, int nt, char** base) {
 // Paths per wave of a single-job render: the context's wave size, but no
 // more than the render needs (its paths, in whole KiB) and no more than
 // kArenaBytes of wave state for its light count.
-constexpr uint64_t kArenaBytes = 48ull << 30;
+constexpr uint64_t kArenaBytes = 96ull << 30;
 static uint64_t job_wave_paths(const ajg_ctx* ctx, uint64_t needed, int nt) {
   const uint64_t per_path = (wave_bytes(1u << 20, nt, false) >> 20) + 1;
   uint64_t P = std::min<uint64_t>(ctx->wave_paths, (needed + 1023) / 1024 * 1024);
   P = std::min<uint64_t>(P, kArenaBytes / per_path);
+  // the shadow queue (P x nt entries) is indexed by the traversal's 32-bit
+  // signed ray numbers, with 2^31 - 1 reserved
+  P = std::min<uint64_t>(P, ((1ull << 31) - 2) / (uint64_t)nt);
   return std::max<uint64_t>(1024, P / 1024 * 1024);
 }
 

@@ -213,7 +213,7 @@ struct ajg_ctx {
   // paths in flight per single-job wave: big enough that the persistent
   // traversal launches are long against their drain (a render takes no
   // more than it needs, and at most 48 GB of wave state)
-  uint32_t wave_paths = 1u << 27;
+  uint32_t wave_paths = 1u << 28;
   uint64_t hbm_budget = 0;
   uint64_t resident_bytes = 0;
   cudaStream_t stream = nullptr;

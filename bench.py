@@ -337,7 +337,7 @@ def run_ours(args):
                 "unit": "GB/s", "frac": achieved / peak if achieved else None,
                 "traffic": traffic_per_launch(kname, {
                     "res": args.res, "spp": args.spp,
-                    "wave_paths": args.wave_paths or (1 << 27),
+                    "wave_paths": args.wave_paths or (1 << 28),
                     "bvh_width": scene.info()["bvh_width"]}),
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "avg_launch_ms": avg_ms, "launches": int(st[l_k]),
@@ -414,7 +414,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene, no dataset)",
             "config": {**config(args), "bvh_width": scene.info()["bvh_width"],
-                       "wave_paths": args.wave_paths or (1 << 27),
+                       "wave_paths": args.wave_paths or (1 << 28),
                        "trace_overlap": os.environ.get("AJG_TRACE_OVERLAP", "1") != "0"},
             "clocks": clk, "e2e": e2e, "roofline": roofline,
             "cpu_baseline": cpu, "gpu_launches": launches_timed,

@@ -80,10 +80,11 @@ typedef struct ajg_scene ajg_scene;
 
 typedef struct ajg_config {
   int32_t device;            /* CUDA device ordinal */
-  uint32_t wave_paths;       /* paths in flight per wave (0: default 128 Mi;
-                                a render takes no more than its own paths
-                                and at most 48 GB of wave state; the request
-                                loop's default is at most 32 Mi) */
+  uint32_t wave_paths;       /* paths in flight per wave, at most 2^28
+                                (0: default 256 Mi; a render takes no more
+                                than its own paths, at most 96 GB of wave
+                                state, and fewer than 2^31 / (lights + 1);
+                                the request loop's default is at most 32 Mi) */
   uint64_t hbm_budget_bytes; /* admission budget for resident scenes and
                                 films (0: no limit) */
 } ajg_config;
