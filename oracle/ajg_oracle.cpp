@@ -463,11 +463,78 @@ struct Accel {
 
 inline bool tri_test(int mode, const Ray& r, const WtRay& w, const float* tri,
                      float* t, float* u, float* v) {
-  return mode == ORC_TEST_MT ? mt_test(r, tri, t, u, v)
-                             : wt_test(r, w, tri, t, u, v);
+  return mode == ORC_TEST_WATERTIGHT ? wt_test(r, w, tri, t, u, v)
+                                     : mt_test(r, tri, t, u, v);
+}
+
+/* IntersectP (ploc_aggregate.cpp:152-160): the near corner chosen per axis
+ * by the direction's sign, Vector::max()/min() folding Max(a, b) = a < b ?
+ * b : a and Min(a, b) = b < a ? b : a (math/vector.h:36-45, 380-400), no
+ * widening. */
+inline float ref_max(float a, float b) { return a < b ? b : a; }
+inline float ref_min(float a, float b) { return b < a ? b : a; }
+inline bool ref_slab(const Box& b, const Ray& r, V3 inv) {
+  const bool nx = inv.x < 0.f, ny = inv.y < 0.f, nz = inv.z < 0.f;
+  const float n0 = ((nx ? b.hi.x : b.lo.x) - r.o.x) * inv.x;
+  const float n1 = ((ny ? b.hi.y : b.lo.y) - r.o.y) * inv.y;
+  const float n2 = ((nz ? b.hi.z : b.lo.z) - r.o.z) * inv.z;
+  const float f0 = ((nx ? b.lo.x : b.hi.x) - r.o.x) * inv.x;
+  const float f1 = ((ny ? b.lo.y : b.hi.y) - r.o.y) * inv.y;
+  const float f2 = ((nz ? b.lo.z : b.hi.z) - r.o.z) * inv.z;
+  const float tn = ref_max(ref_max(n0, n1), n2);
+  const float tf = ref_min(ref_min(f0, f1), f2);
+  if (tn > tf) return false;
+  return tn < r.tmax && tf > r.tmin;
+}
+
+/* PLOCAggregate::Intersect / IntersectAux (ploc_aggregate.cpp:329-391):
+ * depth first, left child before right, each node's slab test against the
+ * current t_max, which a hit shrinks to its t (Triangle::Intersect,
+ * :184-216, accepts t in (t_min, t_max)). */
+Hit trace_closest_ref(const Accel& acc, Ray r) {
+  Hit h{std::numeric_limits<float>::infinity(), 0.f, 0.f, -1};
+  V3 inv = mk(1.f / r.d.x, 1.f / r.d.y, 1.f / r.d.z);
+  SmallStack st;
+  st.push(0);
+  while (!st.empty()) {
+    const Node& nd = acc.nodes[st.pop()];
+    if (!ref_slab(nd.b, r, inv)) continue;
+    if (nd.count) {
+      const int32_t prim = (int32_t)acc.perm[nd.first];
+      float t, u, v;
+      if (mt_test(r, acc.tris + 9 * (int64_t)prim, &t, &u, &v) && t < h.t) {
+        h = Hit{t, u, v, prim};
+        r.tmax = t;
+      }
+    } else {
+      st.push(nd.first + 1);
+      st.push(nd.first);
+    }
+  }
+  return h;
+}
+
+/* PLOCAggregate::Occlude / OccludeAux (ploc_aggregate.cpp:337-365). */
+bool trace_any_ref(const Accel& acc, const Ray& r) {
+  V3 inv = mk(1.f / r.d.x, 1.f / r.d.y, 1.f / r.d.z);
+  SmallStack st;
+  st.push(0);
+  float t, u, v;
+  while (!st.empty()) {
+    const Node& nd = acc.nodes[st.pop()];
+    if (!ref_slab(nd.b, r, inv)) continue;
+    if (nd.count) {
+      if (mt_test(r, acc.tris + 9 * acc.perm[nd.first], &t, &u, &v)) return true;
+    } else {
+      st.push(nd.first + 1);
+      st.push(nd.first);
+    }
+  }
+  return false;
 }
 
 Hit trace_closest(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
+  if (mode == ORC_TEST_REF_ORDER && use_bvh) return trace_closest_ref(acc, r);
   Hit h{std::numeric_limits<float>::infinity(), 0.f, 0.f, -1};
   WtRay w = wt_setup(r);
   auto consider = [&](int32_t prim) {
@@ -499,6 +566,7 @@ Hit trace_closest(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
 }
 
 bool trace_any(const Accel& acc, const Ray& r, int mode, bool use_bvh) {
+  if (mode == ORC_TEST_REF_ORDER && use_bvh) return trace_any_ref(acc, r);
   WtRay w = wt_setup(r);
   float t, u, v;
   if (!use_bvh) {

@@ -63,7 +63,13 @@ enum {
 };
 enum { ORC_LIGHT_DIRECTIONAL = 0, ORC_LIGHT_ENV = 1, ORC_LIGHT_AREA = 2 };
 enum { ORC_GEOM_QUAD = 0, ORC_GEOM_CUBE = 1, ORC_GEOM_MESH = 2 };
-enum { ORC_TEST_MT = 0, ORC_TEST_WATERTIGHT = 1 };
+/* ORC_TEST_REF_ORDER: Moller-Trumbore inside the reference's own traversal
+ * (its slab test, left child first, a strictly closer hit replacing the
+ * best), so that of two triangles at one t the first visited wins, as in
+ * PLOCAggregate::Intersect (ploc_aggregate.cpp:329-391) -- the mode that
+ * pins the oracle to the reference bit for bit on rays that hit an edge.
+ * The other two modes give ties to the lowest primitive index. */
+enum { ORC_TEST_MT = 0, ORC_TEST_WATERTIGHT = 1, ORC_TEST_REF_ORDER = 2 };
 
 /* SPPMRenderer::Render restated (sppm.cpp:180-296) over a scene of
  * orc_scene_create; see ajg_oracle.cpp for the sampler streams.

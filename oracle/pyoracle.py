@@ -128,6 +128,15 @@ class OracleScene:
         assert rc == 0
         return li, film
 
+    def render_window(self, camera, params, seed, x0, y0, w, h, threads=None):
+        """Per-sample radiance [h, w, spp, 3] of a window of the film (one
+        pixel range per row), each pixel keyed as in the full render."""
+        W = int(_c(camera, np.float32)[34])
+        rows = [self.render(camera, params, seed,
+                            pixel_range=((y0 + r) * W + x0, (y0 + r) * W + x0 + w),
+                            per_sample=True, threads=threads)[0] for r in range(h)]
+        return np.stack(rows)
+
     def close(self):
         if self.h:
             lib().orc_scene_destroy(self.h)
@@ -262,6 +271,9 @@ def ref():
         L.ref_scene_render.argtypes = [C.c_void_p, _f64p, C.c_uint64, _f32p,
                                        _f32p]
         L.ref_scene_render.restype = C.c_int
+        L.ref_scene_render_window.argtypes = [C.c_void_p, _f64p, C.c_uint64, C.c_int,
+                                              C.c_int, C.c_int, C.c_int, _f32p]
+        L.ref_scene_render_window.restype = C.c_int
         L.ref_camera_rays.argtypes = [C.c_void_p, _f32p, C.c_int64, _f32p]
         L.ref_has_diffuse.argtypes = [_f32p]
         L.ref_has_diffuse.restype = C.c_int
@@ -396,6 +408,18 @@ class RefScene:
         rc = ref().ref_scene_render(self.h, p, seed, li, film)
         assert rc == 0
         return li, film
+
+    def render_window(self, params, seed, x0, y0, w, h):
+        """Per-sample radiance [h, w, spp, 3] of a window of the film, each
+        pixel keyed as in the full render."""
+        spp = int(params["spp"])
+        p = np.array([spp, params.get("min_bounces", 5),
+                      params.get("max_bounces", 10), params.get("cont_prob", 0.9),
+                      params.get("use_mis", 1), 0, 0, 0], np.float64)
+        li = np.zeros((h, w, spp, 3), np.float32)
+        rc = ref().ref_scene_render_window(self.h, p, seed, x0, y0, w, h, li)
+        assert rc == 0, rc
+        return li
 
     def sppm(self, params, seed=0):
         """SPPMRenderer::Render over the reference's own SPPM functions (see

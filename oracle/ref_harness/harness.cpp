@@ -564,6 +564,41 @@ int ref_scene_render(void* h, const double* params, uint64_t seed,
   return 0;
 }
 
+/* Per-sample radiance of a window [x0, x0+w) x [y0, y0+h) of the film, the
+ * pixels keyed as in the full render (SetSeed(x + y * W)), so a window of a
+ * large film gives exactly the full render's samples there without tracing
+ * the rest.  out_li [h][w][spp][3]. */
+int ref_scene_render_window(void* h, const double* params, uint64_t seed,
+                            int x0, int y0, int w, int hh, float* out_li) {
+  auto* s = static_cast<HScene*>(h);
+  PTRendererArgs a{(int)params[0], 16, (int)params[1], (int)params[2],
+                   (float)params[3], params[4] != 0, 20};
+  auto integ = std::dynamic_pointer_cast<Integrator>(CreatePTRenderer(a));
+  if (!integ || !s->camera) return -1;
+  const int W = s->width, H = s->height, spp = a.spp;
+  if (x0 < 0 || y0 < 0 || w < 0 || hh < 0 || x0 + w > W || y0 + hh > H) return -2;
+  MemoryArena arena;
+  CounterSampler smp;
+  smp.seed = seed;
+  for (int y = y0; y < y0 + hh; ++y)
+    for (int x = x0; x < x0 + w; ++x) {
+      smp.SetSeed(x + y * W);
+      for (int k = 0; k < spp; ++k) {
+        smp.Begin((uint32_t)k);
+        const float u = x + smp.Next1D();
+        const float v = y + smp.Next1D();
+        auto ray = s->camera->GenerateRay(Vector2f{u, v}, smp.Next2D());
+        auto li = integ->Li(ray, s->scene.get(), &smp, arena);
+        float* o = out_li + 3 * (((int64_t)(y - y0) * w + (x - x0)) * spp + k);
+        o[0] = li.value[0];
+        o[1] = li.value[1];
+        o[2] = li.value[2];
+      }
+      arena.Release();
+    }
+  return 0;
+}
+
 /* Camera rays straight from ThinLensCamera::GenerateRay, for the raygen
  * parity check: raster [n][4] (x, y, lens u, lens v) -> rays [n][6]. */
 void ref_camera_rays(void* h, const float* raster, int64_t n, float* rays) {

@@ -1,3 +1,5 @@
+import json
+import os
 import sys
 from pathlib import Path
 
@@ -22,3 +24,17 @@ def golden():
         with np.load(GOLDEN / name) as z:
             return {k: z[k] for k in z.files}
     return load
+
+
+@pytest.fixture(scope="session")
+def parity_report():
+    """A dict the parity tests record their measured agreement in; written
+    at the end of the session to the JSON file named by $AJG_PARITY_REPORT
+    (merged with what the file holds), when that is set."""
+    rep = {}
+    yield rep
+    path = os.environ.get("AJG_PARITY_REPORT")
+    if path and rep:
+        old = json.loads(Path(path).read_text()) if os.path.exists(path) else {}
+        old.update(rep)
+        Path(path).write_text(json.dumps(old, indent=1, sort_keys=True) + "\n")

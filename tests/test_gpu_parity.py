@@ -34,6 +34,43 @@ def same_bits(a, b):
     return np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
 
 
+def film_sigma(li, W, H):
+    """Standard deviation [H, W, 3] of each film pixel's radiance sum from
+    the per-sample radiance li [H*W, spp, 3]: a sample at (x, y) lands on
+    targets (x-1..x, y-1..y) and row/column -1 folds into 0 (film.cpp:27-63),
+    so target (tx, ty) sums the sums of sources tx..tx+1, ty..ty+1, the
+    source at 0 twice on a folded axis."""
+    li = np.asarray(li, np.float64).reshape(H, W, -1, 3)
+    fin = np.isfinite(li).all(axis=(2, 3))
+    v = np.where(fin[..., None], li.shape[2] * np.nan_to_num(li).var(2), 0.0)
+    out = np.zeros((H, W, 3))
+    for dy in (0, 1):
+        for dx in (0, 1):
+            m = np.ones((H, W))
+            if dy == 0:
+                m[0, :] *= 2
+            if dx == 0:
+                m[:, 0] *= 2
+            src = np.zeros((H, W, 3))
+            src[:H - dy, :W - dx] = v[dy:, dx:]
+            out += (m ** 2)[..., None] * src
+    return np.sqrt(out)
+
+
+def film_agreement(film, ref_film, li_ref):
+    """(fraction of pixels whose radiance sums agree within 1e-5 relative,
+    fraction within 3 sigma of the sum's sample spread) over the pixels both
+    films hold finite; the weights must be equal bit for bit."""
+    H, W = film.shape[:2]
+    assert np.array_equal(film[..., 3], np.asarray(ref_film[..., 3], np.float32))
+    a = np.asarray(film[..., :3], np.float64)
+    b = np.asarray(ref_film[..., :3], np.float64)
+    ok = np.isfinite(a).all(-1) & np.isfinite(b).all(-1)
+    rel = (np.abs(a - b) <= 1e-5 * np.maximum(np.abs(b), 1e-3)).all(-1)
+    sig = (np.abs(a - b) <= 3 * film_sigma(li_ref, W, H) + 1e-5 * np.abs(b) + 1e-6).all(-1)
+    return float(rel[ok].mean()), float(sig[ok].mean())
+
+
 # ------------------------------------------------------------------ PLOC --
 @pytest.mark.parametrize("case", ["ploc_cornell.npz", "ploc_ico4.npz",
                                   "ploc_soup.npz", "ploc_flat.npz"])
@@ -313,11 +350,22 @@ def params_of(g):
                               use_mis=bool(p[4]))
 
 
-@pytest.mark.parametrize("case", ["render_cornell.npz", "render_ico.npz",
-                                  "render_cornell_nomis.npz", "render_area.npz",
-                                  "render_area_nomis.npz", "render_materials.npz",
-                                  "render_materials_nomis.npz"])
-def test_render_per_sample_matches_reference(ctx, golden, case):
+# Per fixture, the least fraction of samples within 1e-4 relative of the
+# reference's and of film pixels within 1e-5 relative, below the measured
+# GB300 values (in the parity report).
+RENDER_BOUNDS = {
+    "render_cornell.npz": (1.0, 1.0),
+    "render_ico.npz": (0.99, 0.99),
+    "render_cornell_nomis.npz": (1.0, 1.0),
+    "render_area.npz": (0.99, 0.97),
+    "render_area_nomis.npz": (0.99, 0.97),
+    "render_materials.npz": (0.99, 0.97),
+    "render_materials_nomis.npz": (0.99, 0.97),
+}
+
+
+@pytest.mark.parametrize("case", list(RENDER_BOUNDS))
+def test_render_per_sample_matches_reference(ctx, golden, case, parity_report):
     """Shared counter sampler: each sample's radiance equals the reference's
     within float32 tolerance, apart from rare paths that a last-ulp
     difference of CUDA's transcendentals sends another way.  The area-light
@@ -330,7 +378,6 @@ def test_render_per_sample_matches_reference(ctx, golden, case):
     li = r.RenderSamples(sc, flat.camera)
     ref = g["li"]
     close = np.isclose(li, ref, rtol=1e-4, atol=1e-6, equal_nan=True).all(axis=-1)
-    assert close.mean() > 0.99, close.mean()
     # per-pixel means agree within 3 sigma of the sample spread (pixels
     # without a non-finite sample)
     spp = ref.shape[1]
@@ -339,18 +386,24 @@ def test_render_per_sample_matches_reference(ctx, golden, case):
     m_gpu, m_ref = li[fin].mean(1), ref[fin].mean(1)
     sigma = np.maximum(ref[fin].std(1), 1e-3) / np.sqrt(spp)
     within = (np.abs(m_gpu - m_ref) <= 3 * sigma + 1e-5).all(axis=-1)
-    assert within.mean() > 0.99
     # the film from Render() is the footprint sum of the same samples
     film = r.Render(sc, flat.camera)
-    fg, fr = film.rgbw[..., :3], g["film"][..., :3]
-    ok_g, ok_r = np.isfinite(fg).all(-1), np.isfinite(fr).all(-1)
-    assert (ok_g == ok_r).mean() > 0.97
-    np.testing.assert_allclose(fg[ok_g & ok_r], fr[ok_g & ok_r], rtol=1e-3,
-                               atol=1e-3 * spp)
-    assert np.array_equal(film.rgbw[..., 3], g["film"][..., 3])
+    ok_g = np.isfinite(film.rgbw[..., :3]).all(-1)
+    ok_r = np.isfinite(g["film"][..., :3]).all(-1)
+    film_rel, film_3s = film_agreement(film.rgbw, g["film"], ref)
+    parity_report[case] = dict(samples_within_1e4=float(close.mean()),
+                               pixel_means_within_3sigma=float(within.mean()),
+                               film_within_1e5=film_rel, film_within_3sigma=film_3s,
+                               film_finite_agree=float((ok_g == ok_r).mean()))
+    msg = str(parity_report[case])
+    lo_s, lo_f = RENDER_BOUNDS[case]
+    assert close.mean() >= lo_s, msg
+    assert within.mean() >= 0.99, msg
+    assert film_rel >= lo_f and film_3s >= 0.99, msg
+    assert (ok_g == ok_r).mean() > 0.97, msg
 
 
-def test_render_matches_oracle_film_and_is_deterministic(ctx):
+def test_render_matches_oracle_film_and_is_deterministic(ctx, parity_report):
     sc_spec = S.cornell_box(48, 40)
     flat = S.flatten(sc_spec)
     sc = api.GpuScene(ctx, flat)
@@ -360,8 +413,10 @@ def test_render_matches_oracle_film_and_is_deterministic(ctx):
     f2 = r.Render(sc, flat.camera).rgbw.copy()
     assert same_bits(f1, f2)
     li_o, film_o = O.render(flat, dict(spp=16, min_bounces=3, max_bounces=8), seed=3)
-    assert np.array_equal(f1[..., 3], film_o[..., 3].astype(np.float32))
-    np.testing.assert_allclose(f1[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
+    rel, s3 = film_agreement(f1, film_o, li_o)
+    parity_report["cornell_48x40x16_film"] = dict(film_within_1e5=rel,
+                                                  film_within_3sigma=s3)
+    assert rel >= 0.999 and s3 >= 0.9999, (rel, s3)
 
 
 @pytest.mark.parametrize("width", LAYOUTS[1:])
@@ -426,7 +481,7 @@ def _area_no_mesh(w, h):
 
 
 @pytest.mark.parametrize("use_mis", [True, False])
-def test_area_lights_match_oracle_per_sample(ctx, use_mis):
+def test_area_lights_match_oracle_per_sample(ctx, use_mis, parity_report):
     """Quad (one- and two-sided), mesh and cube emitters at a size the
     reference fixtures do not reach, against the oracle sample by sample."""
     flat = S.flatten(S.cornell_area(40, 32))
@@ -438,6 +493,8 @@ def test_area_lights_match_oracle_per_sample(ctx, use_mis):
                                  use_mis=int(use_mis)), seed=11)
     ref = ref.reshape(li.shape)
     close = np.isclose(li, ref, rtol=1e-4, atol=1e-6, equal_nan=True).all(axis=-1)
+    parity_report[f"area_40x32x8_mis{int(use_mis)}"] = dict(
+        samples_within_1e4=float(close.mean()))
     assert close.mean() > 0.99, close.mean()
     if use_mis:  # the mesh emitter's NaN samples are there, as in the reference
         assert np.isnan(ref).any()
@@ -464,7 +521,7 @@ def test_area_lights_tree_independent(ctx, width):
     assert same_bits(a, b)
 
 
-def test_area_lights_wave_split_and_film(ctx):
+def test_area_lights_wave_split_and_film(ctx, parity_report):
     """Small waves give the same samples; the film equals the oracle's."""
     flat = S.flatten(_area_no_mesh(24, 20))
     args = api.PTRendererArgs(spp=8, min_bounces=3, max_bounces=8)
@@ -474,9 +531,10 @@ def test_area_lights_wave_split_and_film(ctx):
     small.close()
     assert same_bits(a, b)
     film = api.PTRenderer(args, seed=2).Render(api.GpuScene(ctx, flat), flat.camera).rgbw
-    _, film_o = O.render(flat, dict(spp=8, min_bounces=3, max_bounces=8), seed=2)
-    assert np.array_equal(film[..., 3], film_o[..., 3].astype(np.float32))
-    np.testing.assert_allclose(film[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
+    li_o, film_o = O.render(flat, dict(spp=8, min_bounces=3, max_bounces=8), seed=2)
+    rel, s3 = film_agreement(film, film_o, li_o)
+    parity_report["area_24x20x8_film"] = dict(film_within_1e5=rel, film_within_3sigma=s3)
+    assert rel >= 0.99 and s3 >= 0.999, (rel, s3)
 
 
 def test_invalid_emitters_are_rejected(ctx):
@@ -521,7 +579,7 @@ def test_invalid_emitters_are_rejected(ctx):
 
 # -------------------------------------------------------- more materials --
 @pytest.mark.parametrize("use_mis", [True, False])
-def test_materials_match_oracle_per_sample(ctx, use_mis):
+def test_materials_match_oracle_per_sample(ctx, use_mis, parity_report):
     """Plastic, mirror, metal, glass and a null-material emitter at 40x32x8
     against the oracle; tree layouts and wave sizes give the same samples."""
     flat = S.flatten(S.material_box(40, 32))
@@ -531,6 +589,8 @@ def test_materials_match_oracle_per_sample(ctx, use_mis):
                                  use_mis=int(use_mis)), seed=21)
     ref = ref.reshape(li.shape)
     close = np.isclose(li, ref, rtol=1e-4, atol=1e-6, equal_nan=True).all(axis=-1)
+    parity_report[f"materials_40x32x8_mis{int(use_mis)}"] = dict(
+        samples_within_1e4=float(close.mean()))
     assert close.mean() > 0.98, close.mean()
     for width in (2, 0x108):
         b = api.PTRenderer(args, seed=21).RenderSamples(
@@ -599,7 +659,7 @@ def test_sppm_matches_oracle_and_is_stable(ctx):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("min_b", [-1, 0])
-def test_roulette_from_the_first_bounce_matches_oracle(ctx, min_b):
+def test_roulette_from_the_first_bounce_matches_oracle(ctx, min_b, parity_report):
     """min_bounces -1 rolls the roulette before bounce 0 (paths can end
     before their camera ray is traced: ray generation then compacts its
     queue); 0 rolls it from bounce 1 on.  Film weights are exact and the
@@ -608,6 +668,8 @@ def test_roulette_from_the_first_bounce_matches_oracle(ctx, min_b):
     sc = api.GpuScene(ctx, flat)
     args = api.PTRendererArgs(spp=16, min_bounces=min_b, max_bounces=8)
     f = api.PTRenderer(args, seed=7).Render(sc, flat.camera).rgbw
-    _, film_o = O.render(flat, dict(spp=16, min_bounces=min_b, max_bounces=8), seed=7)
-    assert np.array_equal(f[..., 3], film_o[..., 3].astype(np.float32))
-    np.testing.assert_allclose(f[..., :3], film_o[..., :3], rtol=1e-3, atol=0.05)
+    li_o, film_o = O.render(flat, dict(spp=16, min_bounces=min_b, max_bounces=8), seed=7)
+    rel, s3 = film_agreement(f, film_o, li_o)
+    parity_report[f"cornell_roulette_{min_b}_film"] = dict(film_within_1e5=rel,
+                                                          film_within_3sigma=s3)
+    assert rel >= 0.999 and s3 >= 0.9999, (rel, s3)
