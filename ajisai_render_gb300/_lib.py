@@ -100,6 +100,11 @@ class Stats(C.Structure):
             "closest_ms", "any_ms", "shade_ms")]
 
 
+class LaunchRecord(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("ms", C.c_float), ("rays", C.c_uint64),
+                ("nodes", C.c_uint64), ("tris", C.c_uint64)]
+
+
 class JobDesc(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("params", RenderParams),
                 ("window", C.c_uint32 * 4), ("progress_spp", C.c_uint32),
@@ -128,6 +133,7 @@ class ServeStats(C.Structure):
 
 
 assert C.sizeof(Material) == 64 and C.sizeof(Light) == 48
+assert C.sizeof(LaunchRecord) == 32
 assert C.sizeof(Camera) == 144 and C.sizeof(RenderParams) == 32
 
 _P = C.c_void_p
@@ -138,6 +144,8 @@ SIGNATURES = {
     "ajg_last_error": ([_P], C.c_char_p),
     "ajg_get_stats": ([_P, C.POINTER(Stats), C.c_int], C.c_int),
     "ajg_set_profiling": ([_P, C.c_int], C.c_int),
+    "ajg_get_launch_log": ([_P, C.POINTER(LaunchRecord), C.c_uint32,
+                            C.POINTER(C.c_uint32), C.c_int], C.c_int),
     "ajg_scene_create": ([_P, C.POINTER(MeshDesc), C.c_uint32, C.POINTER(Material),
                           C.c_uint32, C.POINTER(Light), C.c_uint32,
                           C.POINTER(SceneOpts), C.POINTER(_P)], C.c_int),

@@ -65,6 +65,20 @@ class Context:
         self.check(self.lib.ajg_get_stats(self.h, C.byref(s), int(reset)))
         return {n: getattr(s, n) for n, _ in s._fields_}
 
+    KINDS = ("closest", "any", "shade")
+
+    def launch_log(self, reset: bool = True) -> list:
+        """The launches timed since the last reset (profiling on): per
+        launch its kind, device ms, and the rays, node visits and triangle
+        tests of that launch alone."""
+        n = C.c_uint32()
+        self.check(self.lib.ajg_get_launch_log(self.h, None, 0, C.byref(n), 0))
+        recs = (_lib.LaunchRecord * max(1, n.value))()
+        self.check(self.lib.ajg_get_launch_log(self.h, recs, n.value, C.byref(n),
+                                               int(reset)))
+        return [{"kind": self.KINDS[r.kind], "ms": r.ms, "rays": r.rays,
+                 "nodes": r.nodes, "tris": r.tris} for r in recs[:n.value]]
+
     def bsdf_query(self, materials, ng, ns, wo, wi, sam, op):
         """BSDF::EvalAll+PdfAll (op 0) or SampleAll (op 1) after
         Material::Shade, one query per row; returns [n, 8]."""

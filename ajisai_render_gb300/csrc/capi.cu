@@ -46,6 +46,7 @@ int check_device(ajg_ctx* ctx) {
                      : e == kDevQueueOverflow    ? "queue capacity exceeded"
                      : e == kDevIterationBound   ? "iteration bound reached"
                      : e == kDevSortOutOfBounds  ? "sort out of bounds"
+                     : e == kDevTableOutOfBounds ? "wave table index out of bounds"
                                                  : "unknown device guard";
   return fail(ctx, AJG_ERR_DEVICE, std::string("device guard: ") + what);
 }
@@ -287,12 +288,59 @@ int ajg_destroy_context(ajg_ctx* ctx) {
   cudaFree(ctx->d_error);
   cudaFree(ctx->d_fetch);
   cudaFree(ctx->d_counters);
+  if (ctx->h_snaps) cudaFreeHost(ctx->h_snaps);
   cudaStreamSynchronize(ctx->trace_stream);
   cudaEventDestroy(ctx->ev_queue);
   cudaEventDestroy(ctx->ev_hits);
   cudaStreamDestroy(ctx->trace_stream);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+  return AJG_OK;
+}
+
+// Turns the recorded event pairs into milliseconds per kind and launch
+// records (after the context's stream is synchronised).
+static void resolve_timings(ajg_ctx* ctx) {
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    ctx->kind_ms[p.kind] += ms;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+    ajg_launch_record r{};
+    r.kind = (uint32_t)p.kind;
+    r.ms = ms;
+    if (p.snap >= 0) {
+      const TraceCounters c = ctx->h_snaps[p.snap];
+      const TraceCounters& l = ctx->last_snap[p.kind];
+      r.rays = c.rays - l.rays;
+      r.nodes = c.nodes - l.nodes;
+      r.tris = c.tris - l.tris;
+      ctx->last_snap[p.kind] = c;
+    }
+    if (ctx->launch_log.size() < (size_t)kLaunchLogCap)
+      ctx->launch_log.push_back(r);
+  }
+  ctx->pending.clear();
+}
+
+int ajg_get_launch_log(ajg_ctx* ctx, ajg_launch_record* out, uint32_t capacity,
+                       uint32_t* count, int reset) {
+  if (!ctx || !count) return fail(ctx, AJG_ERR_INVALID, "NULL argument");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream), "launch log");
+  CK(cudaStreamSynchronize(ctx->trace_stream), "launch log");
+  resolve_timings(ctx);
+  *count = (uint32_t)ctx->launch_log.size();
+  if (out)
+    std::memcpy(out, ctx->launch_log.data(),
+                sizeof(ajg_launch_record) *
+                    std::min<size_t>(capacity, ctx->launch_log.size()));
+  if (reset) {
+    ctx->launch_log.clear();
+    ctx->n_snaps = 0;
+  }
   return AJG_OK;
 }
 
@@ -313,14 +361,7 @@ int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset) {
   out->nodes_visited = c[0].nodes + c[1].nodes;
   out->tris_tested = c[0].tris + c[1].tris;
   out->paths = ctx->paths_total;
-  for (auto& p : ctx->pending) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, p.a, p.b);
-    ctx->kind_ms[p.kind] += ms;
-    cudaEventDestroy(p.a);
-    cudaEventDestroy(p.b);
-  }
-  ctx->pending.clear();
+  resolve_timings(ctx);
   out->kernel_launches = ctx->kernel_launches;
   out->closest_launches = ctx->kind_launches[kKindClosest];
   out->any_launches = ctx->kind_launches[kKindAny];
@@ -330,6 +371,7 @@ int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset) {
   out->shade_ms = ctx->kind_ms[kKindShade];
   if (reset) {
     CK(cudaMemset(ctx->d_counters, 0, sizeof(c)), "stats");
+    for (auto& l : ctx->last_snap) l = TraceCounters{};
     ctx->paths_total = 0;
     ctx->kernel_launches = 0;
     for (int k = 0; k < kKinds; ++k) {
@@ -343,6 +385,19 @@ int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset) {
 int ajg_set_profiling(ajg_ctx* ctx, int enable) {
   if (!ctx) return fail(nullptr, AJG_ERR_INVALID, "NULL context");
   std::lock_guard<std::mutex> lk(ctx->mu);
+  if (enable && !ctx->h_snaps) {
+    cudaSetDevice(ctx->device);
+    CK(cudaHostAlloc((void**)&ctx->h_snaps,
+                     sizeof(TraceCounters) * kLaunchLogCap, cudaHostAllocDefault),
+       "launch log");
+  }
+  if (enable && !ctx->profiling) {
+    // counters the log's first deltas start from
+    CK(cudaStreamSynchronize(ctx->stream), "profiling");
+    CK(cudaMemcpy(ctx->last_snap, ctx->d_counters, sizeof(ctx->last_snap),
+                  cudaMemcpyDeviceToHost),
+       "profiling");
+  }
   ctx->profiling = enable != 0;
   return AJG_OK;
 }

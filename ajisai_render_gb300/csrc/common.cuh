@@ -128,7 +128,8 @@ enum DeviceError : uint32_t {
   kDevStackOverflow = 1,
   kDevQueueOverflow = 2,
   kDevIterationBound = 3,
-  kDevSortOutOfBounds = 4
+  kDevSortOutOfBounds = 4,
+  kDevTableOutOfBounds = 5  // a multi-job wave's job, scene or chunk index
 };
 __device__ __forceinline__ void raise_device_error(uint32_t* flag,
                                                    uint32_t code) {

@@ -68,6 +68,32 @@ struct WaveArgs {
   VisPointD* vp;  // SPPM camera pass: the visible points (else null)
 };
 
+// Multi-job table guards: a job or scene index past its table records
+// kDevTableOutOfBounds in the request loop's error word (the wave's jobs
+// then fail with AJG_ERR_DEVICE) and is replaced by 0, so that no read
+// leaves the tables the host uploaded for the wave.
+__device__ __forceinline__ uint32_t mj_job(const MJTables& t, uint32_t jid) {
+  if (jid < t.hdr->n_jobs) return jid;
+  raise_device_error(t.err, kDevTableOutOfBounds);
+  return 0;
+}
+__device__ __forceinline__ uint32_t mj_scene(const MJTables& t, uint32_t sid) {
+  if (sid < t.hdr->n_scenes) return sid;
+  raise_device_error(t.err, kDevTableOutOfBounds);
+  return 0;
+}
+// A wave whose header is out of range (more chunks than the kernels'
+// shared offset tables hold, or more paths than the arena) runs nothing.
+__device__ __forceinline__ bool mj_wave_ok(const MJTables& t) {
+  const WaveHeader& h = *t.hdr;
+  if (h.n_chunks <= (uint32_t)kMaxWaveChunks && h.n_jobs <= (uint32_t)kMaxWaveChunks &&
+      h.n_scenes <= (uint32_t)kMaxWaveChunks && h.n_paths <= h.cap_paths)
+    return true;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    raise_device_error(t.err, kDevTableOutOfBounds);
+  return false;
+}
+
 // Where a kernel finds the job and the scene of a path: the kernel
 // arguments (single job) or the wave tables (multi-job).
 template <bool MJ>
@@ -93,7 +119,7 @@ struct Src<true> {
   }
   static __device__ __forceinline__ const DeviceScene& scene(
       const WaveArgs&, const MJTables& t, uint32_t jid) {
-    return t.scenes[t.jobs[jid].scene];
+    return t.scenes[mj_scene(t, t.jobs[jid].scene)];
   }
 };
 
@@ -150,6 +176,7 @@ __global__ void __launch_bounds__(kShadeThreads)
   if (all_alive && blockIdx.x == 0 && threadIdx.x == 0)
     atomicAdd(&w.counts[0], n_paths);
   if constexpr (MJ) {
+    if (!mj_wave_ok(t)) return;  // uniform: every thread reads one header
     n_paths = t.hdr->n_paths;
     n_chunks = t.hdr->n_chunks;
     for (uint32_t c = threadIdx.x; c < n_chunks; c += blockDim.x)
@@ -170,14 +197,15 @@ __global__ void __launch_bounds__(kShadeThreads)
       const uint32_t q = p - C.path_off;
       const uint32_t i = C.pix0 + q / C.S;
       const uint32_t sample = C.s0 + q % C.S;
-      const JobRec& R = t.jobs[C.job];
+      const uint32_t jid = mj_job(t, C.job);
+      const JobRec& R = t.jobs[jid];
       const int x = (int)(R.j.x0 + i % R.j.win_w);
       const int y = (int)(R.j.y0 + i / R.j.win_w);
       const uint64_t key =
           path_key(R.j.seed, (uint32_t)y * R.j.film_w + (uint32_t)x, sample);
-      w.pjob[p] = C.job;
+      w.pjob[p] = jid;
       w.pkey[p] = key;
-      sid = R.scene;
+      sid = mj_scene(t, R.scene);
       raygen_path(R.cam, R.j, key, x, y, ro, rd, T, alive);
     } else {
       uint32_t pixel, sample;
@@ -203,7 +231,7 @@ __global__ void __launch_bounds__(kShadeThreads)
 
 __device__ __forceinline__ void retarget(TraceScene& ts, const MJTables& t,
                                          uint32_t sid) {
-  const DeviceScene& sc = t.scenes[sid];
+  const DeviceScene& sc = t.scenes[mj_scene(t, sid)];
   ts.bvh = sc.bvh;
   ts.tris = sc.tris;
   ts.max_visits = sc.num_inner + 1;
@@ -262,7 +290,7 @@ __global__ void __launch_bounds__(kClassifyThreads)
         const float4* shade = s.shade;
         const float* materials = s.materials;
         if constexpr (MJ) {
-          const DeviceScene& sc = t.scenes[__float_as_uint(ro[k].w)];
+          const DeviceScene& sc = t.scenes[mj_scene(t, __float_as_uint(ro[k].w))];
           shade = sc.shade;
           materials = sc.materials;
         }
@@ -352,7 +380,7 @@ __global__ void __launch_bounds__(kShadeThreads)
     const float4 o4 = w.sq_o[i], d4 = w.sq_d[i];
     const uint32_t slot = __float_as_uint(d4.w);
     const uint32_t p = slot / NT;
-    const uint32_t jid = MJ ? w.pjob[p] : 0u;
+    const uint32_t jid = MJ ? mj_job(t, w.pjob[p]) : 0u;
     const JobParams& J = Src<MJ>::job(a, t, jid);
     const DeviceScene& s = Src<MJ>::scene(a, t, jid);
     const F3 o = xyz(o4), d = xyz(d4);
@@ -451,7 +479,7 @@ __global__ void k_shade_miss(WaveArgs a, MJTables t, WaveBufs w, int b,
     const uint32_t p = w.qpath[cur][list[j]];
     float4 env = a.j.env_rgb;
     if constexpr (MJ) {
-      const uint32_t jid = w.pjob[p];
+      const uint32_t jid = mj_job(t, w.pjob[p]);
       const JobParams& J = t.jobs[jid].j;
       if (!(b == 0 || !J.use_mis) || Src<true>::scene(a, t, jid).env < 0)
         continue;
@@ -490,11 +518,11 @@ __global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
     if (hit) {
       k = list[j];
       p = w.qpath[cur][k];
-      if constexpr (MJ) jid = w.pjob[p];
+      if constexpr (MJ) jid = mj_job(t, w.pjob[p]);
     }
     const JobParams& J = Src<MJ>::job(a, t, jid);
     const DeviceScene& s = Src<MJ>::scene(a, t, jid);
-    const uint32_t sid = MJ ? t.jobs[jid].scene : 0u;
+    const uint32_t sid = MJ ? mj_scene(t, t.jobs[jid].scene) : 0u;
     HitInfo hi;
     BsdfT<MAT> f;
     F3 T = mk3(0, 0, 0);
@@ -759,9 +787,13 @@ __global__ void __launch_bounds__(kShadeThreads)
     const uint32_t p = w.qpath[cur][k];
     int nl = (int)a.s.num_lights;
     if constexpr (MJ) {
-      const JobParams& J = t.jobs[w.pjob[p]].j;
+      const JobParams& J = t.jobs[mj_job(t, w.pjob[p])].j;
       if (!J.use_mis) continue;
       nl = J.nl;
+      if (nl + 1 > (int)NT) {  // the arena holds NT terms per path
+        raise_device_error(t.err, kDevTableOutOfBounds);
+        continue;
+      }
     }
     const F3 T = xyz(w.thr_shade[p]);
     F3 direct = mk3(0.f, 0.f, 0.f);
@@ -829,6 +861,7 @@ __global__ void k_film_add(WaveArgs a, MJTables t,
   __shared__ uint32_t s_off[MJ ? kMaxWaveChunks : 1];
   uint32_t n_chunks = 0;
   if constexpr (MJ) {
+    if (!mj_wave_ok(t)) return;  // uniform: every thread reads one header
     n_pix = t.hdr->n_pix;
     n_chunks = t.hdr->n_chunks;
     for (uint32_t c = threadIdx.x; c < n_chunks; c += blockDim.x)
@@ -839,8 +872,12 @@ __global__ void k_film_add(WaveArgs a, MJTables t,
        i += gridDim.x * blockDim.x) {
     if constexpr (MJ) {
       const Chunk C = t.chunks[find_le(s_off, n_chunks, i)];
-      const JobRec& R = t.jobs[C.job];
+      const JobRec& R = t.jobs[mj_job(t, C.job)];
       const uint32_t li = i - C.pix_off;
+      if (C.path_off + (uint64_t)(li + 1) * C.S > t.hdr->n_paths) {
+        raise_device_error(t.err, kDevTableOutOfBounds);
+        continue;
+      }
       film_pixel(rad, C.path_off + (uint64_t)li * C.S, C.S, C.pix0 + li,
                  R.fsum, R.fcomp, R.fsum64, R.j.drop_nonfinite != 0);
     } else {

@@ -108,6 +108,9 @@ struct Chunk {
 // Header of the per-wave tables in device memory.
 struct WaveHeader {
   uint32_t n_chunks, n_paths, n_pix, n_jobs;
+  // bounds the multi-job kernels check every table index against: the
+  // scene table's entries and the wave arena's paths
+  uint32_t n_scenes, cap_paths, pad0, pad1;
 };
 
 constexpr int kMaxWaveChunks = 1024;
@@ -147,6 +150,7 @@ struct MJTables {
   const JobRec* jobs;
   const Chunk* chunks;
   const WaveHeader* hdr;
+  uint32_t* err;  // the request loop's device error word
 };
 
 // Compressed wide nodes (bvh_width W | kBvhCompressed, W = 4 or 8; 80 bytes
@@ -197,7 +201,9 @@ enum KernelKind { kKindClosest = 0, kKindAny = 1, kKindShade = 2, kKinds = 3 };
 struct PendingTiming {
   cudaEvent_t a, b;
   int kind;
+  int64_t snap;  // the traversal counters' snapshot after it (-1: none)
 };
+constexpr int kLaunchLogCap = 65536;
 
 }  // namespace ajg
 
@@ -233,6 +239,13 @@ struct ajg_ctx {
   unsigned long long kernel_launches = 0;
   bool profiling = false;
   std::vector<ajg::PendingTiming> pending;
+  // per-launch log while profiling: pinned snapshots of the launching
+  // kind's cumulative traversal counters, taken in stream order after each
+  // timed traversal launch, and the resolved records
+  ajg::TraceCounters* h_snaps = nullptr;  // [kLaunchLogCap]
+  int64_t n_snaps = 0;
+  std::vector<ajg_launch_record> launch_log;
+  ajg::TraceCounters last_snap[2] = {};
   double kind_ms[ajg::kKinds] = {0, 0, 0};
   unsigned long long kind_launches[ajg::kKinds] = {0, 0, 0};
   // wavefront arena (grown on demand, reused across renders)
@@ -273,7 +286,13 @@ struct KernelTimer {
   ~KernelTimer() {
     if (a) {
       cudaEventRecord(b, st);
-      ctx->pending.push_back(PendingTiming{a, b, kind});
+      int64_t snap = -1;
+      if (kind != kKindShade && ctx->h_snaps && ctx->n_snaps < kLaunchLogCap) {
+        snap = ctx->n_snaps++;
+        cudaMemcpyAsync(ctx->h_snaps + snap, ctx->d_counters + kind,
+                        sizeof(TraceCounters), cudaMemcpyDeviceToHost, st);
+      }
+      ctx->pending.push_back(PendingTiming{a, b, kind, snap});
     }
   }
 };

@@ -514,6 +514,8 @@ bool Server::plan_and_launch() {
   hdr->n_paths = path_off;
   hdr->n_pix = pix_off;
   hdr->n_jobs = (uint32_t)plan.size();
+  hdr->n_scenes = n_sc;
+  hdr->cap_paths = (uint32_t)P;
   cudaMemcpyAsync(d_tables, h, table_bytes, cudaMemcpyHostToDevice, st);
 
   InFlight f{};
@@ -704,6 +706,7 @@ static int ensure_server(ajg_ctx* ctx, Server** out) {
       s->t.jobs = reinterpret_cast<const JobRec*>(cur);
       cur += align256(sizeof(JobRec) * kMaxWaveChunks);
       s->t.chunks = reinterpret_cast<const Chunk*>(cur);
+      s->t.err = s->d_err;
       // in-flight slots: the default depth plus one; deeper settings reuse
       // them only after their wave retired (retire_oldest runs first)
       for (int i = 0; i < 9 && ok; ++i) {

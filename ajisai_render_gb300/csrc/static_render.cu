@@ -10,7 +10,9 @@
 // as the process runs.  All calls on a device share it and it keeps the
 // previous call's contents, so each call clears the film part before use,
 // and calls whose GPU work overlaps (different streams, or several contexts
-// on one device) race on it.
+// on one device) race on it.  Every launch of a call is ordered on the
+// caller's stream: the traversal launches the context overlaps on its trace
+// stream are forked from that stream and joined back into it by events.
 #include <mutex>
 #include <string>
 

@@ -249,6 +249,22 @@ AJG_API int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset);
  * measurements; adds two event records per launch). */
 AJG_API int ajg_set_profiling(ajg_ctx* ctx, int enable);
 
+/* One launch timed while profiling is on: its kind (0 closest-hit
+ * traversal, 1 any-hit traversal, 2 shading), device time, and the rays,
+ * node visits and triangle tests of that launch alone (0 for shading).
+ * No counterpart in the reference. */
+typedef struct ajg_launch_record {
+  uint32_t kind;
+  float ms;
+  uint64_t rays, nodes, tris;
+} ajg_launch_record; /* 32 bytes */
+/* The launches timed since the last reset, in launch order: up to
+ * `capacity` records into `out` (NULL: none), their number in `*count`;
+ * `reset` clears the log.  The log holds the last 65,536 launches of a
+ * profiling run.  Blocking (waits for the context's work). */
+AJG_API int ajg_get_launch_log(ajg_ctx* ctx, ajg_launch_record* out,
+                               uint32_t capacity, uint32_t* count, int reset);
+
 /* ---- scenes (PLOCAggregate::Build + DefaultScene) --------------------- */
 AJG_API int ajg_scene_create(ajg_ctx* ctx, const ajg_mesh_desc* meshes,
                              uint32_t num_meshes,
@@ -365,7 +381,12 @@ AJG_API int ajg_render_device(ajg_scene* scene, const ajg_camera* cam,
  * AJG_ERR_INVALID.  The first call on a device looks the array's address up
  * and should come before any stream capture.  All calls on a device share
  * the array: each clears what it needs, and calls whose GPU work overlaps
- * (other streams, other contexts) race on it. */
+ * (other streams, other contexts) race on it.  Unlike ajg_render_device,
+ * whose work runs on the context's stream joined to `stream`, every launch
+ * is ordered on `stream` itself (NULL: the legacy default stream); the
+ * closest-hit launches the context overlaps on its trace stream fork from
+ * `stream` and join back into it by events, so the film in d_out_rgbw is
+ * complete when `stream` reaches the call's end. */
 AJG_API int ajg_render_static(ajg_scene* scene, const ajg_camera* cam,
                               const ajg_render_params* params,
                               float* d_out_rgbw, void* stream);
