@@ -68,9 +68,11 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-jobs", type=int, default=48)
-    ap.add_argument("--serve-jobs", type=int, default=64)
-    ap.add_argument("--serve-load", type=float, default=0.8,
-                    help="arrival rate as a fraction of the batched throughput")
+    ap.add_argument("--serve-jobs", type=int, default=340,
+                    help="jobs per load point of the serving sweep")
+    ap.add_argument("--serve-loads", default="0.6,0.9,1.5",
+                    help="arrival rates of the serving sweep, as fractions of the "
+                         "batched throughput")
     ap.add_argument("--rmse-crop", type=int, default=32)
     ap.add_argument("--rmse-spp", type=int, default=4096)
     ap.add_argument("--wave-paths", type=int, default=0,
@@ -82,9 +84,11 @@ def parse():
                     help="run the SPPM section alone (one JSON line)")
     ap.add_argument("--sppm-iters", type=int, default=32)
     ap.add_argument("--sppm-photons", type=int, default=4_000_000)
-    ap.add_argument("--large", action="store_true",
-                    help="also run the large-scene workload (26.2 M triangles, "
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the large-scene workload (26.2 M triangles, "
                          "1920x1080, 1024 spp, depth 32, FP64 crop reference)")
+    ap.add_argument("--no-cornell", action="store_true",
+                    help="skip the Cornell-box workload (256x256, 64 spp, depth 8)")
     ap.add_argument("--large-ref-spp", type=int, default=65536)
     ap.add_argument("--bvh-width", type=lambda v: (int(v[:-1]) | 0x100) if v.endswith("c")
                     else int(v), default=0,
@@ -164,18 +168,38 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_launch(kernel, workload):
-    """DRAM bytes per launch of the kernel from the committed ncu summary,
-    when it was captured on this workload (resolution, spp, wave size, tree
-    width); None otherwise."""
+def committed_profile(kernel, scene, bvh_width):
+    """The committed ncu figures of a traversal kernel (profiles/traffic.json,
+    a small capture of the same kernel: per captured launch its rays, DRAM
+    bytes, time, L1/L2 hit rates and throughput, threads per warp
+    instruction), when they were taken on this scene and tree layout; None
+    otherwise."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     d = json.loads(p.read_text())
     k = d.get(kernel)
-    if not k or d.get("workload") != workload:
+    if not k or d.get("scene") != scene or d.get("bvh_width") != bvh_width:
         return None
-    return float(k["dram_bytes_per_launch"])
+    return {**k, "source": d.get("source"), "captured": d.get("captured")}
+
+
+def scaled_traffic(prof, rays_per_launch):
+    """DRAM bytes per launch of this run: each launch's rays times the
+    captured DRAM bytes per ray of the same bounce (later bounces take the
+    last captured bounce's figure), averaged over the launches."""
+    bpr = [b for b in prof["dram_bytes_per_ray"] if b is not None]
+    if not bpr or not rays_per_launch:
+        return None
+    tot = sum(r * bpr[min(i, len(bpr) - 1)] for i, r in enumerate(rays_per_launch))
+    return tot / len(rays_per_launch)
+
+
+def time_weighted(prof, key):
+    """A captured per-launch figure averaged with the launches' times as
+    weights."""
+    ms = np.asarray(prof["ms"], np.float64)
+    return float(np.dot(ms, np.asarray(prof[key], np.float64)) / ms.sum())
 
 
 # ------------------------------------------------------------- CPU side --
@@ -200,8 +224,9 @@ def cpu_sample(flat, seconds, threads, spp):
                   threads=threads)
     dt = time.perf_counter() - t
     samples = len(rows) * W * spp
+    build_s = sc.build_seconds
     sc.close()
-    return samples / dt / 1e6, len(rows), dt
+    return samples / dt / 1e6, len(rows), dt, build_s
 
 
 def run_reference(args):
@@ -219,7 +244,7 @@ def run_reference(args):
         cpu_sample(flat, 0.5, threads, args.spp)
     vals, npxs, secs = [], [], []
     for _ in range(args.steps):
-        v, npx, dt = cpu_sample(flat, per_step, threads, args.spp)
+        v, npx, dt, _ = cpu_sample(flat, per_step, threads, args.spp)
         vals.append(v)
         npxs.append(npx)
         secs.append(dt)
@@ -316,6 +341,7 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     prof_ms = pa.elapsed_time(pb)
     st = ctx.stats()
+    log = ctx.launch_log(reset=True)
     ctx.set_profiling(False)
     value, total_s = whole_job_rate(dist, world, samples_per_step * args.steps,
                                     total_ms / 1e3, dev)
@@ -333,12 +359,29 @@ def run_ours(args):
     avg_ms = st[ms_k] / launches
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     peak, peak_kind = peaks()
+    launches_k = [r for r in log if r["kind"] == dom]
+    rays_per_launch = float(np.mean([r["rays"] for r in launches_k])) if launches_k else 0.0
+    prof = committed_profile(kname, "icosphere1310k", scene.info()["bvh_width"])
+    traffic = scaled_traffic(prof, [r["rays"] for r in launches_k]) if prof else None
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak if achieved else None,
-                "traffic": traffic_per_launch(kname, {
-                    "res": args.res, "spp": args.spp,
-                    "wave_paths": args.wave_paths or (1 << 28),
-                    "bvh_width": scene.info()["bvh_width"]}),
+                "traffic": traffic,
+                "traffic_note": ("DRAM bytes per ray of a small capture of the same kernel "
+                                 "on the same scene (per bounce), times this run's rays "
+                                 "per launch" if prof else None),
+                "traffic_source": prof["source"] if prof else None,
+                # where the gathers are served: the same capture's cache figures,
+                # weighted by launch time (ncu: L1TEX and L2 throughput as a
+                # fraction of their peaks, hit rates, active threads per warp
+                # instruction = SIMT efficiency x 32)
+                "cache": None if not prof else {
+                    k: time_weighted(prof, k) for k in (
+                        "l1_throughput_pct", "l2_throughput_pct", "l1_hit_rate_pct",
+                        "l2_hit_rate_pct", "threads_per_warp_inst")},
+                "rays_per_launch": [int(r["rays"]) for r in launches_k],
+                "other_kind_rays_per_launch": [int(r["rays"]) for r in log
+                                               if r["kind"] not in (dom, "shade")],
+                "ms_per_launch": [round(float(r["ms"]), 3) for r in launches_k],
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "avg_launch_ms": avg_ms, "launches": int(st[l_k]),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
@@ -382,19 +425,28 @@ def run_ours(args):
                "d2h_bytes_per_step": int(d2h), "ms_per_step": dt / args.steps * 1e3}
 
     cpu = None
+    rays_per_sample = (st["closest_rays"] + st["any_rays"]) / samples_per_step
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, npx, dt = cpu_sample(flat, args.cpu_seconds, threads, args.spp)
+        v, npx, dt, build_s = cpu_sample(flat, args.cpu_seconds, threads, args.spp)
         cpu = {"value": v, "unit": "Msamples/s", "cores": threads, "kind": "port",
                "sample": f"{npx} image rows spread over the film x {args.res} px x "
                          f"{args.spp} spp ({dt:.1f} s), oracle port of the reference "
-                         "path, all host threads"}
+                         "path, all host threads",
+               "ploc_build_ms": build_s * 1e3,
+               "ploc_build_note": "the oracle's PLOCAggregate::Build restatement, one "
+                                  "host thread, 1,310,722 triangles",
+               "mrays_s": v * rays_per_sample,
+               "mrays_note": "samples/s times the rays per sample the GPU counted on "
+                             "the same job (the same paths: shared counter sampler)"}
 
     img = out.float().cpu().numpy()
     nonfinite = int((~np.isfinite(img)).any(-1).sum())
 
-    batched = served = large = sppm = None
-    if rank == 0 and world == 1 and args.large:
+    batched = served = large = sppm = cornell = None
+    if rank == 0 and world == 1 and not args.no_cornell:
+        cornell = run_cornell(args, local)
+    if rank == 0 and world == 1 and not args.no_large:
         large = run_large(args, local)
     if rank == 0 and world == 1 and not args.no_sppm:
         sppm = run_sppm(args, local)
@@ -429,7 +481,8 @@ def run_ours(args):
                        "tris_per_ray": st[f"{kind}_tris"] / max(1, st[f"{kind}_rays"])}
                 for kind in ("closest", "any")},
             "step_ms": step_ms, "nonfinite_pixels": nonfinite,
-            "batched": batched, "served": served, "large": large,
+            "mrays_s": value * rays_per_sample,
+            "cornell": cornell, "batched": batched, "served": served, "large": large,
             "sppm": sppm, "impl": "ours"}))
     scene.release()
     ctx.close()
@@ -533,25 +586,25 @@ def run_batched(ctx, args):
     }
 
 
-def run_served(ctx, args, capacity_samples_s):
-    """Poisson arrivals of render jobs over 8 resident scenes; progressive
-    results every 16 spp; latency from submission to the final result."""
-    from ajisai_render_gb300 import api
+def serve_plan(n, seed):
+    """n jobs of the serving workload: scene index (of 8), resolution
+    {256,512,1024}^2, spp log-uniform 4-1024, camera on a seeded sphere."""
     from ajisai_render_gb300 import scenes as S
-    jobs8, built, tris = build_mix(ctx, 8, seed=2)
-    rng = np.random.default_rng(5)
-    n = args.serve_jobs
+    rng = np.random.default_rng(seed)
     plan = []
-    for i in range(n):
+    for _ in range(n):
         k = int(rng.integers(0, 8))
         res = int(rng.choice([256, 512, 1024]))
         spp = int(round(np.exp(rng.uniform(np.log(4), np.log(1024)))))
-        cam = S._orbit_camera(rng, res, res)
-        plan.append((k, res, spp, cam))
-    mean_samples = np.mean([r * r * s for _, r, s, _ in plan])
-    rate = args.serve_load * capacity_samples_s / mean_samples  # jobs per second
-    gaps = rng.exponential(1.0 / rate, n)
-    ctx.configure_serving("fair", wave_paths=args.batch_wave_paths)
+        plan.append((k, res, spp, S._orbit_camera(rng, res, res)))
+    return plan, rng
+
+
+def serve_point(ctx, built, plan, rng, rate, capacity_samples_s):
+    """Poisson arrivals of the planned jobs at `rate` jobs/s; progressive
+    results every 16 spp; returns the load point's statistics."""
+    from ajisai_render_gb300 import api
+    gaps = rng.exponential(1.0 / rate, len(plan))
     submitted = []
     t0 = time.perf_counter()
     at = 0.0
@@ -561,31 +614,135 @@ def run_served(ctx, args, capacity_samples_s):
         if dt > 0:
             time.sleep(dt)
         r = api.PTRenderer(api.PTRendererArgs(spp=spp, min_bounces=MIN_B,
-                                              max_bounces=BATCH_DEPTH), seed=i_seed(k, res, spp))
+                                              max_bounces=BATCH_DEPTH),
+                           seed=i_seed(k, res, spp))
         submitted.append(ctx.submit(built[k][0], cam, r, progress_spp=16))
+    t_arrived = time.perf_counter() - t0
     sts = [j.wait() for j in submitted]
-    t_end = time.perf_counter()
     for j in submitted:
         j.release()
-    lat = np.array([s["done_ms"] - s["submit_ms"] for s in sts])
-    first = np.array([s["first_result_ms"] - s["submit_ms"] for s in sts])
-    done = sum(1 for s in sts if s["state_name"] == "done")
-    samples = sum(r * r * s for _, r, s, _ in plan)
-    span_ms = max(s["done_ms"] for s in sts) - min(s["submit_ms"] for s in sts)
+    sub = np.array([s["submit_ms"] for s in sts])
+    start = np.array([s["start_ms"] for s in sts])
+    done_t = np.array([s["done_ms"] for s in sts])
+    lat = done_t - sub
+    first = np.array([s["first_result_ms"] for s in sts]) - sub
+    size = np.array([r * r * s for _, r, s, _ in plan], np.float64)
+    # slowdown: latency over the job's own service time at the measured
+    # capacity (a job alone at idle)
+    slow = lat / (size / capacity_samples_s * 1e3)
+    # jobs in the system (submitted, not done) and waiting for admission,
+    # sampled at every submission
+    in_sys = [int(((sub <= t) & (done_t > t)).sum()) for t in sub]
+    waiting = [int(((sub <= t) & (start > t)).sum()) for t in sub]
+    q = len(in_sys) // 4
+    span_ms = done_t.max() - sub.min()
+    pct = lambda a, p: float(np.percentile(a, p))
     return {
-        "workload": f"{n} jobs, Poisson arrivals at {args.serve_load:.0%} of the batched "
-                    f"throughput ({rate:.2f} jobs/s), 8 resident scenes ({tris:,} triangles), "
-                    "res {256,512,1024}^2, spp log-uniform 4-1024, camera on a seeded sphere, "
-                    "depth 12, progressive results every 16 spp, fair scheduling, "
-                    "HBM budget 150 GB",
-        "jobs_done": done,
-        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-        "mean_ms": float(lat.mean()),
-        "first_result_p50_ms": float(np.percentile(first, 50)),
-        "first_result_p99_ms": float(np.percentile(first, 99)),
-        "msamples_s": samples / (span_ms / 1e3) / 1e6,
-        "wall_s": t_end - t0,
+        "jobs": len(plan), "jobs_done": sum(1 for s in sts if s["state_name"] == "done"),
+        "rate_jobs_s": rate, "arrivals_s": t_arrived,
+        "msamples_s": float(size.sum() / (span_ms / 1e3) / 1e6),
+        "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "mean_ms": float(lat.mean()),
+        "first_result_p50_ms": pct(first, 50), "first_result_p99_ms": pct(first, 99),
+        "slowdown_p50": pct(slow, 50), "slowdown_p99": pct(slow, 99),
+        "admission_wait_p99_ms": pct(start - sub, 99),
+        "jobs_in_system_max": int(max(in_sys)),
+        "jobs_in_system_by_quarter": [float(np.mean(in_sys[i * q:(i + 1) * q]))
+                                      for i in range(4)] if q else [],
+        "jobs_waiting_max": int(max(waiting)),
     }
+
+
+def run_served(ctx, args, capacity_samples_s):
+    """The serving sweep: Poisson arrivals of render jobs over 8 resident
+    scenes at several rates (fractions of the batched throughput), the
+    highest past saturation; progressive results every 16 spp, fair
+    scheduling; latency from submission to the final result."""
+    jobs8, built, tris = build_mix(ctx, 8, seed=2)
+    ctx.configure_serving("fair", wave_paths=args.batch_wave_paths)
+    loads = [float(x) for x in args.serve_loads.split(",") if x]
+    points = []
+    t0 = time.perf_counter()
+    for i, load in enumerate(loads):
+        plan, rng = serve_plan(args.serve_jobs, seed=5 + i)
+        mean_samples = np.mean([r * r * s for _, r, s, _ in plan])
+        rate = load * capacity_samples_s / mean_samples
+        pt = serve_point(ctx, built, plan, rng, rate, capacity_samples_s)
+        pt["offered_load"] = load
+        points.append(pt)
+    total = sum(p["jobs"] for p in points)
+    below = [p for p in points if p["offered_load"] < 1.0] or points
+    head = max(below, key=lambda p: p["offered_load"]) if below else None
+    return {
+        "workload": f"{args.serve_jobs} jobs per load point ({total} in all; the "
+                    "configuration's 10,000-job run is unmeasured), Poisson arrivals at "
+                    f"{', '.join(f'{x:.0%}' for x in loads)} of the batched throughput "
+                    f"({capacity_samples_s / 1e6:.0f} Msamples/s), 8 resident scenes "
+                    f"({tris:,} triangles), res {{256,512,1024}}^2, spp log-uniform 4-1024, "
+                    "camera on a seeded sphere, depth 12, progressive results every 16 spp, "
+                    "fair scheduling, HBM budget 150 GB",
+        "points": points,
+        # the headline latency: the busiest load point below saturation
+        "p50_ms": head["p50_ms"] if head else None,
+        "p99_ms": head["p99_ms"] if head else None,
+        "latency_at_load": head["offered_load"] if head else None,
+        "saturated_msamples_s": max((p["msamples_s"] for p in points), default=None),
+        "wall_s": time.perf_counter() - t0,
+    }
+
+
+def run_cornell(args, local):
+    """The Cornell-style box at its full size (256x256, 64 spp, depth 8,
+    roulette after bounce 3): GPU throughput, the oracle's on all host
+    threads over the whole film, and both images' RMSE against an
+    FP64-accumulated 8192-spp render."""
+    import torch
+    from ajisai_render_gb300 import api
+    from ajisai_render_gb300 import scenes as S
+    from oracle import pyoracle as O
+    flat = S.flatten(S.cornell_box(256, 256))
+    ctx = api.Context(local)
+    try:
+        scene = api.GpuScene(ctx, flat, api.CreatePLOCAggregate(14))
+        p = dict(spp=64, min_bounces=3, max_bounces=8)
+        rend = api.PTRenderer(api.PTRendererArgs(**p), seed=1)
+        out = torch.empty((256, 256, 4), dtype=torch.float32, device="cuda")
+        stream = torch.cuda.current_stream()
+        for _ in range(3):
+            rend.render_device(scene, flat.camera, out.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        reps = 20
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            rend.render_device(scene, flat.camera, out.data_ptr(), stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        samples = 256 * 256 * 64
+        conv = api.PTRenderer(api.PTRendererArgs(spp=8192, min_bounces=3, max_bounces=8),
+                              seed=99, fp64_film=True).Render(scene, flat.camera).rgbw
+        d_conv = torch.from_numpy(conv).cuda()
+        e_gpu, _ = ctx.image_rmse(out.data_ptr(), d_conv.data_ptr(), 256, 256)
+        res = {"workload": "Cornell-style box (34 triangles), 256x256, 64 spp, depth 8, "
+                           "roulette after bounce 3, directional 3.0 + environment 0.2",
+               "msamples_s": samples / (ms / 1e3) / 1e6, "ms_per_render": ms,
+               "rmse_vs_fp64_8192spp": e_gpu}
+        if not args.no_cpu:
+            threads = os.cpu_count() or 1
+            osc = O.OracleScene(flat, 14)
+            t = time.perf_counter()
+            _, film_o = osc.render(flat.camera, p, seed=1, threads=threads)
+            cdt = time.perf_counter() - t
+            osc.close()
+            d_o = torch.from_numpy(film_o.astype(np.float32)).cuda()
+            e_cpu, _ = ctx.image_rmse(d_o.data_ptr(), d_conv.data_ptr(), 256, 256)
+            res["cpu_baseline"] = {"value": samples / cdt / 1e6, "unit": "Msamples/s",
+                                   "cores": threads, "kind": "port",
+                                   "sample": f"the whole film at full size ({cdt:.2f} s)",
+                                   "rmse_vs_fp64_8192spp": e_cpu}
+        return res
+    finally:
+        ctx.close()
 
 
 def run_large(args, local):
@@ -646,9 +803,41 @@ def run_large(args, local):
                                       "reference_spp": args.large_ref_spp, "rmse": e,
                                       "pixels": npx, "reference_s": ref_s},
                 "nonfinite_pixels": int((~np.isfinite(img)).any(-1).sum()),
-                "scene_generation_s": gen_s}
+                "scene_generation_s": gen_s,
+                "cpu_baseline": None if args.no_cpu else large_cpu(flat, args)}
     finally:
         ctx.close()
+
+
+def large_cpu(flat, args):
+    """The oracle on the large scene: its PLOC build (one host thread) and
+    the render on all host threads over whole image rows spread over the
+    film, as many as fit a few seconds."""
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    sc = O.OracleScene(flat, RADIUS)
+    W, H = int(flat.camera[34]), int(flat.camera[35])
+    params = dict(spp=1024, min_bounces=MIN_B, max_bounces=32)
+    t = time.perf_counter()
+    sc.render(flat.camera, params, seed=21, pixel_range=((H // 2) * W, (H // 2 + 1) * W),
+              threads=threads)
+    per_row = time.perf_counter() - t
+    nrows = int(max(1, min(H, 0.5 * args.cpu_seconds / max(per_row, 1e-6))))
+    rows = np.linspace(0, H - 1, nrows).round().astype(int)
+    t = time.perf_counter()
+    for y in rows:
+        sc.render(flat.camera, params, seed=21, pixel_range=(y * W, (y + 1) * W),
+                  threads=threads)
+    dt = time.perf_counter() - t
+    build_s = sc.build_seconds
+    sc.close()
+    return {"value": len(rows) * W * 1024 / dt / 1e6, "unit": "Msamples/s",
+            "cores": threads, "kind": "port",
+            "sample": f"{len(rows)} image rows spread over the film x {W} px x 1024 spp "
+                      f"({dt:.1f} s), all host threads",
+            "ploc_build_ms": build_s * 1e3,
+            "ploc_build_note": "the oracle's PLOCAggregate::Build restatement, one host "
+                               f"thread, {flat.n_tris:,} triangles"}
 
 
 SPPM_RES = 512

@@ -61,14 +61,22 @@ def test_reference_arm_runs_on_rank_zero_only():
     assert r.stdout.strip() == ""
 
 
-def test_committed_traffic_only_for_its_workload():
+def test_committed_profile_only_for_its_scene_and_layout():
     sys.path.insert(0, str(ROOT))
     import json
     import bench
     d = json.loads((ROOT / "profiles" / "traffic.json").read_text())
-    w = d["workload"]
-    got = bench.traffic_per_launch("k_shadow", dict(w))
-    assert got == float(d["k_shadow"]["dram_bytes_per_launch"])
-    assert bench.traffic_per_launch("k_shadow", {**w, "res": w["res"] // 2}) is None
-    assert bench.traffic_per_launch("k_shadow", {**w, "wave_paths": 1 << 25}) is None
-    assert bench.traffic_per_launch("k_nothing", dict(w)) is None
+    got = bench.committed_profile("k_shadow", d["scene"], d["bvh_width"])
+    bpr = got["dram_bytes_per_ray"]
+    assert bpr == d["k_shadow"]["dram_bytes_per_ray"] and min(bpr) > 0
+    assert all(0 < h <= 100 for h in got["l2_hit_rate_pct"])
+    assert all(1 <= t <= 32 for t in got["threads_per_warp_inst"])
+    assert bench.committed_profile("k_shadow", "cornell", d["bvh_width"]) is None
+    assert bench.committed_profile("k_shadow", d["scene"], 2) is None
+    assert bench.committed_profile("k_nothing", d["scene"], d["bvh_width"]) is None
+    # each launch takes its bounce's bytes per ray, later ones the last bounce's
+    rays = [1000, 100, 10, 10, 1]
+    want = (1000 * bpr[0] + 100 * bpr[1] + 10 * bpr[2] + 10 * bpr[2] + bpr[2]) / 5
+    assert abs(bench.scaled_traffic(got, rays) - want) < 1e-6 * want
+    w = bench.time_weighted(got, "l2_hit_rate_pct")
+    assert min(got["l2_hit_rate_pct"]) <= w <= max(got["l2_hit_rate_pct"])
