@@ -6,7 +6,8 @@ Each .cu file compiles in parallel to an object under _build/obj, then one
 shared library links them with the static CUDA runtime.  Every file is
 compiled with -fmad=false (device) and -ffp-contract=off (host): no
 multiply-add is contracted, so the non-transcendental arithmetic matches the
-reference compiled for baseline x86-64 bit for bit.
+reference compiled for baseline x86-64 bit for bit (a build with
+AJG_SHADE_FMA=1 contracts the shading unit's arithmetic only).
 """
 from __future__ import annotations
 
@@ -43,8 +44,17 @@ def headers():
     return sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
-def flags(extra=()):
-    return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
+# AJG_SHADE_FMA=1: the shading translation units (integrator.cu: ray
+# generation, shading, film; capi.cu: the BSDF and camera-ray query kernels
+# that share the shading code) are compiled with multiply-add contraction;
+# the traversal units keep -fmad=false either way (bit-exact hits).
+SHADE_FMA = os.environ.get("AJG_SHADE_FMA", "0") == "1"
+FMA_UNITS = ("integrator.cu", "capi.cu")
+
+
+def flags(extra=(), fmad=False):
+    return [*ARCH, "-O3", "-lineinfo", "-std=c++17",
+            "-fmad=true" if fmad else "-fmad=false",
             "--expt-relaxed-constexpr", "-Xcompiler",
             "-fPIC,-ffp-contract=off,-fvisibility=hidden",
             "-I", str(INCLUDE), *extra]
@@ -68,7 +78,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     procs = []
     for s in srcs:
         o = obj / (s.stem + ".o")
-        cmd = [cc, *flags(EXTRA), "-c", str(s), "-o", str(o)]
+        cmd = [cc, *flags(EXTRA, SHADE_FMA and s.name in FMA_UNITS), "-c", str(s),
+               "-o", str(o)]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         procs.append((s, o, subprocess.Popen(cmd, stdout=subprocess.PIPE,

@@ -51,7 +51,6 @@ __device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
   else
     return warp_append(counter, pred);
 }
-constexpr int kTraceThreads = 128;
 #ifndef AJG_SHADE_MIN_BLOCKS
 // blocks per SM the shading kernels are compiled for: 512 threads, up to
 // 128 registers, no spills (1024 threads: 64)
@@ -67,32 +66,6 @@ struct WaveArgs {
   uint32_t pix0, S, s0, n_paths;
   VisPointD* vp;  // SPPM camera pass: the visible points (else null)
 };
-
-// Multi-job table guards: a job or scene index past its table records
-// kDevTableOutOfBounds in the request loop's error word (the wave's jobs
-// then fail with AJG_ERR_DEVICE) and is replaced by 0, so that no read
-// leaves the tables the host uploaded for the wave.
-__device__ __forceinline__ uint32_t mj_job(const MJTables& t, uint32_t jid) {
-  if (jid < t.hdr->n_jobs) return jid;
-  raise_device_error(t.err, kDevTableOutOfBounds);
-  return 0;
-}
-__device__ __forceinline__ uint32_t mj_scene(const MJTables& t, uint32_t sid) {
-  if (sid < t.hdr->n_scenes) return sid;
-  raise_device_error(t.err, kDevTableOutOfBounds);
-  return 0;
-}
-// A wave whose header is out of range (more chunks than the kernels'
-// shared offset tables hold, or more paths than the arena) runs nothing.
-__device__ __forceinline__ bool mj_wave_ok(const MJTables& t) {
-  const WaveHeader& h = *t.hdr;
-  if (h.n_chunks <= (uint32_t)kMaxWaveChunks && h.n_jobs <= (uint32_t)kMaxWaveChunks &&
-      h.n_scenes <= (uint32_t)kMaxWaveChunks && h.n_paths <= h.cap_paths)
-    return true;
-  if (blockIdx.x == 0 && threadIdx.x == 0)
-    raise_device_error(t.err, kDevTableOutOfBounds);
-  return false;
-}
 
 // Where a kernel finds the job and the scene of a path: the kernel
 // arguments (single job) or the wave tables (multi-job).
@@ -229,41 +202,6 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
-__device__ __forceinline__ void retarget(TraceScene& ts, const MJTables& t,
-                                         uint32_t sid) {
-  const DeviceScene& sc = t.scenes[mj_scene(t, sid)];
-  ts.bvh = sc.bvh;
-  ts.tris = sc.tris;
-  ts.max_visits = sc.num_inner + 1;
-}
-
-// Closest hits of the path queue.
-template <int TEST, bool MJ, int W>
-__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
-    k_extend(DeviceScene s, MJTables t, const float4* __restrict__ ro,
-             const float4* __restrict__ rd, const uint32_t* __restrict__ count,
-             uint32_t* fetch_next, ajg_hit* __restrict__ hits,
-             TraceCounters* ctr, uint32_t* err) {
-  const uint32_t n = *count;
-  uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k, TraceScene& ts) {
-    const float4 o = ro[k], d = rd[k];
-    if constexpr (MJ) retarget(ts, t, __float_as_uint(o.w));
-    return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
-  };
-  auto finish = [&](uint32_t k, const Hit& h, bool) {
-    ajg_hit o2;
-    o2.t = h.t;
-    o2.u = h.u;
-    o2.v = h.v;
-    o2.prim = h.prim;
-    hits[k] = o2;
-  };
-  trace_persistent<TEST, false, W>(trace_scene(s), n, fetch_next, fetch,
-                                   finish, nr, nn, nt, err);
-  flush_counters(ctr, nr, nn, nt);
-}
-
 // Files every queue slot under its hit's shading class (a miss, Lambertian,
 // Disney, or one of the other material types), so that shading runs in
 // class-specialised kernels; warps stay converged, so each list append is
@@ -311,58 +249,6 @@ __global__ void __launch_bounds__(kClassifyThreads)
     }
 #endif
   }
-}
-
-template <int TEST, bool MJ, int W>
-__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
-    k_shadow(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
-             const float4* __restrict__ sq_d,
-             const uint16_t* __restrict__ sq_scene,
-             const uint32_t* __restrict__ count, uint32_t* fetch_next,
-             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err) {
-  const uint32_t n = *count;
-  uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k, TraceScene& ts) {
-    const float4 o = sq_o[k], d = sq_d[k];
-    if constexpr (MJ) retarget(ts, t, sq_scene[k]);
-    return make_query(xyz(o), xyz(d), kRayEps, o.w);
-  };
-  auto finish = [&](uint32_t k, const Hit&, bool occ) {
-    if (!occ) vis[__float_as_uint(sq_d[k].w)] = 1;
-  };
-  trace_persistent<TEST, true, W>(trace_scene(s), n, fetch_next, fetch,
-                                  finish, nr, nn, nt, err);
-  flush_counters(ctr, nr, nn, nt);
-}
-
-// Closest hits of the MIS BSDF rays of scenes with emitters (the queue at
-// the top of the shadow queue's storage, see emit_closest); t and the
-// primitive go to two arrays the material lists' storage lends.
-template <int TEST, bool MJ, int W>
-__global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
-    k_bsdf_trace(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
-                 const float4* __restrict__ sq_d,
-                 const uint16_t* __restrict__ sq_scene,
-                 const uint32_t* __restrict__ count, uint32_t* fetch_next,
-                 uint32_t cap, uint32_t n_max, float* __restrict__ t_hit,
-                 int32_t* __restrict__ prim_hit, TraceCounters* ctr,
-                 uint32_t* err) {
-  // at most one entry per path (n_max = paths of the arena)
-  const uint32_t n = min(*count, n_max);
-  uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k, TraceScene& ts) {
-    const uint32_t i = cap - 1 - k;
-    const float4 o = sq_o[i], d = sq_d[i];
-    if constexpr (MJ) retarget(ts, t, sq_scene[i]);
-    return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
-  };
-  auto finish = [&](uint32_t k, const Hit& h, bool) {
-    t_hit[k] = h.t;
-    prim_hit[k] = h.prim;
-  };
-  trace_persistent<TEST, false, W>(trace_scene(s), n, fetch_next, fetch,
-                                   finish, nr, nn, nt, err);
-  flush_counters(ctr, nr, nn, nt);
 }
 
 // The MIS BSDF term from its closest hit (helper.h:223-264): an escaped ray
@@ -429,12 +315,24 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
+// AJG_SHADOW_OCTANT: a block's shadow rays of one light term are queued
+// grouped by the octant of their direction (a warp of the traversal then
+// takes rays of one octant).
+#ifndef AJG_SHADOW_OCTANT
+#define AJG_SHADOW_OCTANT 0
+#endif
 template <bool MJ>
 __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
                                             uint32_t sid, bool pred,
                                             uint32_t cap, uint32_t* err) {
+#if AJG_SHADOW_OCTANT && AJG_BLOCK_APPEND
+  const int oct = (d.x < 0.f ? 1 : 0) | (d.y < 0.f ? 2 : 0) | (d.z < 0.f ? 4 : 0);
+  const uint32_t k = block_append_binned<8, kShadeThreads / 32>(&w.counts[2],
+                                                                pred ? oct : -1);
+#else
   const uint32_t k = shade_append(&w.counts[2], pred);
+#endif
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -1154,14 +1052,9 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const int gs = kSMs * 8;
   // persistent traversal: resident blocks only
   auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
-    dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
-      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-      const int g = resident_grid((const void*)k_extend<TT, false, WW>,
-                                  kTraceThreads);
-      k_extend<TT, false, WW><<<g, kTraceThreads, 0, es>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], hits,
-          &ctx->d_counters[0], ctx->d_error);
-    });
+    launch_wave_extend(false, s.tri_test, s.width, s, t, w.ro[q], w.rd[q],
+                       &w.counts[q], &w.counts[8], hits, &ctx->d_counters[0],
+                       ctx->d_error, es);
   };
   // Bounce b+1's closest hits run on the trace stream beside bounce b's
   // shadow rays: the two persistent launches fill each other's drain.  The
@@ -1179,26 +1072,16 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
     cudaEventRecord(ctx->ev_hits, ts);
   };
   auto bsdf_closest = [&]() {
-    dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
-      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-      const int g = resident_grid((const void*)k_bsdf_trace<TT, false, WW>,
-                                  kTraceThreads);
-      k_bsdf_trace<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.sq_o, w.sq_d, nullptr, &w.counts[9], &w.counts[10],
-          shadow_cap, (uint32_t)P, reinterpret_cast<float*>(w.lists),
-          reinterpret_cast<int32_t*>(w.lists + P), &ctx->d_counters[0],
-          ctx->d_error);
-    });
+    launch_wave_bsdf_trace(false, s.tri_test, s.width, s, t, w.sq_o, w.sq_d,
+                           nullptr, &w.counts[9], &w.counts[10], shadow_cap,
+                           (uint32_t)P, reinterpret_cast<float*>(w.lists),
+                           reinterpret_cast<int32_t*>(w.lists + P),
+                           &ctx->d_counters[0], ctx->d_error, st);
   };
   auto shadow = [&]() {
-    dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
-      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-      const int g = resident_grid((const void*)k_shadow<TT, false, WW>,
-                                  kTraceThreads);
-      k_shadow<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.sq_o, w.sq_d, nullptr, &w.counts[2], &w.counts[3],
-          w.term_vis, &ctx->d_counters[1], ctx->d_error);
-    });
+    launch_wave_shadow(false, s.tri_test, s.width, s, t, w.sq_o, w.sq_d, nullptr,
+                       &w.counts[2], &w.counts[3], w.term_vis,
+                       &ctx->d_counters[1], ctx->d_error, st);
   };
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);
@@ -1306,17 +1189,6 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   ctx->paths_total += (unsigned long long)npix * prm.spp;
 }
 
-void prepare_mj_kernels() {
-  for (int tt = 0; tt < 2; ++tt)
-    for (int wd : {2, 4, 8, 4 | (int)kBvhCompressed, 8 | (int)kBvhCompressed})
-      dispatch_trace(tt, wd, [&](auto T, auto Wd) {
-        constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-        resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
-        resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
-        resident_grid((const void*)k_bsdf_trace<TT, true, WW>, kTraceThreads);
-      });
-}
-
 void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                      int NT, int bounces, int tri_test, int width, bool emit,
                      TraceCounters* ctr, uint32_t* err, cudaStream_t st,
@@ -1327,13 +1199,8 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
   auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
-    dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
-      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-      const int g =
-          resident_grid((const void*)k_extend<TT, true, WW>, kTraceThreads);
-      k_extend<TT, true, WW><<<g, kTraceThreads, 0, es>>>(
-          s, t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], hits, ctr, err);
-    });
+    launch_wave_extend(true, tri_test, width, s, t, w.ro[q], w.rd[q],
+                       &w.counts[q], &w.counts[8], hits, ctr, err, es);
   };
   // bounce b+1's closest hits on the trace stream beside bounce b's shadow
   // rays, as in the single-job waves (run_waves)
@@ -1378,24 +1245,14 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
         shadow_cap, err);
     if (overlap && b + 1 < bounces)
       extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2);
-    dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
-      constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-      const int g =
-          resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
-      k_shadow<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[2], &w.counts[3],
-          w.term_vis, ctr + 1, err);
-    });
+    launch_wave_shadow(true, tri_test, width, s, t, w.sq_o, w.sq_d, w.sq_scene,
+                       &w.counts[2], &w.counts[3], w.term_vis, ctr + 1, err, st);
     if (emit) {
-      dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
-        constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
-        const int g = resident_grid((const void*)k_bsdf_trace<TT, true, WW>,
-                                    kTraceThreads);
-        k_bsdf_trace<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-            s, t, w.sq_o, w.sq_d, w.sq_scene, &w.counts[9], &w.counts[10],
-            shadow_cap, (uint32_t)P, reinterpret_cast<float*>(w.lists),
-            reinterpret_cast<int32_t*>(w.lists + P), ctr, err);
-      });
+      launch_wave_bsdf_trace(true, tri_test, width, s, t, w.sq_o, w.sq_d,
+                             w.sq_scene, &w.counts[9], &w.counts[10], shadow_cap,
+                             (uint32_t)P, reinterpret_cast<float*>(w.lists),
+                             reinterpret_cast<int32_t*>(w.lists + P), ctr, err,
+                             st);
       k_bsdf_emit<true><<<gs, kShadeThreads, 0, st>>>(
           a, t, w, (uint32_t)NT, shadow_cap, (uint32_t)P,
           reinterpret_cast<const float*>(w.lists),

@@ -153,6 +153,32 @@ struct MJTables {
   uint32_t* err;  // the request loop's device error word
 };
 
+// Multi-job table guards: a job or scene index past its table records
+// kDevTableOutOfBounds in the request loop's error word (the wave's jobs
+// then fail with AJG_ERR_DEVICE) and is replaced by 0, so that no read
+// leaves the tables the host uploaded for the wave.
+__device__ __forceinline__ uint32_t mj_job(const MJTables& t, uint32_t jid) {
+  if (jid < t.hdr->n_jobs) return jid;
+  raise_device_error(t.err, kDevTableOutOfBounds);
+  return 0;
+}
+__device__ __forceinline__ uint32_t mj_scene(const MJTables& t, uint32_t sid) {
+  if (sid < t.hdr->n_scenes) return sid;
+  raise_device_error(t.err, kDevTableOutOfBounds);
+  return 0;
+}
+// A wave whose header is out of range (more chunks than the kernels'
+// shared offset tables hold, or more paths than the arena) runs nothing.
+__device__ __forceinline__ bool mj_wave_ok(const MJTables& t) {
+  const WaveHeader& h = *t.hdr;
+  if (h.n_chunks <= (uint32_t)kMaxWaveChunks && h.n_jobs <= (uint32_t)kMaxWaveChunks &&
+      h.n_scenes <= (uint32_t)kMaxWaveChunks && h.n_paths <= h.cap_paths)
+    return true;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    raise_device_error(t.err, kDevTableOutOfBounds);
+  return false;
+}
+
 // Compressed wide nodes (bvh_width W | kBvhCompressed, W = 4 or 8; 80 bytes
 // for W = 8, 64 for W = 4):
 //   float4 0: node origin (lo corner of the children's union), and
@@ -322,6 +348,31 @@ inline int mj_wave_kernels(int bounces, bool emit) {
 // Looks up the persistent grids of the multi-job kernels (call before a
 // stream capture).
 void prepare_mj_kernels();
+// The traversal launches of the path waves (wave_trace.cu, a translation
+// unit of its own so that its arithmetic is compiled without contraction
+// whatever the shading kernels are compiled with): closest hits of a path
+// queue, any hits of the shadow queue, closest hits of the MIS BSDF queue
+// at the top of the shadow queue's storage.  `mj`: multi-job waves (the
+// scene of each ray from the wave tables).  Grids are the kernels' resident
+// blocks (persistent lanes).
+void launch_wave_extend(bool mj, int tri_test, int width, const DeviceScene& s,
+                        const MJTables& t, const float4* ro, const float4* rd,
+                        const uint32_t* count, uint32_t* fetch_next,
+                        ajg_hit* hits, TraceCounters* ctr, uint32_t* err,
+                        cudaStream_t st);
+void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
+                        const MJTables& t, const float4* sq_o,
+                        const float4* sq_d, const uint16_t* sq_scene,
+                        const uint32_t* count, uint32_t* fetch_next,
+                        uint8_t* vis, TraceCounters* ctr, uint32_t* err,
+                        cudaStream_t st);
+void launch_wave_bsdf_trace(bool mj, int tri_test, int width,
+                            const DeviceScene& s, const MJTables& t,
+                            const float4* sq_o, const float4* sq_d,
+                            const uint16_t* sq_scene, const uint32_t* count,
+                            uint32_t* fetch_next, uint32_t cap, uint32_t n_max,
+                            float* t_hit, int32_t* prim_hit,
+                            TraceCounters* ctr, uint32_t* err, cudaStream_t st);
 // Blocks of `fn` (launched with `threads` threads) resident on the device at
 // once: the grid of a persistent kernel.
 int resident_grid(const void* fn, int threads);

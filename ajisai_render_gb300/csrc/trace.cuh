@@ -234,6 +234,9 @@ constexpr int trace_min_blocks() {
 #ifndef AJG_LEAF_BATCH
 #define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
+#ifndef AJG_REFILL_ANY
+#define AJG_REFILL_ANY AJG_REFILL  // the same threshold for any-hit queries
+#endif
 constexpr int kRefill = AJG_REFILL;
 constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
 
@@ -299,7 +302,8 @@ __device__ __forceinline__ void trace_persistent(
   for (;;) {
     const unsigned idle = __ballot_sync(full, k == kIdle);
     const unsigned done = __ballot_sync(full, k == kDone);
-    if (idle && (__popc(idle) >= kRefill || (idle | done) == full)) {
+    constexpr int kRefillQ = ANY ? AJG_REFILL_ANY : kRefill;
+    if (idle && (__popc(idle) >= kRefillQ || (idle | done) == full)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(next, (uint32_t)__popc(idle));
