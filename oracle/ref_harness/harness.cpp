@@ -355,6 +355,12 @@ void* ref_scene_create(const int32_t* prims, const float* prim_f, int32_t np,
 
 void ref_scene_destroy(void* h) { delete static_cast<HScene*>(h); }
 
+/* The scene's primitives (a std::vector<Rc<Primitive>>), for code that
+ * drives the reference's interfaces with them (the adapters' tests). */
+const void* ref_scene_primitives(void* h) {
+  return &static_cast<HScene*>(h)->prims;
+}
+
 int64_t ref_scene_num_tris(void* h) {
   return (int64_t)static_cast<HScene*>(h)->ploc()->triangles_.size();
 }
