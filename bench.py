@@ -523,7 +523,7 @@ def run_batched(ctx, args):
     both with host results.  Films must be identical bit for bit; each
     image's RMSE against an FP64-accumulated render of a central crop."""
     import torch
-    from ajisai_render_gb300 import api
+    from ajisai_render_gb300 import api, autotune
     t0 = time.perf_counter()
     jobs, built, tris = build_mix(ctx, args.batch_jobs, seed=1)
     gen_s = time.perf_counter() - t0
@@ -538,13 +538,33 @@ def run_batched(ctx, args):
     descs[0][2].Render(descs[0][0], _cam(descs[0][1], 16, 16))
     ctx.render_batch([(descs[0][0], _cam(descs[0][1], 16, 16), descs[0][2])])
     torch.cuda.synchronize()
+    # the request loop's wave size for this batch, tuned on 1/8 of its samples
+    tuned = None
+    if not args.batch_wave_paths:
+        tuned = autotune.tune_batch(ctx, descs)
+    plain, t_each = [], []
     t = time.perf_counter()
-    plain = [r.Render(g, cam) for g, cam, r in descs]
+    for g, cam, r in descs:
+        t1 = time.perf_counter()
+        plain.append(r.Render(g, cam))
+        t_each.append(time.perf_counter() - t1)
     t_plain = time.perf_counter() - t
     t = time.perf_counter()
     batched = ctx.render_batch(descs)
     t_batch = time.perf_counter() - t
     identical = all(_same_bits(f.rgbw, p.rgbw) for (f, _), p in zip(batched, plain))
+    # the plain arm by job size: where its time goes
+    sizes = np.array([j["res"] ** 2 * j["spp"] for j in jobs], np.float64)
+    classes = {}
+    for name, lo, hi in (("small (< 4 M samples)", 0, 4e6),
+                         ("medium (4-64 M samples)", 4e6, 64e6),
+                         ("large (>= 64 M samples)", 64e6, np.inf)):
+        m = (sizes >= lo) & (sizes < hi)
+        if m.any():
+            te = float(np.sum(np.array(t_each)[m]))
+            classes[name] = {"jobs": int(m.sum()), "samples": int(sizes[m].sum()),
+                             "plain_s": te,
+                             "plain_msamples_s": float(sizes[m].sum() / te / 1e6)}
     # FP64 references of a central crop (+1 row/column of footprint sources)
     c = args.rmse_crop
     refs = []
@@ -576,14 +596,47 @@ def run_batched(ctx, args):
         "plain_msamples_s": samples / t_plain / 1e6,
         "speedup_vs_plain": t_plain / t_batch,
         "batched_s": t_batch, "plain_s": t_plain,
+        "plain_by_job_size": classes,
+        "autotuned": tuned,
         "films_bit_identical": bool(identical),
         "rmse_vs_fp64": {"crop": c, "reference_spp": args.rmse_spp,
                          "median": float(np.median(rmse)), "max": float(rmse.max()),
                          "min": float(rmse.min()), "equal_for_both_arms": bool(identical)},
         "results": "host buffers (device-to-host copy of every film inside the timing)",
         "scene_generation_and_build_s": gen_s, "reference_render_s": t_ref,
+        "small_jobs": small_mix(ctx, built, jobs),
         "_capacity": samples / t_batch,
     }
+
+
+def small_mix(ctx, built, jobs):
+    """A sub-mix of small jobs over the same scenes (128^2 or 256^2, 16-64
+    spp): the jobs whose plain renders leave the GPU underused, rendered one
+    by one and as one batch."""
+    from ajisai_render_gb300 import api
+    rng = np.random.default_rng(11)
+    descs, samples = [], 0
+    for (g, cam), j in zip(built, jobs):
+        res = int(rng.choice([128, 256]))
+        spp = int(round(np.exp(rng.uniform(np.log(16), np.log(64)))))
+        r = api.PTRenderer(api.PTRendererArgs(spp=spp, min_bounces=MIN_B,
+                                              max_bounces=BATCH_DEPTH), seed=13)
+        descs.append((g, _cam(cam, res, res), r))
+        samples += res * res * spp
+    ctx.render_batch(descs[:2])
+    t = time.perf_counter()
+    plain = [r.Render(g, cam) for g, cam, r in descs]
+    t_plain = time.perf_counter() - t
+    t = time.perf_counter()
+    batched = ctx.render_batch(descs)
+    t_batch = time.perf_counter() - t
+    return {"workload": f"{len(descs)} jobs over the batched workload's scenes, "
+                        "res {128,256}^2, spp log-uniform 16-64, depth 12",
+            "samples": int(samples), "plain_msamples_s": samples / t_plain / 1e6,
+            "batched_msamples_s": samples / t_batch / 1e6,
+            "speedup_vs_plain": t_plain / t_batch,
+            "films_bit_identical": all(_same_bits(f.rgbw, p.rgbw)
+                                       for (f, _), p in zip(batched, plain))}
 
 
 def serve_plan(n, seed):
