@@ -129,7 +129,7 @@ class ServeStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "jobs_submitted", "jobs_done", "jobs_cancelled", "jobs_failed", "waves",
         "paths", "results_delivered", "graph_builds", "kernel_launches",
-        "active_bytes")]
+        "active_bytes")] + [("busy_ms", C.c_double)]
 
 
 assert C.sizeof(Material) == 64 and C.sizeof(Light) == 48

@@ -5,6 +5,8 @@
 #include "common.cuh"
 
 namespace ajg {
+// (internal linkage: several translation units include this header)
+namespace {
 
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
@@ -106,4 +108,5 @@ inline void device_scan(const uint32_t* in, uint32_t* out, uint64_t n,
   k_scan_add<<<(unsigned)tiles, kScanThreads, 0, s>>>(out, n, totals);
 }
 
+}  // namespace
 }  // namespace ajg

@@ -31,7 +31,7 @@
 static_assert(sizeof(ajg_job_desc) == 224, "ajg_job_desc layout");
 static_assert(sizeof(ajg_job_status) == 56, "ajg_job_status layout");
 static_assert(sizeof(ajg_serve_opts) == 16, "ajg_serve_opts layout");
-static_assert(sizeof(ajg_serve_stats) == 80, "ajg_serve_stats layout");
+static_assert(sizeof(ajg_serve_stats) == 88, "ajg_serve_stats layout");
 static_assert(sizeof(ajg_scene_info) == 48, "ajg_scene_info layout");
 static_assert(sizeof(ajg_emitter) == 32, "ajg_emitter layout");
 static_assert(sizeof(ajg_sppm_params) == 40, "ajg_sppm_params layout");
@@ -85,6 +85,7 @@ struct Report {
 };
 
 struct InFlight {
+  cudaEvent_t ev0 = nullptr;  // recorded before the wave's work
   cudaEvent_t ev;
   std::vector<Job*> jobs;
   std::vector<Report> reports;
@@ -519,6 +520,8 @@ bool Server::plan_and_launch() {
   cudaMemcpyAsync(d_tables, h, table_bytes, cudaMemcpyHostToDevice, st);
 
   InFlight f{};
+  cudaEventCreate(&f.ev0);
+  cudaEventRecord(f.ev0, st);
   // the closest-hit MIS BSDF pass runs when a scene of the wave has emitters
   bool emit = false;
   for (const Plan& p : plan) emit |= p.job->scene->d.tri_emit != nullptr;
@@ -569,7 +572,7 @@ bool Server::plan_and_launch() {
   *f.err = 0;
   cudaMemcpyAsync(f.err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
   cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st);
-  cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming);
+  cudaEventCreate(&f.ev);
   cudaEventRecord(f.ev, st);
   {
     std::lock_guard<std::mutex> lk(mu);
@@ -588,10 +591,17 @@ void Server::retire_oldest() {
   InFlight f = std::move(inflight.front());
   inflight.pop_front();
   cudaEventSynchronize(f.ev);
+  float wave_ms = 0.f;
+  if (f.ev0 && cudaEventElapsedTime(&wave_ms, f.ev0, f.ev) != cudaSuccess) {
+    cudaGetLastError();
+    wave_ms = 0.f;
+  }
+  if (f.ev0) cudaEventDestroy(f.ev0);
   cudaEventDestroy(f.ev);
   const uint32_t guard = *f.err;
   err_words.push_back(f.err);
   std::lock_guard<std::mutex> lk(mu);
+  stats.busy_ms += wave_ms;
   // host copies out of the staging memory, under the lock so that
   // ajg_job_read sees whole results
   for (const Report& r : f.reports) {

@@ -53,16 +53,20 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
              const float4* __restrict__ sq_d,
              const uint16_t* __restrict__ sq_scene,
              const uint32_t* __restrict__ count, uint32_t* fetch_next,
-             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err) {
+             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err,
+             const uint32_t* __restrict__ perm) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
+  // the queue entry of the lane's current ray (a lane traces one at a time)
+  uint32_t cur = 0;
   auto fetch = [&](uint32_t k, TraceScene& ts) {
-    const float4 o = sq_o[k], d = sq_d[k];
-    if constexpr (MJ) retarget(ts, t, sq_scene[k]);
+    cur = perm ? perm[k] : k;
+    const float4 o = sq_o[cur], d = sq_d[cur];
+    if constexpr (MJ) retarget(ts, t, sq_scene[cur]);
     return make_query(xyz(o), xyz(d), kRayEps, o.w);
   };
-  auto finish = [&](uint32_t k, const Hit&, bool occ) {
-    if (!occ) vis[__float_as_uint(sq_d[k].w)] = 1;
+  auto finish = [&](uint32_t, const Hit&, bool occ) {
+    if (!occ) vis[__float_as_uint(sq_d[cur].w)] = 1;
   };
   trace_persistent<TEST, true, W>(trace_scene(s), n, fetch_next, fetch,
                                   finish, nr, nn, nt, err);
@@ -125,17 +129,17 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
                         const float4* sq_d, const uint16_t* sq_scene,
                         const uint32_t* count, uint32_t* fetch_next,
                         uint8_t* vis, TraceCounters* ctr, uint32_t* err,
-                        cudaStream_t st) {
+                        cudaStream_t st, const uint32_t* perm) {
   dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
     constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
     if (mj) {
       const int g = resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
       k_shadow<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err);
+          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err, perm);
     } else {
       const int g = resident_grid((const void*)k_shadow<TT, false, WW>, kTraceThreads);
       k_shadow<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err);
+          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err, perm);
     }
   });
 }

@@ -658,6 +658,7 @@ def serve_point(ctx, built, plan, rng, rate, capacity_samples_s):
     results every 16 spp; returns the load point's statistics."""
     from ajisai_render_gb300 import api
     gaps = rng.exponential(1.0 / rate, len(plan))
+    st0 = ctx.serve_stats()
     submitted = []
     t0 = time.perf_counter()
     at = 0.0
@@ -689,11 +690,19 @@ def serve_point(ctx, built, plan, rng, rate, capacity_samples_s):
     waiting = [int(((sub <= t) & (start > t)).sum()) for t in sub]
     q = len(in_sys) // 4
     span_ms = done_t.max() - sub.min()
+    st1 = ctx.serve_stats()
+    busy_ms = st1["busy_ms"] - st0["busy_ms"]
     pct = lambda a, p: float(np.percentile(a, p))
     return {
         "jobs": len(plan), "jobs_done": sum(1 for s in sts if s["state_name"] == "done"),
         "rate_jobs_s": rate, "arrivals_s": t_arrived,
         "msamples_s": float(size.sum() / (span_ms / 1e3) / 1e6),
+        # the device's side: waves, their summed device time, and the
+        # throughput while a wave ran
+        "waves": int(st1["waves"] - st0["waves"]),
+        "gpu_busy_frac": float(busy_ms / span_ms) if span_ms > 0 else None,
+        "msamples_s_while_busy": float(size.sum() / (busy_ms / 1e3) / 1e6)
+        if busy_ms > 0 else None,
         "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "mean_ms": float(lat.mean()),
         "first_result_p50_ms": pct(first, 50), "first_result_p99_ms": pct(first, 99),
         "slowdown_p50": pct(slow, 50), "slowdown_p99": pct(slow, 99),

@@ -461,6 +461,9 @@ typedef struct ajg_serve_stats {
   uint64_t waves, paths, results_delivered, graph_builds;
   uint64_t kernel_launches;
   uint64_t active_bytes;  /* films and result buffers held now */
+  double busy_ms;         /* summed device time of the retired waves (CUDA
+                             events around each wave's work on the loop's
+                             stream, its result copies included) */
 } ajg_serve_stats;
 
 /* Scheduling options; takes effect for the waves planned after the call. */

@@ -86,7 +86,7 @@ def test_serving_structs_match_header(lib):
     assert C.sizeof(_lib.JobDesc) == 8 + 144 + 32 + 16 + 8 + 16
     assert C.sizeof(_lib.JobStatus) == 24 + 32
     assert C.sizeof(_lib.ServeOpts) == 16
-    assert C.sizeof(_lib.ServeStats) == 80
+    assert C.sizeof(_lib.ServeStats) == 88
     assert C.sizeof(_lib.SceneInfo) == 48
 
 
