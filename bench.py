@@ -70,6 +70,12 @@ def parse():
     ap.add_argument("--batch-jobs", type=int, default=48)
     ap.add_argument("--serve-jobs", type=int, default=340,
                     help="jobs per load point of the serving sweep")
+    ap.add_argument("--serve-policy", choices=["fair", "fifo"], default="fair")
+    ap.add_argument("--serve-capacity", type=float, default=0.0,
+                    help="Msamples/s the serving loads are fractions of (0: the "
+                         "batched run's throughput)")
+    ap.add_argument("--only-serve", action="store_true",
+                    help="run the serving sweep alone (one JSON line)")
     ap.add_argument("--serve-loads", default="0.6,0.9,1.5",
                     help="arrival rates of the serving sweep, as fractions of the "
                          "batched throughput")
@@ -482,6 +488,10 @@ def run_ours(args):
                 for kind in ("closest", "any")},
             "step_ms": step_ms, "nonfinite_pixels": nonfinite,
             "mrays_s": value * rays_per_sample,
+            # the metric's latency half: p99 of the serving sweep's busiest
+            # load point below saturation (its offered load beside it)
+            "p99_job_latency_ms": served["p99_ms"] if served else None,
+            "p99_at_offered_load": served["latency_at_load"] if served else None,
             "cornell": cornell, "batched": batched, "served": served, "large": large,
             "sppm": sppm, "impl": "ours"}))
     scene.release()
@@ -720,7 +730,7 @@ def run_served(ctx, args, capacity_samples_s):
     highest past saturation; progressive results every 16 spp, fair
     scheduling; latency from submission to the final result."""
     jobs8, built, tris = build_mix(ctx, 8, seed=2)
-    ctx.configure_serving("fair", wave_paths=args.batch_wave_paths)
+    ctx.configure_serving(args.serve_policy, wave_paths=args.batch_wave_paths)
     loads = [float(x) for x in args.serve_loads.split(",") if x]
     points = []
     t0 = time.perf_counter()
@@ -741,7 +751,7 @@ def run_served(ctx, args, capacity_samples_s):
                     f"({capacity_samples_s / 1e6:.0f} Msamples/s), 8 resident scenes "
                     f"({tris:,} triangles), res {{256,512,1024}}^2, spp log-uniform 4-1024, "
                     "camera on a seeded sphere, depth 12, progressive results every 16 spp, "
-                    "fair scheduling, HBM budget 150 GB",
+                    f"{args.serve_policy} scheduling, HBM budget 150 GB",
         "points": points,
         # the headline latency: the busiest load point below saturation
         "p50_ms": head["p50_ms"] if head else None,
@@ -969,6 +979,18 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_serve:
+        # the serving sweep alone (tuning runs), loads relative to
+        # --serve-capacity
+        from ajisai_render_gb300 import api
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        ctx = api.Context(local, wave_paths=args.batch_wave_paths,
+                          hbm_budget_bytes=150 << 30)
+        cap = (args.serve_capacity or 337.0) * 1e6
+        print(json.dumps({"served": run_served(ctx, args, cap),
+                          "wave_paths": args.batch_wave_paths,
+                          "policy": args.serve_policy}))
+        ctx.close()
     elif args.only_sppm:
         # the SPPM section alone (profiling runs)
         print(json.dumps({"sppm": run_sppm(args, int(os.environ.get("LOCAL_RANK", "0")))}))
