@@ -1,4 +1,6 @@
-// BVH2 traversal for closest-hit and any-hit queries.
+// Closest-hit and any-hit traversal over the PLOC tree: the binary tree as
+// built, or (the default) the tree collapsed into 4-wide nodes, 8-wide, or
+// 4/8-wide with quantised boxes.
 //
 // Results are defined independently of the tree shape and of the visiting
 // order: the closest hit is the minimum t over every triangle the test
@@ -6,10 +8,14 @@
 // never culls a box that can hold such a hit -- it is the reference's slab
 // test, (bound - o) * inv_dir (ploc_aggregate.cpp:154-162), with the far
 // distance widened by 1 + 2*gamma(3) (Pharr, Jakob, Humphreys, PBRT 3rd ed.,
-// 3.9.2) and inclusive comparisons against the current best t.  Children are
-// visited nearest first; leaf children are tested as soon as their box
-// passes.  The per-thread stack lives in registers/local memory and is
-// guarded: overflow sets the device error word and ends the ray.
+// 3.9.2) and inclusive comparisons against the current best t.  Lanes are
+// persistent (trace_persistent): one node visit per iteration, a lane whose
+// ray finished takes the next from a shared counter.  Closest-hit rays visit
+// the nearest interior child and push the others farthest first; any-hit
+// rays take the children in order; a wide node's passing leaf children are
+// tested after its box tests.  Each lane's stack keeps its top 16 entries
+// in a shared-memory ring and the rest in local memory, and is guarded:
+// overflow sets the device error word and ends the ray.
 #pragma once
 #include <type_traits>
 

@@ -385,6 +385,8 @@ def run_ours(args):
                         "l1_throughput_pct", "l2_throughput_pct", "l1_hit_rate_pct",
                         "l2_hit_rate_pct", "threads_per_warp_inst")},
                 "rays_per_launch": [int(r["rays"]) for r in launches_k],
+                "nodes_per_ray_per_launch": [round(r["nodes"] / max(1, r["rays"]), 2)
+                                             for r in launches_k],
                 "other_kind_rays_per_launch": [int(r["rays"]) for r in log
                                                if r["kind"] not in (dom, "shade")],
                 "ms_per_launch": [round(float(r["ms"]), 3) for r in launches_k],
@@ -588,14 +590,25 @@ def run_batched(ctx, args):
     t = time.perf_counter()
     ref_out = ctx.render_batch(refs)
     t_ref = time.perf_counter() - t
-    rmse = []
+    rmse, trimmed, nonfinite = [], [], []
     for (film, _), (ref, _), (_, _, _, win) in zip(batched, ref_out, refs):
         x0, y0, w, h = win
         cw, ch = min(c, w), min(c, h)
-        a = torch.from_numpy(np.ascontiguousarray(film.rgbw[y0:y0 + ch, x0:x0 + cw])).cuda()
-        b = torch.from_numpy(np.ascontiguousarray(ref.rgbw[:ch, :cw])).cuda()
+        fa = np.ascontiguousarray(film.rgbw[y0:y0 + ch, x0:x0 + cw])
+        fb = np.ascontiguousarray(ref.rgbw[:ch, :cw])
+        a = torch.from_numpy(fa).cuda()
+        b = torch.from_numpy(fb).cuda()
         e, _ = ctx.image_rmse(a.data_ptr(), b.data_ptr(), cw, ch)
         rmse.append(e)
+        # a robust error beside it: the RMSE without the worst 1% of the
+        # crop's pixels (a single firefly dominates the plain RMSE)
+        ia = fa[..., :3].astype(np.float64) / np.maximum(fa[..., 3:], 1e-30)
+        ib = fb[..., :3].astype(np.float64) / np.maximum(fb[..., 3:], 1e-30)
+        sq = ((ia - ib) ** 2).mean(-1).ravel()
+        sq = np.sort(sq[np.isfinite(sq)])
+        keep = sq[:max(1, int(len(sq) * 0.99))]
+        trimmed.append(float(np.sqrt(keep.mean())))
+        nonfinite.append(int((~np.isfinite(film.rgbw)).any(-1).sum()))
     rmse = np.array(rmse)
     return {
         "workload": f"{len(jobs)} jobs over their own scenes ({tris:,} triangles in all, "
@@ -611,7 +624,12 @@ def run_batched(ctx, args):
         "films_bit_identical": bool(identical),
         "rmse_vs_fp64": {"crop": c, "reference_spp": args.rmse_spp,
                          "median": float(np.median(rmse)), "max": float(rmse.max()),
-                         "min": float(rmse.min()), "equal_for_both_arms": bool(identical)},
+                         "min": float(rmse.min()), "equal_for_both_arms": bool(identical),
+                         "trimmed_99pct_median": float(np.median(trimmed)),
+                         "trimmed_99pct_max": float(np.max(trimmed)),
+                         "per_image": [round(float(x), 6) for x in rmse],
+                         "per_image_trimmed_99pct": [round(x, 6) for x in trimmed]},
+        "nonfinite_pixels_per_image": nonfinite,
         "results": "host buffers (device-to-host copy of every film inside the timing)",
         "scene_generation_and_build_s": gen_s, "reference_render_s": t_ref,
         "small_jobs": small_mix(ctx, built, jobs),
@@ -724,6 +742,23 @@ def serve_point(ctx, built, plan, rng, rate, capacity_samples_s):
     }
 
 
+def serve_plain(built, plan):
+    """The plain single-job tracer on jobs of the serving workload: each job
+    rendered alone through ajg_render (host film), one after another."""
+    from ajisai_render_gb300 import api
+    samples = 0
+    t = time.perf_counter()
+    for k, res, spp, cam in plan:
+        r = api.PTRenderer(api.PTRendererArgs(spp=spp, min_bounces=MIN_B,
+                                              max_bounces=BATCH_DEPTH),
+                           seed=i_seed(k, res, spp))
+        r.Render(built[k][0], cam)
+        samples += res * res * spp
+    dt = time.perf_counter() - t
+    return {"jobs": len(plan), "samples": int(samples), "s": dt,
+            "msamples_s": samples / dt / 1e6}
+
+
 def run_served(ctx, args, capacity_samples_s):
     """The serving sweep: Poisson arrivals of render jobs over 8 resident
     scenes at several rates (fractions of the batched throughput), the
@@ -742,6 +777,8 @@ def run_served(ctx, args, capacity_samples_s):
         pt["offered_load"] = load
         points.append(pt)
     total = sum(p["jobs"] for p in points)
+    # the same workload through the plain tracer: the first jobs of a plan
+    plain = serve_plain(built, serve_plan(min(40, args.serve_jobs), seed=5)[0])
     below = [p for p in points if p["offered_load"] < 1.0] or points
     head = max(below, key=lambda p: p["offered_load"]) if below else None
     return {
@@ -758,6 +795,9 @@ def run_served(ctx, args, capacity_samples_s):
         "p99_ms": head["p99_ms"] if head else None,
         "latency_at_load": head["offered_load"] if head else None,
         "saturated_msamples_s": max((p["msamples_s"] for p in points), default=None),
+        "plain": plain,
+        "saturated_vs_plain": (max((p["msamples_s"] for p in points), default=0.0) /
+                               plain["msamples_s"]),
         "wall_s": time.perf_counter() - t0,
     }
 
