@@ -237,6 +237,9 @@ constexpr int trace_min_blocks() {
 #define AJG_SMEM_STACK 16  // stack entries per lane in shared memory (a power
                            // of two; 0: the whole stack in local memory)
 #endif
+#ifndef AJG_ANY_RING
+#define AJG_ANY_RING AJG_SMEM_STACK  // the same for any-hit queries
+#endif
 #ifndef AJG_LEAF_BATCH
 #define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
@@ -269,29 +272,43 @@ __device__ __forceinline__ void trace_persistent(
   // The top kShort entries of each lane's stack live in shared memory (a
   // ring: entry i in slot i % kShort, lane-interleaved); a push evicts the
   // entry kShort below the top to the local array, a pop refills its slot.
-  constexpr int kShort = AJG_SMEM_STACK;
+  // Any-hit entries hold the node alone: every pushed box passed against
+  // the ray's fixed t_max, so the pop needs no distance.
+  constexpr int kShort = ANY ? AJG_ANY_RING : AJG_SMEM_STACK;
   static_assert((kShort & (kShort - 1)) == 0, "a power of two");
-  __shared__ int2 s_ring[kShort * 128];
-  int2* const ring = s_ring + threadIdx.x;
+  using Slot = std::conditional_t<ANY, int, int2>;
+  __shared__ Slot s_ring[kShort * 128];
+  Slot* const ring = s_ring + threadIdx.x;
   auto push = [&](int nd, float t) {
     const int slot = sp & (kShort - 1);
-    if (sp >= kShort) {
-      const int2 old = ring[slot * 128];
-      stack_node[sp - kShort] = old.x;
-      stack_t[sp - kShort] = __int_as_float(old.y);
+    if constexpr (ANY) {
+      if (sp >= kShort) stack_node[sp - kShort] = ring[slot * 128];
+      ring[slot * 128] = nd;
+    } else {
+      if (sp >= kShort) {
+        const int2 old = ring[slot * 128];
+        stack_node[sp - kShort] = old.x;
+        stack_t[sp - kShort] = __int_as_float(old.y);
+      }
+      ring[slot * 128] = make_int2(nd, __float_as_int(t));
     }
-    ring[slot * 128] = make_int2(nd, __float_as_int(t));
     ++sp;
   };
   auto pop = [&](int& nd, float& t) {
     --sp;
     const int slot = sp & (kShort - 1);
-    const int2 v = ring[slot * 128];
-    nd = v.x;
-    t = __int_as_float(v.y);
-    if (sp >= kShort)
-      ring[slot * 128] =
-          make_int2(stack_node[sp - kShort], __float_as_int(stack_t[sp - kShort]));
+    if constexpr (ANY) {
+      nd = ring[slot * 128];
+      t = -__int_as_float(0x7f800000);
+      if (sp >= kShort) ring[slot * 128] = stack_node[sp - kShort];
+    } else {
+      const int2 v = ring[slot * 128];
+      nd = v.x;
+      t = __int_as_float(v.y);
+      if (sp >= kShort)
+        ring[slot * 128] = make_int2(stack_node[sp - kShort],
+                                     __float_as_int(stack_t[sp - kShort]));
+    }
   };
 #else
   auto push = [&](int nd, float t) {
