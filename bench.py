@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--serve-policy", choices=["fair", "fifo"], default="fair")
     ap.add_argument("--serve-capacity", type=float, default=0.0,
                     help="Msamples/s the serving loads are fractions of (0: the "
-                         "batched run's throughput)")
+                         "plain tracer's throughput on the serving workload)")
     ap.add_argument("--only-serve", action="store_true",
                     help="run the serving sweep alone (one JSON line)")
     ap.add_argument("--serve-loads", default="0.6,0.9,1.5",
@@ -463,7 +463,7 @@ def run_ours(args):
                            hbm_budget_bytes=150 << 30)
         batched = run_batched(bctx, args)
         if not args.no_serve:
-            served = run_served(bctx, args, batched["_capacity"])
+            served = run_served(bctx, args, args.serve_capacity * 1e6)
         batched.pop("_capacity")
         bctx.close()
     if rank == 0:
@@ -620,6 +620,10 @@ def run_batched(ctx, args):
         "speedup_vs_plain": t_plain / t_batch,
         "batched_s": t_batch, "plain_s": t_plain,
         "plain_by_job_size": classes,
+        # what batching could reach on this mix if every sample ran at the
+        # plain rate of the biggest jobs
+        "speedup_bound_at_large_job_rate": t_plain / (samples / (1e6 * max(
+            c["plain_msamples_s"] for c in classes.values()))) if classes else None,
         "autotuned": tuned,
         "films_bit_identical": bool(identical),
         "rmse_vs_fp64": {"crop": c, "reference_spp": args.rmse_spp,
@@ -759,12 +763,18 @@ def serve_plain(built, plan):
             "msamples_s": samples / dt / 1e6}
 
 
-def run_served(ctx, args, capacity_samples_s):
+def run_served(ctx, args, capacity_samples_s=0.0):
     """The serving sweep: Poisson arrivals of render jobs over 8 resident
-    scenes at several rates (fractions of the batched throughput), the
+    scenes at several rates -- fractions of the plain tracer's throughput on
+    the same workload (40 jobs of it rendered one by one first), the
     highest past saturation; progressive results every 16 spp, fair
     scheduling; latency from submission to the final result."""
     jobs8, built, tris = build_mix(ctx, 8, seed=2)
+    # the same workload through the plain tracer (jobs of another seed): the
+    # capacity the load points are fractions of
+    plain = serve_plain(built, serve_plan(min(40, args.serve_jobs), seed=4)[0])
+    if not capacity_samples_s:
+        capacity_samples_s = plain["msamples_s"] * 1e6
     ctx.configure_serving(args.serve_policy, wave_paths=args.batch_wave_paths)
     loads = [float(x) for x in args.serve_loads.split(",") if x]
     points = []
@@ -777,15 +787,14 @@ def run_served(ctx, args, capacity_samples_s):
         pt["offered_load"] = load
         points.append(pt)
     total = sum(p["jobs"] for p in points)
-    # the same workload through the plain tracer: the first jobs of a plan
-    plain = serve_plain(built, serve_plan(min(40, args.serve_jobs), seed=5)[0])
     below = [p for p in points if p["offered_load"] < 1.0] or points
     head = max(below, key=lambda p: p["offered_load"]) if below else None
     return {
         "workload": f"{args.serve_jobs} jobs per load point ({total} in all; the "
                     "configuration's 10,000-job run is unmeasured), Poisson arrivals at "
-                    f"{', '.join(f'{x:.0%}' for x in loads)} of the batched throughput "
-                    f"({capacity_samples_s / 1e6:.0f} Msamples/s), 8 resident scenes "
+                    f"{', '.join(f'{x:.0%}' for x in loads)} of the plain tracer's "
+                    f"throughput on this workload ({capacity_samples_s / 1e6:.0f} "
+                    "Msamples/s), 8 resident scenes "
                     f"({tris:,} triangles), res {{256,512,1024}}^2, spp log-uniform 4-1024, "
                     "camera on a seeded sphere, depth 12, progressive results every 16 spp, "
                     f"{args.serve_policy} scheduling, HBM budget 150 GB",
@@ -1026,8 +1035,7 @@ def main():
         local = int(os.environ.get("LOCAL_RANK", "0"))
         ctx = api.Context(local, wave_paths=args.batch_wave_paths,
                           hbm_budget_bytes=150 << 30)
-        cap = (args.serve_capacity or 337.0) * 1e6
-        print(json.dumps({"served": run_served(ctx, args, cap),
+        print(json.dumps({"served": run_served(ctx, args, args.serve_capacity * 1e6),
                           "wave_paths": args.batch_wave_paths,
                           "policy": args.serve_policy}))
         ctx.close()
