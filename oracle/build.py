@@ -21,6 +21,9 @@ BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 ORACLE_SO = BUILD / "libajg_oracle.so"
 REF_SO = REF_OUT / "libajref.so"
+# Where the reference's sources are mounted (read-only) in the development
+# container; AJG_REFERENCE_ROOT points the recipe elsewhere.  Absent on the
+# GPU hosts, where only the restatement is built.
 REFERENCE_ROOT = Path(os.environ.get("AJG_REFERENCE_ROOT", "/root/reference"))
 
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off",
