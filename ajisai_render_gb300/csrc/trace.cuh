@@ -240,6 +240,10 @@ constexpr int trace_min_blocks() {
 #ifndef AJG_ANY_RING
 #define AJG_ANY_RING AJG_SMEM_STACK  // the same for any-hit queries
 #endif
+#ifndef AJG_CLOSEST_STACK_T
+#define AJG_CLOSEST_STACK_T 1  // 0: closest-hit entries without the box's
+                               // entry distance (popped boxes are re-tested)
+#endif
 #ifndef AJG_LEAF_BATCH
 #define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
@@ -274,14 +278,15 @@ __device__ __forceinline__ void trace_persistent(
   // entry kShort below the top to the local array, a pop refills its slot.
   // Any-hit entries hold the node alone: every pushed box passed against
   // the ray's fixed t_max, so the pop needs no distance.
+  constexpr bool kNodeOnly = ANY || !AJG_CLOSEST_STACK_T;
   constexpr int kShort = ANY ? AJG_ANY_RING : AJG_SMEM_STACK;
   static_assert((kShort & (kShort - 1)) == 0, "a power of two");
-  using Slot = std::conditional_t<ANY, int, int2>;
+  using Slot = std::conditional_t<kNodeOnly, int, int2>;
   __shared__ Slot s_ring[kShort * 128];
   Slot* const ring = s_ring + threadIdx.x;
   auto push = [&](int nd, float t) {
     const int slot = sp & (kShort - 1);
-    if constexpr (ANY) {
+    if constexpr (kNodeOnly) {
       if (sp >= kShort) stack_node[sp - kShort] = ring[slot * 128];
       ring[slot * 128] = nd;
     } else {
@@ -297,7 +302,7 @@ __device__ __forceinline__ void trace_persistent(
   auto pop = [&](int& nd, float& t) {
     --sp;
     const int slot = sp & (kShort - 1);
-    if constexpr (ANY) {
+    if constexpr (kNodeOnly) {
       nd = ring[slot * 128];
       t = -__int_as_float(0x7f800000);
       if (sp >= kShort) ring[slot * 128] = stack_node[sp - kShort];
