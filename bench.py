@@ -391,6 +391,12 @@ def run_ours(args):
                                                if r["kind"] not in (dom, "shade")],
                 "ms_per_launch": [round(float(r["ms"]), 3) for r in launches_k],
                 "algorithmic_bytes_per_launch": bytes_per_launch,
+                # the same fraction with the nominal 80-byte 4-wide node
+                # (six planes of four floats and four 32-bit references) in
+                # place of this layout's 128-byte, 64-byte-aligned node
+                "frac_at_80_byte_nodes": ((st[n_k] * 80 + st[t_k] * TRI_BYTES) / launches
+                                          / (avg_ms / 1e3) / 1e9 / peak)
+                if avg_ms > 0 and node_bytes == 128 else None,
                 "avg_launch_ms": avg_ms, "launches": int(st[l_k]),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "kernel_time_share": st[ms_k] / max(1e-9, prof_ms),
