@@ -1145,8 +1145,10 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const uint32_t shadow_cap = (uint32_t)(P * nt);
   const int gs = kSMs * 8;
   // persistent traversal: resident blocks only
+  const DeviceScene s_closest = closest_view(s);
   auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
-    launch_wave_extend(false, s.tri_test, s.width, s, t, w.ro[q], w.rd[q],
+    launch_wave_extend(false, s_closest.tri_test, s_closest.width, s_closest, t,
+                       w.ro[q], w.rd[q],
                        &w.counts[q], &w.counts[8], hits, &ctx->d_counters[0],
                        ctx->d_error, es);
   };
@@ -1166,7 +1168,8 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
     cudaEventRecord(ctx->ev_hits, ts);
   };
   auto bsdf_closest = [&]() {
-    launch_wave_bsdf_trace(false, s.tri_test, s.width, s, t, w.sq_o, w.sq_d,
+    launch_wave_bsdf_trace(false, s_closest.tri_test, s_closest.width, s_closest, t,
+                           w.sq_o, w.sq_d,
                            nullptr, &w.counts[9], &w.counts[10], shadow_cap,
                            (uint32_t)P, reinterpret_cast<float*>(w.lists),
                            reinterpret_cast<int32_t*>(w.lists + P),

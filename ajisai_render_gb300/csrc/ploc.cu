@@ -813,14 +813,21 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     return set_err(ctx, AJG_ERR_INVALID,
                    "bvh_width must be 0, 2, 4 or 8 (4 and 8 optionally "
                    "| AJG_BVH_COMPRESSED)");
+#ifndef AJG_HYBRID_CLOSEST
+#define AJG_HYBRID_CLOSEST 0
+#endif
+  // the binary layout: the tree itself (width 2), or beside a plain 4-wide
+  // tree for the closest-hit launches (AJG_HYBRID_CLOSEST)
+  const bool hybrid = AJG_HYBRID_CLOSEST && width == 4 && n > 1;
   float4* bvh =
       width == 2 ? (float4*)keep(inner * 4 * sizeof(float4)) : nullptr;
+  float4* bvh_bin = hybrid ? (float4*)keep(inner * 4 * sizeof(float4)) : nullptr;
   float4* slot_tris = (float4*)keep(n * 3 * sizeof(float4));
   float4* shade = (float4*)keep(n * sizeof(float4));
   float* corner = any_normals ? (float*)keep(n * 9 * sizeof(float)) : nullptr;
   float4* ploc_nodes = (float4*)keep(m * sizeof(PNode));
   int32_t* perm_keep = (int32_t*)keep(n * sizeof(int32_t));
-  if ((width == 2 && !bvh) || !slot_tris || !shade ||
+  if ((width == 2 && !bvh) || (hybrid && !bvh_bin) || !slot_tris || !shade ||
       (any_normals && !corner) ||
       !ploc_nodes || !perm_keep)
     return set_err(ctx, AJG_ERR_OOM, "device allocation failed (scene)");
@@ -972,6 +979,11 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
       k_bvh2_single<<<1, 1, 0, st>>>(nodes, bvh);
     }
   } else {
+    if (hybrid) {
+      k_inner_flags<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, flags);
+      device_scan(flags, mi, m, true, scratch, st);
+      k_bvh2<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, mi, bvh_bin);
+    }
     // wide layout: collapse level by level into a worst-case buffer, then
     // keep the nodes made
     const uint64_t node_f4 =
@@ -1063,6 +1075,8 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     return set_err(ctx, AJG_ERR_DEVICE, "device guard tripped in PLOC build");
 
   s->d.bvh = bvh;
+  s->d.bvh_closest = bvh_bin;
+  s->d.num_inner_closest = hybrid ? (uint32_t)inner : 0u;
   s->d.tris = slot_tris;
   s->d.shade = shade;
   s->d.corner = corner;

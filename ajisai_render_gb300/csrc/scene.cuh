@@ -49,7 +49,23 @@ struct DeviceScene {
   const float* emit_pts = nullptr;  // [k][3]
   uint32_t num_area = 0;
   uint32_t mat_mask = 0;  // bit t: a material of type t is present
+  // AJG_HYBRID_CLOSEST builds: the binary layout of the same tree beside
+  // the wide one, for the single-job closest-hit launches (null otherwise)
+  const float4* bvh_closest = nullptr;
+  uint32_t num_inner_closest = 0;
 };
+
+// The scene as the closest-hit launches of a single-job wave see it: the
+// binary layout where the build kept one beside the wide tree.
+inline DeviceScene closest_view(const DeviceScene& s) {
+  DeviceScene c = s;
+  if (s.bvh_closest) {
+    c.bvh = s.bvh_closest;
+    c.num_inner = s.num_inner_closest;
+    c.width = 2;
+  }
+  return c;
+}
 
 // Light record types ([12] floats, type in [0]): the two of the ABI, and the
 // area light of an emissive primitive:
