@@ -88,7 +88,8 @@ class SceneInfo(C.Structure):
     _fields_ = [("num_triangles", C.c_uint64), ("num_nodes", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("ploc_iterations", C.c_uint32),
                 ("build_ms", C.c_float), ("bvh_width", C.c_uint32),
-                ("bvh_node_bytes", C.c_uint32), ("bvh_nodes", C.c_uint64)]
+                ("bvh_node_bytes", C.c_uint32), ("bvh_nodes", C.c_uint64),
+                ("closest_node_bytes", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Stats(C.Structure):

@@ -800,7 +800,8 @@ static int trace_host(ajg_scene* s, const ajg_ray* rays, uint64_t n,
   } else {
     DevBuf<ajg_hit> dh;
     CK(dh.alloc(n, st), "trace: alloc");
-    launch_trace_closest(s->d, dr.p, n, dh.p, ctx->d_fetch, &ctx->d_counters[0],
+    launch_trace_closest(closest_view(s->d), dr.p, n, dh.p, ctx->d_fetch,
+                         &ctx->d_counters[0],
                          ctx->d_error, st);
     CK(cudaMemcpyAsync(out, dh.p, n * sizeof(ajg_hit), cudaMemcpyDeviceToHost, st),
        "trace: copy out");
@@ -831,7 +832,7 @@ int ajg_trace_closest_device(ajg_scene* s, const ajg_ray* d_rays, uint64_t n,
   CK(cudaMemsetAsync(ctx->d_fetch, 0, sizeof(uint32_t), ctx->stream),
      "trace_closest_device");
   KernelTimer tm(ctx, ctx->stream, kKindClosest);
-  launch_trace_closest(s->d, d_rays, n, d_hits, ctx->d_fetch,
+  launch_trace_closest(closest_view(s->d), d_rays, n, d_hits, ctx->d_fetch,
                        &ctx->d_counters[0], ctx->d_error, ctx->stream);
   CK(cudaGetLastError(), "trace_closest_device");
   return AJG_OK;

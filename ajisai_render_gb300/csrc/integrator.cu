@@ -1306,7 +1306,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
   auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
-    launch_wave_extend(true, tri_test, width, s, t, w.ro[q], w.rd[q],
+    launch_wave_extend(true, tri_test, closest_width(width), s, t, w.ro[q], w.rd[q],
                        &w.counts[q], &w.counts[8], hits, ctr, err, es);
   };
   // bounce b+1's closest hits on the trace stream beside bounce b's shadow
@@ -1355,7 +1355,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
     launch_wave_shadow(true, tri_test, width, s, t, w.sq_o, w.sq_d, w.sq_scene,
                        &w.counts[2], &w.counts[3], w.term_vis, ctr + 1, err, st);
     if (emit) {
-      launch_wave_bsdf_trace(true, tri_test, width, s, t, w.sq_o, w.sq_d,
+      launch_wave_bsdf_trace(true, tri_test, closest_width(width), s, t, w.sq_o, w.sq_d,
                              w.sq_scene, &w.counts[9], &w.counts[10], shadow_cap,
                              (uint32_t)P, reinterpret_cast<float*>(w.lists),
                              reinterpret_cast<int32_t*>(w.lists + P), ctr, err,

@@ -813,12 +813,9 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
     return set_err(ctx, AJG_ERR_INVALID,
                    "bvh_width must be 0, 2, 4 or 8 (4 and 8 optionally "
                    "| AJG_BVH_COMPRESSED)");
-#ifndef AJG_HYBRID_CLOSEST
-#define AJG_HYBRID_CLOSEST 0
-#endif
   // the binary layout: the tree itself (width 2), or beside a plain 4-wide
-  // tree for the closest-hit launches (AJG_HYBRID_CLOSEST)
-  const bool hybrid = AJG_HYBRID_CLOSEST && width == 4 && n > 1;
+  // tree for the closest-hit traversal (closest_width)
+  const bool hybrid = closest_width(width) != width;
   float4* bvh =
       width == 2 ? (float4*)keep(inner * 4 * sizeof(float4)) : nullptr;
   float4* bvh_bin = hybrid ? (float4*)keep(inner * 4 * sizeof(float4)) : nullptr;
@@ -979,10 +976,12 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
       k_bvh2_single<<<1, 1, 0, st>>>(nodes, bvh);
     }
   } else {
-    if (hybrid) {
+    if (hybrid && n > 1) {
       k_inner_flags<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, flags);
       device_scan(flags, mi, m, true, scratch, st);
       k_bvh2<<<grid_for(m, 256), 256, 0, st>>>(nodes, m, mi, bvh_bin);
+    } else if (hybrid) {
+      k_bvh2_single<<<1, 1, 0, st>>>(nodes, bvh_bin);
     }
     // wide layout: collapse level by level into a worst-case buffer, then
     // keep the nodes made
@@ -1077,6 +1076,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   s->d.bvh = bvh;
   s->d.bvh_closest = bvh_bin;
   s->d.num_inner_closest = hybrid ? (uint32_t)inner : 0u;
+  s->info.closest_node_bytes = 0;  // set with bvh_node_bytes below
   s->d.tris = slot_tris;
   s->d.shade = shade;
   s->d.corner = corner;
@@ -1097,6 +1097,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
                                                 : CwLayout<4>::kFloat4)
                                : 32u * (uint32_t)wn);
   s->info.bvh_nodes = num_nodes;
+  s->info.closest_node_bytes = hybrid ? 64u : s->info.bvh_node_bytes;
   for (int k = 0; k < 6; ++k) s->world[k] = world[k];
   // lights are fitted to the world bounds (default_scene.cpp:41-48)
   const F3 center = (whi + wlo) / 2.f;

@@ -49,14 +49,29 @@ struct DeviceScene {
   const float* emit_pts = nullptr;  // [k][3]
   uint32_t num_area = 0;
   uint32_t mat_mask = 0;  // bit t: a material of type t is present
-  // AJG_HYBRID_CLOSEST builds: the binary layout of the same tree beside
-  // the wide one, for the single-job closest-hit launches (null otherwise)
+  // the binary layout of the same tree kept beside a plain 4-wide one for
+  // the closest-hit traversal (null for other layouts and with
+  // AJG_HYBRID_CLOSEST=0)
   const float4* bvh_closest = nullptr;
   uint32_t num_inner_closest = 0;
 };
 
-// The scene as the closest-hit launches of a single-job wave see it: the
-// binary layout where the build kept one beside the wide tree.
+// Closest-hit rays walk the binary layout of the tree, any-hit rays the
+// 4-wide one, when the scene keeps both (the default for the 4-wide tree):
+// measured on the single-job workload, closest-hit traversal is faster over
+// the binary nodes (nearest child first, tighter culling by the current
+// hit) and any-hit traversal over the wide ones.
+#ifndef AJG_HYBRID_CLOSEST
+#define AJG_HYBRID_CLOSEST 1
+#endif
+constexpr bool kHybridClosest = AJG_HYBRID_CLOSEST != 0;
+// The layout closest-hit launches use for scenes of layout `width`.
+inline int closest_width(int width) {
+  return kHybridClosest && width == 4 ? 2 : width;
+}
+
+// The scene as the closest-hit launches see it: the binary layout where
+// the build kept one beside the wide tree.
 inline DeviceScene closest_view(const DeviceScene& s) {
   DeviceScene c = s;
   if (s.bvh_closest) {

@@ -32,7 +32,7 @@ static_assert(sizeof(ajg_job_desc) == 224, "ajg_job_desc layout");
 static_assert(sizeof(ajg_job_status) == 56, "ajg_job_status layout");
 static_assert(sizeof(ajg_serve_opts) == 16, "ajg_serve_opts layout");
 static_assert(sizeof(ajg_serve_stats) == 88, "ajg_serve_stats layout");
-static_assert(sizeof(ajg_scene_info) == 48, "ajg_scene_info layout");
+static_assert(sizeof(ajg_scene_info) == 56, "ajg_scene_info layout");
 static_assert(sizeof(ajg_emitter) == 32, "ajg_emitter layout");
 static_assert(sizeof(ajg_sppm_params) == 40, "ajg_sppm_params layout");
 

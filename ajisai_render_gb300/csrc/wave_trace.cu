@@ -12,12 +12,20 @@ namespace {
 
 constexpr int kTraceThreads = 128;
 
+// The tree of the ray's scene; closest-hit kernels of the binary layout
+// (W = 2) take the binary tree a 4-wide scene keeps beside its wide one.
+template <int W>
 __device__ __forceinline__ void retarget(TraceScene& ts, const MJTables& t,
                                          uint32_t sid) {
   const DeviceScene& sc = t.scenes[mj_scene(t, sid)];
-  ts.bvh = sc.bvh;
+  if (W == 2 && sc.bvh_closest) {
+    ts.bvh = sc.bvh_closest;
+    ts.max_visits = sc.num_inner_closest + 1;
+  } else {
+    ts.bvh = sc.bvh;
+    ts.max_visits = sc.num_inner + 1;
+  }
   ts.tris = sc.tris;
-  ts.max_visits = sc.num_inner + 1;
 }
 
 // Closest hits of the path queue.
@@ -31,7 +39,7 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
   uint32_t nn = 0, nt = 0, nr = 0;
   auto fetch = [&](uint32_t k, TraceScene& ts) {
     const float4 o = ro[k], d = rd[k];
-    if constexpr (MJ) retarget(ts, t, __float_as_uint(o.w));
+    if constexpr (MJ) retarget<W>(ts, t, __float_as_uint(o.w));
     return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
   };
   auto finish = [&](uint32_t k, const Hit& h, bool) {
@@ -62,7 +70,7 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
   auto fetch = [&](uint32_t k, TraceScene& ts) {
     cur = perm ? perm[k] : k;
     const float4 o = sq_o[cur], d = sq_d[cur];
-    if constexpr (MJ) retarget(ts, t, sq_scene[cur]);
+    if constexpr (MJ) retarget<W>(ts, t, sq_scene[cur]);
     return make_query(xyz(o), xyz(d), kRayEps, o.w);
   };
   auto finish = [&](uint32_t, const Hit&, bool occ) {
@@ -91,7 +99,7 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
   auto fetch = [&](uint32_t k, TraceScene& ts) {
     const uint32_t i = cap - 1 - k;
     const float4 o = sq_o[i], d = sq_d[i];
-    if constexpr (MJ) retarget(ts, t, sq_scene[i]);
+    if constexpr (MJ) retarget<W>(ts, t, sq_scene[i]);
     return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
   };
   auto finish = [&](uint32_t k, const Hit& h, bool) {

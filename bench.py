@@ -360,7 +360,8 @@ def run_ours(args):
     dom = max(kinds, key=lambda k: st[kinds[k][0]])
     ms_k, l_k, n_k, t_k, kname = kinds[dom]
     launches = max(1, st[l_k])
-    node_bytes = scene.info()["bvh_node_bytes"]
+    # closest-hit rays walk the binary layout kept beside a 4-wide tree
+    node_bytes = scene.info()["closest_node_bytes" if dom == "closest" else "bvh_node_bytes"]
     bytes_per_launch = (st[n_k] * node_bytes + st[t_k] * TRI_BYTES) / launches
     avg_ms = st[ms_k] / launches
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None

@@ -225,6 +225,10 @@ typedef struct ajg_scene_info {
   uint32_t bvh_width;      /* node width of the traversal tree */
   uint32_t bvh_node_bytes; /* bytes per traversal node */
   uint64_t bvh_nodes;      /* traversal nodes */
+  uint32_t closest_node_bytes; /* bytes per node of the tree the closest-hit
+                                  traversal walks: the binary layout (64)
+                                  beside a plain 4-wide tree, else as above */
+  uint32_t reserved;
 } ajg_scene_info;
 
 typedef struct ajg_stats {

@@ -87,7 +87,7 @@ def test_serving_structs_match_header(lib):
     assert C.sizeof(_lib.JobStatus) == 24 + 32
     assert C.sizeof(_lib.ServeOpts) == 16
     assert C.sizeof(_lib.ServeStats) == 88
-    assert C.sizeof(_lib.SceneInfo) == 48
+    assert C.sizeof(_lib.SceneInfo) == 56
 
 
 def test_context_creation_reports_missing_device(lib):
