@@ -652,12 +652,13 @@ int sppm_render(ajg_scene* sc, const ajg_camera& cam, const ajg_sppm_params& p,
       for (int depth = 1; depth <= p.photon_max_depth; ++depth) {
         cudaMemsetAsync(&q.counts[cur ^ 1], 0, sizeof(uint32_t), st);
         cudaMemsetAsync(&q.counts[2], 0, sizeof(uint32_t), st);
-        const DeviceScene sc = closest_view(s);
-        dispatch_trace(sc.tri_test, sc.width, [&](auto T, auto Wd) {
+        // photon rays keep the wide tree: over the binary layout the
+        // photon pass measured 8% slower (long rays from the lights)
+        dispatch_trace(s.tri_test, s.width, [&](auto T, auto Wd) {
           constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
           const int gr = resident_grid((const void*)k_photon_extend<TT, WW>, 128);
           k_photon_extend<TT, WW><<<gr, 128, 0, st>>>(
-              sc, q.ro[cur], q.rd[cur], &q.counts[cur], &q.counts[2], q.hits,
+              s, q.ro[cur], q.rd[cur], &q.counts[cur], &q.counts[2], q.hits,
               &ctx->d_counters[0], ctx->d_error);
         });
         k_photon_shade<<<gs, kThreads, 0, st>>>(a, px, g, q, cur, depth,
