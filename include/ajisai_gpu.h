@@ -169,7 +169,11 @@ typedef struct ajg_scene_opts {
                              quantised child boxes (same hits: the traversal
                              result does not depend on the tree and the
                              quantised boxes enclose the exact ones); 0: the
-                             library's default, 4 */
+                             library's default, 4.  With the plain 4-wide
+                             tree the binary layout is kept beside it and
+                             closest-hit rays walk that one (the faster
+                             closest-hit tree; any-hit and photon rays keep
+                             the 4-wide one) */
 } ajg_scene_opts;
 
 /* Thin-lens camera: the two matrices ThinLensCamera keeps
