@@ -501,6 +501,13 @@ def run_ours(args):
             # load point below saturation (its offered load beside it)
             "p99_job_latency_ms": served["p99_ms"] if served else None,
             "p99_at_offered_load": served["latency_at_load"] if served else None,
+            # the metric's comparison: batched / served throughput over the
+            # plain single-job tracer on the same mixes (films bit-identical)
+            "batched_vs_plain": batched["speedup_vs_plain"] if batched else None,
+            "small_jobs_batched_vs_plain": (batched["small_jobs"]["speedup_vs_plain"]
+                                            if batched else None),
+            "served_vs_plain_at_saturation": (served["saturated_vs_plain"]
+                                              if served else None),
             "cornell": cornell, "batched": batched, "served": served, "large": large,
             "sppm": sppm, "impl": "ours"}))
     scene.release()
