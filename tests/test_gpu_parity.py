@@ -471,6 +471,39 @@ def test_trace_counters(ctx):
     assert st["closest_rays"] == 1000 and st["closest_nodes"] >= 1000
 
 
+def test_launch_log_matches_the_counters():
+    """Profiling on: one record per traversal and shading launch, in order,
+    whose per-launch rays, nodes and triangles add up to the counters; the
+    closest-hit tree of the default 4-wide scene is the binary layout kept
+    beside it (64-byte nodes)."""
+    c = api.Context(0)
+    flat = S.flatten(S.icosphere_scene(4, 1, 48, 40))
+    sc = api.GpuScene(c, flat, api.CreatePLOCAggregate(16))
+    info = sc.info()
+    assert info["bvh_width"] == 4 and info["bvh_node_bytes"] == 128
+    assert info["closest_node_bytes"] == 64
+    r = api.PTRenderer(api.PTRendererArgs(spp=4, min_bounces=2, max_bounces=6), seed=3)
+    r.Render(sc, flat.camera)
+    c.stats(reset=True)
+    c.launch_log(reset=True)
+    c.set_profiling(True)
+    r.Render(sc, flat.camera)
+    log = c.launch_log(reset=True)
+    st = c.stats()
+    c.set_profiling(False)
+    for kind in ("closest", "any"):
+        recs = [x for x in log if x["kind"] == kind]
+        assert len(recs) == st[f"{kind}_launches"] >= 6
+        assert sum(x["rays"] for x in recs) == st[f"{kind}_rays"]
+        assert sum(x["nodes"] for x in recs) == st[f"{kind}_nodes"]
+        assert sum(x["tris"] for x in recs) == st[f"{kind}_tris"]
+        assert all(x["ms"] > 0 for x in recs)
+    assert log[0]["kind"] == "closest" and log[0]["rays"] == 48 * 40 * 4
+    assert c.launch_log() == []
+    sc.release()
+    c.close()
+
+
 # ------------------------------------------------------------ area lights --
 def _area_no_mesh(w, h):
     """cornell_area without its emissive mesh (whose straddling sampler

@@ -124,6 +124,17 @@ def test_batch_equals_alone(ctx, scenes, policy, wave):
     ctx.configure_serving("fair")
 
 
+def test_serve_stats_count_wave_device_time(ctx, scenes):
+    """The request loop sums each retired wave's device time."""
+    before = ctx.serve_stats()
+    sc, cam, r = scenes["box"][0], scenes["box"][1], api.PTRenderer(
+        api.PTRendererArgs(spp=4, min_bounces=2, max_bounces=6), seed=2)
+    ctx.render_batch([(sc, cam, r)])
+    after = ctx.serve_stats()
+    assert after["waves"] > before["waves"]
+    assert after["busy_ms"] > before["busy_ms"]
+
+
 def test_batch_of_many_small_jobs_shares_waves(ctx, scenes):
     """Forty jobs small enough to share waves."""
     rng = np.random.default_rng(1)
