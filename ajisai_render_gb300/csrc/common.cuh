@@ -193,42 +193,6 @@ __device__ __forceinline__ uint32_t block_append(uint32_t* counters,
   return cls >= 0 ? s_base[cls][warp] + rank : 0xffffffffu;
 }
 
-// Stream compaction of a whole block into one queue with the block's items
-// grouped by bin: each thread passes its item's bin in [0, NB) (-1: none)
-// and gets its slot; the block takes one range of the queue (one atomicAdd)
-// in which bin 0's items come first, then bin 1's, ..., each bin's in
-// thread order.  Every thread of the block must call it.
-template <int NB, int NW>
-__device__ __forceinline__ uint32_t block_append_binned(uint32_t* counter,
-                                                        int bin) {
-  __shared__ uint32_t s_cnt[NB][NW];
-  __shared__ uint32_t s_base;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  uint32_t rank = 0;
-#pragma unroll
-  for (int c = 0; c < NB; ++c) {
-    const unsigned b = __ballot_sync(0xffffffffu, bin == c);
-    if (lane == 0) s_cnt[c][warp] = (uint32_t)__popc(b);
-    if (bin == c) rank = (uint32_t)__popc(b & lt);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t tot = 0;
-    for (int c = 0; c < NB; ++c)
-      for (int v = 0; v < NW; ++v) {
-        const uint32_t x = s_cnt[c][v];
-        s_cnt[c][v] = tot;
-        tot += x;
-      }
-    s_base = tot ? atomicAdd(counter, tot) : 0u;
-  }
-  __syncthreads();
-  const uint32_t slot = bin >= 0 ? s_base + s_cnt[bin][warp] + rank : 0xffffffffu;
-  __syncthreads();  // s_cnt is reused by the next call
-  return slot;
-}
-
 // Maximum of v over the block (every thread must call it).
 template <int NW>
 __device__ __forceinline__ uint32_t block_max(uint32_t v) {

@@ -31,7 +31,6 @@
 #include <mutex>
 #include <string>
 
-#include "scan.cuh"
 #include "shade.cuh"
 #include "trace.cuh"
 
@@ -316,24 +315,12 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
-// AJG_SHADOW_OCTANT: a block's shadow rays of one light term are queued
-// grouped by the octant of their direction (a warp of the traversal then
-// takes rays of one octant).
-#ifndef AJG_SHADOW_OCTANT
-#define AJG_SHADOW_OCTANT 0
-#endif
 template <bool MJ>
 __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
                                             uint32_t sid, bool pred,
                                             uint32_t cap, uint32_t* err) {
-#if AJG_SHADOW_OCTANT && AJG_BLOCK_APPEND
-  const int oct = (d.x < 0.f ? 1 : 0) | (d.y < 0.f ? 2 : 0) | (d.z < 0.f ? 4 : 0);
-  const uint32_t k = block_append_binned<8, kShadeThreads / 32>(&w.counts[2],
-                                                                pred ? oct : -1);
-#else
   const uint32_t k = shade_append(&w.counts[2], pred);
-#endif
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -363,87 +350,6 @@ __device__ __forceinline__ void emit_closest(const WaveBufs& w, F3 o, F3 d,
   w.sq_o[i] = make_float4(o.x, o.y, o.z, pdf);
   w.sq_d[i] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
   if constexpr (MJ) w.sq_scene[i] = (uint16_t)sid;
-}
-
-// Shadow rays grouped by direction (AJG_SHADOW_BINS > 0): the any-hit
-// traversal takes the queue through a permutation that lists the rays bin
-// by bin -- an octahedral grid of kSBinSide^2 direction cells -- and, within
-// a bin, tile by tile of the queue (kSBinTile rays), so that a warp's rays
-// run in similar directions from nearby origins (the queue is in path order,
-// and paths are in pixel order).  The rays themselves stay where they are.
-#ifndef AJG_SHADOW_BINS
-#define AJG_SHADOW_BINS 0
-#endif
-#ifndef AJG_SBIN_SIDE
-#define AJG_SBIN_SIDE 8
-#endif
-#ifndef AJG_SBIN_TILE
-#define AJG_SBIN_TILE 8192
-#endif
-constexpr int kSBinSide = AJG_SBIN_SIDE;
-constexpr int kSBins = kSBinSide * kSBinSide;
-constexpr int kSBinTile = AJG_SBIN_TILE;
-constexpr int kSBinThreads = 256;
-
-__device__ __forceinline__ int shadow_bin(float4 d) {
-  const float a = fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
-  float u = d.x / a, v = d.y / a;
-  if (d.z < 0.f) {  // fold the lower hemisphere over the diagonals
-    const float fu = (1.f - fabsf(v)) * (u >= 0.f ? 1.f : -1.f);
-    const float fv = (1.f - fabsf(u)) * (v >= 0.f ? 1.f : -1.f);
-    u = fu;
-    v = fv;
-  }
-  const int iu = min(kSBinSide - 1, max(0, (int)((u * 0.5f + 0.5f) * kSBinSide)));
-  const int iv = min(kSBinSide - 1, max(0, (int)((v * 0.5f + 0.5f) * kSBinSide)));
-  return iv * kSBinSide + iu;
-}
-
-// hist[bin * n_tiles + tile]: the tile's rays in the bin (0 past the queue)
-__global__ void __launch_bounds__(kSBinThreads)
-    k_sbin_count(const float4* __restrict__ sq_d,
-                 const uint32_t* __restrict__ count, uint32_t* __restrict__ hist,
-                 uint32_t n_tiles) {
-  __shared__ uint32_t h[kSBins];
-  const uint32_t n = *count;
-  for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    for (int b = threadIdx.x; b < kSBins; b += blockDim.x) h[b] = 0;
-    __syncthreads();
-    const uint64_t lo = (uint64_t)tile * kSBinTile;
-    for (uint64_t i = lo + threadIdx.x; i < lo + kSBinTile && i < n;
-         i += blockDim.x)
-      atomicAdd(&h[shadow_bin(sq_d[i])], 1u);
-    __syncthreads();
-    for (int b = threadIdx.x; b < kSBins; b += blockDim.x)
-      hist[(uint64_t)b * n_tiles + tile] = h[b];
-    __syncthreads();
-  }
-}
-
-// perm[offs[bin * n_tiles + tile] + rank] = ray (offs: the exclusive scan
-// of hist)
-__global__ void __launch_bounds__(kSBinThreads)
-    k_sbin_scatter(const float4* __restrict__ sq_d,
-                   const uint32_t* __restrict__ count,
-                   const uint32_t* __restrict__ offs, uint32_t n_tiles,
-                   uint32_t* __restrict__ perm) {
-  __shared__ uint32_t base[kSBins];
-  const uint32_t n = *count;
-  for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    const uint64_t lo = (uint64_t)tile * kSBinTile;
-    if (lo >= n) break;
-    for (int b = threadIdx.x; b < kSBins; b += blockDim.x)
-      base[b] = offs[(uint64_t)b * n_tiles + tile];
-    __syncthreads();
-    for (uint64_t i = lo + threadIdx.x; i < lo + kSBinTile && i < n;
-         i += blockDim.x)
-      perm[atomicAdd(&base[shadow_bin(sq_d[i])], 1u)] = (uint32_t)i;
-    __syncthreads();
-  }
-}
-
-uint32_t sbin_tiles(uint64_t cap) {
-  return (uint32_t)((cap + kSBinTile - 1) / kSBinTile);
 }
 
 // Escaped paths: the environment counts only for camera rays
@@ -994,12 +900,6 @@ uint64_t wave_bytes(uint64_t P, int nt, bool mj) {
   if (mj) add(slots * 2);      // sq_scene
   add(P * 4 * 4);              // shading-class lists
   add(64);                     // counts
-  if (AJG_SHADOW_BINS) {
-    const uint64_t hist = (uint64_t)kSBins * sbin_tiles(slots);
-    add(slots * 4);                             // sq_perm
-    add(hist * 4);                              // sbin_hist
-    add(scan_scratch_words(hist) * 4);          // scan scratch
-  }
   return b;
 }
 
@@ -1028,12 +928,6 @@ WaveBufs carve_wave(char* base, uint64_t P, int nt, bool mj) {
   if (mj) w.sq_scene = carve<uint16_t>(cur, P * nt);
   w.lists = carve<uint32_t>(cur, P * 4);
   w.counts = carve<uint32_t>(cur, 16);
-  if (AJG_SHADOW_BINS) {
-    const uint64_t hist = (uint64_t)kSBins * sbin_tiles(P * nt);
-    w.sq_perm = carve<uint32_t>(cur, P * nt);
-    w.sbin_hist = carve<uint32_t>(cur, hist);
-    w.sbin_scratch = carve<uint32_t>(cur, scan_scratch_words(hist));
-  }
   return w;
 }
 
@@ -1176,19 +1070,9 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
                            &ctx->d_counters[0], ctx->d_error, st);
   };
   auto shadow = [&]() {
-    if (w.sq_perm) {
-      const uint32_t tiles = sbin_tiles((uint64_t)shadow_cap);
-      const uint64_t hist = (uint64_t)kSBins * tiles;
-      const int g = (int)std::min<uint32_t>(tiles, (uint32_t)kSMs * 8);
-      k_sbin_count<<<g, kSBinThreads, 0, st>>>(w.sq_d, &w.counts[2], w.sbin_hist,
-                                               tiles);
-      device_scan(w.sbin_hist, w.sbin_hist, hist, true, w.sbin_scratch, st);
-      k_sbin_scatter<<<g, kSBinThreads, 0, st>>>(w.sq_d, &w.counts[2], w.sbin_hist,
-                                                 tiles, w.sq_perm);
-    }
     launch_wave_shadow(false, s.tri_test, s.width, s, t, w.sq_o, w.sq_d, nullptr,
                        &w.counts[2], &w.counts[3], w.term_vis,
-                       &ctx->d_counters[1], ctx->d_error, st, w.sq_perm);
+                       &ctx->d_counters[1], ctx->d_error, st);
   };
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);

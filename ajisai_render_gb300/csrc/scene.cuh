@@ -173,12 +173,6 @@ struct WaveBufs {
   uint32_t* counts;  // [0],[1] path queues, [2] shadow queue, [3] shadow
                      // fetch, [4..7] lists, [8] extend fetch, [9] closest
                      // MIS BSDF queue, [10] its fetch
-  // shadow rays grouped by direction before the any-hit traversal (null
-  // unless built with AJG_SHADOW_BINS): the order the traversal takes the
-  // queue in, the per-(bin, tile) counts and their scan's scratch
-  uint32_t* sq_perm;
-  uint32_t* sbin_hist;
-  uint32_t* sbin_scratch;
 };
 
 // Tables of a multi-job wave in device memory.
@@ -402,7 +396,7 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
                         const float4* sq_d, const uint16_t* sq_scene,
                         const uint32_t* count, uint32_t* fetch_next,
                         uint8_t* vis, TraceCounters* ctr, uint32_t* err,
-                        cudaStream_t st, const uint32_t* perm = nullptr);
+                        cudaStream_t st);
 void launch_wave_bsdf_trace(bool mj, int tri_test, int width,
                             const DeviceScene& s, const MJTables& t,
                             const float4* sq_o, const float4* sq_d,

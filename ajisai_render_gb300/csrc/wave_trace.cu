@@ -61,14 +61,13 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
              const float4* __restrict__ sq_d,
              const uint16_t* __restrict__ sq_scene,
              const uint32_t* __restrict__ count, uint32_t* fetch_next,
-             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err,
-             const uint32_t* __restrict__ perm) {
+             uint8_t* __restrict__ vis, TraceCounters* ctr, uint32_t* err) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
   // the queue entry of the lane's current ray (a lane traces one at a time)
   uint32_t cur = 0;
   auto fetch = [&](uint32_t k, TraceScene& ts) {
-    cur = perm ? perm[k] : k;
+    cur = k;
     const float4 o = sq_o[cur], d = sq_d[cur];
     if constexpr (MJ) retarget<W>(ts, t, sq_scene[cur]);
     return make_query(xyz(o), xyz(d), kRayEps, o.w);
@@ -137,17 +136,17 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
                         const float4* sq_d, const uint16_t* sq_scene,
                         const uint32_t* count, uint32_t* fetch_next,
                         uint8_t* vis, TraceCounters* ctr, uint32_t* err,
-                        cudaStream_t st, const uint32_t* perm) {
+                        cudaStream_t st) {
   dispatch_trace(tri_test, width, [&](auto T, auto Wd) {
     constexpr int TT = decltype(T)::value, WW = decltype(Wd)::value;
     if (mj) {
       const int g = resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
       k_shadow<TT, true, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err, perm);
+          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err);
     } else {
       const int g = resident_grid((const void*)k_shadow<TT, false, WW>, kTraceThreads);
       k_shadow<TT, false, WW><<<g, kTraceThreads, 0, st>>>(
-          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err, perm);
+          s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err);
     }
   });
 }
