@@ -206,9 +206,9 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 
 // Persistent-lane traversal.  Each lane owns one ray at a time and runs one
 // node visit per loop iteration; lanes whose ray finished take new rays from
-// a shared counter (warp-aggregated, once at least kRefill lanes of the warp
-// are idle), so lanes are not left idle at ray boundaries waiting for the
-// warp's slowest ray.  FETCH(k, ts) returns the k-th ray; FINISH(k, hit,
+// a shared counter (warp-aggregated, once at least AJG_REFILL (closest hit)
+// or AJG_REFILL_ANY (any hit) lanes of the warp are idle), so lanes are not
+// left idle at ray boundaries waiting for the warp's slowest ray.  FETCH(k, ts) returns the k-th ray; FINISH(k, hit,
 // occluded) stores its result.
 //
 // L is the tree layout: 2 is the binary PLOC tree (64-byte nodes holding
@@ -221,7 +221,7 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 // closest hits the nearest interior child is visited next and the others
 // are pushed farthest first.
 #ifndef AJG_REFILL
-#define AJG_REFILL 16
+#define AJG_REFILL 24  // closest-hit queries
 #endif
 // Blocks of 128 threads per SM the traversal kernels over 2- and 4-wide
 // trees are compiled for: 8 caps them at 64 registers, which they fit without
@@ -248,7 +248,7 @@ constexpr int trace_min_blocks() {
 #define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
 #ifndef AJG_REFILL_ANY
-#define AJG_REFILL_ANY AJG_REFILL  // the same threshold for any-hit queries
+#define AJG_REFILL_ANY 16  // any-hit queries
 #endif
 constexpr int kRefill = AJG_REFILL;
 constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
