@@ -229,9 +229,14 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris,
 #ifndef AJG_TRACE_MIN_BLOCKS
 #define AJG_TRACE_MIN_BLOCKS 8
 #endif
+#ifndef AJG_TRACE_MIN_BLOCKS_BIN
+#define AJG_TRACE_MIN_BLOCKS_BIN AJG_TRACE_MIN_BLOCKS  // the binary layout
+#endif
 template <int L>
 constexpr int trace_min_blocks() {
-  return (L & ~kBvhCompressed) == 8 ? 1 : AJG_TRACE_MIN_BLOCKS;
+  return (L & ~kBvhCompressed) == 8 ? 1
+         : L == 2                   ? AJG_TRACE_MIN_BLOCKS_BIN
+                                    : AJG_TRACE_MIN_BLOCKS;
 }
 #ifndef AJG_SMEM_STACK
 #define AJG_SMEM_STACK 16  // stack entries per lane in shared memory (a power
