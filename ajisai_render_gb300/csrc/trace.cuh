@@ -255,6 +255,10 @@ constexpr int trace_min_blocks() {
 #ifndef AJG_REFILL_ANY
 #define AJG_REFILL_ANY 16  // any-hit queries
 #endif
+#ifndef AJG_OCC_CACHE
+#define AJG_OCC_CACHE 0  // 1: any-hit lanes first test the triangle that
+                         // occluded their previous ray
+#endif
 constexpr int kRefill = AJG_REFILL;
 constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
 
@@ -275,6 +279,23 @@ __device__ __forceinline__ void trace_persistent(
   Hit hit;
   int node = 0, sp = 0;
   uint32_t visits = 0;
+  // Any-hit queries: the leaf slot (and tree) of the triangle that occluded
+  // the lane's previous ray.  Neighbouring queue entries are rays of one
+  // pixel toward one light, so that triangle often occludes the next ray as
+  // well; a hit on it is an occlusion the traversal would report too (the
+  // box tests are conservative), so the answer does not change.
+  int occ = -1;
+  const float4* occ_tris = nullptr;
+  auto leaf = [&](const float4* __restrict__ tp, int slot) {
+    const bool f = leaf_test<TEST, ANY>(tp, slot, r, w, hit);
+    if constexpr (ANY && AJG_OCC_CACHE) {
+      if (f) {
+        occ = slot;
+        occ_tris = tp;
+      }
+    }
+    return f;
+  };
   int stack_node[kStack];
   float stack_t[kStack];
 #if AJG_SMEM_STACK > 0
@@ -353,6 +374,16 @@ __device__ __forceinline__ void trace_persistent(
           node = 0;
           sp = 0;
           visits = 0;
+          if constexpr (ANY && AJG_OCC_CACHE) {
+            if (occ >= 0 && occ_tris == ts.tris) {
+              ++n_tris;
+              if (leaf_test<TEST, ANY>(ts.tris, occ, r, w, hit)) {
+                ++n_rays;
+                finish(kk, hit, true);
+                k = kIdle;
+              }
+            }
+          }
         } else {
           k = kDone;
         }
@@ -388,7 +419,7 @@ __device__ __forceinline__ void trace_persistent(
         const int rc = c == 0 ? r0 : r1;
         if (hc && rc < 0 && !finished) {
           ++n_tris;
-          finished = leaf_test<TEST, ANY>(tris, ~rc, r, w, hit);
+          finished = leaf(tris, ~rc);
         }
         if (hc && rc < 0) {
           if (c == 0)
@@ -459,7 +490,7 @@ __device__ __forceinline__ void trace_persistent(
 #else
             if (h && ref[c] < 0 && !finished) {
               ++n_tris;
-              finished = leaf_test<TEST, ANY>(tris, ~ref[c], r, w, hit);
+              finished = leaf(tris, ~ref[c]);
             }
 #endif
             if (h && ref[c] >= 0) inner |= 1u << c;
@@ -516,8 +547,7 @@ __device__ __forceinline__ void trace_persistent(
 #else
             if (!finished) {
               ++n_tris;
-              finished = leaf_test<TEST, ANY>(
-                  tris, (int)(tbase + __popc(lmask & below)), r, w, hit);
+              finished = leaf(tris, (int)(tbase + __popc(lmask & below)));
             }
 #endif
           }
@@ -530,7 +560,7 @@ __device__ __forceinline__ void trace_persistent(
 #pragma unroll
         for (int j = 0; j < W; ++j)
           if (j == i) slot = leaf_slot[j];
-        finished = leaf_test<TEST, ANY>(tris, slot, r, w, hit);
+        finished = leaf(tris, slot);
       }
 #endif
       if (!finished && inner && ANY) {
