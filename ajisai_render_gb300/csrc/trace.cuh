@@ -13,7 +13,11 @@
 // ray finished takes the next from a shared counter.  Closest-hit rays visit
 // the nearest interior child and push the others farthest first; any-hit
 // rays take the children in order; a wide node's passing leaf children are
-// tested after its box tests.  Each lane's stack keeps its top 16 entries
+// tested after its box tests, or -- any-hit rays over the plain wide tree --
+// held until the warp's next leaf pass, in which every lane holding some
+// tests one (the lanes that found leaves in a visit are a few of the 32, and
+// the pass gathers their tests into fewer warp instructions).  Each lane's
+// stack keeps its top 16 entries
 // in a shared-memory ring and the rest in local memory, and is guarded:
 // overflow sets the device error word and ends the ray.
 #pragma once
@@ -253,11 +257,17 @@ constexpr int trace_min_blocks() {
 #define AJG_LEAF_BATCH 1  // 0: test each leaf child at its own call site
 #endif
 #ifndef AJG_REFILL_ANY
-#define AJG_REFILL_ANY 16  // any-hit queries
+#define AJG_REFILL_ANY 12  // any-hit queries
 #endif
-#ifndef AJG_OCC_CACHE
-#define AJG_OCC_CACHE 0  // 1: any-hit lanes first test the triangle that
-                         // occluded their previous ray
+#ifndef AJG_LEAF_DEFER
+#define AJG_LEAF_DEFER 6  // any-hit queries over a plain wide tree: lanes
+                          // keep a node's leaf children pending, and the warp
+                          // tests pending leaves together once this many
+                          // lanes hold some (0: each visit tests its leaves)
+#endif
+#ifndef AJG_LEAF_DEFER_CLOSEST
+#define AJG_LEAF_DEFER_CLOSEST 0  // the same for closest-hit queries over
+                                  // the binary layout
 #endif
 constexpr int kRefill = AJG_REFILL;
 constexpr int kEmptyRef = (int)0x80000000;  // unused child of a wide node
@@ -279,23 +289,19 @@ __device__ __forceinline__ void trace_persistent(
   Hit hit;
   int node = 0, sp = 0;
   uint32_t visits = 0;
-  // Any-hit queries: the leaf slot (and tree) of the triangle that occluded
-  // the lane's previous ray.  Neighbouring queue entries are rays of one
-  // pixel toward one light, so that triangle often occludes the next ray as
-  // well; a hit on it is an occlusion the traversal would report too (the
-  // box tests are conservative), so the answer does not change.
-  int occ = -1;
-  const float4* occ_tris = nullptr;
-  auto leaf = [&](const float4* __restrict__ tp, int slot) {
-    const bool f = leaf_test<TEST, ANY>(tp, slot, r, w, hit);
-    if constexpr (ANY && AJG_OCC_CACHE) {
-      if (f) {
-        occ = slot;
-        occ_tris = tp;
-      }
-    }
-    return f;
-  };
+  // Deferred leaves: a node visit records its leaf children (mask `pend`,
+  // slots pend_slot[child]) instead of testing them, and a lane holding
+  // pending leaves visits no node (nor pops one) until the warp's next leaf
+  // pass.  That pass comes once kLeafPass lanes (or all active ones) hold
+  // some; each of them tests one, and a lane whose leaves are done pops its
+  // next node against the hit they left.  Every node is visited with the
+  // same hit as without deferral, so the visits and the result are the
+  // same: only the grouping of the leaf tests into warp instructions moves.
+  constexpr int kLeafPass = ANY ? ((!CMP && W >= 4) ? AJG_LEAF_DEFER : 0)
+                                : (W == 2 ? AJG_LEAF_DEFER_CLOSEST : 0);
+  constexpr bool kDefer = kLeafPass > 0;
+  unsigned pend = 0;
+  int pend_slot[W];
   int stack_node[kStack];
   float stack_t[kStack];
 #if AJG_SMEM_STACK > 0
@@ -374,22 +380,52 @@ __device__ __forceinline__ void trace_persistent(
           node = 0;
           sp = 0;
           visits = 0;
-          if constexpr (ANY && AJG_OCC_CACHE) {
-            if (occ >= 0 && occ_tris == ts.tris) {
-              ++n_tris;
-              if (leaf_test<TEST, ANY>(ts.tris, occ, r, w, hit)) {
-                ++n_rays;
-                finish(kk, hit, true);
-                k = kIdle;
-              }
-            }
-          }
         } else {
           k = kDone;
         }
       }
     }
     if (__all_sync(full, k == kDone)) break;
+    if constexpr (kDefer) {
+      const bool act = k >= 0 && k != kDone;
+      const unsigned pm = __ballot_sync(full, act && pend != 0);
+      const unsigned am = __ballot_sync(full, act);
+      if (pm && (__popc(pm) >= kLeafPass || pm == am)) {
+        // the leaf pass
+        if (pend) {
+          const int c = __ffs(pend) - 1;
+          pend &= pend - 1;
+          int slot = 0;
+#pragma unroll
+          for (int j = 0; j < W; ++j)
+            if (j == c) slot = pend_slot[j];
+          ++n_tris;
+          bool fin = leaf_test<TEST, ANY>(ts.tris, slot, r, w, hit);
+          if (!fin && !pend && node < 0) {
+            // the visit's deferred pop
+            fin = true;
+            while (sp > 0) {
+              int nd;
+              float st;
+              pop(nd, st);
+              if (st <= (ANY ? r.tmax : fminf(hit.t, r.tmax))) {
+                node = nd;
+                fin = false;
+                break;
+              }
+            }
+          }
+          if (fin) {
+            pend = 0;
+            ++n_rays;
+            finish((uint32_t)k, hit, hit.prim >= 0);
+            k = kIdle;
+          }
+        }
+        continue;
+      }
+      if (pend) continue;  // waits for the leaf pass
+    }
     if (k < 0 || k == kDone) continue;
 
     // one node visit
@@ -399,6 +435,7 @@ __device__ __forceinline__ void trace_persistent(
       raise_device_error(err, kDevIterationBound);
       finish((uint32_t)k, hit, hit.prim >= 0);
       k = kIdle;
+      pend = 0;
       continue;
     }
     const float4* __restrict__ bvh = ts.bvh;
@@ -417,9 +454,12 @@ __device__ __forceinline__ void trace_persistent(
       for (int c = 0; c < 2; ++c) {
         const bool hc = c == 0 ? h0 : h1;
         const int rc = c == 0 ? r0 : r1;
-        if (hc && rc < 0 && !finished) {
+        if (kDefer && hc && rc < 0) {
+          pend |= 1u << c;
+          pend_slot[c] = ~rc;
+        } else if (hc && rc < 0 && !finished) {
           ++n_tris;
-          finished = leaf(tris, ~rc);
+          finished = leaf_test<TEST, ANY>(tris, ~rc, r, w, hit);
         }
         if (hc && rc < 0) {
           if (c == 0)
@@ -486,11 +526,16 @@ __device__ __forceinline__ void trace_persistent(
                                  phz[j], r, lim, t0);
             tn[c] = t0;
 #if AJG_LEAF_BATCH
-            if (h && ref[c] < 0) leaf_slot[nleaf++] = ~ref[c];
+            if (kDefer && h && ref[c] < 0) {
+              pend |= 1u << c;
+              pend_slot[c] = ~ref[c];
+            } else if (h && ref[c] < 0) {
+              leaf_slot[nleaf++] = ~ref[c];
+            }
 #else
             if (h && ref[c] < 0 && !finished) {
               ++n_tris;
-              finished = leaf(tris, ~ref[c]);
+              finished = leaf_test<TEST, ANY>(tris, ~ref[c], r, w, hit);
             }
 #endif
             if (h && ref[c] >= 0) inner |= 1u << c;
@@ -547,7 +592,8 @@ __device__ __forceinline__ void trace_persistent(
 #else
             if (!finished) {
               ++n_tris;
-              finished = leaf(tris, (int)(tbase + __popc(lmask & below)));
+              finished = leaf_test<TEST, ANY>(
+                  tris, (int)(tbase + __popc(lmask & below)), r, w, hit);
             }
 #endif
           }
@@ -560,7 +606,7 @@ __device__ __forceinline__ void trace_persistent(
 #pragma unroll
         for (int j = 0; j < W; ++j)
           if (j == i) slot = leaf_slot[j];
-        finished = leaf(tris, slot);
+        finished = leaf_test<TEST, ANY>(tris, slot, r, w, hit);
       }
 #endif
       if (!finished && inner && ANY) {
@@ -627,7 +673,9 @@ __device__ __forceinline__ void trace_persistent(
         }
       }
     }
-    if (!finished && !descend) {
+    if (kDefer && !finished && !descend && pend) {
+      node = -1;  // pops after the leaf pass
+    } else if (!finished && !descend) {
       // pop, skipping boxes a closer hit has since excluded
       finished = true;
       while (sp > 0) {
@@ -646,6 +694,7 @@ __device__ __forceinline__ void trace_persistent(
       ++n_rays;
       finish((uint32_t)k, hit, hit.prim >= 0);
       k = kIdle;
+      pend = 0;
     }
   }
 }
