@@ -492,10 +492,12 @@ __device__ __forceinline__ void trace_persistent(
       int ref[W];
       unsigned inner = 0;  // interior children whose box passed
 #if AJG_LEAF_BATCH
-      // leaf children whose box passed, tested after the box tests from
-      // one call site (all lanes with an i-th leaf test it together)
+      // leaf children whose box passed (mask `leaves`, slot per child, both
+      // indexed by the child so that they stay in registers), tested after
+      // the box tests from one call site (all lanes with an i-th leaf test
+      // it together)
       int leaf_slot[W];
-      int nleaf = 0;
+      unsigned leaves = 0;
 #endif
       if constexpr (!CMP) {
         constexpr int G = W / 4;  // float4 groups per plane
@@ -530,7 +532,8 @@ __device__ __forceinline__ void trace_persistent(
               pend |= 1u << c;
               pend_slot[c] = ~ref[c];
             } else if (h && ref[c] < 0) {
-              leaf_slot[nleaf++] = ~ref[c];
+              leaf_slot[c] = ~ref[c];
+              leaves |= 1u << c;
             }
 #else
             if (h && ref[c] < 0 && !finished) {
@@ -588,7 +591,8 @@ __device__ __forceinline__ void trace_persistent(
             inner |= 1u << c;
           } else {
 #if AJG_LEAF_BATCH
-            leaf_slot[nleaf++] = (int)(tbase + __popc(lmask & below));
+            leaf_slot[c] = (int)(tbase + __popc(lmask & below));
+            leaves |= 1u << c;
 #else
             if (!finished) {
               ++n_tris;
@@ -600,12 +604,14 @@ __device__ __forceinline__ void trace_persistent(
         }
       }
 #if AJG_LEAF_BATCH
-      for (int i = 0; i < nleaf && !finished; ++i) {
+      while (leaves && !finished) {
+        const int c = __ffs(leaves) - 1;
+        leaves &= leaves - 1;
         ++n_tris;
         int slot = 0;
 #pragma unroll
         for (int j = 0; j < W; ++j)
-          if (j == i) slot = leaf_slot[j];
+          if (j == c) slot = leaf_slot[j];
         finished = leaf_test<TEST, ANY>(tris, slot, r, w, hit);
       }
 #endif
