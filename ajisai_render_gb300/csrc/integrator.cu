@@ -56,6 +56,15 @@ __device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
 // 128 registers, no spills (1024 threads: 64)
 #define AJG_SHADE_MIN_BLOCKS (512 / AJG_SHADE_THREADS)
 #endif
+#ifndef AJG_SHADE_MIN_BLOCKS_DIFFUSE
+// the Lambertian kernels: 1024 threads, 64 registers, no spills
+#define AJG_SHADE_MIN_BLOCKS_DIFFUSE (1024 / AJG_SHADE_THREADS)
+#endif
+template <int MAT>
+constexpr int shade_min_blocks() {
+  return MAT == AJG_MAT_DIFFUSE ? AJG_SHADE_MIN_BLOCKS_DIFFUSE
+                                : AJG_SHADE_MIN_BLOCKS;
+}
 constexpr int kMaxLights = 15;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -383,7 +392,7 @@ __global__ void k_shade_miss(WaveArgs a, MJTables t, WaveBufs w, int b,
 // (helper.h:100-133), the MIS BSDF sample (helper.h:209-265), the
 // continuation sample (pt.cpp:215-223) and the next bounce's roulette.
 template <int MAT, bool MJ>
-__global__ void __launch_bounds__(kShadeThreads, AJG_SHADE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kShadeThreads, shade_min_blocks<MAT>())
     k_shade(WaveArgs a, MJTables t, WaveBufs w, int b, int cur,
             const uint32_t* __restrict__ list,
             const uint32_t* __restrict__ list_count, uint32_t NT,
