@@ -56,6 +56,12 @@ __device__ __forceinline__ uint32_t shade_append(uint32_t* counter,
 // 128 registers, no spills (1024 threads: 64)
 #define AJG_SHADE_MIN_BLOCKS (512 / AJG_SHADE_THREADS)
 #endif
+#ifndef AJG_SHADE_GRID
+#define AJG_SHADE_GRID 256  // single-job shading grid: blocks per SM
+#endif
+#ifndef AJG_MJ_SHADE_GRID
+#define AJG_MJ_SHADE_GRID 8  // multi-job shading grid: blocks per SM
+#endif
 #ifndef AJG_SHADE_MIN_BLOCKS_DIFFUSE
 // the Lambertian kernels: 1024 threads, 64 registers, no spills
 #define AJG_SHADE_MIN_BLOCKS_DIFFUSE (1024 / AJG_SHADE_THREADS)
@@ -1091,6 +1097,10 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       a.S = (uint32_t)Sw;
       a.s0 = (uint32_t)s0;
       a.n_paths = (uint32_t)(n_pix * Sw);
+      // shading grids: many short blocks (the block-wide loop waits on its
+      // slowest warp each round; small blocks of work keep the SMs evenly
+      // busy to the end), never more than the wave's paths need
+      const int gsh = grid_for(a.n_paths, kShadeThreads, kSMs * AJG_SHADE_GRID);
       cudaMemsetAsync(w.counts, 0, 64, st);
       KernelTimer{ctx, st, -1};
       k_raygen<false><<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads,
@@ -1124,21 +1134,22 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
           k_shade_miss<false><<<gs, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists, &w.counts[4]);
         }
-        {
+        // one shading launch per material class the scene has
+        if (s.mat_mask & (1u << AJG_MAT_DIFFUSE)) {
           KernelTimer tm(ctx, st, ks);
-          k_shade<AJG_MAT_DIFFUSE, false><<<gs, kShadeThreads, 0, st>>>(
+          k_shade<AJG_MAT_DIFFUSE, false><<<gsh, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists + P, &w.counts[5], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
-        {
+        if (s.mat_mask & (1u << AJG_MAT_DISNEY)) {
           KernelTimer tm(ctx, st, ks);
-          k_shade<AJG_MAT_DISNEY, false><<<gs, kShadeThreads, 0, st>>>(
+          k_shade<AJG_MAT_DISNEY, false><<<gsh, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
         if (s.mat_mask >> AJG_MAT_MIRROR) {
           KernelTimer tm(ctx, st, ks);
-          k_shade<kMatOther, false><<<gs, kShadeThreads, 0, st>>>(
+          k_shade<kMatOther, false><<<gsh, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)nt,
               shadow_cap, ctx->d_error);
         }
@@ -1198,6 +1209,7 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
   WaveArgs a{};
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
+  const int gsh = grid_for(P, kShadeThreads, kSMs * AJG_MJ_SHADE_GRID);
   auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
     launch_wave_extend(true, tri_test, closest_width(width), s, t, w.ro[q], w.rd[q],
                        &w.counts[q], &w.counts[8], hits, ctr, err, es);
@@ -1234,13 +1246,13 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                                          w.lists, &w.counts[4], (uint32_t)P);
     k_shade_miss<true><<<gs, kShadeThreads, 0, st>>>(a, t, wb, b, q, w.lists,
                                                      &w.counts[4]);
-    k_shade<AJG_MAT_DIFFUSE, true><<<gs, kShadeThreads, 0, st>>>(
+    k_shade<AJG_MAT_DIFFUSE, true><<<gsh, kShadeThreads, 0, st>>>(
         a, t, wb, b, q, w.lists + P, &w.counts[5], (uint32_t)NT, shadow_cap,
         err);
-    k_shade<AJG_MAT_DISNEY, true><<<gs, kShadeThreads, 0, st>>>(
+    k_shade<AJG_MAT_DISNEY, true><<<gsh, kShadeThreads, 0, st>>>(
         a, t, wb, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
         shadow_cap, err);
-    k_shade<kMatOther, true><<<gs, kShadeThreads, 0, st>>>(
+    k_shade<kMatOther, true><<<gsh, kShadeThreads, 0, st>>>(
         a, t, wb, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)NT,
         shadow_cap, err);
     if (overlap && b + 1 < bounces)
