@@ -65,7 +65,7 @@ class Context:
         self.check(self.lib.ajg_get_stats(self.h, C.byref(s), int(reset)))
         return {n: getattr(s, n) for n, _ in s._fields_}
 
-    KINDS = ("closest", "any", "shade")
+    KINDS = ("closest", "any", "shade", "any_packets", "closest_packets")
 
     def launch_log(self, reset: bool = True) -> list:
         """The launches timed since the last reset (profiling on): per

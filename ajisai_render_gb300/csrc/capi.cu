@@ -255,6 +255,12 @@ int ajg_create_context(const ajg_config* cfg, ajg_ctx** out) {
   if (cfg) ctx->hbm_budget = cfg->hbm_budget_bytes;
   if (const char* ov = std::getenv("AJG_TRACE_OVERLAP"))
     ctx->overlap = std::strcmp(ov, "0") != 0;
+  if (const char* pk = std::getenv("AJG_PACKET_SHADOW"))
+    ctx->packet_shadow = std::atoi(pk);
+  if (const char* pb = std::getenv("AJG_PACKET_BOUNCES"))
+    ctx->packet_bounces = std::atoi(pb);
+  if (const char* pc = std::getenv("AJG_PACKET_CAMERA"))
+    ctx->packet_camera = std::strcmp(pc, "0") != 0;
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) !=
           cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->trace_stream, cudaStreamNonBlocking) !=
@@ -312,11 +318,12 @@ static void resolve_timings(ajg_ctx* ctx) {
     r.ms = ms;
     if (p.snap >= 0) {
       const TraceCounters c = ctx->h_snaps[p.snap];
-      const TraceCounters& l = ctx->last_snap[p.kind];
+      const int slot = counter_slot(p.kind);
+      const TraceCounters& l = ctx->last_snap[slot];
       r.rays = c.rays - l.rays;
       r.nodes = c.nodes - l.nodes;
       r.tris = c.tris - l.tris;
-      ctx->last_snap[p.kind] = c;
+      ctx->last_snap[slot] = c;
     }
     if (ctx->launch_log.size() < (size_t)kLaunchLogCap)
       ctx->launch_log.push_back(r);
@@ -363,11 +370,13 @@ int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset) {
   out->paths = ctx->paths_total;
   resolve_timings(ctx);
   out->kernel_launches = ctx->kernel_launches;
-  out->closest_launches = ctx->kind_launches[kKindClosest];
-  out->any_launches = ctx->kind_launches[kKindAny];
+  out->closest_launches =
+      ctx->kind_launches[kKindClosest] + ctx->kind_launches[kKindClosestPacket];
+  out->any_launches =
+      ctx->kind_launches[kKindAny] + ctx->kind_launches[kKindAnyPacket];
   out->shade_launches = ctx->kind_launches[kKindShade];
-  out->closest_ms = ctx->kind_ms[kKindClosest];
-  out->any_ms = ctx->kind_ms[kKindAny];
+  out->closest_ms = ctx->kind_ms[kKindClosest] + ctx->kind_ms[kKindClosestPacket];
+  out->any_ms = ctx->kind_ms[kKindAny] + ctx->kind_ms[kKindAnyPacket];
   out->shade_ms = ctx->kind_ms[kKindShade];
   if (reset) {
     CK(cudaMemset(ctx->d_counters, 0, sizeof(c)), "stats");

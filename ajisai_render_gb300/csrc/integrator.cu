@@ -330,20 +330,26 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
+// A shadow ray: to the shadow queue, or -- `top`, the coherent terms of a
+// single job without emitters -- to the coherent queue, whose entry k sits
+// at cap - 1 - k of the same storage (the two cannot meet: a path appends at
+// most NT entries to them together).  `top` is uniform over the block.
 template <bool MJ>
 __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
                                             uint32_t sid, bool pred,
-                                            uint32_t cap, uint32_t* err) {
-  const uint32_t k = shade_append(&w.counts[2], pred);
+                                            uint32_t cap, uint32_t* err,
+                                            bool top = false) {
+  const uint32_t k = shade_append(&w.counts[top ? 11 : 2], pred);
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
     return;
   }
-  w.sq_o[k] = make_float4(o.x, o.y, o.z, tmax);
-  w.sq_d[k] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
-  if constexpr (MJ) w.sq_scene[k] = (uint16_t)sid;
+  const uint32_t i = top ? cap - 1 - k : k;
+  w.sq_o[i] = make_float4(o.x, o.y, o.z, tmax);
+  w.sq_d[i] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
+  if constexpr (MJ) w.sq_scene[i] = (uint16_t)sid;
 }
 
 // The closest-hit queue of MIS BSDF rays in scenes with emitters: entry k
@@ -402,7 +408,9 @@ __global__ void __launch_bounds__(kShadeThreads, shade_min_blocks<MAT>())
     k_shade(WaveArgs a, MJTables t, WaveBufs w, int b, int cur,
             const uint32_t* __restrict__ list,
             const uint32_t* __restrict__ list_count, uint32_t NT,
-            uint32_t shadow_cap, uint32_t* err) {
+            uint32_t shadow_cap, uint32_t* err, uint32_t coh = 0) {
+  // coh: bit l set -- light term l's shadow rays go to the coherent queue
+  // (bit 31: the MIS BSDF term's); single jobs without emitters only
   const uint32_t n = *list_count;
   const int nxt = cur ^ 1;
   // warp-uniform loop (block-uniform for a single job): every lane of a
@@ -564,7 +572,7 @@ __global__ void __launch_bounds__(kShadeThreads, shade_min_blocks<MAT>())
           w.term_vis[slot] = 0;
         }
         emit_shadow<MJ>(w, so, sd, tmax, p * NT + l, sid, emit, shadow_cap,
-                        err);
+                        err, !MJ && l < 31 && ((coh >> l) & 1u));
         if (on) dim += draws;
       }
       {
@@ -614,7 +622,8 @@ __global__ void __launch_bounds__(kShadeThreads, shade_min_blocks<MAT>())
           dim += 3;
         }
         emit_shadow<MJ>(w, so, sd, __int_as_float(0x7f800000),
-                        p * NT + (NT - 1), sid, emit, shadow_cap, err);
+                        p * NT + (NT - 1), sid, emit, shadow_cap, err,
+                        !MJ && ((coh >> 31) & 1u));
         // (a single job's scene without emitters never fills this queue:
         // skip its block-wide append; the condition is uniform)
         if (MJ || s.tri_emit)
@@ -1038,6 +1047,8 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const int kc = timers ? kKindClosest : -1;
   const int ka = timers ? kKindAny : -1;
   const int ks = timers ? kKindShade : -1;
+  const int kcp = timers ? kKindClosestPacket : -1;
+  const int kap = timers ? kKindAnyPacket : -1;
   const MJTables t{};
 
   WaveArgs a;
@@ -1055,11 +1066,18 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const int gs = kSMs * 8;
   // persistent traversal: resident blocks only
   const DeviceScene s_closest = closest_view(s);
-  auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
-    launch_wave_extend(false, s_closest.tri_test, s_closest.width, s_closest, t,
-                       w.ro[q], w.rd[q],
-                       &w.counts[q], &w.counts[8], hits, &ctx->d_counters[0],
-                       ctx->d_error, es);
+  // bounce 0's camera rays (a pixel's samples side by side in the queue) as
+  // masked packets over the binary layout (AJG_PACKET_CAMERA)
+  const bool cam_packets = ctx->packet_camera && s_closest.width == 2;
+  auto extend = [&](int q, ajg_hit* hits, cudaStream_t es, bool cam) {
+    if (cam)
+      launch_wave_extend_packet(s_closest.tri_test, s_closest, w.ro[q], w.rd[q],
+                                &w.counts[q], &w.counts[8], hits,
+                                &ctx->d_counters[0], ctx->d_error, es);
+    else
+      launch_wave_extend(false, s_closest.tri_test, s_closest.width, s_closest,
+                         t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], hits,
+                         &ctx->d_counters[0], ctx->d_error, es);
   };
   // Bounce b+1's closest hits run on the trace stream beside bounce b's
   // shadow rays: the two persistent launches fill each other's drain.  The
@@ -1068,12 +1086,12 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   // written after k_accumulate of bounce b on the render stream.
   const bool overlap = ctx->overlap && !ctx->profiling && w.hits2 != nullptr;
   cudaStream_t ts = ctx->trace_stream;
-  auto extend_ahead = [&](int q, ajg_hit* hits) {
+  auto extend_ahead = [&](int q, ajg_hit* hits, bool cam) {
     cudaEventRecord(ctx->ev_queue, st);
     cudaStreamWaitEvent(ts, ctx->ev_queue, 0);
     cudaMemsetAsync(&w.counts[8], 0, sizeof(uint32_t), ts);
-    KernelTimer tm(ctx, ts, kc);
-    extend(q, hits, ts);
+    KernelTimer tm(ctx, ts, cam ? kcp : kc);
+    extend(q, hits, ts, cam);
     cudaEventRecord(ctx->ev_hits, ts);
   };
   auto bsdf_closest = [&]() {
@@ -1088,6 +1106,24 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
     launch_wave_shadow(false, s.tri_test, s.width, s, t, w.sq_o, w.sq_d, nullptr,
                        &w.counts[2], &w.counts[3], w.term_vis,
                        &ctx->d_counters[1], ctx->d_error, st);
+  };
+  // Coherent shadow rays: at bounce 0 a shading block's rays of one light
+  // term are a pixel's samples (one origin region; toward a directional
+  // light, one direction), traced as masked packets from a queue of their
+  // own.  Single jobs without emitters (the BSDF rays of scenes with
+  // emitters use the top of the storage) over the plain 4-wide tree.
+  uint32_t coh0 = 0;
+  if (ctx->packet_shadow > 0 && !s.tri_emit && s.width == 4 && a.j.use_mis) {
+    for (int l = 0; l < (int)s.num_lights && l < 31; ++l)
+      if (ctx->packet_shadow == 2 ||
+          (int)sc->host_lights[12 * l] == AJG_LIGHT_DIRECTIONAL)
+        coh0 |= 1u << l;
+    if (ctx->packet_shadow >= 2) coh0 |= 1u << 31;  // 3: directional + BSDF
+  }
+  auto shadow_packets = [&]() {
+    launch_wave_shadow_packet(s.tri_test, s, w.sq_o, w.sq_d, &w.counts[11],
+                              &w.counts[12], shadow_cap, w.term_vis,
+                              &ctx->d_counters[1], ctx->d_error, st);
   };
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);
@@ -1106,22 +1142,24 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
       k_raygen<false><<<grid_for(a.n_paths, kShadeThreads, gs), kShadeThreads,
                         0, st>>>(a, t, w);
       int q = 0;
-      if (overlap && a.j.max_b > 0) extend_ahead(0, w.hits);
+      if (overlap && a.j.max_b > 0) extend_ahead(0, w.hits, cam_packets);
       for (int b = 0; b < a.j.max_b; ++b) {
         WaveBufs wb = w;
+        const uint32_t coh = b < ctx->packet_bounces ? coh0 : 0u;
         if (overlap) {
           wb.hits = (b & 1) ? w.hits2 : w.hits;
           cudaStreamWaitEvent(st, ctx->ev_hits, 0);
         }
-        // next queue, shadow queue, fetch counters and material lists
+        // next queue, shadow queues, fetch counters and material lists
         cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
         if (overlap) {
           cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
-          cudaMemsetAsync(&w.counts[9], 0, 2 * sizeof(uint32_t), st);
+          cudaMemsetAsync(&w.counts[9], 0, 4 * sizeof(uint32_t), st);
         } else {
-          cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
-          KernelTimer tm(ctx, st, kc);
-          extend(q, w.hits, st);
+          cudaMemsetAsync(&w.counts[2], 0, 11 * sizeof(uint32_t), st);
+          const bool cam = b == 0 && cam_packets;
+          KernelTimer tm(ctx, st, cam ? kcp : kc);
+          extend(q, w.hits, st, cam);
         }
         {
           KernelTimer tm(ctx, st, -1);
@@ -1139,26 +1177,30 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
           KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DIFFUSE, false><<<gsh, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists + P, &w.counts[5], (uint32_t)nt,
-              shadow_cap, ctx->d_error);
+              shadow_cap, ctx->d_error, coh);
         }
         if (s.mat_mask & (1u << AJG_MAT_DISNEY)) {
           KernelTimer tm(ctx, st, ks);
           k_shade<AJG_MAT_DISNEY, false><<<gsh, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)nt,
-              shadow_cap, ctx->d_error);
+              shadow_cap, ctx->d_error, coh);
         }
         if (s.mat_mask >> AJG_MAT_MIRROR) {
           KernelTimer tm(ctx, st, ks);
           k_shade<kMatOther, false><<<gsh, kShadeThreads, 0, st>>>(
               a, t, wb, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)nt,
-              shadow_cap, ctx->d_error);
+              shadow_cap, ctx->d_error, coh);
         }
         if (overlap && b + 1 < a.j.max_b)
-          extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2);
+          extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2, false);
         if (a.j.use_mis) {
           {
             KernelTimer tm(ctx, st, ka);
             shadow();
+          }
+          if (coh) {
+            KernelTimer tm(ctx, st, kap);
+            shadow_packets();
           }
           if (s.tri_emit) {
             {

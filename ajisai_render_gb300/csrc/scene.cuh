@@ -172,7 +172,8 @@ struct WaveBufs {
                      // and other hits
   uint32_t* counts;  // [0],[1] path queues, [2] shadow queue, [3] shadow
                      // fetch, [4..7] lists, [8] extend fetch, [9] closest
-                     // MIS BSDF queue, [10] its fetch
+                     // MIS BSDF queue, [10] its fetch, [11] coherent shadow
+                     // queue (single jobs without emitters), [12] its fetch
 };
 
 // Tables of a multi-job wave in device memory.
@@ -254,7 +255,23 @@ struct Buffer {
 
 // Event pairs recorded around launches while profiling is on; resolved into
 // milliseconds when the stats are read.
-enum KernelKind { kKindClosest = 0, kKindAny = 1, kKindShade = 2, kKinds = 3 };
+// Launch kinds of the profiling log; the packet traversals count their
+// rays in the closest-hit (kKindClosestPacket) and any-hit (kKindAnyPacket)
+// counters.
+enum KernelKind {
+  kKindClosest = 0,
+  kKindAny = 1,
+  kKindShade = 2,
+  kKindAnyPacket = 3,
+  kKindClosestPacket = 4,
+  kKinds = 5
+};
+// The traversal counters (ajg_ctx::d_counters) a launch kind adds to.
+inline int counter_slot(int kind) {
+  return kind == kKindAnyPacket ? kKindAny
+         : kind == kKindClosestPacket ? kKindClosest
+                                      : kind;
+}
 struct PendingTiming {
   cudaEvent_t a, b;
   int kind;
@@ -287,6 +304,15 @@ struct ajg_ctx {
   cudaStream_t trace_stream = nullptr;
   cudaEvent_t ev_queue = nullptr, ev_hits = nullptr;
   bool overlap = true;
+  // single jobs without emitters over the plain 4-wide tree: the light terms
+  // of bounce 0 whose shadow rays are traced as masked packets
+  // (AJG_PACKET_SHADOW: 0 none, 1 directional lights, 2 every term, 3
+  // directional lights and the MIS BSDF ray)
+  int packet_shadow = 1;
+  int packet_bounces = 1;  // bounces 0 .. packet_bounces-1 (AJG_PACKET_BOUNCES)
+  // single jobs whose closest hits walk the binary layout: bounce 0's camera
+  // rays traced as masked packets (AJG_PACKET_CAMERA=0 turns it off)
+  bool packet_camera = true;
   std::mutex mu;
   std::string last_error;
   uint32_t* d_error = nullptr;            // device error flag
@@ -303,8 +329,8 @@ struct ajg_ctx {
   int64_t n_snaps = 0;
   std::vector<ajg_launch_record> launch_log;
   ajg::TraceCounters last_snap[2] = {};
-  double kind_ms[ajg::kKinds] = {0, 0, 0};
-  unsigned long long kind_launches[ajg::kKinds] = {0, 0, 0};
+  double kind_ms[ajg::kKinds] = {};
+  unsigned long long kind_launches[ajg::kKinds] = {};
   // wavefront arena (grown on demand, reused across renders)
   std::vector<ajg::Buffer> arena;
   uint64_t arena_paths = 0;
@@ -346,7 +372,7 @@ struct KernelTimer {
       int64_t snap = -1;
       if (kind != kKindShade && ctx->h_snaps && ctx->n_snaps < kLaunchLogCap) {
         snap = ctx->n_snaps++;
-        cudaMemcpyAsync(ctx->h_snaps + snap, ctx->d_counters + kind,
+        cudaMemcpyAsync(ctx->h_snaps + snap, ctx->d_counters + counter_slot(kind),
                         sizeof(TraceCounters), cudaMemcpyDeviceToHost, st);
       }
       ctx->pending.push_back(PendingTiming{a, b, kind, snap});
@@ -397,6 +423,19 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
                         const uint32_t* count, uint32_t* fetch_next,
                         uint8_t* vis, TraceCounters* ctr, uint32_t* err,
                         cudaStream_t st);
+// A single job's camera rays (the binary layout) and coherent shadow rays
+// (entry k at cap - 1 - k of the shadow queue's storage; the plain 4-wide
+// tree) as masked packets.
+void launch_wave_extend_packet(int tri_test, const DeviceScene& s,
+                               const float4* ro, const float4* rd,
+                               const uint32_t* count, uint32_t* fetch_next,
+                               ajg_hit* hits, TraceCounters* ctr, uint32_t* err,
+                               cudaStream_t st);
+void launch_wave_shadow_packet(int tri_test, const DeviceScene& s,
+                               const float4* sq_o, const float4* sq_d,
+                               const uint32_t* count, uint32_t* fetch_next,
+                               uint32_t cap, uint8_t* vis, TraceCounters* ctr,
+                               uint32_t* err, cudaStream_t st);
 void launch_wave_bsdf_trace(bool mj, int tri_test, int width,
                             const DeviceScene& s, const MJTables& t,
                             const float4* sq_o, const float4* sq_d,

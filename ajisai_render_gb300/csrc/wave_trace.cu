@@ -1,7 +1,9 @@
 // Traversal kernels of the path waves: closest hits of a path queue
 // (k_extend), any hits of the shadow queue (k_shadow) and closest hits of
 // the MIS BSDF rays of scenes with emitters (k_bsdf_trace), each in a
-// single-job form and a multi-job form whose rays carry their scene index.
+// single-job form and a multi-job form whose rays carry their scene index;
+// and for single jobs the packet traversals of bounce 0's camera rays
+// (k_extend_packet) and directional-light shadow rays (k_shadow_packet).
 // A translation unit of its own: the traversal's arithmetic (the slab and
 // triangle tests) must not be contracted into multiply-adds, so that hits
 // stay bit-exact, while the shading kernels may be built with contraction.
@@ -11,6 +13,10 @@ namespace ajg {
 namespace {
 
 constexpr int kTraceThreads = 128;
+#ifndef AJG_PACKET_MIN_BLOCKS
+#define AJG_PACKET_MIN_BLOCKS 8  // blocks of 128 per SM the packet kernels
+                                 // are compiled for (64 registers)
+#endif
 
 // The tree of the ray's scene; closest-hit kernels of the binary layout
 // (W = 2) take the binary tree a 4-wide scene keeps beside its wide one.
@@ -77,6 +83,59 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
   };
   trace_persistent<TEST, true, W>(trace_scene(s), n, fetch_next, fetch,
                                   finish, nr, nn, nt, err);
+  flush_counters(ctr, nr, nn, nt);
+}
+
+// Closest hits of a single job's camera rays (bounce 0's path queue: a
+// pixel's samples side by side) as masked packets over the binary layout.
+template <int TEST>
+__global__ void __launch_bounds__(kPacketThreads, AJG_PACKET_MIN_BLOCKS)
+    k_extend_packet(DeviceScene s, const float4* __restrict__ ro,
+                    const float4* __restrict__ rd,
+                    const uint32_t* __restrict__ count, uint32_t* fetch_next,
+                    ajg_hit* __restrict__ hits, TraceCounters* ctr,
+                    uint32_t* err) {
+  const uint32_t n = *count;
+  uint32_t nn = 0, nt = 0, nr = 0;
+  auto fetch = [&](uint32_t k, TraceScene&) {
+    const float4 o = ro[k], d = rd[k];
+    return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
+  };
+  auto finish = [&](uint32_t k, const Hit& h, bool) {
+    ajg_hit o2;
+    o2.t = h.t;
+    o2.u = h.u;
+    o2.v = h.v;
+    o2.prim = h.prim;
+    hits[k] = o2;
+  };
+  trace_packet_closest<TEST>(trace_scene(s), n, fetch_next, fetch, finish, nr,
+                             nn, nt, err);
+  flush_counters(ctr, nr, nn, nt);
+}
+
+// Any hits of a single job's coherent shadow rays (the queue at the top of
+// the shadow queue's storage: entry k at cap - 1 - k) as masked packets over
+// the plain 4-wide tree.
+template <int TEST>
+__global__ void __launch_bounds__(kPacketThreads, AJG_PACKET_MIN_BLOCKS)
+    k_shadow_packet(DeviceScene s, const float4* __restrict__ sq_o,
+                    const float4* __restrict__ sq_d,
+                    const uint32_t* __restrict__ count, uint32_t* fetch_next,
+                    uint32_t cap, uint8_t* __restrict__ vis,
+                    TraceCounters* ctr, uint32_t* err) {
+  const uint32_t n = min(*count, cap);
+  uint32_t nn = 0, nt = 0, nr = 0;
+  auto fetch = [&](uint32_t k, TraceScene&) {
+    const uint32_t i = cap - 1 - k;
+    const float4 o = sq_o[i], d = sq_d[i];
+    return make_query(xyz(o), xyz(d), kRayEps, o.w);
+  };
+  auto finish = [&](uint32_t k, const Hit&, bool occ) {
+    if (!occ) vis[__float_as_uint(sq_d[cap - 1 - k].w)] = 1;
+  };
+  trace_packet_any<TEST>(trace_scene(s), n, fetch_next, fetch, finish, nr, nn,
+                         nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
@@ -149,6 +208,42 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
           s, t, sq_o, sq_d, sq_scene, count, fetch_next, vis, ctr, err);
     }
   });
+}
+
+void launch_wave_extend_packet(int tri_test, const DeviceScene& s,
+                               const float4* ro, const float4* rd,
+                               const uint32_t* count, uint32_t* fetch_next,
+                               ajg_hit* hits, TraceCounters* ctr, uint32_t* err,
+                               cudaStream_t st) {
+  if (tri_test == AJG_TRI_WATERTIGHT) {
+    const int g = resident_grid((const void*)k_extend_packet<AJG_TRI_WATERTIGHT>,
+                                kPacketThreads);
+    k_extend_packet<AJG_TRI_WATERTIGHT><<<g, kPacketThreads, 0, st>>>(
+        s, ro, rd, count, fetch_next, hits, ctr, err);
+  } else {
+    const int g = resident_grid(
+        (const void*)k_extend_packet<AJG_TRI_MOLLER_TRUMBORE>, kPacketThreads);
+    k_extend_packet<AJG_TRI_MOLLER_TRUMBORE><<<g, kPacketThreads, 0, st>>>(
+        s, ro, rd, count, fetch_next, hits, ctr, err);
+  }
+}
+
+void launch_wave_shadow_packet(int tri_test, const DeviceScene& s,
+                               const float4* sq_o, const float4* sq_d,
+                               const uint32_t* count, uint32_t* fetch_next,
+                               uint32_t cap, uint8_t* vis, TraceCounters* ctr,
+                               uint32_t* err, cudaStream_t st) {
+  if (tri_test == AJG_TRI_WATERTIGHT) {
+    const int g = resident_grid((const void*)k_shadow_packet<AJG_TRI_WATERTIGHT>,
+                                kPacketThreads);
+    k_shadow_packet<AJG_TRI_WATERTIGHT><<<g, kPacketThreads, 0, st>>>(
+        s, sq_o, sq_d, count, fetch_next, cap, vis, ctr, err);
+  } else {
+    const int g = resident_grid(
+        (const void*)k_shadow_packet<AJG_TRI_MOLLER_TRUMBORE>, kPacketThreads);
+    k_shadow_packet<AJG_TRI_MOLLER_TRUMBORE><<<g, kPacketThreads, 0, st>>>(
+        s, sq_o, sq_d, count, fetch_next, cap, vis, ctr, err);
+  }
 }
 
 void launch_wave_bsdf_trace(bool mj, int tri_test, int width,

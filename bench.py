@@ -353,21 +353,28 @@ def run_ours(args):
                                     total_ms / 1e3, dev)
     total_ms = total_s * 1e3
 
+    # per kernel, from the per-launch log: the per-lane traversals (kinds
+    # closest, any) and the packet traversals of bounce 0's camera and
+    # directional-light shadow rays (closest_packets, any_packets)
+    by_kind = {}
+    for r in log:
+        by_kind.setdefault(r["kind"], []).append(r)
+    kind_ms = {k: float(sum(r["ms"] for r in v)) for k, v in by_kind.items()}
+
     # roofline of the dominant traversal kernel
-    kinds = {"closest": ("closest_ms", "closest_launches", "closest_nodes", "closest_tris",
-                         "k_extend"),
-             "any": ("any_ms", "any_launches", "any_nodes", "any_tris", "k_shadow")}
-    dom = max(kinds, key=lambda k: st[kinds[k][0]])
-    ms_k, l_k, n_k, t_k, kname = kinds[dom]
-    launches = max(1, st[l_k])
+    kinds = {"closest": "k_extend", "any": "k_shadow"}
+    dom = max(kinds, key=lambda k: kind_ms.get(k, 0.0))
+    kname = kinds[dom]
+    launches_k = by_kind.get(dom, [])
+    launches = max(1, len(launches_k))
+    n_nodes = sum(r["nodes"] for r in launches_k)
+    n_tris = sum(r["tris"] for r in launches_k)
     # closest-hit rays walk the binary layout kept beside a 4-wide tree
     node_bytes = scene.info()["closest_node_bytes" if dom == "closest" else "bvh_node_bytes"]
-    bytes_per_launch = (st[n_k] * node_bytes + st[t_k] * TRI_BYTES) / launches
-    avg_ms = st[ms_k] / launches
+    bytes_per_launch = (n_nodes * node_bytes + n_tris * TRI_BYTES) / launches
+    avg_ms = kind_ms.get(dom, 0.0) / launches
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     peak, peak_kind = peaks()
-    launches_k = [r for r in log if r["kind"] == dom]
-    rays_per_launch = float(np.mean([r["rays"] for r in launches_k])) if launches_k else 0.0
     prof = committed_profile(kname, "icosphere1310k", scene.info()["bvh_width"])
     traffic = scaled_traffic(prof, [r["rays"] for r in launches_k]) if prof else None
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
@@ -395,12 +402,12 @@ def run_ours(args):
                 # the same fraction with the nominal 80-byte 4-wide node
                 # (six planes of four floats and four 32-bit references) in
                 # place of this layout's 128-byte, 64-byte-aligned node
-                "frac_at_80_byte_nodes": ((st[n_k] * 80 + st[t_k] * TRI_BYTES) / launches
+                "frac_at_80_byte_nodes": ((n_nodes * 80 + n_tris * TRI_BYTES) / launches
                                           / (avg_ms / 1e3) / 1e9 / peak)
                 if avg_ms > 0 and node_bytes == 128 else None,
-                "avg_launch_ms": avg_ms, "launches": int(st[l_k]),
+                "avg_launch_ms": avg_ms, "launches": len(launches_k),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel_time_share": st[ms_k] / max(1e-9, prof_ms),
+                "kernel_time_share": kind_ms.get(dom, 0.0) / max(1e-9, prof_ms),
                 "rays_per_s": (st["closest_rays"] + st["any_rays"]) / (prof_ms / 1e3),
                 "measured_on": "one extra step with CUDA events around each launch"}
 
@@ -486,10 +493,17 @@ def run_ours(args):
             "clocks": clk, "e2e": e2e, "roofline": roofline,
             "cpu_baseline": cpu, "gpu_launches": launches_timed,
             "ploc_build_ms": scene.info()["build_ms"],
-            "kernel_ms_per_step": {"k_extend": st["closest_ms"],
-                                   "k_shadow": st["any_ms"],
-                                   "k_shade": st["shade_ms"],
+            "kernel_ms_per_step": {"k_extend": kind_ms.get("closest", 0.0),
+                                   "k_extend_packet": kind_ms.get("closest_packets", 0.0),
+                                   "k_shadow": kind_ms.get("any", 0.0),
+                                   "k_shadow_packet": kind_ms.get("any_packets", 0.0),
+                                   "k_shade": kind_ms.get("shade", 0.0),
                                    "step_under_events": prof_ms},
+            # bounce 0's packet launches: rays and node visits per ray
+            "packet_stats": {k: {"rays": int(sum(r["rays"] for r in v)),
+                                 "nodes_per_ray": sum(r["nodes"] for r in v)
+                                 / max(1, sum(r["rays"] for r in v))}
+                             for k, v in by_kind.items() if k.endswith("_packets")},
             "trace_stats": {
                 kind: {"rays_per_step": st[f"{kind}_rays"],
                        "nodes_per_ray": st[f"{kind}_nodes"] / max(1, st[f"{kind}_rays"]),

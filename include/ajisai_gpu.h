@@ -258,9 +258,11 @@ AJG_API int ajg_get_stats(ajg_ctx* ctx, ajg_stats* out, int reset);
 AJG_API int ajg_set_profiling(ajg_ctx* ctx, int enable);
 
 /* One launch timed while profiling is on: its kind (0 closest-hit
- * traversal, 1 any-hit traversal, 2 shading), device time, and the rays,
- * node visits and triangle tests of that launch alone (0 for shading).
- * No counterpart in the reference. */
+ * traversal, 1 any-hit traversal, 2 shading, 3 any-hit traversal of coherent
+ * shadow rays as packets, 4 closest-hit traversal of camera rays as
+ * packets), device time, and the rays, node visits and triangle tests of
+ * that launch alone (0 for shading).  The statistics count kinds 3 and 4
+ * with 1 and 0.  No counterpart in the reference. */
 typedef struct ajg_launch_record {
   uint32_t kind;
   float ms;

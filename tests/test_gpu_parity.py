@@ -1,5 +1,7 @@
 """GPU parity through the C ABI: PLOC trees, ray hits, BSDF values, camera
 rays and renders against the reference's golden vectors and the oracle."""
+import os
+
 import numpy as np
 import pytest
 
@@ -451,6 +453,53 @@ def test_wave_splitting_does_not_change_results():
     small.close()
 
 
+def _context_with(env):
+    """A context created with the given AJG_* variables set (read once, at
+    context creation)."""
+    old = {k: os.environ.get(k) for k in env}
+    try:
+        os.environ.update(env)
+        return api.Context(0)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k)
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("shadow,camera", [("1", "0"), ("2", "0"), ("0", "1"),
+                                           ("1", "1")])
+def test_packet_traversal_gives_the_same_samples(shadow, camera):
+    """Bounce 0's shadow rays traced as masked packets (AJG_PACKET_SHADOW=1:
+    the directional light's, 2: every light term's and the MIS BSDF ray's)
+    and its camera rays as packets (AJG_PACKET_CAMERA=1) give bit-identical
+    samples and films, and the same number of closest- and any-hit rays, as
+    the per-lane traversal -- on the single-job scene at 64 spp and on the
+    Cornell box (the watertight test too)."""
+    base = _context_with({"AJG_PACKET_SHADOW": "0", "AJG_PACKET_CAMERA": "0"})
+    pk = _context_with({"AJG_PACKET_SHADOW": shadow, "AJG_PACKET_CAMERA": camera})
+    cases = [(S.icosphere_scene(5, 2, 40, 32), 64, 0),
+             (S.cornell_box(24, 24), 16, 0), (S.cornell_box(24, 24), 16, 1)]
+    for spec, spp, tri_test in cases:
+        flat = S.flatten(spec)
+        args = api.PTRendererArgs(spp=spp, min_bounces=3, max_bounces=10)
+        out = []
+        for c in (base, pk):
+            sc = api.GpuScene(c, flat, api.CreatePLOCAggregate(16, tri_test=tri_test))
+            c.stats(reset=True)
+            li = api.PTRenderer(args, seed=11).RenderSamples(sc, flat.camera)
+            st = c.stats()
+            film = api.PTRenderer(args, seed=11).Render(sc, flat.camera)
+            out.append((li, film.rgbw, st["closest_rays"], st["any_rays"]))
+            sc.release()
+        assert same_bits(out[0][0], out[1][0])
+        assert same_bits(out[0][1], out[1][1])
+        assert out[0][2:] == out[1][2:] and min(out[0][2:]) > 0
+    pk.close()
+    base.close()
+
+
 def test_invalid_scene_is_rejected(ctx):
     from ajisai_render_gb300._lib import AjgError
     fl = S.flatten(S.cornell_box(8, 8))
@@ -492,13 +541,14 @@ def test_launch_log_matches_the_counters():
     st = c.stats()
     c.set_profiling(False)
     for kind in ("closest", "any"):
-        recs = [x for x in log if x["kind"] == kind]
+        recs = [x for x in log if x["kind"] in (kind, kind + "_packets")]
         assert len(recs) == st[f"{kind}_launches"] >= 6
         assert sum(x["rays"] for x in recs) == st[f"{kind}_rays"]
         assert sum(x["nodes"] for x in recs) == st[f"{kind}_nodes"]
         assert sum(x["tris"] for x in recs) == st[f"{kind}_tris"]
         assert all(x["ms"] > 0 for x in recs)
-    assert log[0]["kind"] == "closest" and log[0]["rays"] == 48 * 40 * 4
+    assert log[0]["kind"] in ("closest", "closest_packets")
+    assert log[0]["rays"] == 48 * 40 * 4
     assert c.launch_log() == []
     sc.release()
     c.close()
