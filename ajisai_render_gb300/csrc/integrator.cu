@@ -330,17 +330,27 @@ __global__ void __launch_bounds__(kShadeThreads)
   }
 }
 
-// A shadow ray: to the shadow queue, or -- `top`, the coherent terms of a
-// single job without emitters -- to the coherent queue, whose entry k sits
+// A shadow ray: to the shadow queue, or -- `top`, the coherent rays of bounce
+// 0 in waves without emitters -- to the coherent queue, whose entry k sits
 // at cap - 1 - k of the same storage (the two cannot meet: a path appends at
-// most NT entries to them together).  `top` is uniform over the block.
+// most NT entries to them together).  Without `split`, `top` is uniform over
+// the block (one append); with `split` (uniform) each lane picks its queue
+// (an append to each).
 template <bool MJ>
 __device__ __forceinline__ void emit_shadow(const WaveBufs& w, F3 o, F3 d,
                                             float tmax, uint32_t slot,
                                             uint32_t sid, bool pred,
                                             uint32_t cap, uint32_t* err,
-                                            bool top = false) {
-  const uint32_t k = shade_append(&w.counts[top ? 11 : 2], pred);
+                                            bool top = false,
+                                            bool split = false) {
+  uint32_t k;
+  if (split) {
+    const uint32_t kb = shade_append(&w.counts[2], pred && !top);
+    const uint32_t kt = shade_append(&w.counts[11], pred && top);
+    k = top ? kt : kb;
+  } else {
+    k = shade_append(&w.counts[top ? 11 : 2], pred);
+  }
   if (!pred) return;
   if (k >= cap) {
     raise_device_error(err, kDevQueueOverflow);
@@ -410,7 +420,8 @@ __global__ void __launch_bounds__(kShadeThreads, shade_min_blocks<MAT>())
             const uint32_t* __restrict__ list_count, uint32_t NT,
             uint32_t shadow_cap, uint32_t* err, uint32_t coh = 0) {
   // coh: bit l set -- light term l's shadow rays go to the coherent queue
-  // (bit 31: the MIS BSDF term's); single jobs without emitters only
+  // (bit 31: the MIS BSDF term's); multi-job waves: nonzero -- every lane's
+  // directional-light rays go there.  Waves without emitters only.
   const uint32_t n = *list_count;
   const int nxt = cur ^ 1;
   // warp-uniform loop (block-uniform for a single job): every lane of a
@@ -571,8 +582,15 @@ __global__ void __launch_bounds__(kShadeThreads, shade_min_blocks<MAT>())
           w.term_f[slot] = make_float4(fo.x, fo.y, fo.z, 0.f);
           w.term_vis[slot] = 0;
         }
+        // to the packet queue: this term's rays (a single job), or a lane's
+        // directional-light rays when its job's footprint allows packets
+        // (multi-job lanes differ in their l-th light and their job)
+        const bool top =
+            MJ ? (coh != 0 && on && J.packets &&
+                  (int)L[0] == AJG_LIGHT_DIRECTIONAL)
+               : (l < 31 && ((coh >> l) & 1u));
         emit_shadow<MJ>(w, so, sd, tmax, p * NT + l, sid, emit, shadow_cap,
-                        err, !MJ && l < 31 && ((coh >> l) & 1u));
+                        err, top, MJ && coh != 0);
         if (on) dim += draws;
       }
       {
@@ -999,6 +1017,46 @@ int check_render(ajg_ctx* ctx, const DeviceScene& s, const ajg_camera& cam,
   return AJG_OK;
 }
 
+// Whether a pixel's samples fall within a few triangles of each other, so
+// that bounce 0's directional-light shadow rays pay as packets (a packet
+// walks the union of its rays' traversals, which near their origins grows
+// with the triangles they span): the pixel's footprint at the world box's
+// centre -- the angle between the rays through the film centre and the
+// pixel beside it, times the camera's distance to that centre -- against
+// kPacketSpread median triangle edges.
+static bool packets_pay(const ajg_scene* sc, const ajg_camera& cam) {
+  auto apply = [](const float* m, const float v[4], float o[4]) {
+    for (int r = 0; r < 4; ++r) {
+      o[r] = 0.f;
+      for (int c = 0; c < 4; ++c) o[r] += m[c * 4 + r] * v[c];
+    }
+  };
+  const float cx = 0.5f * (float)cam.width, cy = 0.5f * (float)cam.height;
+  const float p0[4] = {cx, cy, 1.f, 1.f}, p1[4] = {cx + 1.f, cy, 1.f, 1.f};
+  float q0[4], q1[4];
+  apply(cam.raster2camera, p0, q0);
+  apply(cam.raster2camera, p1, q1);
+  auto unit = [](const float q[4], double u[3]) {
+    const double n = std::sqrt((double)q[0] * q[0] + (double)q[1] * q[1] +
+                               (double)q[2] * q[2]);
+    for (int k = 0; k < 3; ++k) u[k] = n > 0 ? q[k] / n : 0.0;
+  };
+  double u0[3], u1[3];
+  unit(q0, u0);
+  unit(q1, u1);
+  const double angle = std::sqrt((u1[0] - u0[0]) * (u1[0] - u0[0]) +
+                                 (u1[1] - u0[1]) * (u1[1] - u0[1]) +
+                                 (u1[2] - u0[2]) * (u1[2] - u0[2]));
+  const float* m = cam.camera2world;  // column-major: translation in 12..14
+  double dist2 = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double c = 0.5 * ((double)sc->world[k] + sc->world[k + 3]);
+    const double e = (double)m[12 + k] / (m[15] != 0.f ? m[15] : 1.f) - c;
+    dist2 += e * e;
+  }
+  return angle * std::sqrt(dist2) <= (double)sc->d.packet_spread;
+}
+
 JobParams make_job_params(const ajg_scene* sc, const ajg_camera& cam,
                           const ajg_render_params& prm) {
   const DeviceScene& s = sc->d;
@@ -1026,6 +1084,7 @@ JobParams make_job_params(const ajg_scene* sc, const ajg_camera& cam,
   j.x0 = j.y0 = 0;
   j.win_w = cam.width;
   j.win_h = cam.height;
+  j.packets = packets_pay(sc, cam) ? 1 : 0;
   return j;
 }
 
@@ -1071,9 +1130,9 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   const bool cam_packets = ctx->packet_camera && s_closest.width == 2;
   auto extend = [&](int q, ajg_hit* hits, cudaStream_t es, bool cam) {
     if (cam)
-      launch_wave_extend_packet(s_closest.tri_test, s_closest, w.ro[q], w.rd[q],
-                                &w.counts[q], &w.counts[8], hits,
-                                &ctx->d_counters[0], ctx->d_error, es);
+      launch_wave_extend_packet(false, s_closest.tri_test, s_closest, t,
+                                w.ro[q], w.rd[q], &w.counts[q], &w.counts[8],
+                                hits, &ctx->d_counters[0], ctx->d_error, es);
     else
       launch_wave_extend(false, s_closest.tri_test, s_closest.width, s_closest,
                          t, w.ro[q], w.rd[q], &w.counts[q], &w.counts[8], hits,
@@ -1113,7 +1172,8 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
   // own.  Single jobs without emitters (the BSDF rays of scenes with
   // emitters use the top of the storage) over the plain 4-wide tree.
   uint32_t coh0 = 0;
-  if (ctx->packet_shadow > 0 && !s.tri_emit && s.width == 4 && a.j.use_mis) {
+  if (ctx->packet_shadow > 0 && !s.tri_emit && s.width == 4 && a.j.use_mis &&
+      (a.j.packets || ctx->packet_shadow >= 2)) {
     for (int l = 0; l < (int)s.num_lights && l < 31; ++l)
       if (ctx->packet_shadow == 2 ||
           (int)sc->host_lights[12 * l] == AJG_LIGHT_DIRECTIONAL)
@@ -1121,9 +1181,10 @@ static void run_waves(ajg_scene* sc, const ajg_camera& cam,
     if (ctx->packet_shadow >= 2) coh0 |= 1u << 31;  // 3: directional + BSDF
   }
   auto shadow_packets = [&]() {
-    launch_wave_shadow_packet(s.tri_test, s, w.sq_o, w.sq_d, &w.counts[11],
-                              &w.counts[12], shadow_cap, w.term_vis,
-                              &ctx->d_counters[1], ctx->d_error, st);
+    launch_wave_shadow_packet(false, s.tri_test, s, t, w.sq_o, w.sq_d, nullptr,
+                              &w.counts[11], &w.counts[12], shadow_cap,
+                              w.term_vis, &ctx->d_counters[1], ctx->d_error,
+                              st);
   };
   for (uint64_t s0 = 0; s0 < prm.spp; s0 += S) {
     const uint64_t Sw = std::min<uint64_t>(S, prm.spp - s0);
@@ -1246,43 +1307,56 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                      int NT, int bounces, int tri_test, int width, bool emit,
                      TraceCounters* ctr, uint32_t* err, cudaStream_t st,
                      cudaStream_t ts, cudaEvent_t ev_queue,
-                     cudaEvent_t ev_hits) {
+                     cudaEvent_t ev_hits, bool cam_packets,
+                     bool shadow_packets) {
   const DeviceScene s{};
   WaveArgs a{};
   const uint32_t shadow_cap = (uint32_t)(P * NT);
   const int gs = kSMs * 8;
   const int gsh = grid_for(P, kShadeThreads, kSMs * AJG_MJ_SHADE_GRID);
-  auto extend = [&](int q, ajg_hit* hits, cudaStream_t es) {
-    launch_wave_extend(true, tri_test, closest_width(width), s, t, w.ro[q], w.rd[q],
-                       &w.counts[q], &w.counts[8], hits, ctr, err, es);
+  // bounce 0's camera rays (each chunk's paths a pixel's samples side by
+  // side) as masked packets when the closest hits walk binary trees
+  const bool cam_ok = cam_packets && closest_width(width) == 2;
+  // and its directional-light shadow rays, in waves without emitters over
+  // plain 4-wide trees
+  const bool shadow_ok = shadow_packets && !emit && width == 4;
+  auto extend = [&](int q, ajg_hit* hits, cudaStream_t es, bool cam) {
+    if (cam)
+      launch_wave_extend_packet(true, tri_test, s, t, w.ro[q], w.rd[q],
+                                &w.counts[q], &w.counts[8], hits, ctr, err, es);
+    else
+      launch_wave_extend(true, tri_test, closest_width(width), s, t, w.ro[q],
+                         w.rd[q], &w.counts[q], &w.counts[8], hits, ctr, err,
+                         es);
   };
   // bounce b+1's closest hits on the trace stream beside bounce b's shadow
   // rays, as in the single-job waves (run_waves)
   const bool overlap = ts && ev_queue && ev_hits && w.hits2;
-  auto extend_ahead = [&](int q, ajg_hit* hits) {
+  auto extend_ahead = [&](int q, ajg_hit* hits, bool cam) {
     cudaEventRecord(ev_queue, st);
     cudaStreamWaitEvent(ts, ev_queue, 0);
     cudaMemsetAsync(&w.counts[8], 0, sizeof(uint32_t), ts);
-    extend(q, hits, ts);
+    extend(q, hits, ts, cam);
     cudaEventRecord(ev_hits, ts);
   };
   cudaMemsetAsync(w.counts, 0, 64, st);
   k_raygen<true><<<gs, kShadeThreads, 0, st>>>(a, t, w);
   int q = 0;
-  if (overlap && bounces > 0) extend_ahead(0, w.hits);
+  if (overlap && bounces > 0) extend_ahead(0, w.hits, cam_ok);
   for (int b = 0; b < bounces; ++b) {
     WaveBufs wb = w;
     if (overlap) {
       wb.hits = (b & 1) ? w.hits2 : w.hits;
       cudaStreamWaitEvent(st, ev_hits, 0);
     }
+    const uint32_t coh = b == 0 && shadow_ok ? 1u : 0u;
     cudaMemsetAsync(&w.counts[q ^ 1], 0, sizeof(uint32_t), st);
     if (overlap) {
       cudaMemsetAsync(&w.counts[2], 0, 6 * sizeof(uint32_t), st);
-      cudaMemsetAsync(&w.counts[9], 0, 2 * sizeof(uint32_t), st);
+      cudaMemsetAsync(&w.counts[9], 0, 4 * sizeof(uint32_t), st);
     } else {
-      cudaMemsetAsync(&w.counts[2], 0, 9 * sizeof(uint32_t), st);
-      extend(q, w.hits, st);
+      cudaMemsetAsync(&w.counts[2], 0, 11 * sizeof(uint32_t), st);
+      extend(q, w.hits, st, b == 0 && cam_ok);
     }
     k_classify<true><<<gs, kClassifyThreads, 0, st>>>(s, t, w.ro[q], &w.counts[q], wb.hits,
                                          w.lists, &w.counts[4], (uint32_t)P);
@@ -1290,17 +1364,21 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                                                      &w.counts[4]);
     k_shade<AJG_MAT_DIFFUSE, true><<<gsh, kShadeThreads, 0, st>>>(
         a, t, wb, b, q, w.lists + P, &w.counts[5], (uint32_t)NT, shadow_cap,
-        err);
+        err, coh);
     k_shade<AJG_MAT_DISNEY, true><<<gsh, kShadeThreads, 0, st>>>(
         a, t, wb, b, q, w.lists + 2 * P, &w.counts[6], (uint32_t)NT,
-        shadow_cap, err);
+        shadow_cap, err, coh);
     k_shade<kMatOther, true><<<gsh, kShadeThreads, 0, st>>>(
         a, t, wb, b, q, w.lists + 3 * P, &w.counts[7], (uint32_t)NT,
-        shadow_cap, err);
+        shadow_cap, err, coh);
     if (overlap && b + 1 < bounces)
-      extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2);
+      extend_ahead(q ^ 1, (b & 1) ? w.hits : w.hits2, false);
     launch_wave_shadow(true, tri_test, width, s, t, w.sq_o, w.sq_d, w.sq_scene,
                        &w.counts[2], &w.counts[3], w.term_vis, ctr + 1, err, st);
+    if (coh)
+      launch_wave_shadow_packet(true, tri_test, s, t, w.sq_o, w.sq_d,
+                                w.sq_scene, &w.counts[11], &w.counts[12],
+                                shadow_cap, w.term_vis, ctr + 1, err, st);
     if (emit) {
       launch_wave_bsdf_trace(true, tri_test, closest_width(width), s, t, w.sq_o, w.sq_d,
                              w.sq_scene, &w.counts[9], &w.counts[10], shadow_cap,

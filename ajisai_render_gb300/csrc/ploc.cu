@@ -14,9 +14,11 @@
 // The result is bit-identical to the reference's node array; it is then
 // re-laid out for traversal (two child boxes per interior node, leaf slots
 // holding the triangles in Morton order).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "scan.cuh"
 #include "scene.cuh"
@@ -775,6 +777,26 @@ int set_err(ajg_ctx* ctx, int code, const std::string& msg) {
   return code;
 }
 
+// The scene's typical triangle size: the median longest edge over up to
+// 4,096 evenly spaced triangles.
+float median_edge(const float* t, uint64_t n) {
+  const uint64_t k = std::min<uint64_t>(n, 4096);
+  std::vector<float> e(k);
+  for (uint64_t i = 0; i < k; ++i) {
+    const float* p = t + 9 * (i * n / k);
+    float m = 0.f;
+    for (int a = 0; a < 3; ++a) {
+      const float* u = p + 3 * a;
+      const float* v = p + 3 * ((a + 1) % 3);
+      const float dx = u[0] - v[0], dy = u[1] - v[1], dz = u[2] - v[2];
+      m = std::max(m, dx * dx + dy * dy + dz * dz);
+    }
+    e[i] = std::sqrt(m);
+  }
+  std::nth_element(e.begin(), e.begin() + k / 2, e.end());
+  return e[k / 2];
+}
+
 }  // namespace
 
 int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
@@ -1107,6 +1129,7 @@ int build_scene(ajg_ctx* ctx, ajg_scene* s, const float* h_tris,
   d += half.y * half.y;
   d += half.z * half.z;
   s->d.radius = sqrtf(d);
+  s->d.packet_spread = kPacketSpread * median_edge(h_tris, n);
   return AJG_OK;
 }
 

@@ -54,7 +54,15 @@ struct DeviceScene {
   // AJG_HYBRID_CLOSEST=0)
   const float4* bvh_closest = nullptr;
   uint32_t num_inner_closest = 0;
+  // kPacketSpread times the scene's median triangle edge: a render traces
+  // bounce 0's directional-light shadow rays as packets when a pixel's
+  // footprint at the scene is within it
+  float packet_spread = 0.f;
 };
+#ifndef AJG_PACKET_SPREAD
+#define AJG_PACKET_SPREAD 4.0f
+#endif
+constexpr float kPacketSpread = AJG_PACKET_SPREAD;
 
 // Closest-hit rays walk the binary layout of the tree, any-hit rays the
 // 4-wide one, when the scene keeps both (the default for the 4-wide tree):
@@ -107,6 +115,8 @@ struct JobParams {
   int32_t drop_nonfinite;
   uint32_t film_w, film_h;
   uint32_t x0, y0, win_w, win_h;
+  int32_t packets;  // bounce 0's directional-light shadow rays as packets
+  int32_t pad;
 };
 
 // SPPM's visible point (TracerVP's result, sppm.cpp:77-92): the hit, its
@@ -310,9 +320,12 @@ struct ajg_ctx {
   // directional lights and the MIS BSDF ray)
   int packet_shadow = 1;
   int packet_bounces = 1;  // bounces 0 .. packet_bounces-1 (AJG_PACKET_BOUNCES)
-  // single jobs whose closest hits walk the binary layout: bounce 0's camera
-  // rays traced as masked packets (AJG_PACKET_CAMERA=0 turns it off)
-  bool packet_camera = true;
+  // bounce 0's camera rays traced as masked packets over the binary layout
+  // (AJG_PACKET_CAMERA=1; off by default: an exact tie in t between two
+  // triangles, a ray through their shared edge, can resolve to the other
+  // primitive when the packet visits them in another order, so the hits
+  // are not bit-identical with the per-lane traversal's)
+  bool packet_camera = false;
   std::mutex mu;
   std::string last_error;
   uint32_t* d_error = nullptr;            // device error flag
@@ -397,10 +410,15 @@ void enqueue_mj_wave(const MJTables& t, const WaveBufs& w, uint64_t P,
                      int NT, int bounces, int tri_test, int width, bool emit,
                      TraceCounters* ctr, uint32_t* err, cudaStream_t st,
                      cudaStream_t ts = nullptr, cudaEvent_t ev_queue = nullptr,
-                     cudaEvent_t ev_hits = nullptr);
-// Kernels of a multi-job wave launched per wave (for launch counts).
-inline int mj_wave_kernels(int bounces, bool emit) {
-  return 2 + (emit ? 10 : 8) * bounces;
+                     cudaEvent_t ev_hits = nullptr, bool cam_packets = false,
+                     bool shadow_packets = false);
+// Kernels of a multi-job wave launched per wave (for launch counts):
+// `shadow_packets` adds bounce 0's packet traversal of its directional-light
+// rays (waves without emitters over plain 4-wide trees).
+inline int mj_wave_kernels(int bounces, bool emit, int width = 0,
+                           bool shadow_packets = false) {
+  return 2 + (emit ? 10 : 8) * bounces +
+         (shadow_packets && !emit && width == 4 && bounces > 0 ? 1 : 0);
 }
 // Looks up the persistent grids of the multi-job kernels (call before a
 // stream capture).
@@ -426,13 +444,15 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
 // A single job's camera rays (the binary layout) and coherent shadow rays
 // (entry k at cap - 1 - k of the shadow queue's storage; the plain 4-wide
 // tree) as masked packets.
-void launch_wave_extend_packet(int tri_test, const DeviceScene& s,
-                               const float4* ro, const float4* rd,
-                               const uint32_t* count, uint32_t* fetch_next,
-                               ajg_hit* hits, TraceCounters* ctr, uint32_t* err,
+void launch_wave_extend_packet(bool mj, int tri_test, const DeviceScene& s,
+                               const MJTables& t, const float4* ro,
+                               const float4* rd, const uint32_t* count,
+                               uint32_t* fetch_next, ajg_hit* hits,
+                               TraceCounters* ctr, uint32_t* err,
                                cudaStream_t st);
-void launch_wave_shadow_packet(int tri_test, const DeviceScene& s,
-                               const float4* sq_o, const float4* sq_d,
+void launch_wave_shadow_packet(bool mj, int tri_test, const DeviceScene& s,
+                               const MJTables& t, const float4* sq_o,
+                               const float4* sq_d, const uint16_t* sq_scene,
                                const uint32_t* count, uint32_t* fetch_next,
                                uint32_t cap, uint8_t* vis, TraceCounters* ctr,
                                uint32_t* err, cudaStream_t st);

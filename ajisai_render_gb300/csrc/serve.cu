@@ -224,7 +224,8 @@ cudaGraphExec_t Server::graph_for(int bounces, int tri_test, int width,
       cudaSuccess)
     return nullptr;
   enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, emit, d_ctr, d_err,
-                  st, ctx->overlap ? ts : nullptr, ev_queue, ev_hits);
+                  st, ctx->overlap ? ts : nullptr, ev_queue, ev_hits,
+                  ctx->packet_camera, ctx->packet_shadow > 0);
   if (cudaStreamEndCapture(st, &g) != cudaSuccess || !g) return nullptr;
   if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
   cudaGraphDestroy(g);
@@ -531,7 +532,8 @@ bool Server::plan_and_launch() {
   } else {  // capture unavailable: the same launches on the stream
     cudaGetLastError();
     enqueue_mj_wave(t, w, P, NT, bounces, tri_test, width, emit, d_ctr, d_err,
-                    st, ctx->overlap ? ts : nullptr, ev_queue, ev_hits);
+                    st, ctx->overlap ? ts : nullptr, ev_queue, ev_hits,
+                    ctx->packet_camera, ctx->packet_shadow > 0);
   }
   // results this wave completes
   for (const Plan& p : plan) {
@@ -578,7 +580,9 @@ bool Server::plan_and_launch() {
     std::lock_guard<std::mutex> lk(mu);
     ++stats.waves;
     stats.paths += path_off;
-    stats.kernel_launches += mj_wave_kernels(bounces, emit) + f.reports.size();
+    stats.kernel_launches +=
+        mj_wave_kernels(bounces, emit, width, ctx->packet_shadow > 0) +
+        f.reports.size();
   }
   inflight.push_back(std::move(f));
   ++wave_no;

@@ -723,11 +723,15 @@ __device__ __forceinline__ void trace_persistent(
 // the warp's, in shared memory.  The packet visits each node at most once
 // (the tree's interior nodes + 1 bound its visits, as for one ray) and its
 // stack holds at most 3 entries per level, as one ray's does.
+// Rays of a multi-job wave carry their scene: FETCH(k, sid) returns the ray
+// and its scene index, SCENE(sid, ts) points `ts` at that scene's tree, and
+// the warp walks one packet per scene its 32 rays hold.
 constexpr int kPacketThreads = 128;
-template <int TEST, class FETCH, class FINISH>
+template <int TEST, class FETCH, class FINISH, class SCENE>
 __device__ __forceinline__ void trace_packet_any(
-    TraceScene ts, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
-    uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris, uint32_t* err) {
+    TraceScene ts0, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
+    SCENE scene_of, uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris,
+    uint32_t* err) {
   constexpr int W = 4;
   constexpr int kStack = StackDepth<W>::value;
   const unsigned full = 0xffffffffu;
@@ -741,7 +745,8 @@ __device__ __forceinline__ void trace_packet_any(
     if (base >= n) break;
     const uint32_t kk = base + (uint32_t)lane;
     const bool act = kk < n;
-    const RayQ r = act ? fetch(kk, ts)
+    uint32_t sid = 0;
+    const RayQ r = act ? fetch(kk, sid)
                        : make_query(mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 1.f),
                                     0.f, 0.f);
     WtSetup w;
@@ -750,91 +755,99 @@ __device__ __forceinline__ void trace_packet_any(
     hit.t = __int_as_float(0x7f800000);
     hit.prim = -1;
     hit.u = hit.v = 0.f;
-    unsigned live = __ballot_sync(full, act);  // lanes not yet occluded
-    unsigned mask = live;                      // lanes visiting `node`
-    int node = 0, sp = 0;
-    uint32_t visits = 0;
-    while (mask) {
-      if (++visits > ts.max_visits) {
-        raise_device_error(err, kDevIterationBound);
-        break;
-      }
-      const bool in = (mask >> lane) & 1u;
-      if (in) ++n_nodes;
-      const float4* nd = ts.bvh + (uint64_t)node * (2 * W);
-      float4 q[8];
-#pragma unroll
-      for (int i = 0; i < 8; i += 2) ldg_node(nd + i, q[i], q[i + 1]);
-      const float* plx = &q[0].x;
-      const float* phx = &q[1].x;
-      const float* ply = &q[2].x;
-      const float* phy = &q[3].x;
-      const float* plz = &q[4].x;
-      const float* phz = &q[5].x;
-      const float* prf = &q[6].x;
-      int ref[W];
-      unsigned hm[W];
-#pragma unroll
-      for (int j = 0; j < W; ++j) {
-        ref[j] = __float_as_int(prf[j]);
-        float t0;
-        const bool h = in && ref[j] != kEmptyRef &&
-                       slab2(plx[j], phx[j], ply[j], phy[j], plz[j], phz[j], r,
-                             r.tmax, t0);
-        hm[j] = __ballot_sync(full, h);
-      }
-      // leaf children first: the lanes whose ray passed the box test them
-#pragma unroll
-      for (int j = 0; j < W; ++j) {
-        if (ref[j] < 0 && ref[j] != kEmptyRef) {
-          const unsigned m = hm[j] & live;
-          if (m) {
-            bool occ = false;
-            if ((m >> lane) & 1u) {
-              ++n_tris;
-              occ = leaf_test<TEST, true>(ts.tris, ~ref[j], r, w, hit);
-            }
-            live &= ~__ballot_sync(full, occ);
-          }
-        }
-      }
-      // interior children in child order: the first is visited next, the
-      // others pushed (popped last first)
-      int nxt = -1;
-      unsigned nmask = 0;
-#pragma unroll
-      for (int j = 0; j < W; ++j) {
-        if (ref[j] >= 0) {
-          const unsigned m = hm[j] & live;
-          if (m) {
-            if (nxt < 0) {
-              nxt = ref[j];
-              nmask = m;
-            } else if (sp < kStack) {
-              stk[sp] = make_int2(ref[j], (int)m);  // every lane, same value
-              ++sp;
-            } else {
-              raise_device_error(err, kDevStackOverflow);
-              live = 0;
-            }
-          }
-        }
-      }
-      if (!live) break;
-      if (nxt >= 0) {
-        node = nxt;
-        mask = nmask;
-        continue;
-      }
-      mask = 0;
-      while (sp > 0) {
-        --sp;
-        const int2 e = stk[sp];
-        const unsigned m = (unsigned)e.y & live;
-        if (m) {
-          node = e.x;
-          mask = m;
+    unsigned todo = __ballot_sync(full, act);  // lanes of scenes not walked
+    while (todo) {
+      const uint32_t s0 = __shfl_sync(full, sid, __ffs(todo) - 1);
+      // lanes not yet occluded: the packet of scene s0
+      unsigned live = __ballot_sync(full, ((todo >> lane) & 1u) && sid == s0);
+      todo &= ~live;
+      TraceScene ts = ts0;
+      scene_of(s0, ts);
+      unsigned mask = live;  // lanes visiting `node`
+      int node = 0, sp = 0;
+      uint32_t visits = 0;
+      while (mask) {
+        if (++visits > ts.max_visits) {
+          raise_device_error(err, kDevIterationBound);
           break;
+        }
+        const bool in = (mask >> lane) & 1u;
+        if (in) ++n_nodes;
+        const float4* nd = ts.bvh + (uint64_t)node * (2 * W);
+        float4 q[8];
+  #pragma unroll
+        for (int i = 0; i < 8; i += 2) ldg_node(nd + i, q[i], q[i + 1]);
+        const float* plx = &q[0].x;
+        const float* phx = &q[1].x;
+        const float* ply = &q[2].x;
+        const float* phy = &q[3].x;
+        const float* plz = &q[4].x;
+        const float* phz = &q[5].x;
+        const float* prf = &q[6].x;
+        int ref[W];
+        unsigned hm[W];
+  #pragma unroll
+        for (int j = 0; j < W; ++j) {
+          ref[j] = __float_as_int(prf[j]);
+          float t0;
+          const bool h = in && ref[j] != kEmptyRef &&
+                         slab2(plx[j], phx[j], ply[j], phy[j], plz[j],
+                               phz[j], r, r.tmax, t0);
+          hm[j] = __ballot_sync(full, h);
+        }
+        // leaf children first: the lanes whose ray passed the box test them
+  #pragma unroll
+        for (int j = 0; j < W; ++j) {
+          if (ref[j] < 0 && ref[j] != kEmptyRef) {
+            const unsigned m = hm[j] & live;
+            if (m) {
+              bool occ = false;
+              if ((m >> lane) & 1u) {
+                ++n_tris;
+                occ = leaf_test<TEST, true>(ts.tris, ~ref[j], r, w, hit);
+              }
+              live &= ~__ballot_sync(full, occ);
+            }
+          }
+        }
+        // interior children in child order: the first is visited next, the
+        // others pushed (popped last first)
+        int nxt = -1;
+        unsigned nmask = 0;
+  #pragma unroll
+        for (int j = 0; j < W; ++j) {
+          if (ref[j] >= 0) {
+            const unsigned m = hm[j] & live;
+            if (m) {
+              if (nxt < 0) {
+                nxt = ref[j];
+                nmask = m;
+              } else if (sp < kStack) {
+                stk[sp] = make_int2(ref[j], (int)m);  // every lane, same value
+                ++sp;
+              } else {
+                raise_device_error(err, kDevStackOverflow);
+                live = 0;
+              }
+            }
+          }
+        }
+        if (!live) break;
+        if (nxt >= 0) {
+          node = nxt;
+          mask = nmask;
+          continue;
+        }
+        mask = 0;
+        while (sp > 0) {
+          --sp;
+          const int2 e = stk[sp];
+          const unsigned m = (unsigned)e.y & live;
+          if (m) {
+            node = e.x;
+            mask = m;
+            break;
+          }
         }
       }
     }
@@ -856,10 +869,16 @@ __device__ __forceinline__ void trace_packet_any(
 // first; the other is pushed with the packet's nearest entry distance to
 // it, and on the pop a lane whose hit is nearer than that distance (so
 // nearer than its own) leaves the entry's lanes.
-template <int TEST, class FETCH, class FINISH>
+//
+// Rays of a multi-job wave carry their scene: FETCH(k, sid) returns the
+// ray and its scene index, SCENE(sid, ts) points `ts` at that scene's tree,
+// and the warp walks one packet per scene its 32 rays hold (one, in all but
+// the warps that straddle two jobs' chunks).
+template <int TEST, class FETCH, class FINISH, class SCENE>
 __device__ __forceinline__ void trace_packet_closest(
-    TraceScene ts, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
-    uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris, uint32_t* err) {
+    TraceScene ts0, uint32_t n, uint32_t* next, FETCH fetch, FINISH finish,
+    SCENE scene_of, uint32_t& n_rays, uint32_t& n_nodes, uint32_t& n_tris,
+    uint32_t* err) {
   constexpr int kStack = StackDepth<2>::value;
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -874,7 +893,8 @@ __device__ __forceinline__ void trace_packet_closest(
     if (base >= n) break;
     const uint32_t kk = base + (uint32_t)lane;
     const bool act = kk < n;
-    const RayQ r = act ? fetch(kk, ts)
+    uint32_t sid = 0;
+    const RayQ r = act ? fetch(kk, sid)
                        : make_query(mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 1.f),
                                     0.f, 0.f);
     WtSetup w;
@@ -883,79 +903,87 @@ __device__ __forceinline__ void trace_packet_closest(
     hit.t = __int_as_float(0x7f800000);
     hit.prim = -1;
     hit.u = hit.v = 0.f;
-    unsigned mask = __ballot_sync(full, act);  // lanes visiting `node`
-    int node = 0, sp = 0;
-    uint32_t visits = 0;
-    while (mask) {
-      if (++visits > ts.max_visits) {
-        raise_device_error(err, kDevIterationBound);
-        break;
-      }
-      const bool in = (mask >> lane) & 1u;
-      if (in) ++n_nodes;
-      float4 n0, n1, n2, n3;
-      ldg_node(ts.bvh + 4 * (uint64_t)node, n0, n1);
-      ldg_node(ts.bvh + 4 * (uint64_t)node + 2, n2, n3);
-      const float lim = fminf(hit.t, r.tmax);
-      float tn0 = 0.f, tn1 = 0.f;
-      const bool h0 =
-          in && slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
-      const bool h1 =
-          in && slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
-      const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
-      unsigned m0 = __ballot_sync(full, h0), m1 = __ballot_sync(full, h1);
-      if (r0 < 0) {
-        if (h0) {
-          ++n_tris;
-          leaf_test<TEST, false>(ts.tris, ~r0, r, w, hit);
-        }
-        m0 = 0;
-      }
-      if (r1 < 0) {
-        if (h1) {
-          ++n_tris;
-          leaf_test<TEST, false>(ts.tris, ~r1, r, w, hit);
-        }
-        m1 = 0;
-      }
-      if (m0 && m1) {
-        const unsigned both = m0 & m1;
-        const unsigned pref0 =
-            __ballot_sync(full, ((both >> lane) & 1u) && tn0 <= tn1);
-        const bool go0 = 2 * __popc(pref0) >= __popc(both);
-        const unsigned far_m = go0 ? m1 : m0;
-        float ft = ((far_m >> lane) & 1u) ? (go0 ? tn1 : tn0)
-                                          : __int_as_float(0x7f800000);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-          ft = fminf(ft, __shfl_xor_sync(full, ft, o));
-        if (sp >= kStack) {
-          raise_device_error(err, kDevStackOverflow);
+    unsigned todo = __ballot_sync(full, act);  // lanes of scenes not walked
+    while (todo) {
+      const uint32_t s0 = __shfl_sync(full, sid, __ffs(todo) - 1);
+      // lanes visiting `node`: the packet of scene s0
+      unsigned mask = __ballot_sync(full, ((todo >> lane) & 1u) && sid == s0);
+      todo &= ~mask;
+      TraceScene ts = ts0;
+      scene_of(s0, ts);
+      int node = 0, sp = 0;
+      uint32_t visits = 0;
+      while (mask) {
+        if (++visits > ts.max_visits) {
+          raise_device_error(err, kDevIterationBound);
           break;
         }
-        stk[sp] = make_int2(go0 ? r1 : r0, (int)far_m);  // every lane, same
-        stt[sp] = ft;                                    // values
-        ++sp;
-        node = go0 ? r0 : r1;
-        mask = go0 ? m0 : m1;
-        continue;
-      }
-      if (m0 | m1) {
-        node = m0 ? r0 : r1;
-        mask = m0 | m1;
-        continue;
-      }
-      mask = 0;
-      while (sp > 0) {
-        --sp;
-        const int2 e = stk[sp];
-        const float et = stt[sp];
-        const unsigned m =
-            (unsigned)e.y & __ballot_sync(full, et <= fminf(hit.t, r.tmax));
-        if (m) {
-          node = e.x;
-          mask = m;
-          break;
+        const bool in = (mask >> lane) & 1u;
+        if (in) ++n_nodes;
+        float4 n0, n1, n2, n3;
+        ldg_node(ts.bvh + 4 * (uint64_t)node, n0, n1);
+        ldg_node(ts.bvh + 4 * (uint64_t)node + 2, n2, n3);
+        const float lim = fminf(hit.t, r.tmax);
+        float tn0 = 0.f, tn1 = 0.f;
+        const bool h0 =
+            in && slab2(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r, lim, tn0);
+        const bool h1 =
+            in && slab2(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r, lim, tn1);
+        const int r0 = __float_as_int(n3.x), r1 = __float_as_int(n3.y);
+        unsigned m0 = __ballot_sync(full, h0), m1 = __ballot_sync(full, h1);
+        if (r0 < 0) {
+          if (h0) {
+            ++n_tris;
+            leaf_test<TEST, false>(ts.tris, ~r0, r, w, hit);
+          }
+          m0 = 0;
+        }
+        if (r1 < 0) {
+          if (h1) {
+            ++n_tris;
+            leaf_test<TEST, false>(ts.tris, ~r1, r, w, hit);
+          }
+          m1 = 0;
+        }
+        if (m0 && m1) {
+          const unsigned both = m0 & m1;
+          const unsigned pref0 =
+              __ballot_sync(full, ((both >> lane) & 1u) && tn0 <= tn1);
+          const bool go0 = 2 * __popc(pref0) >= __popc(both);
+          const unsigned far_m = go0 ? m1 : m0;
+          float ft = ((far_m >> lane) & 1u) ? (go0 ? tn1 : tn0)
+                                            : __int_as_float(0x7f800000);
+  #pragma unroll
+          for (int o = 16; o > 0; o >>= 1)
+            ft = fminf(ft, __shfl_xor_sync(full, ft, o));
+          if (sp >= kStack) {
+            raise_device_error(err, kDevStackOverflow);
+            break;
+          }
+          stk[sp] = make_int2(go0 ? r1 : r0, (int)far_m);  // every lane, same
+          stt[sp] = ft;                                    // values
+          ++sp;
+          node = go0 ? r0 : r1;
+          mask = go0 ? m0 : m1;
+          continue;
+        }
+        if (m0 | m1) {
+          node = m0 ? r0 : r1;
+          mask = m0 | m1;
+          continue;
+        }
+        mask = 0;
+        while (sp > 0) {
+          --sp;
+          const int2 e = stk[sp];
+          const float et = stt[sp];
+          const unsigned m =
+              (unsigned)e.y & __ballot_sync(full, et <= fminf(hit.t, r.tmax));
+          if (m) {
+            node = e.x;
+            mask = m;
+            break;
+          }
         }
       }
     }

@@ -86,20 +86,25 @@ __global__ void __launch_bounds__(kTraceThreads, trace_min_blocks<W>())
   flush_counters(ctr, nr, nn, nt);
 }
 
-// Closest hits of a single job's camera rays (bounce 0's path queue: a
-// pixel's samples side by side) as masked packets over the binary layout.
-template <int TEST>
+// Closest hits of bounce 0's camera rays (a pixel's samples side by side in
+// the path queue) as masked packets over the binary layout; in multi-job
+// waves a packet per scene the warp's rays hold.
+template <int TEST, bool MJ>
 __global__ void __launch_bounds__(kPacketThreads, AJG_PACKET_MIN_BLOCKS)
-    k_extend_packet(DeviceScene s, const float4* __restrict__ ro,
+    k_extend_packet(DeviceScene s, MJTables t, const float4* __restrict__ ro,
                     const float4* __restrict__ rd,
                     const uint32_t* __restrict__ count, uint32_t* fetch_next,
                     ajg_hit* __restrict__ hits, TraceCounters* ctr,
                     uint32_t* err) {
   const uint32_t n = *count;
   uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k, TraceScene&) {
+  auto fetch = [&](uint32_t k, uint32_t& sid) {
     const float4 o = ro[k], d = rd[k];
+    if constexpr (MJ) sid = __float_as_uint(o.w);
     return make_query(xyz(o), xyz(d), kRayEps, __int_as_float(0x7f800000));
+  };
+  auto scene_of = [&](uint32_t sid, TraceScene& ts) {
+    if constexpr (MJ) retarget<2>(ts, t, sid);
   };
   auto finish = [&](uint32_t k, const Hit& h, bool) {
     ajg_hit o2;
@@ -109,33 +114,39 @@ __global__ void __launch_bounds__(kPacketThreads, AJG_PACKET_MIN_BLOCKS)
     o2.prim = h.prim;
     hits[k] = o2;
   };
-  trace_packet_closest<TEST>(trace_scene(s), n, fetch_next, fetch, finish, nr,
-                             nn, nt, err);
+  trace_packet_closest<TEST>(trace_scene(s), n, fetch_next, fetch, finish,
+                             scene_of, nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
-// Any hits of a single job's coherent shadow rays (the queue at the top of
-// the shadow queue's storage: entry k at cap - 1 - k) as masked packets over
-// the plain 4-wide tree.
-template <int TEST>
+// Any hits of bounce 0's coherent shadow rays (the queue at the top of the
+// shadow queue's storage: entry k at cap - 1 - k) as masked packets over the
+// plain 4-wide tree; in multi-job waves a packet per scene the warp's rays
+// hold.
+template <int TEST, bool MJ>
 __global__ void __launch_bounds__(kPacketThreads, AJG_PACKET_MIN_BLOCKS)
-    k_shadow_packet(DeviceScene s, const float4* __restrict__ sq_o,
+    k_shadow_packet(DeviceScene s, MJTables t, const float4* __restrict__ sq_o,
                     const float4* __restrict__ sq_d,
+                    const uint16_t* __restrict__ sq_scene,
                     const uint32_t* __restrict__ count, uint32_t* fetch_next,
                     uint32_t cap, uint8_t* __restrict__ vis,
                     TraceCounters* ctr, uint32_t* err) {
   const uint32_t n = min(*count, cap);
   uint32_t nn = 0, nt = 0, nr = 0;
-  auto fetch = [&](uint32_t k, TraceScene&) {
+  auto fetch = [&](uint32_t k, uint32_t& sid) {
     const uint32_t i = cap - 1 - k;
     const float4 o = sq_o[i], d = sq_d[i];
+    if constexpr (MJ) sid = sq_scene[i];
     return make_query(xyz(o), xyz(d), kRayEps, o.w);
+  };
+  auto scene_of = [&](uint32_t sid, TraceScene& ts) {
+    if constexpr (MJ) retarget<4>(ts, t, sid);
   };
   auto finish = [&](uint32_t k, const Hit&, bool occ) {
     if (!occ) vis[__float_as_uint(sq_d[cap - 1 - k].w)] = 1;
   };
-  trace_packet_any<TEST>(trace_scene(s), n, fetch_next, fetch, finish, nr, nn,
-                         nt, err);
+  trace_packet_any<TEST>(trace_scene(s), n, fetch_next, fetch, finish,
+                         scene_of, nr, nn, nt, err);
   flush_counters(ctr, nr, nn, nt);
 }
 
@@ -210,39 +221,59 @@ void launch_wave_shadow(bool mj, int tri_test, int width, const DeviceScene& s,
   });
 }
 
-void launch_wave_extend_packet(int tri_test, const DeviceScene& s,
-                               const float4* ro, const float4* rd,
-                               const uint32_t* count, uint32_t* fetch_next,
-                               ajg_hit* hits, TraceCounters* ctr, uint32_t* err,
+void launch_wave_extend_packet(bool mj, int tri_test, const DeviceScene& s,
+                               const MJTables& t, const float4* ro,
+                               const float4* rd, const uint32_t* count,
+                               uint32_t* fetch_next, ajg_hit* hits,
+                               TraceCounters* ctr, uint32_t* err,
                                cudaStream_t st) {
+  auto go = [&](auto T, auto M) {
+    constexpr int TT = decltype(T)::value;
+    constexpr bool MM = decltype(M)::value;
+    const int g = resident_grid((const void*)k_extend_packet<TT, MM>, kPacketThreads);
+    k_extend_packet<TT, MM><<<g, kPacketThreads, 0, st>>>(
+        s, t, ro, rd, count, fetch_next, hits, ctr, err);
+  };
+  using WT = std::integral_constant<int, AJG_TRI_WATERTIGHT>;
+  using MT = std::integral_constant<int, AJG_TRI_MOLLER_TRUMBORE>;
   if (tri_test == AJG_TRI_WATERTIGHT) {
-    const int g = resident_grid((const void*)k_extend_packet<AJG_TRI_WATERTIGHT>,
-                                kPacketThreads);
-    k_extend_packet<AJG_TRI_WATERTIGHT><<<g, kPacketThreads, 0, st>>>(
-        s, ro, rd, count, fetch_next, hits, ctr, err);
+    if (mj)
+      go(WT{}, std::true_type{});
+    else
+      go(WT{}, std::false_type{});
   } else {
-    const int g = resident_grid(
-        (const void*)k_extend_packet<AJG_TRI_MOLLER_TRUMBORE>, kPacketThreads);
-    k_extend_packet<AJG_TRI_MOLLER_TRUMBORE><<<g, kPacketThreads, 0, st>>>(
-        s, ro, rd, count, fetch_next, hits, ctr, err);
+    if (mj)
+      go(MT{}, std::true_type{});
+    else
+      go(MT{}, std::false_type{});
   }
 }
 
-void launch_wave_shadow_packet(int tri_test, const DeviceScene& s,
-                               const float4* sq_o, const float4* sq_d,
+void launch_wave_shadow_packet(bool mj, int tri_test, const DeviceScene& s,
+                               const MJTables& t, const float4* sq_o,
+                               const float4* sq_d, const uint16_t* sq_scene,
                                const uint32_t* count, uint32_t* fetch_next,
                                uint32_t cap, uint8_t* vis, TraceCounters* ctr,
                                uint32_t* err, cudaStream_t st) {
+  auto go = [&](auto T, auto M) {
+    constexpr int TT = decltype(T)::value;
+    constexpr bool MM = decltype(M)::value;
+    const int g = resident_grid((const void*)k_shadow_packet<TT, MM>, kPacketThreads);
+    k_shadow_packet<TT, MM><<<g, kPacketThreads, 0, st>>>(
+        s, t, sq_o, sq_d, sq_scene, count, fetch_next, cap, vis, ctr, err);
+  };
+  using WT = std::integral_constant<int, AJG_TRI_WATERTIGHT>;
+  using MT = std::integral_constant<int, AJG_TRI_MOLLER_TRUMBORE>;
   if (tri_test == AJG_TRI_WATERTIGHT) {
-    const int g = resident_grid((const void*)k_shadow_packet<AJG_TRI_WATERTIGHT>,
-                                kPacketThreads);
-    k_shadow_packet<AJG_TRI_WATERTIGHT><<<g, kPacketThreads, 0, st>>>(
-        s, sq_o, sq_d, count, fetch_next, cap, vis, ctr, err);
+    if (mj)
+      go(WT{}, std::true_type{});
+    else
+      go(WT{}, std::false_type{});
   } else {
-    const int g = resident_grid(
-        (const void*)k_shadow_packet<AJG_TRI_MOLLER_TRUMBORE>, kPacketThreads);
-    k_shadow_packet<AJG_TRI_MOLLER_TRUMBORE><<<g, kPacketThreads, 0, st>>>(
-        s, sq_o, sq_d, count, fetch_next, cap, vis, ctr, err);
+    if (mj)
+      go(MT{}, std::true_type{});
+    else
+      go(MT{}, std::false_type{});
   }
 }
 
@@ -280,6 +311,14 @@ void prepare_mj_kernels() {
         resident_grid((const void*)k_shadow<TT, true, WW>, kTraceThreads);
         resident_grid((const void*)k_bsdf_trace<TT, true, WW>, kTraceThreads);
       });
+  resident_grid((const void*)k_extend_packet<AJG_TRI_MOLLER_TRUMBORE, true>,
+                kPacketThreads);
+  resident_grid((const void*)k_extend_packet<AJG_TRI_WATERTIGHT, true>,
+                kPacketThreads);
+  resident_grid((const void*)k_shadow_packet<AJG_TRI_MOLLER_TRUMBORE, true>,
+                kPacketThreads);
+  resident_grid((const void*)k_shadow_packet<AJG_TRI_WATERTIGHT, true>,
+                kPacketThreads);
 }
 
 }  // namespace ajg

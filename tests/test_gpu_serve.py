@@ -24,6 +24,14 @@ def with_lights(scene, lights):
     return scene
 
 
+def three_light_box():
+    """The Cornell box under two directional lights and an environment."""
+    return with_lights(S.cornell_box(64, 64),
+                       [S.DirectionalLight((0.3, 1.0, 0.2), 3.0),
+                        S.DirectionalLight((-0.5, 1.0, 0.1), 1.5, 5.0),
+                        S.EnvLight(0.3)])
+
+
 @pytest.fixture(scope="module")
 def scenes(ctx):
     """Scenes of different sizes, materials, light sets and triangle tests."""
@@ -35,10 +43,7 @@ def scenes(ctx):
     env_only = with_lights(S.icosphere_scene(2, 11, 64, 64), [S.EnvLight(0.7)])
     area = S.cornell_area(64, 64)
     mats = S.material_box(64, 64)
-    three = with_lights(S.cornell_box(64, 64),
-                        [S.DirectionalLight((0.3, 1.0, 0.2), 3.0),
-                         S.DirectionalLight((-0.5, 1.0, 0.1), 1.5, 5.0),
-                         S.EnvLight(0.3)])
+    three = three_light_box()
     out = {
         "box": (api.GpuScene(ctx, box), box.camera),
         "ico": (api.GpuScene(ctx, ico), ico.camera),
@@ -122,6 +127,44 @@ def test_batch_equals_alone(ctx, scenes, policy, wave):
         assert st["spp_done"] == j[3].args.spp
         assert same_bits(film.rgbw, r), j[0]
     ctx.configure_serving("fair")
+
+
+def test_batch_without_packet_traversal_is_the_same(ctx, scenes):
+    """Multi-job waves trace bounce 0's directional-light shadow rays as
+    packets (a packet per scene a warp's rays hold; lanes pick the packet
+    queue by their own light's type and job); a context with packets off
+    renders the same mix to the same films bit for bit."""
+    import os
+    old = {k: os.environ.get(k) for k in ("AJG_PACKET_SHADOW",)}
+    try:
+        os.environ.update({"AJG_PACKET_SHADOW": "0"})
+        plain = api.Context(0, wave_paths=1 << 20)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k)
+            else:
+                os.environ[k] = v
+    ico = S.icosphere_scene(3, 7, 64, 64)
+    own = {"box": api.GpuScene(plain, S.cornell_box(64, 64)),
+           "ico": api.GpuScene(plain, ico),
+           "three": api.GpuScene(plain, three_light_box()),
+           "ico_wt": api.GpuScene(plain, ico, api.CreatePLOCAggregate(14, tri_test=1)),
+           "env_only": api.GpuScene(plain, with_lights(S.icosphere_scene(2, 11, 64, 64),
+                                                       [S.EnvLight(0.7)]))}
+    jobs = [(n, 40, 32, renderer(20, seed=i, max_b=10))
+            for i, n in enumerate(["box", "ico", "three", "ico_wt", "env_only", "ico"])]
+    ctx.configure_serving("fair")
+    out = ctx.render_batch([(scenes[n][0], cam_at(scenes[n][1], w, h), r)
+                            for n, w, h, r in jobs])
+    ref = plain.render_batch([(own[n], cam_at(scenes[n][1], w, h), r)
+                              for n, w, h, r in jobs])
+    for (film, st), (rfilm, rst), j in zip(out, ref, jobs):
+        assert st["state_name"] == rst["state_name"] == "done", j[0]
+        assert same_bits(film.rgbw, rfilm.rgbw), j[0]
+    for sc in own.values():
+        sc.release()
+    plain.close()
 
 
 def test_serve_stats_count_wave_device_time(ctx, scenes):
