@@ -5,10 +5,15 @@
 // Results are defined independently of the tree shape and of the visiting
 // order: the closest hit is the minimum t over every triangle the test
 // accepts, ties in t going to the lowest primitive index, and the node test
-// never culls a box that can hold such a hit -- it is the reference's slab
-// test, (bound - o) * inv_dir (ploc_aggregate.cpp:154-162), with the far
-// distance widened by 1 + 2*gamma(3) (Pharr, Jakob, Humphreys, PBRT 3rd ed.,
-// 3.9.2) and inclusive comparisons against the current best t.  Lanes are
+// does not cull a box that can hold a nearer hit -- it is the reference's
+// slab test, (bound - o) * inv_dir (ploc_aggregate.cpp:154-162), with the
+// far distance widened by 1 + 2*gamma(3) (Pharr, Jakob, Humphreys, PBRT 3rd
+// ed., 3.9.2) and inclusive comparisons against the current best t.  The
+// one exception is an exact tie in t (a ray through an edge two triangles
+// share) whose lower-index triangle's box is entered at a distance that
+// rounds above that t: found second, that triangle's box is culled, so the
+// visiting order picks the winner; a ray's order is fixed, so its result is
+// reproducible.  Any hits do not depend on the order at all.  Lanes are
 // persistent (trace_persistent): one node visit per iteration, a lane whose
 // ray finished takes the next from a shared counter.  Closest-hit rays visit
 // the nearest interior child and push the others farthest first; any-hit
@@ -20,10 +25,10 @@
 // stack keeps its top 16 entries
 // in a shared-memory ring and the rest in local memory, and is guarded:
 // overflow sets the device error word and ends the ray.  Coherent rays -- a
-// pixel's camera rays, its shadow rays toward a directional light -- are
-// traced as masked packets instead (trace_packet_closest, trace_packet_any):
-// a warp walks the tree once for its 32 rays, each lane testing the boxes
-// and triangles its own ray reaches.
+// pixel's shadow rays toward a directional light, and on request its camera
+// rays -- are traced as masked packets instead (trace_packet_any,
+// trace_packet_closest): a warp walks the tree once for its 32 rays, each
+// lane testing the boxes and triangles its own ray reaches.
 #pragma once
 #include <type_traits>
 
@@ -862,13 +867,14 @@ __device__ __forceinline__ void trace_packet_any(
 // over the binary tree, the counterpart of trace_packet_any: each lane tests
 // the node's two child boxes against its own ray and current hit, a child
 // is visited for the lanes that passed it, and a leaf's triangle is tested
-// by exactly those lanes -- a lane never skips a node it would visit alone,
-// and the closest hit (ties to the lowest primitive index, inclusive
-// comparisons) does not depend on the visiting order.  Of
-// two children the packet takes first the one most of its lanes reach
+// by exactly those lanes -- a lane never skips a node it would visit alone.
+// Of two children the packet takes first the one most of its lanes reach
 // first; the other is pushed with the packet's nearest entry distance to
 // it, and on the pop a lane whose hit is nearer than that distance (so
-// nearer than its own) leaves the entry's lanes.
+// nearer than its own) leaves the entry's lanes.  The packet visits in
+// another order than a single ray, so an exact tie at a shared edge (see
+// the top of this file) can resolve to the other triangle: the camera-ray
+// packets that use it are off by default (AJG_PACKET_CAMERA).
 //
 // Rays of a multi-job wave carry their scene: FETCH(k, sid) returns the
 // ray and its scene index, SCENE(sid, ts) points `ts` at that scene's tree,

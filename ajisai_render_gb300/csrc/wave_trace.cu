@@ -2,8 +2,8 @@
 // (k_extend), any hits of the shadow queue (k_shadow) and closest hits of
 // the MIS BSDF rays of scenes with emitters (k_bsdf_trace), each in a
 // single-job form and a multi-job form whose rays carry their scene index;
-// and for single jobs the packet traversals of bounce 0's camera rays
-// (k_extend_packet) and directional-light shadow rays (k_shadow_packet).
+// and the packet traversals of bounce 0's directional-light shadow rays
+// (k_shadow_packet) and, on request, camera rays (k_extend_packet).
 // A translation unit of its own: the traversal's arithmetic (the slab and
 // triangle tests) must not be contracted into multiply-adds, so that hits
 // stay bit-exact, while the shading kernels may be built with contraction.

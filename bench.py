@@ -201,6 +201,24 @@ def scaled_traffic(prof, rays_per_launch):
     return tot / len(rays_per_launch)
 
 
+def any_hit_total(by_kind, node_bytes, peak):
+    """Algorithmic bytes (node visits x node size + triangle tests x 48 B)
+    of every any-hit launch of the profiled step -- the per-lane kernel and
+    the packet launches -- over their summed device time, per launch kind
+    and together, against the measured HBM copy rate."""
+    out = {}
+    for name, kinds in (("k_shadow", ("any",)), ("k_shadow_packet", ("any_packets",)),
+                        ("together", ("any", "any_packets"))):
+        recs = [r for k in kinds for r in by_kind.get(k, [])]
+        ms = float(sum(r["ms"] for r in recs))
+        rays = int(sum(r["rays"] for r in recs))
+        b = float(sum(r["nodes"] * node_bytes + r["tris"] * TRI_BYTES for r in recs))
+        gbs = b / (ms / 1e3) / 1e9 if ms > 0 else None
+        out[name] = {"rays": rays, "ms": ms, "algorithmic_bytes": b,
+                     "achieved_gbs": gbs, "frac": gbs / peak if gbs else None}
+    return out
+
+
 def time_weighted(prof, key):
     """A captured per-launch figure averaged with the launches' times as
     weights."""
@@ -372,6 +390,7 @@ def run_ours(args):
     # closest-hit rays walk the binary layout kept beside a 4-wide tree
     node_bytes = scene.info()["closest_node_bytes" if dom == "closest" else "bvh_node_bytes"]
     bytes_per_launch = (n_nodes * node_bytes + n_tris * TRI_BYTES) / launches
+    node_bytes_any = scene.info()["bvh_node_bytes"]
     avg_ms = kind_ms.get(dom, 0.0) / launches
     achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else None
     peak, peak_kind = peaks()
@@ -405,6 +424,11 @@ def run_ours(args):
                 "frac_at_80_byte_nodes": ((n_nodes * 80 + n_tris * TRI_BYTES) / launches
                                           / (avg_ms / 1e3) / 1e9 / peak)
                 if avg_ms > 0 and node_bytes == 128 else None,
+                # the any-hit traversal as a whole: the per-lane kernel and
+                # bounce 0's packet launch together (a packet reads a node
+                # once for up to 32 lanes, so the packets' algorithmic rate
+                # is not bounded by the HBM copy rate)
+                "any_hit_all_kernels": any_hit_total(by_kind, node_bytes_any, peak),
                 "avg_launch_ms": avg_ms, "launches": len(launches_k),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "kernel_time_share": kind_ms.get(dom, 0.0) / max(1e-9, prof_ms),
