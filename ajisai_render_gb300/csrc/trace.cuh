@@ -780,7 +780,7 @@ __device__ __forceinline__ void trace_packet_any(
         if (in) ++n_nodes;
         const float4* nd = ts.bvh + (uint64_t)node * (2 * W);
         float4 q[8];
-  #pragma unroll
+#pragma unroll
         for (int i = 0; i < 8; i += 2) ldg_node(nd + i, q[i], q[i + 1]);
         const float* plx = &q[0].x;
         const float* phx = &q[1].x;
@@ -791,7 +791,7 @@ __device__ __forceinline__ void trace_packet_any(
         const float* prf = &q[6].x;
         int ref[W];
         unsigned hm[W];
-  #pragma unroll
+#pragma unroll
         for (int j = 0; j < W; ++j) {
           ref[j] = __float_as_int(prf[j]);
           float t0;
@@ -801,7 +801,7 @@ __device__ __forceinline__ void trace_packet_any(
           hm[j] = __ballot_sync(full, h);
         }
         // leaf children first: the lanes whose ray passed the box test them
-  #pragma unroll
+#pragma unroll
         for (int j = 0; j < W; ++j) {
           if (ref[j] < 0 && ref[j] != kEmptyRef) {
             const unsigned m = hm[j] & live;
@@ -819,7 +819,7 @@ __device__ __forceinline__ void trace_packet_any(
         // others pushed (popped last first)
         int nxt = -1;
         unsigned nmask = 0;
-  #pragma unroll
+#pragma unroll
         for (int j = 0; j < W; ++j) {
           if (ref[j] >= 0) {
             const unsigned m = hm[j] & live;
@@ -959,7 +959,7 @@ __device__ __forceinline__ void trace_packet_closest(
           const unsigned far_m = go0 ? m1 : m0;
           float ft = ((far_m >> lane) & 1u) ? (go0 ? tn1 : tn0)
                                             : __int_as_float(0x7f800000);
-  #pragma unroll
+#pragma unroll
           for (int o = 16; o > 0; o >>= 1)
             ft = fminf(ft, __shfl_xor_sync(full, ft, o));
           if (sp >= kStack) {
