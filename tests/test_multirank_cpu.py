@@ -80,3 +80,27 @@ def test_committed_profile_only_for_its_scene_and_layout():
     assert abs(bench.scaled_traffic(got, rays) - want) < 1e-6 * want
     w = bench.time_weighted(got, "l2_hit_rate_pct")
     assert min(got["l2_hit_rate_pct"]) <= w <= max(got["l2_hit_rate_pct"])
+
+
+def test_any_hit_total_sums_both_any_hit_kernels():
+    """The bench's any-hit summary: algorithmic bytes (node visits x node
+    size + triangle tests x 48 B) over device time, for the per-lane kernel,
+    the packet launches and both together."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    log = {"any": [{"ms": 10.0, "rays": 100, "nodes": 1000, "tris": 200},
+                   {"ms": 30.0, "rays": 300, "nodes": 3000, "tris": 600}],
+           "any_packets": [{"ms": 10.0, "rays": 50, "nodes": 800, "tris": 100}],
+           "shade": [{"ms": 99.0, "rays": 0, "nodes": 0, "tris": 0}]}
+    got = bench.any_hit_total(log, 128, 1000.0)
+    lane = 4000 * 128 + 800 * 48
+    assert got["k_shadow"]["rays"] == 400 and got["k_shadow"]["ms"] == 40.0
+    assert abs(got["k_shadow"]["achieved_gbs"] - lane / 0.04 / 1e9) < 1e-12
+    assert got["together"]["rays"] == 450 and got["together"]["ms"] == 50.0
+    both = lane + 800 * 128 + 100 * 48
+    assert abs(got["together"]["algorithmic_bytes"] - both) < 1e-6
+    assert abs(got["together"]["frac"] - both / 0.05 / 1e9 / 1000.0) < 1e-12
+    # no packet launches (packets off): zero rays, no rate
+    off = bench.any_hit_total({"any": log["any"]}, 128, 1000.0)
+    assert off["k_shadow_packet"] == {"rays": 0, "ms": 0.0, "algorithmic_bytes": 0.0,
+                                      "achieved_gbs": None, "frac": None}
